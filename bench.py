@@ -1,0 +1,373 @@
+"""Benchmark: NeuralODE forward+adjoint gradient evaluations per second on GB300.
+
+Workload (the batched headline configuration): u0 in R^{64 x 16384} ~ N(0,1);
+MLP 64->256->256->64 tanh with Glorot-uniform weights; tspan (0,1); 20 uniform
+saveat points; Tsit5 abstol 1e-7 reltol 1e-5; targets from a seeded stable
+linear ODE du/dt = M u (M = Q diag(-U(0.1,2)) Q^T); MSE loss;
+InterpolatingAdjoint with checkpoints at the save points.
+
+One step = one gradient evaluation: forward solve, fused MSE loss at the save
+points, adjoint solve, parameter-gradient reduction.
+
+  value : grad evals/s with inputs resident in HBM (device C-ABI entry points),
+          device time from CUDA events on the library's stream.
+  e2e   : the same through the host-pointer path a caller uses: every step copies
+          u0 and the targets host->device from pinned memory and reads the loss
+          and dL/dp back.
+
+Multi-GPU: the reference couples the whole batch through one step-size
+controller, so N > 1 runs N independent replicas (weak scaling, no collective
+on the data path); `value` is the sum over ranks.
+
+`--impl reference` times the CPU path on the host cores instead: the FP64
+oracle restatement of the same algorithm (the reference's Julia stack is not
+available on this machine), on a bounded sample of the batch, scaled to the
+workload's unit.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "diffeqflux.jl_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "NeuralODE grad evals/sec, BF16-TC vs plain FP32 GPU, at <=1e-3 rel err vs FP64"
+UNIT = "grad_evals/s"
+
+
+def workload(S=64, H=256, B=16384, nsave=20, seed=1):
+    from scipy.linalg import expm
+    rng = np.random.default_rng(seed)
+    dims = [S, H, H, S]
+    parts = []
+    for i in range(3):
+        lim = np.sqrt(6.0 / (dims[i] + dims[i + 1]))
+        W = rng.uniform(-lim, lim, size=(dims[i + 1], dims[i]))
+        parts += [W.T.reshape(-1), np.zeros(dims[i + 1])]
+    p = np.concatenate(parts).astype(np.float32)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    Q, _ = np.linalg.qr(rng.standard_normal((S, S)))
+    M = Q @ np.diag(-rng.uniform(0.1, 2.0, S)) @ Q.T
+    ts = np.linspace(0.0, 1.0, nsave)
+    tgt = np.stack([expm(M * t) @ u0.astype(np.float64) for t in ts], axis=-1).astype(np.float32)
+    return dict(S=S, H=H, B=B, dims=dims, p=p, u0=u0, ts=ts, target=tgt, tspan=(0.0, 1.0),
+                abstol=1e-7, reltol=1e-5)
+
+
+def gemm_flops_per_rhs(dims, B):
+    return 2.0 * B * sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference(wl, sample_b, max_seconds=25.0):
+    """Forward + InterpolatingAdjoint gradient of the FP64 oracle on `sample_b`
+    trajectories; returns (grad evals/s scaled to the full batch, seconds, cores)."""
+    from oracle import mlp as omlp
+    from oracle import tsit5 as ots
+    om = omlp.MLP(wl["dims"], ["tanh", "tanh", "identity"])
+    rhs = omlp.MLPRHS(om, wl["p"].astype(np.float64))
+    u0 = wl["u0"][:, :sample_b].astype(np.float64)
+    tg = wl["target"][:, :sample_b, :].astype(np.float64)
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        us, fwd = ots.solve_forward(rhs, u0, 0.0, 1.0, wl["ts"], wl["abstol"], wl["reltol"])
+        g = 2.0 * (us - tg) / us.size
+        ots.adjoint_interpolating(rhs, fwd, wl["ts"], g, 0.0, wl["abstol"], wl["reltol"])
+        n += 1
+        el = time.perf_counter() - t0
+        if el > max_seconds or n >= 3:
+            break
+    per_eval = el / n
+    # the oracle is vectorised over the batch, so cost grows linearly in B
+    full = per_eval * (wl["B"] / sample_b)
+    try:
+        import threadpoolctl
+        cores = max(i.get("num_threads", 1) for i in threadpoolctl.threadpool_info()) or 1
+    except Exception:
+        cores = os.cpu_count()
+    return 1.0 / full, el, n, cores
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    wl = workload(B=args.batch)
+    sample = min(args.cpu_sample, wl["B"])
+    vals = []
+    for _ in range(args.warmup and 1):
+        cpu_reference(wl, sample, max_seconds=5.0)
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        v, el, n, cores = cpu_reference(wl, sample, max_seconds=args.cpu_seconds)
+        vals.append(v)
+    v = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "neuralode_b16384_s64_h256x2_tanh_nsave20", "batch": wl["B"],
+                   "state": wl["S"], "hidden": wl["H"], "nsave": 20, "abstol": 1e-7, "reltol": 1e-5,
+                   "sensealg": "InterpolatingAdjoint"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{sample} of {wl['B']} trajectories per gradient evaluation, "
+                                   f"FP64 numpy oracle, cost scaled linearly to the batch"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t_all,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import ctypes as C
+
+    import torch
+
+    import gbnde
+    from gbnde import _lib
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    wl = workload(B=args.batch)
+    S, B = wl["S"], wl["B"]
+    model = gbnde.Chain(gbnde.Dense(S, wl["H"], "tanh"), gbnde.Dense(wl["H"], wl["H"], "tanh"),
+                        gbnde.Dense(wl["H"], S))
+    solver = gbnde.Solver(model, args.precision, local)
+    lib = solver.lib
+    desc = gbnde.Solver.solve_desc(0.0, 1.0, wl["ts"], wl["abstol"], wl["reltol"], 0)
+    ns = len(wl["ts"])
+    dev = torch.device("cuda", local)
+    # column-major device buffers
+    u0_d = torch.from_numpy(np.ascontiguousarray(wl["u0"].T)).to(dev)
+    tg_d = torch.from_numpy(np.ascontiguousarray(np.transpose(wl["target"], (2, 1, 0)))).to(dev)
+    p_d = torch.from_numpy(wl["p"]).to(dev)
+    us_d = torch.empty((ns, B, S), dtype=torch.float32, device=dev)
+    dl_d = torch.empty_like(us_d)
+    du0_d = torch.empty((B, S), dtype=torch.float32, device=dev)
+    dp_d = torch.empty(solver.nparams, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    solver.set_params_device(p_d)
+    torch.cuda.synchronize()
+    lstream = torch.cuda.ExternalStream(lib.gbnde_stream(solver.h), device=dev)
+
+    st_f = _lib.Stats()
+    st_b = _lib.Stats()
+    loss = C.c_double()
+
+    def grad_eval():
+        _lib.check(lib.gbnde_forward_device(solver.h, C.byref(desc), S, B, u0_d.data_ptr(),
+                                            us_d.data_ptr(), C.byref(st_f)))
+        _lib.check(lib.gbnde_loss_device(solver.h, us_d.data_ptr(), tg_d.data_ptr(), 1,
+                                         dl_d.data_ptr(), C.byref(loss)))
+        _lib.check(lib.gbnde_backward_device(solver.h, dl_d.data_ptr(), du0_d.data_ptr(),
+                                             dp_d.data_ptr(), C.byref(st_b)))
+
+    for _ in range(args.warmup):
+        grad_eval()
+    torch.cuda.synchronize()
+    # ---- timed region: device-resident inputs ----------------------------------
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    total_ms = 0.0
+    k_fwd = k_bwd = 0.0
+    flops = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)           # L2 flush between steps (256 MB > 129 MB L2)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(lstream)
+        grad_eval()
+        e1.record(lstream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        fm, bm = C.c_double(), C.c_double()
+        lib.gbnde_last_kernel_ms(solver.h, C.byref(fm), C.byref(bm))
+        k_fwd += fm.value
+        k_bwd += bm.value
+        F = gemm_flops_per_rhs(wl["dims"], B)
+        flops_b = F * st_b.nf_recompute + 3.0 * F * st_b.nf_adj
+        flops += flops_b
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    t_max = total_ms
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    ms_per_step = t_max / args.steps
+    value = world * args.steps / (t_max / 1000.0)
+
+    # ---- e2e: host buffers, copies inside the timed region ---------------------
+    u0_h = torch.from_numpy(np.ascontiguousarray(wl["u0"].T)).pin_memory()
+    tg_h = torch.from_numpy(np.ascontiguousarray(np.transpose(wl["target"], (2, 1, 0)))).pin_memory()
+    dp_h = torch.empty(solver.nparams, dtype=torch.float32).pin_memory()
+    h2d = u0_h.numel() * 4 + tg_h.numel() * 4
+    d2h = dp_h.numel() * 4 + 8
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e_ms = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(lstream)
+        with torch.cuda.stream(lstream):
+            u0_d.copy_(u0_h, non_blocking=True)
+            tg_d.copy_(tg_h, non_blocking=True)
+        grad_eval()
+        with torch.cuda.stream(lstream):
+            dp_h.copy_(dp_d, non_blocking=True)
+        e1.record(lstream)
+        e1.synchronize()
+        e_ms += e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e_ms = float(t.item())
+    e2e = world * args.steps / (e_ms / 1000.0)
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak_tf = peaks.get("bf16_tflops", 1900.0)
+    peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
+    bwd_ms_avg = k_bwd / args.steps
+    achieved_tf = (flops / args.steps) / (bwd_ms_avg / 1000.0) / 1e12
+    roof = {"kernel": "bwd_%s_kernel" % args.precision.replace("fp32", "f32"),
+            "bound": "tensor", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+            "frac": achieved_tf / peak_tf, "peak_source": peak_src,
+            "traffic": None,
+            "basis": "GEMM FLOPs of the adjoint launch: F*nf_recompute + 3F*nf_adj, F = 2*B*sum(in*out)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, el, n, cores = cpu_reference(wl, args.cpu_sample, max_seconds=args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{args.cpu_sample} of {B} trajectories, {n} gradient evaluation(s) in "
+                         f"{el:.1f} s, FP64 numpy oracle, scaled linearly to the batch"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+        "data": "synthetic (seeded)",
+        "config": {"workload": "neuralode_b16384_s64_h256x2_tanh_nsave20", "batch": B, "state": S,
+                   "hidden": wl["H"], "nsave": ns, "abstol": 1e-7, "reltol": 1e-5,
+                   "sensealg": "InterpolatingAdjoint", "loss": "MSE", "precision": args.precision,
+                   "l2": "flushed between steps (256 MB write)", "parallelism": "replicas"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps * 5,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "solver": {"nf_fwd": st_f.nf, "naccept": st_f.naccept, "nreject": st_f.nreject,
+                   "nf_recompute": st_b.nf_recompute, "nf_adj": st_b.nf_adj,
+                   "naccept_adj": st_b.naccept_adj, "nreject_adj": st_b.nreject_adj,
+                   "fwd_kernel_ms": k_fwd / args.steps, "bwd_kernel_ms": bwd_ms_avg,
+                   "loss": loss.value},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16"])
+    ap.add_argument("--batch", type=int, default=16384)
+    ap.add_argument("--cpu-sample", type=int, default=256)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

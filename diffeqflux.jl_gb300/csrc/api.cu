@@ -1,0 +1,684 @@
+// api.cu -- host implementation of the C ABI declared in include/gbnde.h.
+//
+// A context owns the parameters (flat ComponentArray order plus a transposed
+// copy for the VJPs), one CUDA stream and the device workspace of the last
+// forward solve (stage buffers, saved states, checkpoints, step log), which
+// gbnde_backward consumes. Buffers grow on demand and are reused.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbnde.h"
+#include "kernels.h"
+
+namespace gbnde {
+int launch_reduce_mu(const float* mu_acc, int nblk, int P, float* out, cudaStream_t st);
+int launch_transpose_params(const MlpDev& m, const float* p, float* wtr, cudaStream_t st);
+int launch_loss(const float* usave, const float* target, size_t n, int kind, float* dL,
+                double* partial, int nblk, cudaStream_t st);
+}  // namespace gbnde
+
+using namespace gbnde;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t _e = (call);                                                             \
+    if (_e != cudaSuccess)                                                               \
+      return fail(GBNDE_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), \
+                  __FILE__, __LINE__);                                                   \
+  } while (0)
+
+struct DBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= n) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(GBNDE_ERR_NOMEM, "cudaMalloc(%zu) failed", bytes);
+    }
+    n = bytes;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+}  // namespace
+
+struct gbnde_ctx {
+  int device = 0;
+  int precision = GBNDE_PREC_FP32;
+  gbnde_mlp_desc desc{};
+  size_t P = 0;
+  int S = 0;  // state dimension
+  cudaStream_t stream = nullptr;
+  MlpDev mlp{};
+  DBuf params, wtr;
+  bool have_params = false;
+  // forward workspace
+  DBuf u0, ubuf, kbuf, usave, ckpt, ckpt_step, steplog, trace, partials, sync, counters, saveat_d, bnd_d;
+  // backward workspace
+  DBuf dldu, dldu0, dldp, lam, ub, kl, ku, ibuf, mu_acc, mu_stage, iv_d, bsync, bcounters, loss_part;
+  // last forward
+  bool have_fwd = false;
+  int B = 0, nsave = 0;
+  double t0 = 0, t1 = 0, abstol = 0, reltol = 0;
+  long long maxiters = 0;
+  int sensealg = 0;
+  std::vector<double> saveat;
+  std::vector<double> steps;  // 2*naccept
+  std::vector<int> ckstep;
+  long long naccept = 0;
+  long long nattempt = 0;
+  int final_cur = 0;
+  int fwd_retcode = 0;
+  const float* usave_dev = nullptr;  // saved states of the last forward (device)
+  cudaStream_t own_stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double fwd_ms = 0.0, bwd_ms = 0.0;
+};
+
+namespace {
+
+int set_device(gbnde_ctx* c) {
+  CK(cudaSetDevice(c->device));
+  return 0;
+}
+
+int choose_tm(int maxdim_rows_total, size_t budget, int* TM) {
+  // rows_total feature rows of TM+4 floats must fit the budget
+  for (int tm = 64; tm >= 8; tm /= 2) {
+    if ((size_t)maxdim_rows_total * (tm + 4) * sizeof(float) <= budget) {
+      *TM = tm;
+      return 0;
+    }
+  }
+  return -1;
+}
+
+constexpr size_t kSmemBudget = 200 * 1024;
+
+}  // namespace
+
+extern "C" {
+
+const char* gbnde_strerror(int code) {
+  switch (code) {
+    case GBNDE_OK: return "ok";
+    case GBNDE_ERR_INVALID: return "invalid argument";
+    case GBNDE_ERR_CUDA: return "CUDA error";
+    case GBNDE_ERR_NOMEM: return "out of memory";
+    case GBNDE_ERR_UNSUPPORTED: return "unsupported";
+    case GBNDE_ERR_STATE: return "invalid call order";
+    case GBNDE_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown error";
+  }
+}
+
+const char* gbnde_last_error(void) { return g_last_error.c_str(); }
+
+int gbnde_create(gbnde_ctx** out, const gbnde_mlp_desc* mlp, int precision, int device) {
+  if (!out || !mlp) return fail(GBNDE_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (mlp->nlayers < 1 || mlp->nlayers > GBNDE_MAX_LAYERS)
+    return fail(GBNDE_ERR_INVALID, "nlayers must be in [1, %d]", GBNDE_MAX_LAYERS);
+  for (int l = 0; l <= mlp->nlayers; ++l)
+    if (mlp->dims[l] < 1 || mlp->dims[l] > 4096)
+      return fail(GBNDE_ERR_INVALID, "dims[%d] = %d out of range", l, mlp->dims[l]);
+  for (int l = 0; l < mlp->nlayers; ++l)
+    if (mlp->act[l] < GBNDE_ACT_IDENTITY || mlp->act[l] > GBNDE_ACT_SOFTPLUS)
+      return fail(GBNDE_ERR_INVALID, "act[%d] = %d unknown", l, mlp->act[l]);
+  const int S = mlp->dims[0] - (mlp->time_input ? 1 : 0);
+  if (S < 1 || mlp->dims[mlp->nlayers] != S)
+    return fail(GBNDE_ERR_INVALID, "output dim %d must equal state dim %d", mlp->dims[mlp->nlayers], S);
+  if (precision != GBNDE_PREC_FP32 && precision != GBNDE_PREC_BF16)
+    return fail(GBNDE_ERR_INVALID, "unknown precision %d", precision);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(GBNDE_ERR_CUDA, "no CUDA device available");
+  }
+  if (device < 0 || device >= ndev) return fail(GBNDE_ERR_INVALID, "device %d out of range", device);
+  gbnde_ctx* c = new gbnde_ctx();
+  c->device = device;
+  c->precision = precision;
+  c->desc = *mlp;
+  c->S = S;
+  if (int r = set_device(c)) {
+    delete c;
+    return r;
+  }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return fail(GBNDE_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  c->own_stream = c->stream;
+  for (auto& e : c->ev) {
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      delete c;
+      return fail(GBNDE_ERR_CUDA, "cudaEventCreate failed");
+    }
+  }
+  size_t off = 0;
+  MlpDev& m = c->mlp;
+  m.nlayers = mlp->nlayers;
+  m.cube = mlp->cube_input;
+  m.timein = mlp->time_input;
+  m.maxdim = 0;
+  for (int l = 0; l <= mlp->nlayers; ++l) {
+    m.dims[l] = mlp->dims[l];
+    m.maxdim = std::max(m.maxdim, mlp->dims[l]);
+  }
+  for (int l = 0; l < mlp->nlayers; ++l) {
+    m.act[l] = mlp->act[l];
+    m.woff[l] = (long long)off;
+    off += (size_t)mlp->dims[l] * mlp->dims[l + 1];
+    m.boff[l] = (long long)off;
+    off += (size_t)mlp->dims[l + 1];
+  }
+  c->P = off;
+  *out = c;
+  return 0;
+}
+
+void gbnde_destroy(gbnde_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  DBuf* bufs[] = {&c->params, &c->wtr, &c->u0, &c->ubuf, &c->kbuf, &c->usave, &c->ckpt,
+                  &c->ckpt_step, &c->steplog, &c->trace, &c->partials, &c->sync, &c->counters, &c->saveat_d,
+                  &c->bnd_d, &c->dldu, &c->dldu0, &c->dldp, &c->lam, &c->ub, &c->kl, &c->ku,
+                  &c->ibuf, &c->mu_acc, &c->mu_stage, &c->iv_d, &c->bsync, &c->bcounters,
+                  &c->loss_part};
+  for (DBuf* b : bufs) b->release();
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+}
+
+size_t gbnde_nparams(const gbnde_ctx* c) { return c ? c->P : 0; }
+
+static int bind_params(gbnde_ctx* c) {
+  MlpDev& m = c->mlp;
+  const float* p = c->params.as<float>();
+  size_t toff = 0;
+  for (int l = 0; l < m.nlayers; ++l) {
+    m.Wt[l] = p + m.woff[l];
+    m.bias[l] = p + m.boff[l];
+    m.W[l] = c->wtr.as<float>() + toff;
+    toff += (size_t)m.dims[l] * m.dims[l + 1];
+  }
+  if (launch_transpose_params(m, p, c->wtr.as<float>(), c->stream))
+    return fail(GBNDE_ERR_CUDA, "transpose kernel launch failed");
+  c->have_params = true;
+  return 0;
+}
+
+static int alloc_params(gbnde_ctx* c) {
+  if (int r = c->params.ensure(c->P * sizeof(float))) return r;
+  if (int r = c->wtr.ensure(c->P * sizeof(float))) return r;
+  return 0;
+}
+
+int gbnde_set_params(gbnde_ctx* c, const float* p, size_t n) {
+  if (!c || !p) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (n != c->P) return fail(GBNDE_ERR_INVALID, "expected %zu parameters, got %zu", c->P, n);
+  if (int r = set_device(c)) return r;
+  if (int r = alloc_params(c)) return r;
+  CK(cudaMemcpyAsync(c->params.p, p, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  return bind_params(c);
+}
+
+int gbnde_set_params_device(gbnde_ctx* c, const float* p, size_t n) {
+  if (!c || !p) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (n != c->P) return fail(GBNDE_ERR_INVALID, "expected %zu parameters, got %zu", c->P, n);
+  if (int r = set_device(c)) return r;
+  if (int r = alloc_params(c)) return r;
+  CK(cudaMemcpyAsync(c->params.p, p, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+  return bind_params(c);
+}
+
+static int validate_desc(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B) {
+  if (!d) return fail(GBNDE_ERR_INVALID, "null solve descriptor");
+  if (S != c->S) return fail(GBNDE_ERR_INVALID, "state dim %d does not match the model (%d)", S, c->S);
+  if (B < 1) return fail(GBNDE_ERR_INVALID, "batch must be >= 1");
+  if (!(d->t1 > d->t0)) return fail(GBNDE_ERR_UNSUPPORTED, "tspan must satisfy t1 > t0");
+  if (!(d->abstol > 0) || !(d->reltol >= 0)) return fail(GBNDE_ERR_INVALID, "tolerances must be positive");
+  if (d->nsave < 1 || !d->saveat) return fail(GBNDE_ERR_INVALID, "saveat must hold >= 1 time");
+  for (int i = 0; i < d->nsave; ++i) {
+    const double s = d->saveat[i];
+    if (!(s >= d->t0 && s <= d->t1)) return fail(GBNDE_ERR_INVALID, "saveat[%d] = %g outside tspan", i, s);
+    if (i > 0 && s < d->saveat[i - 1]) return fail(GBNDE_ERR_INVALID, "saveat must be non-decreasing");
+  }
+  if (d->sensealg != GBNDE_SENSE_INTERPOLATING && d->sensealg != GBNDE_SENSE_BACKSOLVE)
+    return fail(GBNDE_ERR_INVALID, "unknown sensealg %d", d->sensealg);
+  if ((long long)B * S > (1LL << 31)) return fail(GBNDE_ERR_UNSUPPORTED, "S*B too large");
+  return 0;
+}
+
+static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, const float* u0,
+                        bool u0_host, float* usave, bool usave_host, gbnde_stats* stats) {
+  if (!c) return fail(GBNDE_ERR_INVALID, "null context");
+  if (!c->have_params) return fail(GBNDE_ERR_STATE, "parameters not set");
+  if (int r = validate_desc(c, d, S, B)) return r;
+  if (int r = set_device(c)) return r;
+  if (c->precision != GBNDE_PREC_FP32 && c->precision != GBNDE_PREC_BF16)
+    return fail(GBNDE_ERR_UNSUPPORTED, "precision");
+  c->have_fwd = false;
+  const size_t SB = (size_t)S * B;
+  const int nsave = d->nsave;
+  const long long maxiters = d->maxiters > 0 ? d->maxiters : 100000;
+  // checkpoint boundaries: t0 and every save point but the last
+  std::vector<double> bnd;
+  bnd.push_back(d->t0);
+  for (int i = 0; i + 1 < nsave; ++i)
+    if (d->saveat[i] > d->t0) bnd.push_back(d->saveat[i]);
+  const int nb = (int)bnd.size();
+
+  int TM = 0;
+  if (choose_tm(2 * c->mlp.maxdim, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "layer too wide");
+  const int LD = TM + 4;
+  const size_t smem = (size_t)2 * c->mlp.maxdim * LD * sizeof(float);
+  const int ntiles = (B + TM - 1) / TM;
+  int gmax = 0;
+  if (max_grid_fwd_f32(smem, &gmax)) return fail(GBNDE_ERR_CUDA, "occupancy query failed");
+  const int grid = std::min(gmax, ntiles);
+
+  int r = 0;
+  if (u0_host && (r = c->u0.ensure(SB * 4))) return r;
+  if ((r = c->ubuf.ensure(2 * SB * 4)) || (r = c->kbuf.ensure(7 * SB * 4))) return r;
+  if (usave_host && (r = c->usave.ensure(SB * nsave * 4))) return r;
+  if ((r = c->ckpt.ensure(SB * nb * 4)) || (r = c->ckpt_step.ensure(nb * sizeof(int)))) return r;
+  const long long maxsteps = std::min<long long>(maxiters, 1LL << 22);
+  if ((r = c->steplog.ensure(2 * maxsteps * sizeof(double)))) return r;
+  if ((r = c->trace.ensure(4 * maxsteps * sizeof(double)))) return r;
+  if ((r = c->partials.ensure(4 * (size_t)grid * sizeof(double)))) return r;
+  if ((r = c->sync.ensure(64)) || (r = c->counters.ensure(CT_NSLOTS * sizeof(long long) + 16))) return r;
+  if ((r = c->saveat_d.ensure(nsave * sizeof(double))) || (r = c->bnd_d.ensure(nb * sizeof(double)))) return r;
+
+  cudaStream_t st = c->stream;
+  const float* u0d = u0;
+  if (u0_host) {
+    CK(cudaMemcpyAsync(c->u0.p, u0, SB * 4, cudaMemcpyHostToDevice, st));
+    u0d = c->u0.as<float>();
+  }
+  float* usd = usave_host ? c->usave.as<float>() : usave;
+  CK(cudaMemcpyAsync(c->saveat_d.p, d->saveat, nsave * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->bnd_d.p, bnd.data(), nb * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(c->sync.p, 0, 64, st));
+  CK(cudaMemsetAsync(c->counters.p, 0, CT_NSLOTS * sizeof(long long) + 16, st));
+
+  FwdArgs a{};
+  a.mlp = c->mlp;
+  a.S = S;
+  a.B = B;
+  a.TM = TM;
+  a.LD = LD;
+  a.ntiles = ntiles;
+  a.t0 = d->t0;
+  a.t1 = d->t1;
+  a.abstol = d->abstol;
+  a.reltol = d->reltol;
+  a.dt0 = d->dt0;
+  a.dtmin = d->dtmin > 0 ? d->dtmin : 0.0;
+  a.dtmax = d->t1 - d->t0;
+  a.maxiters = maxiters;
+  a.saveat = c->saveat_d.as<double>();
+  a.nsave = nsave;
+  a.bnd = c->bnd_d.as<double>();
+  a.nbnd = nb;
+  a.u0 = u0d;
+  a.ubuf[0] = c->ubuf.as<float>();
+  a.ubuf[1] = c->ubuf.as<float>() + SB;
+  for (int j = 0; j < 7; ++j) a.kbuf[j] = c->kbuf.as<float>() + j * SB;
+  a.usave = usd;
+  a.ckpt = c->ckpt.as<float>();
+  a.max_ckpt = nb;
+  a.ckpt_step = c->ckpt_step.as<int>();
+  a.steplog = c->steplog.as<double>();
+  a.maxsteps = maxsteps;
+  a.trace = c->trace.as<double>();
+  a.partials = c->partials.as<double>();
+  a.bar = c->sync.as<unsigned int>();
+  a.status = reinterpret_cast<int*>(c->sync.as<char>() + 16);
+  a.counters = c->counters.as<long long>();
+  a.tfinal = reinterpret_cast<double*>(c->counters.as<char>() + CT_NSLOTS * sizeof(long long));
+  CK(cudaEventRecord(c->ev[0], st));
+  if (launch_fwd_f32(a, grid, smem, st)) {
+    cudaError_t e = cudaGetLastError();
+    return fail(GBNDE_ERR_CUDA, "forward launch failed: %s", cudaGetErrorString(e));
+  }
+  CK(cudaEventRecord(c->ev[1], st));
+  long long cnt[CT_NSLOTS + 2];
+  int status[4];
+  CK(cudaMemcpyAsync(cnt, c->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(status, a.status, sizeof status, cudaMemcpyDeviceToHost, st));
+  if (usave_host) CK(cudaMemcpyAsync(usave, usd, SB * nsave * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+    c->fwd_ms = ms;
+  }
+  double tfinal;
+  std::memcpy(&tfinal, &cnt[CT_NSLOTS], sizeof(double));
+  const long long nacc = cnt[CT_NACCEPT];
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    stats->nf = cnt[CT_NF];
+    stats->naccept = nacc;
+    stats->nreject = cnt[CT_NREJECT];
+    stats->retcode = status[ST_RETCODE];
+    stats->t_final = tfinal;
+  }
+  c->fwd_retcode = status[ST_RETCODE];
+  if (status[ST_BARRIER]) return fail(GBNDE_ERR_TIMEOUT, "forward grid barrier timed out");
+  // keep what the backward pass needs
+  const long long nlog = std::min(nacc, maxsteps);
+  c->steps.resize(2 * nlog);
+  if (nlog) CK(cudaMemcpy(c->steps.data(), c->steplog.p, 2 * nlog * sizeof(double), cudaMemcpyDeviceToHost));
+  const int nck = (int)cnt[CT_NCKPT];
+  c->ckstep.resize(nck);
+  if (nck) CK(cudaMemcpy(c->ckstep.data(), c->ckpt_step.p, nck * sizeof(int), cudaMemcpyDeviceToHost));
+  c->naccept = nacc;
+  c->nattempt = std::min(cnt[CT_NATTEMPT], maxsteps);
+  c->final_cur = (int)cnt[5];
+  c->B = B;
+  c->nsave = nsave;
+  c->t0 = d->t0;
+  c->t1 = d->t1;
+  c->abstol = d->abstol;
+  c->reltol = d->reltol;
+  c->maxiters = maxiters;
+  c->sensealg = d->sensealg;
+  c->saveat.assign(d->saveat, d->saveat + nsave);
+  c->have_fwd = (status[ST_RETCODE] == GBNDE_RET_SUCCESS) && nacc <= maxsteps;
+  c->usave_dev = usd;
+  return 0;
+}
+
+// Backward intervals, from the last save time down to t0, with the recorded
+// forward steps that cover each and the checkpoint to restart them from.
+static int build_intervals(gbnde_ctx* c, std::vector<Interval>& ivs, int* max_slots,
+                           int* save_last, int* nsave_last) {
+  std::vector<double> times;  // distinct save times and t0, increasing
+  times.push_back(c->t0);
+  for (double s : c->saveat)
+    if (s > times.back()) times.push_back(s);
+  const double tlast = c->saveat.back();
+  *save_last = 0;
+  *nsave_last = 0;
+  for (int i = 0; i < c->nsave; ++i)
+    if (c->saveat[i] == tlast) {
+      if (*nsave_last == 0) *save_last = i;
+      ++*nsave_last;
+    }
+  const long long ns = c->naccept;
+  auto step_tn = [&](long long n) { return c->steps[2 * n]; };
+  *max_slots = 1;
+  ivs.clear();
+  for (int k = (int)times.size() - 1; k >= 1; --k) {
+    const double lo = times[k - 1], hi = times[k];
+    if (hi > tlast) continue;
+    Interval iv{};
+    iv.t_lo = lo;
+    iv.t_hi = hi;
+    // step containing lo: last n with t_n <= lo; step containing hi: last n with t_n < hi
+    long long nlo = 0, nhi = 0;
+    for (long long n = 0; n < ns; ++n) {
+      if (step_tn(n) <= lo) nlo = n;
+      if (step_tn(n) < hi) nhi = n;
+    }
+    iv.nlo = (int)nlo;
+    iv.nhi = (int)nhi;
+    auto it = std::find(c->ckstep.begin(), c->ckstep.end(), (int)nlo);
+    if (c->sensealg == GBNDE_SENSE_INTERPOLATING && it == c->ckstep.end())
+      return fail(GBNDE_ERR_STATE, "no checkpoint for forward step %lld", nlo);
+    iv.ckpt = it == c->ckstep.end() ? 0 : (int)(it - c->ckstep.begin());
+    iv.save_lo = -1;
+    iv.nsave_lo = 0;
+    for (int i = 0; i < c->nsave; ++i)
+      if (c->saveat[i] == lo) {
+        if (iv.nsave_lo == 0) iv.save_lo = i;
+        ++iv.nsave_lo;
+      }
+    *max_slots = std::max(*max_slots, iv.nhi - iv.nlo + 1);
+    ivs.push_back(iv);
+  }
+  return 0;
+}
+
+static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* dLdu0,
+                         float* dLdp, bool out_host, gbnde_stats* stats) {
+  if (!c) return fail(GBNDE_ERR_INVALID, "null context");
+  if (!c->have_fwd) return fail(GBNDE_ERR_STATE, "backward needs a successful forward solve first");
+  if (!dLdu || !dLdu0 || !dLdp) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (int r = set_device(c)) return r;
+  const int S = c->S, B = c->B, nsave = c->nsave;
+  const size_t SB = (size_t)S * B;
+  const int P = (int)c->P;
+  std::vector<Interval> ivs;
+  int max_slots = 1, save_last = 0, nsave_last = 0;
+  if (int r = build_intervals(c, ivs, &max_slots, &save_last, &nsave_last)) return r;
+  const bool backsolve = c->sensealg == GBNDE_SENSE_BACKSOLVE;
+
+  int rows = 0;
+  for (int l = 0; l <= c->mlp.nlayers; ++l) rows += c->mlp.dims[l];
+  rows += 2 * c->mlp.maxdim + S;
+  int TM = 0;
+  if (choose_tm(rows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "network too wide");
+  const int LD = TM + 4;
+  const size_t smem = (size_t)rows * LD * sizeof(float);
+  const int ntiles = (B + TM - 1) / TM;
+  int gmax = 0;
+  if (max_grid_bwd_f32(smem, &gmax)) return fail(GBNDE_ERR_CUDA, "occupancy query failed");
+  const int grid = std::min(gmax, ntiles);
+
+  int r = 0;
+  if (in_host && (r = c->dldu.ensure(SB * nsave * 4))) return r;
+  if (out_host && ((r = c->dldu0.ensure(SB * 4)) || (r = c->dldp.ensure((size_t)P * 4)))) return r;
+  if ((r = c->lam.ensure(2 * SB * 4)) || (r = c->kl.ensure(7 * SB * 4))) return r;
+  if (backsolve && ((r = c->ub.ensure(2 * SB * 4)) || (r = c->ku.ensure(7 * SB * 4)))) return r;
+  if (!backsolve && (r = c->ibuf.ensure((size_t)max_slots * 8 * SB * 4))) return r;
+  if ((r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4))) return r;
+  if ((r = c->iv_d.ensure(std::max<size_t>(1, ivs.size()) * sizeof(Interval)))) return r;
+  if ((r = c->bsync.ensure(64)) || (r = c->bcounters.ensure(CT_NSLOTS * sizeof(long long)))) return r;
+  if ((r = c->partials.ensure(4 * (size_t)grid * sizeof(double)))) return r;
+
+  cudaStream_t st = c->stream;
+  const float* dldu_d = dLdu;
+  if (in_host) {
+    CK(cudaMemcpyAsync(c->dldu.p, dLdu, SB * nsave * 4, cudaMemcpyHostToDevice, st));
+    dldu_d = c->dldu.as<float>();
+  }
+  float* du0_d = out_host ? c->dldu0.as<float>() : dLdu0;
+  float* dp_d = out_host ? c->dldp.as<float>() : dLdp;
+  if (!ivs.empty())
+    CK(cudaMemcpyAsync(c->iv_d.p, ivs.data(), ivs.size() * sizeof(Interval), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(c->bsync.p, 0, 64, st));
+  CK(cudaMemsetAsync(c->bcounters.p, 0, CT_NSLOTS * sizeof(long long), st));
+
+  BwdArgs a{};
+  a.mlp = c->mlp;
+  a.S = S;
+  a.B = B;
+  a.TM = TM;
+  a.LD = LD;
+  a.ntiles = ntiles;
+  a.P = P;
+  a.sensealg = c->sensealg;
+  a.t0 = c->t0;
+  a.abstol = c->abstol;
+  a.reltol = c->reltol;
+  a.dtmax = c->saveat.back() - c->t0;
+  a.maxiters = c->maxiters;
+  a.iv = c->iv_d.as<Interval>();
+  a.niv = (int)ivs.size();
+  a.fsteps = c->steplog.as<double>();
+  a.nfsteps = c->naccept;
+  a.ckpt = c->ckpt.as<float>();
+  a.usave = c->usave_dev;
+  a.dLdu = dldu_d;
+  a.saveat = c->saveat_d.as<double>();
+  a.nsave = nsave;
+  a.save_last = save_last;
+  a.nsave_last = nsave_last;
+  a.ibuf = c->ibuf.as<float>();
+  a.ibuf_slots = max_slots;
+  a.lam[0] = c->lam.as<float>();
+  a.lam[1] = c->lam.as<float>() + SB;
+  a.ub[0] = backsolve ? c->ub.as<float>() : nullptr;
+  a.ub[1] = backsolve ? c->ub.as<float>() + SB : nullptr;
+  for (int j = 0; j < 7; ++j) {
+    a.kl[j] = c->kl.as<float>() + j * SB;
+    a.ku[j] = backsolve ? c->ku.as<float>() + j * SB : nullptr;
+    a.kf[j] = nullptr;
+  }
+  a.mu_acc = c->mu_acc.as<float>();
+  a.mu_stage = c->mu_stage.as<float>();
+  a.dLdu0 = du0_d;
+  a.partials = c->partials.as<double>();
+  a.bar = c->bsync.as<unsigned int>();
+  a.status = reinterpret_cast<int*>(c->bsync.as<char>() + 16);
+  a.counters = c->bcounters.as<long long>();
+  CK(cudaEventRecord(c->ev[2], st));
+  if (launch_bwd_f32(a, grid, smem, st)) {
+    cudaError_t e = cudaGetLastError();
+    return fail(GBNDE_ERR_CUDA, "backward launch failed: %s", cudaGetErrorString(e));
+  }
+  CK(cudaEventRecord(c->ev[3], st));
+  if (launch_reduce_mu(a.mu_acc, grid, P, dp_d, st)) return fail(GBNDE_ERR_CUDA, "reduce launch failed");
+  long long cnt[CT_NSLOTS];
+  int status[4];
+  CK(cudaMemcpyAsync(cnt, c->bcounters.p, sizeof cnt, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(status, a.status, sizeof status, cudaMemcpyDeviceToHost, st));
+  if (out_host) {
+    CK(cudaMemcpyAsync(dLdu0, du0_d, SB * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(dLdp, dp_d, (size_t)P * 4, cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]));
+    c->bwd_ms = ms;
+  }
+  if (stats) {
+    stats->nf_adj = cnt[CT_NF];
+    stats->naccept_adj = cnt[CT_NACCEPT];
+    stats->nreject_adj = cnt[CT_NREJECT];
+    stats->nf_recompute = cnt[CT_NRECOMP];
+    stats->retcode_adj = status[ST_RETCODE];
+  }
+  if (status[ST_BARRIER]) return fail(GBNDE_ERR_TIMEOUT, "backward grid barrier timed out");
+  return 0;
+}
+
+int gbnde_forward(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, const float* u0,
+                  float* usave, gbnde_stats* stats) {
+  if (!u0 || !usave) return fail(GBNDE_ERR_INVALID, "null argument");
+  return forward_impl(c, d, S, B, u0, true, usave, true, stats);
+}
+
+int gbnde_forward_device(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, const float* u0,
+                         float* usave, gbnde_stats* stats) {
+  if (!u0 || !usave) return fail(GBNDE_ERR_INVALID, "null argument");
+  return forward_impl(c, d, S, B, u0, false, usave, false, stats);
+}
+
+int gbnde_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, float* dLdp, gbnde_stats* stats) {
+  return backward_impl(c, dLdu, true, dLdu0, dLdp, true, stats);
+}
+
+int gbnde_backward_device(gbnde_ctx* c, const float* dLdu, float* dLdu0, float* dLdp,
+                          gbnde_stats* stats) {
+  return backward_impl(c, dLdu, false, dLdu0, dLdp, false, stats);
+}
+
+int gbnde_loss_device(gbnde_ctx* c, const float* usave, const float* target, int kind,
+                      float* dLdu, double* loss) {
+  if (!c || !usave || !target || !dLdu || !loss) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (!c->have_fwd) return fail(GBNDE_ERR_STATE, "loss needs a forward solve first");
+  if (kind != 0 && kind != 1) return fail(GBNDE_ERR_INVALID, "unknown loss kind %d", kind);
+  if (int r = set_device(c)) return r;
+  const size_t n = (size_t)c->S * c->B * c->nsave;
+  const int nblk = 304;
+  if (int r = c->loss_part.ensure(nblk * sizeof(double))) return r;
+  if (launch_loss(usave, target, n, kind, dLdu, c->loss_part.as<double>(), nblk, c->stream))
+    return fail(GBNDE_ERR_CUDA, "loss launch failed");
+  std::vector<double> part(nblk);
+  CK(cudaMemcpyAsync(part.data(), c->loss_part.p, nblk * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  double s = 0.0;
+  for (double v : part) s += v;
+  *loss = (kind == 1) ? s / (double)n : s;
+  return 0;
+}
+
+long long gbnde_forward_trace(gbnde_ctx* c, double* out4, long long cap) {
+  if (!c || c->nattempt <= 0) return 0;
+  const long long n = std::min(c->nattempt, cap);
+  if (out4 && n > 0 &&
+      cudaMemcpy(out4, c->trace.p, 4 * n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return c->nattempt;
+}
+
+void* gbnde_stream(gbnde_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int gbnde_set_stream(gbnde_ctx* c, void* stream) {
+  if (!c) return fail(GBNDE_ERR_INVALID, "null context");
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return 0;
+}
+
+int gbnde_last_kernel_ms(gbnde_ctx* c, double* fwd_ms, double* bwd_ms) {
+  if (!c) return fail(GBNDE_ERR_INVALID, "null context");
+  if (fwd_ms) *fwd_ms = c->fwd_ms;
+  if (bwd_ms) *bwd_ms = c->bwd_ms;
+  return 0;
+}
+
+long long gbnde_forward_steps(gbnde_ctx* c, double* t, double* h, long long cap) {
+  if (!c || !c->have_fwd) return 0;
+  const long long n = (long long)c->steps.size() / 2;
+  for (long long i = 0; i < std::min(n, cap); ++i) {
+    if (t) t[i] = c->steps[2 * i];
+    if (h) h[i] = c->steps[2 * i + 1];
+  }
+  return n;
+}
+
+}  // extern "C"

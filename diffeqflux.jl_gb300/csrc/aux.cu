@@ -1,0 +1,65 @@
+// aux.cu -- small helper kernels: transposed weight copy for the VJPs and the
+// fused save-point loss with its cotangent.
+#include "kernels.h"
+
+namespace gbnde {
+
+struct TransposeArgs {
+  const float* src[GBNDE_MAX_LAYERS];
+  float* dst[GBNDE_MAX_LAYERS];
+  int K[GBNDE_MAX_LAYERS], N[GBNDE_MAX_LAYERS];
+  int nlayers;
+};
+
+// dst[n*K + k] = src[k*N + n] for every layer (Lux [in][out] -> [out][in]).
+__global__ void transpose_params_kernel(TransposeArgs a) {
+  for (int l = 0; l < a.nlayers; ++l) {
+    const int K = a.K[l], N = a.N[l];
+    const size_t tot = (size_t)K * N;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot;
+         i += (size_t)gridDim.x * blockDim.x) {
+      const size_t n = i / K, k = i - n * K;
+      a.dst[l][i] = a.src[l][k * N + n];
+    }
+  }
+}
+
+int launch_transpose_params(const MlpDev& m, const float* p, float* wtr, cudaStream_t st) {
+  TransposeArgs a{};
+  a.nlayers = m.nlayers;
+  size_t toff = 0;
+  for (int l = 0; l < m.nlayers; ++l) {
+    a.src[l] = p + m.woff[l];
+    a.dst[l] = wtr + toff;
+    a.K[l] = m.dims[l];
+    a.N[l] = m.dims[l + 1];
+    toff += (size_t)m.dims[l] * m.dims[l + 1];
+  }
+  transpose_params_kernel<<<256, 256, 0, st>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// loss = sum (u - target)^2 (kind 0) or its mean (kind 1); dL = dloss/du.
+// One FP64 partial per block, summed on the host in block order.
+__global__ void loss_kernel(const float* __restrict__ u, const float* __restrict__ tg, size_t n,
+                            int kind, float* __restrict__ dL, double* __restrict__ part) {
+  __shared__ double red[40];
+  const float scale = (kind == 1) ? (float)(2.0 / (double)n) : 2.f;
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float d = u[i] - tg[i];
+    s += (double)d * (double)d;
+    dL[i] = scale * d;
+  }
+  s = block_sum_double(s, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+int launch_loss(const float* usave, const float* target, size_t n, int kind, float* dL,
+                double* partial, int nblk, cudaStream_t st) {
+  loss_kernel<<<nblk, 256, 0, st>>>(usave, target, n, kind, dL, partial);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace gbnde

@@ -1,0 +1,334 @@
+// fwd_f32.cu -- persistent Tsit5 forward solve, plain FP32 form.
+//
+// Replaces, for the batched NeuralODE state, the integrator loop that
+// `solve(prob, Tsit5(); saveat, abstol, reltol)` runs (src/neural_de.jl:55-58):
+// 7-stage FSAL Tsit5 steps, the embedded error estimate with the scaled RMS
+// norm over all S*B entries, PI step-size control with one accept/reject
+// decision per step for the whole batch, the free interpolant at `saveat`
+// points and clipping of the last step to t1.
+//
+// One cooperative launch does the whole solve. CTAs own tiles of TM
+// trajectories; stages of a step need no communication between CTAs, so the
+// only grid-wide synchronisation is one barrier per step, after which every
+// CTA sums the per-CTA error partials in the same fixed order and takes the
+// same controller decision. t, dt and the error reduction are FP64; all
+// state and stage arithmetic is FP32.
+#include "kernels.h"
+
+namespace gbnde {
+
+namespace {
+
+__device__ __forceinline__ float* kb(const FwdArgs& a, int j, bool swp) {
+  if (j == 0) return swp ? a.kbuf[6] : a.kbuf[0];
+  if (j == 6) return swp ? a.kbuf[0] : a.kbuf[6];
+  return a.kbuf[j];
+}
+
+// Load the MLP input of a tile (feature-major) from a per-element producer.
+template <class Fn>
+__device__ __forceinline__ void load_tile_input(const FwdArgs& a, int tile, float* bufA,
+                                                double tstage, Fn&& val) {
+  const int S = a.S, TM = a.TM, LD = a.LD;
+  const size_t base = (size_t)tile * TM * S;
+  const int nvalid = min(TM, a.B - tile * TM);
+  for (int e = threadIdx.x; e < TM * S; e += blockDim.x) {
+    const int m = e / S, s = e - m * S;
+    float v = 0.f;
+    if (m < nvalid) v = val(base + e);
+    if (a.mlp.cube) v = v * v * v;
+    bufA[s * LD + m] = v;
+  }
+  if (a.mlp.timein) {
+    for (int m = threadIdx.x; m < TM; m += blockDim.x) bufA[S * LD + m] = (float)tstage;
+  }
+  __syncthreads();
+}
+
+// Store the tile output (rows [0,S) of `out`) through a per-element consumer.
+template <class Fn>
+__device__ __forceinline__ void store_tile_output(const FwdArgs& a, int tile, const float* out,
+                                                  Fn&& sink) {
+  const int S = a.S, TM = a.TM, LD = a.LD;
+  const size_t base = (size_t)tile * TM * S;
+  const int nvalid = min(TM, a.B - tile * TM);
+  for (int e = threadIdx.x; e < nvalid * S; e += blockDim.x) {
+    const int m = e / S, s = e - m * S;
+    sink(base + e, out[s * LD + m]);
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ size_t tile_elems(const FwdArgs& a, int tile) {
+  return (size_t)min(a.TM, a.B - tile * a.TM) * a.S;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ double red[40];
+  float* bufA = smem;
+  float* bufB = smem + (size_t)a.mlp.maxdim * a.LD;
+  const int G = gridDim.x;
+  const double N = (double)a.S * (double)a.B;
+  const double tdir = a.t1 >= a.t0 ? 1.0 : -1.0;
+  unsigned int gen = 0;
+  int par = 0;
+  bool swp = false;
+  int cur = 0;
+  int ret = GBNDE_RET_SUCCESS;
+  long long nf = 0, naccept = 0, nreject = 0;
+
+  // ---- k1 = f(u0, t0); ubuf[0] = u0 --------------------------------------
+  for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+    load_tile_input(a, tile, bufA, a.t0, [&](size_t g) {
+      const float v = a.u0[g];
+      a.ubuf[0][g] = v;
+      return v;
+    });
+    const float* out = mlp_fwd_tile(a.mlp, bufA, bufB, a.LD, a.TM, nullptr);
+    float* k1 = kb(a, 0, swp);
+    store_tile_output(a, tile, out, [&](size_t g, float v) { k1[g] = v; });
+  }
+  nf = 1;
+
+  int isave = 0;
+  while (isave < a.nsave && a.saveat[isave] == a.t0) {
+    float* dst = a.usave + (size_t)isave * a.S * a.B;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+      const size_t base = (size_t)tile * a.TM * a.S, n = tile_elems(a, tile);
+      for (size_t e = threadIdx.x; e < n; e += blockDim.x) dst[base + e] = a.u0[base + e];
+    }
+    ++isave;
+  }
+
+  // ---- initial step (Hairer's algorithm as the integrator implements it) --
+  double dt;
+  if (a.dt0 > 0.0) {
+    dt = a.dt0;
+  } else {
+    double p0 = 0.0, p1 = 0.0;
+    const float* k1 = kb(a, 0, swp);
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+      const size_t base = (size_t)tile * a.TM * a.S, n = tile_elems(a, tile);
+      for (size_t e = threadIdx.x; e < n; e += blockDim.x) {
+        const float u = a.u0[base + e], f = k1[base + e];
+        const float sk = (float)a.abstol + fabsf(u) * (float)a.reltol;
+        const double x = (double)(u / sk), y = (double)(f / sk);
+        p0 += x * x;
+        p1 += y * y;
+      }
+    }
+    p0 = block_sum_double(p0, red);
+    p1 = block_sum_double(p1, red);
+    double* pp = a.partials + (size_t)par * 2 * G;
+    if (threadIdx.x == 0) {
+      pp[blockIdx.x] = p0;
+      pp[G + blockIdx.x] = p1;
+    }
+    if (!grid_barrier(a.bar, gen, a.status)) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto done; }
+    {
+      const double d0 = sqrt(grid_partials_sum(pp, G, red) / N);
+      const double d1 = sqrt(grid_partials_sum(pp + G, G, red) / N);
+      par ^= 1;
+      const double smalldt = fmax(a.dtmin, 1e-6);
+      double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? smalldt : 0.01 * (d0 / d1);
+      dt0 = fmin(dt0, a.dtmax);
+      const float hf = (float)(tdir * dt0);
+      // f1 = f(u0 + dt0*f0) into the stage-2 buffer (scratch here)
+      float* f1b = kb(a, 1, swp);
+      double p2 = 0.0;
+      for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+        load_tile_input(a, tile, bufA, a.t0 + tdir * dt0,
+                        [&](size_t g) { return a.u0[g] + hf * k1[g]; });
+        const float* out = mlp_fwd_tile(a.mlp, bufA, bufB, a.LD, a.TM, nullptr);
+        store_tile_output(a, tile, out, [&](size_t g, float v) {
+          f1b[g] = v;
+          const float sk = (float)a.abstol + fabsf(a.u0[g]) * (float)a.reltol;
+          const double z = (double)((v - k1[g]) / sk);
+          p2 += z * z;
+        });
+      }
+      nf += 1;
+      p2 = block_sum_double(p2, red);
+      pp = a.partials + (size_t)par * 2 * G;
+      if (threadIdx.x == 0) pp[blockIdx.x] = p2;
+      if (!grid_barrier(a.bar, gen, a.status)) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto done; }
+      const double d2 = sqrt(grid_partials_sum(pp, G, red) / N) / dt0;
+      par ^= 1;
+      const double m = fmax(d1, d2);
+      const double dt1 = (m <= 1e-15) ? fmax(1e-6, dt0 * 1e-3) : pow(10.0, -(2.0 + log10(m)) / 5.0);
+      dt = fmax(a.dtmin, fmin(100.0 * dt0, fmin(dt1, a.dtmax)));
+    }
+  }
+
+  // ---- step loop ------------------------------------------------------------
+  {
+    double t = a.t0, qold = kQoldInit;
+    long long iter = 0;
+    int ib = 0, nck = 0;
+    while (tdir * (a.t1 - t) > 0.0) {
+      if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
+      ++iter;
+      const double rem = fabs(a.t1 - t);
+      const bool clipped = dt >= rem;
+      const double habs = clipped ? rem : dt;
+      const double h = tdir * habs;
+      float* ucur = a.ubuf[cur];
+      float* unew = a.ubuf[cur ^ 1];
+      double perr = 0.0;
+      for (int i = 1; i < 7; ++i) {
+        float ha[6];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) ha[j] = (float)(h * c_tab.a[i][j]);
+        const float* kj[6];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) kj[j] = kb(a, j, swp);
+        float* ki = kb(a, i, swp);
+        float hbt[7];
+#pragma unroll
+        for (int j = 0; j < 7; ++j) hbt[j] = (float)(h * c_tab.btilde[j]);
+        for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+          load_tile_input(a, tile, bufA, t + c_tab.c[i] * h, [&](size_t g) {
+            float s = 0.f;
+            for (int j = 0; j < i; ++j) s = fmaf(ha[j], kj[j][g], s);
+            const float y = ucur[g] + s;
+            if (i == 6) unew[g] = y;
+            return y;
+          });
+          const float* out = mlp_fwd_tile(a.mlp, bufA, bufB, a.LD, a.TM, nullptr);
+          if (i < 6) {
+            store_tile_output(a, tile, out, [&](size_t g, float v) { ki[g] = v; });
+          } else {
+            store_tile_output(a, tile, out, [&](size_t g, float v) {
+              ki[g] = v;
+              float ut = hbt[6] * v;
+#pragma unroll
+              for (int j = 0; j < 6; ++j) ut = fmaf(hbt[j], kj[j][g], ut);
+              const float uo = ucur[g], un = unew[g];
+              const float sc = (float)a.abstol + fmaxf(fabsf(uo), fabsf(un)) * (float)a.reltol;
+              const double r = (double)(ut / sc);
+              perr += isfinite(un) ? r * r : (double)INFINITY;
+            });
+          }
+        }
+      }
+      nf += 6;
+      perr = block_sum_double(perr, red);
+      double* pp = a.partials + (size_t)par * 2 * G;
+      if (threadIdx.x == 0) pp[blockIdx.x] = perr;
+      if (!grid_barrier(a.bar, gen, a.status)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
+      const double eest = sqrt(grid_partials_sum(pp, G, red) / N);
+      par ^= 1;
+      if (!isfinite(eest)) { ret = GBNDE_RET_UNSTABLE; break; }
+      double q11;
+      double q = pi_q(eest, qold, &q11);
+      if (blockIdx.x == 0 && threadIdx.x == 0 && iter - 1 < a.maxsteps) {
+        double* tr = a.trace + 4 * (iter - 1);
+        tr[0] = t;
+        tr[1] = h;
+        tr[2] = eest;
+        tr[3] = eest <= 1.0 ? 1.0 : 0.0;
+      }
+      if (eest <= 1.0) {
+        const double tnew = clipped ? a.t1 : t + h;
+        // saveat points in (t, tnew]
+        while (isave < a.nsave && tdir * (a.saveat[isave] - tnew) <= 0.0) {
+          const double s = a.saveat[isave];
+          float* dst = a.usave + (size_t)isave * a.S * a.B;
+          if (s == tnew) {
+            for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+              const size_t base = (size_t)tile * a.TM * a.S, n = tile_elems(a, tile);
+              for (size_t e = threadIdx.x; e < n; e += blockDim.x) dst[base + e] = unew[base + e];
+            }
+          } else {
+            float bw[7];
+            interp_weights((s - t) / h, bw);
+            float hb[7];
+#pragma unroll
+            for (int j = 0; j < 7; ++j) hb[j] = (float)(h * (double)bw[j]);
+            const float* kk[7];
+#pragma unroll
+            for (int j = 0; j < 7; ++j) kk[j] = kb(a, j, swp);
+            for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+              const size_t base = (size_t)tile * a.TM * a.S, n = tile_elems(a, tile);
+              for (size_t e = threadIdx.x; e < n; e += blockDim.x) {
+                const size_t g = base + e;
+                float acc = 0.f;
+#pragma unroll
+                for (int j = 0; j < 7; ++j) acc = fmaf(hb[j], kk[j][g], acc);
+                dst[g] = ucur[g] + acc;
+              }
+            }
+          }
+          ++isave;
+        }
+        // checkpoint the state at the start of this step if it holds a boundary
+        bool need = false;
+        while (ib < a.nbnd && tdir * (a.bnd[ib] - tnew) < 0.0) { need = true; ++ib; }
+        if (need && nck < a.max_ckpt) {
+          float* dst = a.ckpt + (size_t)nck * a.S * a.B;
+          for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+            const size_t base = (size_t)tile * a.TM * a.S, n = tile_elems(a, tile);
+            for (size_t e = threadIdx.x; e < n; e += blockDim.x) dst[base + e] = ucur[base + e];
+          }
+          if (blockIdx.x == 0 && threadIdx.x == 0) a.ckpt_step[nck] = (int)naccept;
+          ++nck;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0 && naccept < a.maxsteps) {
+          a.steplog[2 * naccept] = t;
+          a.steplog[2 * naccept + 1] = h;
+        }
+        ++naccept;
+        cur ^= 1;
+        swp = !swp;
+        t = tnew;
+        if (q >= 1.0 && q <= 1.0) q = 1.0;
+        qold = fmax(eest, kQoldInit);
+        dt = fmax(fmin(habs / q, a.dtmax), a.dtmin);
+      } else {
+        ++nreject;
+        dt = habs / fmin(1.0 / kQmin, q11 / kGamma);
+        if (a.dtmin > 0.0 && dt <= a.dtmin) { ret = GBNDE_RET_DTLESSTHANMIN; break; }
+      }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.counters[CT_NCKPT] = nck;
+      a.counters[CT_NATTEMPT] = iter;
+      *a.tfinal = t;
+    }
+  }
+
+done:
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.counters[CT_NF] = nf;
+    a.counters[CT_NACCEPT] = naccept;
+    a.counters[CT_NREJECT] = nreject;
+    a.status[ST_RETCODE] = (a.status[ST_BARRIER] != 0) ? GBNDE_RET_BARRIER_TIMEOUT : ret;
+    // which buffer holds the final state: reported through counters slot 5
+    a.counters[5] = cur;
+  }
+}
+
+int max_grid_fwd_f32(size_t smem, int* grid) {
+  cudaError_t e = cudaFuncSetAttribute(fwd_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return -1;
+  int per_sm = 0, dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd_f32_kernel, 256, smem);
+  if (e != cudaSuccess || per_sm < 1) return -1;
+  *grid = per_sm * nsm;
+  return 0;
+}
+
+int launch_fwd_f32(const FwdArgs& a, int grid, size_t smem, cudaStream_t st) {
+  void* args[] = {(void*)&a};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)fwd_f32_kernel, dim3(grid), dim3(256),
+                                              args, smem, st);
+  return e == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace gbnde

@@ -1,0 +1,189 @@
+/*
+ * gbnde.h -- C ABI of the GB300 neural-ODE solver library (libgbnde.so).
+ *
+ * The library replaces, for one GPU (sm_103a), the arithmetic that the
+ * reference reaches through `solve` when a DiffEqFlux layer is called:
+ *
+ *   NeuralODE (x, p, st) -> (sol, st)        src/neural_de.jl:47-61
+ *   FFJORD    (x, ps, st) -> ((logpx,..),st) src/ffjord.jl:138-178
+ *   multiple_shoot(p, data, tsteps, ...)     src/multiple_shooting.jl:36-94
+ *
+ * i.e. OrdinaryDiffEq's Tsit5 + PI controller + saveat interpolation, the
+ * SciMLSensitivity InterpolatingAdjoint / BacksolveAdjoint gradient that the
+ * layers select (src/neural_de.jl:57, src/ffjord.jl:143) and the Lux Dense
+ * chain used as right-hand side. Host code (Julia `ccall`, Python `ctypes`)
+ * keeps the layer constructors and call signatures and calls these entry points.
+ *
+ * Conventions
+ *  - All functions return 0 on success or a negative gbnde_error code; they
+ *    never throw or exit. gbnde_strerror() names the code, gbnde_last_error()
+ *    gives a message for the last failing call on this thread.
+ *  - Arrays are column-major like Julia: a state batch is S x B with one
+ *    trajectory per column (element (s, b) at b*S + s); saved states are
+ *    S x B x nsave. Parameters are the flat vector ComponentArray(ps) gives:
+ *    per Dense layer its weight (out x in, column-major) then its bias.
+ *  - Functions without the _device suffix take HOST pointers and copy
+ *    through pinned staging buffers on the context's stream. The _device
+ *    variants take DEVICE pointers (no copies).
+ *  - A context is not thread-safe; use one per host thread/task. Different
+ *    contexts may run concurrently.
+ *  - Solver outcomes come back in gbnde_stats.retcode (gbnde_retcode), which
+ *    maps onto SciMLBase.ReturnCode; a failed solve is not an API error.
+ */
+#ifndef GBNDE_H
+#define GBNDE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBNDE_MAX_LAYERS 8
+
+typedef struct gbnde_ctx gbnde_ctx;
+
+typedef enum {
+  GBNDE_ACT_IDENTITY = 0,
+  GBNDE_ACT_TANH = 1,
+  GBNDE_ACT_SOFTPLUS = 2
+} gbnde_act;
+
+/* Arithmetic of the MLP right-hand side. FP32: every operation in FP32
+ * (the plain drop-in). BF16: GEMMs on the tensor cores with BF16 operands and
+ * FP32 accumulation; state, stage sums and adjoint quadrature stay FP32;
+ * t, dt and the controller in FP64. */
+typedef enum {
+  GBNDE_PREC_FP32 = 0,
+  GBNDE_PREC_BF16 = 1
+} gbnde_precision;
+
+/* sensealg: InterpolatingAdjoint (default of NeuralODE, src/neural_de.jl:57)
+ * or BacksolveAdjoint (test/BasicNeuralDE/neural_de_tests.jl:36). */
+typedef enum {
+  GBNDE_SENSE_INTERPOLATING = 0,
+  GBNDE_SENSE_BACKSOLVE = 1
+} gbnde_sensealg;
+
+typedef enum {
+  GBNDE_OK = 0,
+  GBNDE_ERR_INVALID = -1,      /* bad argument */
+  GBNDE_ERR_CUDA = -2,         /* CUDA runtime error */
+  GBNDE_ERR_NOMEM = -3,        /* device or pinned allocation failed */
+  GBNDE_ERR_UNSUPPORTED = -4,  /* shape or feature outside this build */
+  GBNDE_ERR_STATE = -5,        /* call order (e.g. backward before forward) */
+  GBNDE_ERR_TIMEOUT = -6       /* a device-side wait gave up (see retcode) */
+} gbnde_error;
+
+/* Solver outcome, SciMLBase.ReturnCode names in comments. */
+typedef enum {
+  GBNDE_RET_SUCCESS = 0,        /* Success */
+  GBNDE_RET_MAXITERS = 1,       /* MaxIters */
+  GBNDE_RET_DTLESSTHANMIN = 2,  /* DtLessThanMin */
+  GBNDE_RET_UNSTABLE = 3,       /* Unstable (non-finite state or error) */
+  GBNDE_RET_BARRIER_TIMEOUT = 4 /* device grid barrier gave up; no result */
+} gbnde_retcode;
+
+/* Chain([x -> x.^3,] Dense(dims[0], dims[1], act[0]), ..., Dense(dims[n-1], dims[n], act[n-1])) */
+typedef struct {
+  int nlayers;
+  int dims[GBNDE_MAX_LAYERS + 1];
+  int act[GBNDE_MAX_LAYERS];
+  int cube_input;  /* 1: the chain starts with the WrappedFunction x -> x.^3 */
+  int time_input;  /* 1: t is appended as an extra input row (FFJORD extension); dims[0] = S + 1 */
+} gbnde_mlp_desc;
+
+/* Keyword surface of solve(prob, Tsit5(); saveat, abstol, reltol, dt, dtmin, maxiters, sensealg) */
+typedef struct {
+  double t0, t1;          /* tspan */
+  double abstol, reltol;
+  double dt0;             /* <= 0: automatic initial step */
+  double dtmin;           /* <= 0: no minimum */
+  long long maxiters;     /* <= 0: 100000 */
+  const double* saveat;   /* host array of nsave times inside [t0, t1], increasing from t0 */
+  int nsave;              /* >= 1 */
+  int sensealg;           /* gbnde_sensealg, used by gbnde_backward */
+  int flags;              /* reserved, 0 */
+} gbnde_solve_desc;
+
+typedef struct {
+  long long nf;           /* RHS evaluations of the forward solve */
+  long long naccept;
+  long long nreject;
+  long long nf_recompute; /* RHS evaluations of the checkpoint recompute (InterpolatingAdjoint) */
+  long long nf_adj;       /* adjoint RHS evaluations (each = forward recompute + VJP) */
+  long long naccept_adj;
+  long long nreject_adj;
+  int retcode;            /* gbnde_retcode of the forward solve */
+  int retcode_adj;        /* gbnde_retcode of the adjoint solve */
+  double t_final;
+} gbnde_stats;
+
+/* ---- context ------------------------------------------------------------ */
+/* Replaces the model/parameter setup that StatefulLuxLayer does per call
+ * (src/neural_de.jl:48). precision: gbnde_precision. device: CUDA ordinal. */
+int gbnde_create(gbnde_ctx** out, const gbnde_mlp_desc* mlp, int precision, int device);
+void gbnde_destroy(gbnde_ctx* ctx);
+size_t gbnde_nparams(const gbnde_ctx* ctx);
+/* p: the flat ComponentArray(ps) vector (src/neural_de.jl:47 `p`). */
+int gbnde_set_params(gbnde_ctx* ctx, const float* p, size_t n);
+int gbnde_set_params_device(gbnde_ctx* ctx, const float* p_dev, size_t n);
+
+/* ---- NeuralODE forward solve ------------------------------------------------
+ * Replaces solve(ODEProblem{false}(dudt, x, tspan, p), Tsit5(); saveat, abstol,
+ * reltol, ...) at src/neural_de.jl:52-58. u0: S x B. usave: S x B x nsave.
+ * Keeps the checkpoints and step log that gbnde_backward needs. */
+int gbnde_forward(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int S, int B,
+                  const float* u0, float* usave, gbnde_stats* stats);
+int gbnde_forward_device(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int S, int B,
+                         const float* u0_dev, float* usave_dev, gbnde_stats* stats);
+
+/* ---- adjoint gradient --------------------------------------------------------
+ * Replaces the pullback of SciMLSensitivity's rrule on solve for
+ * sensealg = InterpolatingAdjoint()/BacksolveAdjoint() (src/neural_de.jl:57).
+ * dL_dusave: S x B x nsave cotangent of the saved states of the last forward.
+ * Outputs dL/du0 (S x B) and dL/dp (nparams). */
+int gbnde_backward(gbnde_ctx* ctx, const float* dL_dusave, float* dL_du0, float* dL_dp,
+                   gbnde_stats* stats);
+int gbnde_backward_device(gbnde_ctx* ctx, const float* dL_dusave_dev, float* dL_du0_dev,
+                          float* dL_dp_dev, gbnde_stats* stats);
+
+/* ---- fused loss at the save points (device pointers) -------------------------
+ * kind 0: sum(abs2, target .- usave) (docs/src/examples/neural_ode.md:41);
+ * kind 1: mean(abs2, ...). Writes dL/dusave and the loss (FP64, host). */
+int gbnde_loss_device(gbnde_ctx* ctx, const float* usave_dev, const float* target_dev,
+                      int kind, float* dL_dusave_dev, double* loss);
+
+/* Accepted steps (t_n, h_n) of the last forward solve; returns the count
+ * (may exceed cap; only cap entries are written). */
+long long gbnde_forward_steps(gbnde_ctx* ctx, double* t, double* h, long long cap);
+
+/* Attempted steps of the last forward solve, 4 doubles each: t_n, h_n, the
+ * error estimate EEst and 1.0 if accepted (the step trace the integrator's
+ * controller acted on). Returns the count (only cap entries are written). */
+long long gbnde_forward_trace(gbnde_ctx* ctx, double* out4, long long cap);
+
+/* The CUDA stream (cudaStream_t) the context launches on, and a way to use
+ * the caller's stream instead (e.g. CUDA.jl's task stream); NULL restores the
+ * context's own stream. No reference counterpart (stream plumbing of the host). */
+void* gbnde_stream(gbnde_ctx* ctx);
+int gbnde_set_stream(gbnde_ctx* ctx, void* stream);
+
+/* Durations (ms, CUDA events on the launching stream) of the last forward and
+ * backward solver kernels. No reference counterpart (instrumentation). */
+int gbnde_last_kernel_ms(gbnde_ctx* ctx, double* fwd_ms, double* bwd_ms);
+
+/* Self-test of the tensor-core building blocks on the current device:
+ * D[128 x N] = A[128 x K] * W[N x K]^T (host arrays, row-major) through bulk
+ * copied SW128 weight images, tcgen05.mma into tensor memory and tcgen05.ld.
+ * mode 0: one BF16 product; mode 1: the five split-BF16 products of the BF16
+ * form. N in {64, 128, 256}, K <= 1024. No reference counterpart (diagnostic). */
+int gbnde_tc_selftest(const float* A, const float* W, int N, int K, int mode, float* D);
+
+const char* gbnde_strerror(int code);
+const char* gbnde_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBNDE_H */

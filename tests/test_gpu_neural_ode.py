@@ -1,0 +1,224 @@
+"""GPU parity of the NeuralODE forward solve and adjoint gradient (FP32 form)
+against the FP64 CPU oracle, through the C ABI.
+
+Mirrors the reference's hot-path tests (test/BasicNeuralDE/neural_de_tests.jl:7-59:
+Chain(Dense(2=>50,tanh), Dense(50=>2)), u0 = [2,0] and a 2x3 batch, default /
+tight tolerances, BacksolveAdjoint, saveat range) but asserts values, not
+only non-zero gradients.
+
+Tolerances (relative, FP32 kernel vs FP64 oracle):
+  * replayed steps (oracle takes the GPU's accepted steps): 2e-5 on saved states
+  * gradients (both adjoints adaptive, FP32 vs FP64 rounding in the controller): 2e-4
+"""
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="no CUDA GPU")]
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _setup(dims, acts, cube, B, seed, bias=0.05):
+    import gbnde
+    rng = np.random.default_rng(seed)
+    layers = [gbnde.cube()] if cube else []
+    layers += [gbnde.Dense(dims[i], dims[i + 1], acts[i]) for i in range(len(acts))]
+    model = gbnde.Chain(*layers)
+    p = model.init_params(rng)
+    off = 0
+    for i in range(len(acts)):
+        off += dims[i] * dims[i + 1]
+        p[off:off + dims[i + 1]] = bias * rng.standard_normal(dims[i + 1])
+        off += dims[i + 1]
+    return model, p, rng
+
+
+def _oracle(model, p):
+    from oracle import mlp as omlp
+    om = omlp.MLP(model.dims, model.acts, cube_input=model.cube_input)
+    return omlp.MLPRHS(om, np.asarray(p, np.float64))
+
+
+def _run_case(model, p, u0, tspan, ts, abstol, reltol, sensealg, precision="fp32"):
+    import gbnde
+    from oracle import tsit5 as ots
+    node = gbnde.NeuralODE(model, tspan, gbnde.Tsit5(precision), saveat=ts, abstol=abstol,
+                           reltol=reltol, sensealg=sensealg)
+    solver = node.solver
+    solver.set_params(p)
+    usave, st = solver.forward(u0, node.desc())
+    assert st.retcode == 0
+    rhs = _oracle(model, p)
+    steps = solver.forward_steps()
+    assert len(steps) == st.naccept
+    # replayed steps: isolates FP32 rounding of the kernel
+    ous, fwd = ots.solve_forward(rhs, u0.astype(np.float64), tspan[0], tspan[1], ts, abstol, reltol,
+                                 steps=steps)
+    # free-running oracle: same controller, FP64 everywhere
+    ous2, fwd2 = ots.solve_forward(_oracle(model, p), u0.astype(np.float64), tspan[0], tspan[1], ts,
+                                   abstol, reltol)
+    rng = np.random.default_rng(7)
+    target = ous + 0.1 * rng.standard_normal(ous.shape)
+    g = 2.0 * (usave.astype(np.float64) - target)
+    du0, dp, sta = solver.backward(g.astype(np.float32))
+    assert sta.retcode_adj == 0
+    if sensealg.code == 0:
+        gu, gp, bint = ots.adjoint_interpolating(rhs, fwd, ts, g, tspan[0], abstol, reltol)
+    else:
+        gu, gp, bint = ots.adjoint_backsolve(rhs, ous, ts, g, tspan[0], abstol, reltol)
+    return dict(usave=usave, ous=ous, ous2=ous2, st=st, fwd2=fwd2, du0=du0, dp=dp, gu=gu, gp=gp,
+                sta=sta, bint=bint)
+
+
+def test_spiral_config_forward_and_gradient():
+    """cube -> Dense(2,50,tanh) -> Dense(50,2), u0=[2,0], tspan (0,1.5), 30 saveat,
+    abstol 1e-7 / reltol 1e-5 (docs/src/examples/neural_ode.md:19-36)."""
+    import gbnde
+    model, p, _ = _setup([2, 50, 2], ["tanh", "identity"], True, 1, 0)
+    u0 = np.array([[2.0], [0.0]], np.float32)
+    ts = np.linspace(0.0, 1.5, 30)
+    r = _run_case(model, p, u0, (0.0, 1.5), ts, 1e-7, 1e-5, gbnde.InterpolatingAdjoint())
+    assert _rel(r["usave"], r["ous"]) < 2e-5
+    # free-running FP64 oracle: at abstol 1e-7 the FP32 rounding floor of the
+    # embedded error estimate makes the FP32 controller take smaller steps, so
+    # only the solution (not the step count) is compared here
+    assert _rel(r["usave"], r["ous2"]) < 1e-4
+    assert _rel(r["du0"], r["gu"]) < 2e-4
+    assert _rel(r["dp"], r["gp"]) < 2e-4
+
+
+@pytest.mark.parametrize("B", [1, 50])
+@pytest.mark.parametrize("tol", [1e-4, 1e-7])
+def test_controller_replays_trace(B, tol):
+    """The PI controller, the initial step and the clipping to t1 act exactly as
+    restated in the oracle, given the error estimates the kernel measured: the
+    kernel's trace of attempted steps (t, h, EEst, accepted) is replayed through
+    the controller formula and every next step size must agree to 1e-12.
+    (The estimates themselves are compared only through the solution: at these
+    tolerances the FP32 rounding floor of EEst differs from the FP64 value.)"""
+    import gbnde
+    from oracle import tableau as T
+    model, p, rng = _setup([2, 50, 2], ["tanh", "identity"], True, B, 0)
+    u0 = (rng.standard_normal((2, B)) + np.array([[2.0], [0.0]])).astype(np.float32)
+    ts = np.linspace(0.0, 1.5, 30)
+    node = gbnde.NeuralODE(model, (0.0, 1.5), gbnde.Tsit5(), saveat=ts, abstol=tol, reltol=tol)
+    s = node.solver
+    s.set_params(p)
+    us, st = s.forward(u0, node.desc())
+    tr = s.forward_trace()
+    assert len(tr) == st.naccept + st.nreject
+    assert st.nf == 2 + 6 * len(tr)
+    t1, qold = 1.5, T.QOLDINIT
+    for i in range(len(tr) - 1):
+        t, h, e, acc = tr[i]
+        tn, hn = tr[i + 1][:2]
+        if e == 0.0:
+            q, q11 = 1.0 / T.QMAX, 0.0
+        else:
+            q11 = e ** T.BETA1
+            q = max(1.0 / T.QMAX, min(1.0 / T.QMIN, q11 / qold ** T.BETA2 / T.GAMMA))
+        if acc:
+            assert tn == (t1 if t + h >= t1 else t + h) or abs(tn - (t + h)) <= 1e-15
+            if T.QSTEADY_MIN <= q <= T.QSTEADY_MAX:
+                q = 1.0
+            qold = max(e, T.QOLDINIT)
+            dt = min(abs(h) / q, 1.5)
+        else:
+            assert tn == t
+            dt = abs(h) / min(1.0 / T.QMIN, q11 / T.GAMMA)
+        assert abs(hn - min(dt, t1 - tn)) <= 1e-12 * hn
+    assert tr[-1][3] and tr[-1][0] + tr[-1][1] >= 1.5 - 1e-12
+
+
+@pytest.mark.parametrize("sense", ["interpolating", "backsolve"])
+@pytest.mark.parametrize("B", [3, 100, 257])
+def test_batched_tanh_mlp(sense, B):
+    """2-hidden-layer tanh MLP, ragged batch sizes (not multiples of the tile)."""
+    import gbnde
+    S, H = 16, 64
+    model, p, rng = _setup([S, H, H, S], ["tanh", "tanh", "identity"], False, B, 1)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    ts = np.linspace(0.0, 1.0, 11)
+    sa = gbnde.InterpolatingAdjoint() if sense == "interpolating" else gbnde.BacksolveAdjoint()
+    r = _run_case(model, p, u0, (0.0, 1.0), ts, 1e-6, 1e-4, sa)
+    assert _rel(r["usave"], r["ous"]) < 2e-5
+    assert _rel(r["du0"], r["gu"]) < 5e-4
+    assert _rel(r["dp"], r["gp"]) < 5e-4
+
+
+def test_config2_shape_small_batch():
+    """State 64, MLP 64->256->256->64 tanh, 20 saveat on (0,1), abstol 1e-7 reltol 1e-5
+    (the batched headline configuration at a batch the FP64 oracle finishes quickly)."""
+    import gbnde
+    S, H, B = 64, 256, 192
+    model, p, rng = _setup([S, H, H, S], ["tanh", "tanh", "identity"], False, B, 2, bias=0.0)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    ts = np.linspace(0.0, 1.0, 20)
+    r = _run_case(model, p, u0, (0.0, 1.0), ts, 1e-7, 1e-5, gbnde.InterpolatingAdjoint())
+    assert _rel(r["usave"], r["ous"]) < 2e-5
+    assert _rel(r["du0"], r["gu"]) < 2e-4
+    assert _rel(r["dp"], r["gp"]) < 2e-4
+
+
+def test_deterministic_bitwise():
+    import gbnde
+    S, H, B = 16, 64, 300
+    model, p, rng = _setup([S, H, H, S], ["tanh", "tanh", "identity"], False, B, 3)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    node = gbnde.NeuralODE(model, (0.0, 1.0), gbnde.Tsit5("fp32"), saveat=np.linspace(0, 1, 5),
+                           abstol=1e-6, reltol=1e-4)
+    s = node.solver
+    s.set_params(p)
+    a, _ = s.forward(u0, node.desc())
+    g = np.ones_like(a)
+    da, pa, _ = s.backward(g)
+    b, _ = s.forward(u0, node.desc())
+    db, pb, _ = s.backward(g)
+    assert np.array_equal(a, b) and np.array_equal(da, db) and np.array_equal(pa, pb)
+
+
+def test_retcodes_maxiters_and_unstable():
+    import gbnde
+    S, H, B = 4, 16, 8
+    model, p, rng = _setup([S, H, S], ["tanh", "identity"], False, B, 4)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    node = gbnde.NeuralODE(model, (0.0, 1.0), gbnde.Tsit5(), saveat=[0.0, 1.0], abstol=1e-9,
+                           reltol=1e-9, maxiters=3)
+    s = node.solver
+    s.set_params(p)
+    _, st = s.forward(u0, node.desc())
+    assert st.retcode == 1  # MaxIters
+    u0[0, 0] = np.nan
+    node2 = gbnde.NeuralODE(model, (0.0, 1.0), gbnde.Tsit5(), saveat=[0.0, 1.0])
+    s2 = node2.solver
+    s2.set_params(p)
+    _, st2 = s2.forward(u0, node2.desc())
+    assert st2.retcode == 3  # Unstable
+    with pytest.raises(gbnde.GbndeError):
+        s2.backward(np.ones((S, B, 2), np.float32))
+
+
+def test_torch_autograd_bridge():
+    import torch
+
+    import gbnde
+    S, H, B = 8, 32, 64
+    model, p, rng = _setup([S, H, S], ["tanh", "identity"], False, B, 5)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    node = gbnde.NeuralODE(model, (0.0, 1.0), gbnde.Tsit5(), saveat=np.linspace(0, 1, 4),
+                           abstol=1e-6, reltol=1e-4)
+    x = torch.tensor(u0, device="cuda", requires_grad=True)
+    pt = torch.tensor(p, device="cuda", requires_grad=True)
+    sol, _ = node(x, pt, {})
+    loss = (sol.array() ** 2).sum()
+    loss.backward()
+    s = node.solver
+    s.set_params(p)
+    us, _ = s.forward(u0, node.desc())
+    du0, dp, _ = s.backward(2.0 * us)
+    assert np.allclose(x.grad.cpu().numpy(), du0, rtol=1e-5, atol=1e-6)
+    assert np.allclose(pt.grad.cpu().numpy(), dp, rtol=1e-5, atol=1e-6)

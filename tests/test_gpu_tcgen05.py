@@ -1,0 +1,43 @@
+"""Tensor-core building blocks (tcgen05.mma, TMEM, bulk-copied SW128 weight
+images, split-BF16 products) against an FP64 matrix product."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="no CUDA GPU")]
+
+
+def _bf16(x):
+    x32 = np.asarray(x, np.float32)
+    b = x32.view(np.uint32).astype(np.uint64)
+    r = ((b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
+    return r.view(np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize("N,K", [(256, 64), (256, 256), (64, 256), (128, 100)])
+def test_tc_gemm_single_and_split(lib, N, K):
+    rng = np.random.default_rng(N + K)
+    A = rng.standard_normal((128, K)).astype(np.float32)
+    W = (rng.standard_normal((N, K)) / np.sqrt(K)).astype(np.float32)
+    fp = C.POINTER(C.c_float)
+    D0 = np.zeros((128, N), np.float32)
+    D1 = np.zeros((128, N), np.float32)
+    rc0 = lib.gbnde_tc_selftest(A.ctypes.data_as(fp), W.ctypes.data_as(fp), N, K, 0, D0.ctypes.data_as(fp))
+    rc1 = lib.gbnde_tc_selftest(A.ctypes.data_as(fp), W.ctypes.data_as(fp), N, K, 1, D1.ctypes.data_as(fp))
+    assert rc0 == 0 and rc1 == 0
+    ref_bf16 = _bf16(A) @ _bf16(W).T
+    ref = A.astype(np.float64) @ W.astype(np.float64).T
+    scale = np.abs(ref).max()
+    # one product: exact bf16 operands, FP32 accumulation
+    assert np.abs(D0 - ref_bf16).max() / scale < 1e-5
+    # five split products, emulated exactly (pieces are exact bf16 values):
+    # W = Wh + Wl, A = Ah + Am + Al; products Wh.Ah + Wh.Am + Wl.Ah + Wh.Al + Wl.Am
+    Wh = _bf16(W); Wl = _bf16(W - Wh)
+    Ah = _bf16(A); Am = _bf16(A - Ah); Al = _bf16(A - Ah - Am)
+    emul = Ah @ Wh.T + Am @ Wh.T + Ah @ Wl.T + Al @ Wh.T + Am @ Wl.T
+    assert np.abs(D1 - emul).max() / scale < 1e-6
+    # and within the 16-bit weight truncation of the FP64 product
+    assert np.abs(D1 - ref).max() / scale < 2e-5
