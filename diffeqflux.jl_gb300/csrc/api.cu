@@ -16,8 +16,18 @@
 
 #include "gbnde.h"
 #include "kernels.h"
+#include "tc_engine.cuh"
 
 namespace gbnde {
+struct FwdTcArgs {
+  FwdArgs f;
+  tc::OpList ops;
+  const float* bias[GBNDE_MAX_LAYERS];
+  float* comp[2];
+  float* dense;
+  long long dense_slots;
+  float* kring;
+};
 int launch_reduce_mu(const float* mu_acc, int nblk, int P, float* out, cudaStream_t st);
 int launch_transpose_params(const MlpDev& m, const float* p, float* wtr, cudaStream_t st);
 int launch_loss(const float* usave, const float* target, size_t n, int kind, float* dL,
@@ -105,6 +115,15 @@ struct gbnde_ctx {
   int fwd_retcode = 0;
   const float* usave_dev = nullptr;  // saved states of the last forward (device)
   cudaStream_t own_stream = nullptr;
+  // tensor-core form: split-BF16 weight images per layer
+  DBuf wimg;
+  size_t wimg_off[GBNDE_MAX_LAYERS] = {};
+  int npad[GBNDE_MAX_LAYERS] = {}, nchunk[GBNDE_MAX_LAYERS] = {};
+  bool tc_shape_ok = false;
+  // dense stage storage of the last forward
+  DBuf comp, dense;
+  long long dense_slots = 0;
+  bool dense_valid = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double fwd_ms = 0.0, bwd_ms = 0.0;
 };
@@ -208,6 +227,14 @@ int gbnde_create(gbnde_ctx** out, const gbnde_mlp_desc* mlp, int precision, int 
     off += (size_t)mlp->dims[l + 1];
   }
   c->P = off;
+  // shapes the tensor-core engine covers: state <= 64, hidden widths <= 256
+  c->tc_shape_ok = !mlp->time_input && S <= 64 && mlp->dims[0] <= 64;
+  for (int l = 1; l < mlp->nlayers; ++l) c->tc_shape_ok = c->tc_shape_ok && mlp->dims[l] <= 256;
+  if (precision == GBNDE_PREC_BF16 && !c->tc_shape_ok) {
+    gbnde_destroy(c);
+    return fail(GBNDE_ERR_UNSUPPORTED,
+                "BF16 form supports state dim <= 64 and hidden widths <= 256 (no time input)");
+  }
   *out = c;
   return 0;
 }
@@ -219,7 +246,7 @@ void gbnde_destroy(gbnde_ctx* c) {
                   &c->ckpt_step, &c->steplog, &c->trace, &c->partials, &c->sync, &c->counters, &c->saveat_d,
                   &c->bnd_d, &c->dldu, &c->dldu0, &c->dldp, &c->lam, &c->ub, &c->kl, &c->ku,
                   &c->ibuf, &c->mu_acc, &c->mu_stage, &c->iv_d, &c->bsync, &c->bcounters,
-                  &c->loss_part};
+                  &c->loss_part, &c->wimg, &c->comp, &c->dense};
   for (DBuf* b : bufs) b->release();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -241,6 +268,12 @@ static int bind_params(gbnde_ctx* c) {
   }
   if (launch_transpose_params(m, p, c->wtr.as<float>(), c->stream))
     return fail(GBNDE_ERR_CUDA, "transpose kernel launch failed");
+  if (c->precision == GBNDE_PREC_BF16 && c->tc_shape_ok) {
+    for (int l = 0; l < m.nlayers; ++l)
+      if (launch_prep_weight_image(m.W[l], m.dims[l + 1], m.dims[l], c->npad[l],
+                                   c->wimg.as<uint8_t>() + c->wimg_off[l], c->stream))
+        return fail(GBNDE_ERR_CUDA, "weight image kernel launch failed");
+  }
   c->have_params = true;
   return 0;
 }
@@ -248,6 +281,16 @@ static int bind_params(gbnde_ctx* c) {
 static int alloc_params(gbnde_ctx* c) {
   if (int r = c->params.ensure(c->P * sizeof(float))) return r;
   if (int r = c->wtr.ensure(c->P * sizeof(float))) return r;
+  if (c->precision == GBNDE_PREC_BF16 && c->tc_shape_ok) {
+    size_t off = 0;
+    for (int l = 0; l < c->mlp.nlayers; ++l) {
+      c->npad[l] = (c->mlp.dims[l + 1] + 15) / 16 * 16;
+      c->nchunk[l] = (c->mlp.dims[l] + 63) / 64;
+      c->wimg_off[l] = off;
+      off += (size_t)c->nchunk[l] * 2 * c->npad[l] * 128;
+    }
+    if (int r = c->wimg.ensure(off)) return r;
+  }
   return 0;
 }
 
@@ -310,12 +353,40 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   if (choose_tm(2 * c->mlp.maxdim, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "layer too wide");
   const int LD = TM + 4;
   const size_t smem = (size_t)2 * c->mlp.maxdim * LD * sizeof(float);
-  const int ntiles = (B + TM - 1) / TM;
+  const bool tcform = c->precision == GBNDE_PREC_BF16;
+  const int ntiles = tcform ? (B + 127) / 128 : (B + TM - 1) / TM;
   int gmax = 0;
-  if (max_grid_fwd_f32(smem, &gmax)) return fail(GBNDE_ERR_CUDA, "occupancy query failed");
+  if (tcform) {
+    if (max_grid_fwd_tc(&gmax)) return fail(GBNDE_ERR_CUDA, "occupancy query failed (tc)");
+  } else if (max_grid_fwd_f32(smem, &gmax)) {
+    return fail(GBNDE_ERR_CUDA, "occupancy query failed");
+  }
   const int grid = std::min(gmax, ntiles);
 
   int r = 0;
+  // dense stage storage: one slot (u_n, k1..k7) per accepted step, within a
+  // quarter of the free device memory
+  {
+    size_t freeb = 0, totb = 0;
+    cudaMemGetInfo(&freeb, &totb);
+    const size_t slot = 8 * SB * sizeof(float);
+    long long want = std::min<long long>(maxiters + 1, 4096);
+    const long long have_now = (long long)(c->dense.n / slot);
+    const long long budget = (long long)((freeb / 4) / slot) + have_now;
+    long long ns = std::min(want, budget);
+    if (ns < 2) ns = 0;
+    if (ns > have_now && have_now < std::min<long long>(want, 64)) {
+      // grow to the smaller of what is wanted and a first chunk of 64 steps,
+      // then on later calls by doubling
+      ns = std::min(ns, std::max<long long>(64, 2 * have_now));
+    }
+    if (ns > 0 && (r = c->dense.ensure((size_t)ns * slot))) {
+      cudaGetLastError();
+      ns = 0;
+    }
+    c->dense_slots = ns > 0 ? (long long)(c->dense.n / slot) : 0;
+  }
+  if (tcform && (r = c->comp.ensure(2 * SB * 4))) return r;
   if (u0_host && (r = c->u0.ensure(SB * 4))) return r;
   if ((r = c->ubuf.ensure(2 * SB * 4)) || (r = c->kbuf.ensure(7 * SB * 4))) return r;
   if (usave_host && (r = c->usave.ensure(SB * nsave * 4))) return r;
@@ -374,8 +445,31 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   a.status = reinterpret_cast<int*>(c->sync.as<char>() + 16);
   a.counters = c->counters.as<long long>();
   a.tfinal = reinterpret_cast<double*>(c->counters.as<char>() + CT_NSLOTS * sizeof(long long));
+  a.dense = c->dense_slots > 0 ? c->dense.as<float>() : nullptr;
+  a.dense_slots = c->dense_slots;
   CK(cudaEventRecord(c->ev[0], st));
-  if (launch_fwd_f32(a, grid, smem, st)) {
+  if (tcform) {
+    FwdTcArgs ta{};
+    ta.f = a;
+    ta.f.ntiles = ntiles;
+    ta.f.TM = 128;
+    ta.ops.nops = c->mlp.nlayers;
+    for (int l = 0; l < c->mlp.nlayers; ++l) {
+      ta.ops.op[l].wimg = c->wimg.as<uint8_t>() + c->wimg_off[l];
+      ta.ops.op[l].npad = c->npad[l];
+      ta.ops.op[l].nchunk = c->nchunk[l];
+      ta.bias[l] = c->mlp.bias[l];
+    }
+    ta.comp[0] = c->comp.as<float>();
+    ta.comp[1] = c->comp.as<float>() + SB;
+    ta.dense = a.dense;
+    ta.dense_slots = a.dense_slots;
+    ta.kring = c->kbuf.as<float>();
+    if (launch_fwd_tc(ta, grid, st)) {
+      cudaError_t e = cudaGetLastError();
+      return fail(GBNDE_ERR_CUDA, "forward (tc) launch failed: %s", cudaGetErrorString(e));
+    }
+  } else if (launch_fwd_f32(a, grid, smem, st)) {
     cudaError_t e = cudaGetLastError();
     return fail(GBNDE_ERR_CUDA, "forward launch failed: %s", cudaGetErrorString(e));
   }
@@ -424,6 +518,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   c->sensealg = d->sensealg;
   c->saveat.assign(d->saveat, d->saveat + nsave);
   c->have_fwd = (status[ST_RETCODE] == GBNDE_RET_SUCCESS) && nacc <= maxsteps;
+  c->dense_valid = c->dense_slots > 0 && nacc < c->dense_slots;
   c->usave_dev = usd;
   return 0;
 }
@@ -510,7 +605,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   if (out_host && ((r = c->dldu0.ensure(SB * 4)) || (r = c->dldp.ensure((size_t)P * 4)))) return r;
   if ((r = c->lam.ensure(2 * SB * 4)) || (r = c->kl.ensure(7 * SB * 4))) return r;
   if (backsolve && ((r = c->ub.ensure(2 * SB * 4)) || (r = c->ku.ensure(7 * SB * 4)))) return r;
-  if (!backsolve && (r = c->ibuf.ensure((size_t)max_slots * 8 * SB * 4))) return r;
+  if (!backsolve && !c->dense_valid && (r = c->ibuf.ensure((size_t)max_slots * 8 * SB * 4))) return r;
   if ((r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4))) return r;
   if ((r = c->iv_d.ensure(std::max<size_t>(1, ivs.size()) * sizeof(Interval)))) return r;
   if ((r = c->bsync.ensure(64)) || (r = c->bcounters.ensure(CT_NSLOTS * sizeof(long long)))) return r;
@@ -556,6 +651,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   a.nsave_last = nsave_last;
   a.ibuf = c->ibuf.as<float>();
   a.ibuf_slots = max_slots;
+  a.dense = (c->dense_valid && !backsolve) ? c->dense.as<float>() : nullptr;
   a.lam[0] = c->lam.as<float>();
   a.lam[1] = c->lam.as<float>() + SB;
   a.ub[0] = backsolve ? c->ub.as<float>() : nullptr;

@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
   for (int ivi = 0; ivi < a.niv && ret == GBNDE_RET_SUCCESS; ++ivi) {
     const Interval iv = a.iv[ivi];
     // ---- recompute the interval's forward steps (InterpolatingAdjoint) ----
-    if (!backsolve) {
+    if (!backsolve && !a.dense) {
       const size_t SB = (size_t)S * a.B;
       const int nst = iv.nhi - iv.nlo + 1;
       for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       float bw[7];
       interp_weights((tt - tn) / h, bw);
       const size_t SB = (size_t)S * a.B;
-      const float* slot = a.ibuf + (size_t)(n - iv.nlo) * 8 * SB;
+      const float* slot = a.dense ? a.dense + (size_t)n * 8 * SB : a.ibuf + (size_t)(n - iv.nlo) * 8 * SB;
       un = slot;
       for (int q = 0; q < 7; ++q) {
         hb[q] = (float)(h * (double)bw[q]);

@@ -19,11 +19,18 @@ namespace gbnde {
 
 namespace {
 
-__device__ __forceinline__ float* kb(const FwdArgs& a, int j, bool swp) {
+// Stage buffer j of the current attempt. Dense mode: slot of accepted step
+// `n` (k1..k7 at positions 1..7); otherwise a ring of 7 with the FSAL swap.
+__device__ __forceinline__ float* kbuf_at(const FwdArgs& a, int j, bool swp, long long n) {
+  if (a.dense) {
+    const size_t SB = (size_t)a.S * a.B;
+    return a.dense + ((size_t)min(n, a.dense_slots - 1) * 8 + 1 + j) * SB;
+  }
   if (j == 0) return swp ? a.kbuf[6] : a.kbuf[0];
   if (j == 6) return swp ? a.kbuf[0] : a.kbuf[6];
   return a.kbuf[j];
 }
+#define kb(a, j, swp) kbuf_at(a, j, swp, naccept)
 
 // Load the MLP input of a tile (feature-major) from a per-element producer.
 template <class Fn>
@@ -85,6 +92,7 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
     load_tile_input(a, tile, bufA, a.t0, [&](size_t g) {
       const float v = a.u0[g];
       a.ubuf[0][g] = v;
+      if (a.dense) a.dense[g] = v;
       return v;
     });
     const float* out = mlp_fwd_tile(a.mlp, bufA, bufB, a.LD, a.TM, nullptr);
@@ -281,8 +289,22 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
           a.steplog[2 * naccept + 1] = h;
         }
         ++naccept;
+        if (a.dense) {
+          const float* k7 = kbuf_at(a, 6, swp, naccept - 1);
+          float* k1n = kbuf_at(a, 0, swp, naccept);
+          const bool slot_ok = naccept < a.dense_slots;
+          float* un = a.dense + (size_t)naccept * 8 * a.S * a.B;
+          for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+            const size_t base = (size_t)tile * a.TM * a.S, n = tile_elems(a, tile);
+            for (size_t e = threadIdx.x; e < n; e += blockDim.x) {
+              k1n[base + e] = k7[base + e];
+              if (slot_ok) un[base + e] = unew[base + e];
+            }
+          }
+        } else {
+          swp = !swp;
+        }
         cur ^= 1;
-        swp = !swp;
         t = tnew;
         if (q >= 1.0 && q <= 1.0) q = 1.0;
         qold = fmax(eest, kQoldInit);

@@ -38,6 +38,8 @@ struct FwdArgs {
   double* steplog;       // 2*maxsteps: (t_n, h_n)
   long long maxsteps;
   double* trace;         // 4*maxsteps: (t, h, EEst, accepted) per attempt
+  float* dense;          // per accepted step n: slot of 8 x S*B floats (u_n, k1..k7), or null
+  long long dense_slots;
   double* partials;      // 2*2*grid
   unsigned int* bar;
   int* status;
@@ -76,6 +78,7 @@ struct BwdArgs {
   int nsave_last;
   float* ibuf;            // interval recompute buffer: slot j = (u_n, k1..k7)
   int ibuf_slots;
+  const float* dense;     // forward dense slots (slot n = step n); when set, no recompute
   float* lam[2];          // adjoint state ping-pong
   float* ub[2];           // Backsolve: co-integrated u ping-pong
   float* kl[7];           // adjoint stage buffers (lambda part)
@@ -91,6 +94,10 @@ struct BwdArgs {
 };
 
 int launch_fwd_f32(const FwdArgs& a, int grid, size_t smem, cudaStream_t st);
+struct FwdTcArgs;
+int launch_fwd_tc(const FwdTcArgs& a, int grid, cudaStream_t st);
+int max_grid_fwd_tc(int* grid);
+int launch_prep_weight_image(const float* W, int N, int K, int Npad, uint8_t* img, cudaStream_t st);
 int max_grid_fwd_f32(size_t smem, int* grid);
 int launch_bwd_f32(const BwdArgs& a, int grid, size_t smem, cudaStream_t st);
 int max_grid_bwd_f32(size_t smem, int* grid);

@@ -1,0 +1,253 @@
+// tc_engine.cuh -- the tensor-core MLP engine shared by the BF16-form solver
+// kernels.
+//
+// A CTA evaluates GEMM "ops" on a tile of 128 trajectories. An op is
+//   D[128 x N] (tensor memory, FP32) = sum over K chunks of the five split
+//   products  A_hi W_hi + A_mid W_hi + A_hi W_lo + A_lo W_hi + A_mid W_lo
+// where A chunks (128 rows x 64 columns, 3 bf16 pieces) are written into a
+// shared-memory ring by the epilogue warps and W chunks (N rows x 64, 2 bf16
+// pieces, pre-swizzled image in global memory) are streamed by a producer
+// warp with bulk copies. Ops alternate between two 256-column accumulator
+// regions so that the epilogue can drain one while the next op accumulates.
+//
+// Warp roles (320 threads): warps 0-7 epilogue (EPI), warp 8 MMA issuer,
+// warp 9 weight producer. The MMA and producer warps run the op list
+// cyclically until the epilogue raises the stop flag.
+#pragma once
+#include "kernels.h"
+#include "tc_ptx.cuh"
+
+namespace gbnde {
+namespace tc {
+
+constexpr int kEpiThreads = 256;
+constexpr int kThreads = 320;
+constexpr int kMmaWarp = 8;
+constexpr int kTmaWarp = 9;
+constexpr int kASlotBytes = 3 * 16384;   // 3 pieces x 128 rows x 128 B
+constexpr int kWSlotBytes = 2 * 32768;   // 2 pieces x 256 rows x 128 B
+constexpr int kARing = 2;
+constexpr int kWRing = 2;
+constexpr int kSmemBytes = 1024 + kARing * kASlotBytes + kWRing * kWSlotBytes;
+constexpr int kMaxOps = 8;
+
+struct GemmOp {
+  const uint8_t* wimg;  // weight image: nchunk x 2 pieces x npad rows x 128 B
+  int npad;             // N rounded up to 16 (<= 256)
+  int nchunk;           // K / 64 (rounded up)
+};
+
+struct OpList {
+  GemmOp op[kMaxOps];
+  int nops;
+};
+
+struct Shared {
+  uint64_t a_full[kARing], a_empty[kARing];
+  uint64_t w_full[kWRing], w_empty[kWRing];
+  uint64_t acc_full[2], acc_empty[2];
+  uint32_t tmem_base;
+  int stop;
+  int err;
+  double red[16];
+};
+
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// Deterministic sum of a double over the 256 epilogue threads.
+__device__ __forceinline__ double epi_sum(double v, Shared& sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5;
+  epi_bar();
+  if ((threadIdx.x & 31) == 0) sh.red[w] = v;
+  epi_bar();
+  double s = 0.0;
+  for (int i = 0; i < 8; ++i) s += sh.red[i];
+  epi_bar();
+  return s;
+}
+
+__device__ __forceinline__ void init_shared(Shared& sh) {
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kARing; ++i) {
+      mbar_init(&sh.a_full[i], kEpiThreads);
+      mbar_init(&sh.a_empty[i], 1);
+    }
+    for (int i = 0; i < kWRing; ++i) {
+      mbar_init(&sh.w_full[i], 1);
+      mbar_init(&sh.w_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&sh.acc_full[i], 1);
+      mbar_init(&sh.acc_empty[i], kEpiThreads);
+    }
+    sh.stop = 0;
+    sh.err = 0;
+    fence_mbar_init();
+  }
+}
+
+// ---- MMA warp ------------------------------------------------------------------------
+// Executes the op list cyclically. Returns when the stop flag is raised (or on
+// a wait timeout, which also raises sh.err).
+__device__ __forceinline__ void mma_loop(const OpList& ops, Shared& sh, uint8_t* aring,
+                                         uint8_t* wring) {
+  volatile int* verr = &sh.err;
+  volatile int* vstop = &sh.stop;
+  const bool leader = (threadIdx.x & 31) == 0;
+  int aslot = 0, wslot = 0;
+  uint32_t aph = 0, wph = 0;
+  uint32_t use[2] = {0, 0};
+  long long g = 0;
+  const int pa[5] = {0, 1, 0, 2, 1};
+  const int pb[5] = {0, 0, 1, 0, 1};
+  while (true) {
+    const GemmOp& op = ops.op[g % ops.nops];
+    const int reg = (int)(g & 1);
+    // accumulator region free?
+    {
+      const uint32_t par = (use[reg] & 1) ^ 1;
+      while (!mbar_try_wait(&sh.acc_empty[reg], par)) {
+        if (*vstop || *verr) return;
+      }
+    }
+    const uint32_t d = sh.tmem_base + (uint32_t)(reg * 256);
+    const uint32_t idesc = idesc_bf16(128, op.npad);
+    const uint32_t wpiece = (uint32_t)op.npad * 128;
+    for (int c = 0; c < op.nchunk; ++c) {
+      // A chunk ready? (bounded by the stop flag: the epilogue may be done)
+      {
+        unsigned long long t0 = 0;
+        while (!mbar_try_wait(&sh.a_full[aslot], aph)) {
+          if (*vstop || *verr) return;
+          if (t0 == 0) t0 = globaltimer_ns();
+          else if (globaltimer_ns() - t0 > 4 * kWaitTimeoutNs) { *verr = 2; return; }
+        }
+      }
+      if (!mbar_wait(&sh.w_full[wslot], wph, verr)) return;
+      tc_fence_after();
+      if (leader) {
+        const uint32_t a0 = smem_u32(aring + aslot * kASlotBytes);
+        const uint32_t b0 = smem_u32(wring + wslot * kWSlotBytes);
+#pragma unroll
+        for (int pr = 0; pr < 5; ++pr) {
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint64_t ad = sdesc_sw128(a0 + pa[pr] * 16384 + kk * 32);
+            const uint64_t bd = sdesc_sw128(b0 + pb[pr] * wpiece + kk * 32);
+            mma_bf16(d, ad, bd, idesc, (c > 0 || pr > 0 || kk > 0) ? 1u : 0u);
+          }
+        }
+        mma_commit(&sh.a_empty[aslot]);
+        mma_commit(&sh.w_empty[wslot]);
+        if (c == op.nchunk - 1) mma_commit(&sh.acc_full[reg]);
+      }
+      __syncwarp();
+      if (++aslot == kARing) { aslot = 0; aph ^= 1; }
+      if (++wslot == kWRing) { wslot = 0; wph ^= 1; }
+    }
+    use[reg] += 1;
+    ++g;
+  }
+}
+
+// ---- weight producer warp -------------------------------------------------------------
+__device__ __forceinline__ void tma_loop(const OpList& ops, Shared& sh, uint8_t* wring) {
+  volatile int* verr = &sh.err;
+  volatile int* vstop = &sh.stop;
+  const bool leader = (threadIdx.x & 31) == 0;
+  int wslot = 0;
+  uint32_t wph = 0;
+  long long g = 0;
+  uint32_t issued[kWRing] = {0, 0};  // copies issued per slot
+  while (!*vstop && !*verr) {
+    const GemmOp& op = ops.op[g % ops.nops];
+    const uint32_t bytes = 2u * (uint32_t)op.npad * 128u;
+    for (int c = 0; c < op.nchunk; ++c) {
+      // wait for the slot to be consumed (phase parity of its previous use)
+      const uint32_t par = wph ^ 1;
+      bool go = false;
+      while (true) {
+        if (mbar_try_wait(&sh.w_empty[wslot], par)) { go = true; break; }
+        if (*vstop || *verr) break;
+      }
+      if (!go) break;
+      if (leader) {
+        mbar_arrive_expect_tx(&sh.w_full[wslot], bytes);
+        bulk_g2s(wring + wslot * kWSlotBytes, op.wimg + (size_t)c * bytes, bytes, &sh.w_full[wslot]);
+      }
+      __syncwarp();
+      issued[wslot] += 1;
+      if (++wslot == kWRing) { wslot = 0; wph ^= 1; }
+    }
+    ++g;
+  }
+  // drain: every issued copy must have landed before the CTA exits
+  for (int s = 0; s < kWRing; ++s) {
+    if (issued[s] == 0) continue;
+    const uint32_t last_par = (issued[s] - 1) & 1;
+    const unsigned long long t0 = globaltimer_ns();
+    while (!mbar_try_wait(&sh.w_full[s], last_par)) {
+      if (globaltimer_ns() - t0 > kWaitTimeoutNs) { *verr = 3; break; }
+    }
+  }
+}
+
+// ---- epilogue helpers --------------------------------------------------------------------
+struct EpiState {
+  int aslot;
+  uint32_t aph;
+  uint32_t use[2];
+  long long g;  // ops consumed
+};
+
+__device__ __forceinline__ void epi_state_init(EpiState& e) {
+  e.aslot = 0;
+  e.aph = 0;
+  e.use[0] = e.use[1] = 0;
+  e.g = 0;
+}
+
+// Write this thread's 32 columns (its row r, column half ch) of an A chunk:
+// values x[0..31] for columns [32*ch, 32*ch+32) of the chunk, split in 3 pieces.
+__device__ __forceinline__ bool epi_write_a(EpiState& e, Shared& sh, uint8_t* aring, int r, int ch,
+                                            const float* x) {
+  volatile int* verr = &sh.err;
+  // slot free? (phase of its previous consumption)
+  if (!mbar_wait(&sh.a_empty[e.aslot], e.aph ^ 1, verr)) return false;
+  uint8_t* base = aring + e.aslot * kASlotBytes;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    uint4 hi, mid, lo;
+    split3_bf16(x + 8 * j, hi, mid, lo);
+    const uint32_t off = sw128_offset(r, 4 * ch + j);
+    *reinterpret_cast<uint4*>(base + off) = hi;
+    *reinterpret_cast<uint4*>(base + 16384 + off) = mid;
+    *reinterpret_cast<uint4*>(base + 32768 + off) = lo;
+  }
+  fence_proxy_async_smem();
+  mbar_arrive(&sh.a_full[e.aslot]);
+  if (++e.aslot == kARing) { e.aslot = 0; e.aph ^= 1; }
+  return true;
+}
+
+// Wait for the accumulator of the next op; returns its TMEM column base.
+__device__ __forceinline__ bool epi_wait_acc(EpiState& e, Shared& sh, uint32_t* col) {
+  const int reg = (int)(e.g & 1);
+  if (!mbar_wait(&sh.acc_full[reg], e.use[reg] & 1, &sh.err)) return false;
+  tc_fence_after();
+  *col = (uint32_t)(reg * 256);
+  return true;
+}
+
+__device__ __forceinline__ void epi_release_acc(EpiState& e, Shared& sh) {
+  const int reg = (int)(e.g & 1);
+  tc_fence_before();
+  mbar_arrive(&sh.acc_empty[reg]);
+  e.use[reg] += 1;
+  e.g += 1;
+}
+
+}  // namespace tc
+}  // namespace gbnde

@@ -1,0 +1,93 @@
+"""BF16 tensor-core form (split-BF16 tcgen05 GEMMs, FP32 state, FP64 control)
+against the FP64 oracle and against the plain FP32 form, through the C ABI.
+
+Tolerances (relative):
+  * saved states vs the oracle replaying the kernel's accepted steps: 2e-5
+  * loss and gradient vs the FP64 oracle (the benchmark's validity bar): 1e-3
+  * saved states vs the FP32 form at the headline batch: 1e-4
+"""
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+from test_gpu_neural_ode import _oracle, _rel, _setup
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="no CUDA GPU")]
+
+
+def _node(model, ts, prec, abstol, reltol, sensealg=None):
+    import gbnde
+    return gbnde.NeuralODE(model, (0.0, float(ts[-1])), gbnde.Tsit5(prec), saveat=ts, abstol=abstol,
+                           reltol=reltol, sensealg=sensealg)
+
+
+@pytest.mark.parametrize("B", [128, 300])
+def test_bf16_forward_and_gradient_vs_oracle(B):
+    from oracle import tsit5 as ots
+    S, H = 64, 256
+    model, p, rng = _setup([S, H, H, S], ["tanh", "tanh", "identity"], False, B, 2, bias=0.02)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    ts = np.linspace(0.0, 1.0, 20)
+    node = _node(model, ts, "bf16", 1e-7, 1e-5)
+    s = node.solver
+    s.set_params(p)
+    us, st = s.forward(u0, node.desc())
+    assert st.retcode == 0
+    steps = s.forward_steps()
+    rhs = _oracle(model, p)
+    ous, fwd = ots.solve_forward(rhs, u0.astype(np.float64), 0.0, 1.0, ts, 1e-7, 1e-5, steps=steps)
+    assert _rel(us, ous) < 2e-5
+    # loss / gradient against the free-running FP64 oracle
+    ous2, fwd2 = ots.solve_forward(_oracle(model, p), u0.astype(np.float64), 0.0, 1.0, ts, 1e-7, 1e-5)
+    tgt = np.zeros_like(ous2)
+    L64 = np.mean((ous2 - tgt) ** 2)
+    L = np.mean((us.astype(np.float64) - tgt) ** 2)
+    assert abs(L - L64) / L64 < 1e-3
+    g = (2.0 * (us.astype(np.float64) - tgt) / us.size).astype(np.float32)
+    du0, dp, sta = s.backward(g)
+    assert sta.retcode_adj == 0
+    gu, gp, _ = ots.adjoint_interpolating(_oracle(model, p), fwd2, ts, 2.0 * (ous2 - tgt) / ous2.size,
+                                          0.0, 1e-7, 1e-5)
+    assert _rel(du0, gu) < 1e-3
+    assert _rel(dp, gp) < 1e-3
+    # the split products keep the step count near the FP64 controller's
+    assert st.naccept + st.nreject <= 3 * (fwd2.naccept + fwd2.nreject) + 4
+
+
+def test_bf16_matches_fp32_form_at_headline_batch():
+    S, H, B = 64, 256, 16384
+    model, p, rng = _setup([S, H, H, S], ["tanh", "tanh", "identity"], False, B, 1, bias=0.0)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    ts = np.linspace(0.0, 1.0, 20)
+    out = {}
+    for prec in ("fp32", "bf16"):
+        node = _node(model, ts, prec, 1e-7, 1e-5)
+        s = node.solver
+        s.set_params(p)
+        us, st = s.forward(u0, node.desc())
+        assert st.retcode == 0
+        g = np.ones_like(us) / us.size
+        du0, dp, sta = s.backward(g)
+        assert sta.retcode_adj == 0
+        out[prec] = (us, du0, dp, st)
+    assert _rel(out["bf16"][0], out["fp32"][0].astype(np.float64)) < 1e-4
+    assert _rel(out["bf16"][1], out["fp32"][1].astype(np.float64)) < 1e-3
+    assert _rel(out["bf16"][2], out["fp32"][2].astype(np.float64)) < 1e-3
+
+
+@pytest.mark.parametrize("S,H,cube", [(2, 50, True), (32, 128, False), (16, 64, False)])
+def test_bf16_small_shapes(S, H, cube):
+    """Padded shapes: state < 64, hidden not a multiple of 64, cube prefix."""
+    from oracle import tsit5 as ots
+    B = 200
+    model, p, rng = _setup([S, H, S], ["tanh", "identity"], cube, B, 3)
+    u0 = rng.standard_normal((S, B)).astype(np.float32) * (0.5 if cube else 1.0)
+    ts = np.linspace(0.0, 1.0, 8)
+    node = _node(model, ts, "bf16", 1e-6, 1e-4)
+    s = node.solver
+    s.set_params(p)
+    us, st = s.forward(u0, node.desc())
+    assert st.retcode == 0
+    ous, _ = ots.solve_forward(_oracle(model, p), u0.astype(np.float64), 0.0, 1.0, ts, 1e-6, 1e-4,
+                               steps=s.forward_steps())
+    assert _rel(us, ous) < 2e-5
