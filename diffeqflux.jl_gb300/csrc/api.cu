@@ -16,19 +16,11 @@
 
 #include "gbnde.h"
 #include "kernels.h"
-#include "tc_engine.cuh"
+#include "tc_args.h"
 
 namespace gbnde {
-struct FwdTcArgs {
-  FwdArgs f;
-  tc::OpList ops;
-  const float* bias[GBNDE_MAX_LAYERS];
-  float* comp[2];
-  float* dense;
-  long long dense_slots;
-  float* kring;
-};
 int launch_reduce_mu(const float* mu_acc, int nblk, int P, float* out, cudaStream_t st);
+
 int launch_transpose_params(const MlpDev& m, const float* p, float* wtr, cudaStream_t st);
 int launch_loss(const float* usave, const float* target, size_t n, int kind, float* dL,
                 double* partial, int nblk, cudaStream_t st);
@@ -119,7 +111,11 @@ struct gbnde_ctx {
   DBuf wimg;
   size_t wimg_off[GBNDE_MAX_LAYERS] = {};
   int npad[GBNDE_MAX_LAYERS] = {}, nchunk[GBNDE_MAX_LAYERS] = {};
+  size_t wtimg_off[GBNDE_MAX_LAYERS] = {};
+  int npadT[GBNDE_MAX_LAYERS] = {}, nchunkT[GBNDE_MAX_LAYERS] = {};
   bool tc_shape_ok = false;
+  bool tc_bwd_ok = false;  // tensor-core adjoint covers this model
+  DBuf timg, thscr, tbpart, tmucomp, tlamcomp;
   // dense stage storage of the last forward
   DBuf comp, dense;
   long long dense_slots = 0;
@@ -230,6 +226,11 @@ int gbnde_create(gbnde_ctx** out, const gbnde_mlp_desc* mlp, int precision, int 
   // shapes the tensor-core engine covers: state <= 64, hidden widths <= 256
   c->tc_shape_ok = !mlp->time_input && S <= 64 && mlp->dims[0] <= 64;
   for (int l = 1; l < mlp->nlayers; ++l) c->tc_shape_ok = c->tc_shape_ok && mlp->dims[l] <= 256;
+  // the tensor-core adjoint also needs an identity output layer and <= 256 on
+  // the N side of every weight-gradient product
+  c->tc_bwd_ok = c->tc_shape_ok && mlp->act[mlp->nlayers - 1] == GBNDE_ACT_IDENTITY;
+  for (int l = 0; l < mlp->nlayers; ++l)
+    c->tc_bwd_ok = c->tc_bwd_ok && std::min(mlp->dims[l], mlp->dims[l + 1]) <= 256;
   if (precision == GBNDE_PREC_BF16 && !c->tc_shape_ok) {
     gbnde_destroy(c);
     return fail(GBNDE_ERR_UNSUPPORTED,
@@ -246,7 +247,8 @@ void gbnde_destroy(gbnde_ctx* c) {
                   &c->ckpt_step, &c->steplog, &c->trace, &c->partials, &c->sync, &c->counters, &c->saveat_d,
                   &c->bnd_d, &c->dldu, &c->dldu0, &c->dldp, &c->lam, &c->ub, &c->kl, &c->ku,
                   &c->ibuf, &c->mu_acc, &c->mu_stage, &c->iv_d, &c->bsync, &c->bcounters,
-                  &c->loss_part, &c->wimg, &c->comp, &c->dense};
+                  &c->loss_part, &c->wimg, &c->comp, &c->dense, &c->timg, &c->thscr,
+                  &c->tbpart, &c->tmucomp, &c->tlamcomp};
   for (DBuf* b : bufs) b->release();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -269,10 +271,14 @@ static int bind_params(gbnde_ctx* c) {
   if (launch_transpose_params(m, p, c->wtr.as<float>(), c->stream))
     return fail(GBNDE_ERR_CUDA, "transpose kernel launch failed");
   if (c->precision == GBNDE_PREC_BF16 && c->tc_shape_ok) {
-    for (int l = 0; l < m.nlayers; ++l)
+    for (int l = 0; l < m.nlayers; ++l) {
       if (launch_prep_weight_image(m.W[l], m.dims[l + 1], m.dims[l], c->npad[l],
                                    c->wimg.as<uint8_t>() + c->wimg_off[l], c->stream))
         return fail(GBNDE_ERR_CUDA, "weight image kernel launch failed");
+      if (launch_prep_weight_image(m.Wt[l], m.dims[l], m.dims[l + 1], c->npadT[l],
+                                   c->wimg.as<uint8_t>() + c->wtimg_off[l], c->stream))
+        return fail(GBNDE_ERR_CUDA, "weight image kernel launch failed");
+    }
   }
   c->have_params = true;
   return 0;
@@ -288,6 +294,13 @@ static int alloc_params(gbnde_ctx* c) {
       c->nchunk[l] = (c->mlp.dims[l] + 63) / 64;
       c->wimg_off[l] = off;
       off += (size_t)c->nchunk[l] * 2 * c->npad[l] * 128;
+    }
+    // transposed weights W^T (N = in, K = out) for the VJP chain
+    for (int l = 0; l < c->mlp.nlayers; ++l) {
+      c->npadT[l] = (c->mlp.dims[l] + 15) / 16 * 16;
+      c->nchunkT[l] = (c->mlp.dims[l + 1] + 63) / 64;
+      c->wtimg_off[l] = off;
+      off += (size_t)c->nchunkT[l] * 2 * c->npadT[l] * 128;
     }
     if (int r = c->wimg.ensure(off)) return r;
   }
@@ -458,6 +471,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
       ta.ops.op[l].wimg = c->wimg.as<uint8_t>() + c->wimg_off[l];
       ta.ops.op[l].npad = c->npad[l];
       ta.ops.op[l].nchunk = c->nchunk[l];
+      ta.ops.op[l].kind = 0;
       ta.bias[l] = c->mlp.bias[l];
     }
     ta.comp[0] = c->comp.as<float>();
@@ -574,6 +588,119 @@ static int build_intervals(gbnde_ctx* c, std::vector<Interval>& ivs, int* max_sl
   return 0;
 }
 
+// Tensor-core adjoint: op list, scratch images and launch. `base` carries the
+// intervals, cotangents and state buffers prepared for the FP32 kernel.
+static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float* dp_d) {
+  const MlpDev& m = c->mlp;
+  const int L = m.nlayers;
+  const int S = c->S, B = c->B;
+  const size_t SB = (size_t)S * B;
+  const int P = (int)c->P;
+  int gmax = 0;
+  if (max_grid_fwd_tc(&gmax)) return fail(GBNDE_ERR_CUDA, "occupancy query failed (tc)");
+  const int ntiles = (B + 127) / 128;
+  const int grid = std::min(gmax, ntiles);
+  BwdTcArgs t{};
+  t.b = base;
+  t.b.ntiles = ntiles;
+  t.b.TM = 128;
+  // weight-gradient operand images per CTA
+  size_t off = 0;
+  for (int l = 0; l < L; ++l) {
+    const int out = m.dims[l + 1], in = m.dims[l];
+    t.a_isA[l] = in > out ? 1 : 0;
+    const int mside = t.a_isA[l] ? in : out;
+    t.nh[l] = (mside + 127) / 128;
+    auto img_bytes = [&](int dim, int isA) -> size_t {
+      return isA ? (size_t)2 * t.nh[l] * 32768 : (size_t)2 * 2 * ((dim + 63) / 64) * 8192;
+    };
+    t.aoff[l] = (long long)off;
+    off += img_bytes(in, t.a_isA[l]);
+    t.doff[l] = (long long)off;
+    off += img_bytes(out, !t.a_isA[l]);
+  }
+  t.img_cta = off;
+  int hv = 0;
+  for (int l = 1; l < L; ++l) {
+    t.hoff[l] = hv;
+    hv += 32 * ((m.dims[l] + 63) / 64);
+  }
+  t.hvals = std::max(hv, 4);
+  int nb = 0;
+  for (int l = 0; l < L; ++l) {
+    t.boffp[l] = nb;
+    nb += 64 * ((m.dims[l + 1] + 63) / 64);
+  }
+  t.nbias = nb;
+  int r = 0;
+  if ((r = c->timg.ensure((size_t)grid * t.img_cta)) ||
+      (r = c->thscr.ensure((size_t)grid * tc::kEpiThreads * t.hvals * 4)) ||
+      (r = c->tbpart.ensure((size_t)grid * 4 * t.nbias * 4)) ||
+      (r = c->tmucomp.ensure((size_t)grid * P * 4)) || (r = c->tlamcomp.ensure(2 * SB * 4)) ||
+      (r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4)))
+    return r;
+  t.b.mu_acc = c->mu_acc.as<float>();
+  t.b.mu_stage = c->mu_stage.as<float>();
+  t.img = c->timg.as<uint8_t>();
+  t.hscr = c->thscr.as<float>();
+  t.bpart = c->tbpart.as<float>();
+  t.mu_comp = c->tmucomp.as<float>();
+  t.lam_comp[0] = c->tlamcomp.as<float>();
+  t.lam_comp[1] = c->tlamcomp.as<float>() + SB;
+  t.b.dense = c->dense.as<float>();
+  for (int l = 0; l < L; ++l) t.bias[l] = m.bias[l];
+  // op list: forward recompute, VJP chain, weight gradients
+  int n = 0;
+  for (int l = 0; l + 1 < L; ++l) {
+    tc::GemmOp& o = t.ops.op[n++];
+    o.kind = 0;
+    o.wimg = c->wimg.as<uint8_t>() + c->wimg_off[l];
+    o.npad = c->npad[l];
+    o.nchunk = c->nchunk[l];
+  }
+  for (int l = L - 1; l >= 0; --l) {
+    tc::GemmOp& o = t.ops.op[n++];
+    o.kind = 0;
+    o.wimg = c->wimg.as<uint8_t>() + c->wtimg_off[l];
+    o.npad = c->npadT[l];
+    o.nchunk = c->nchunkT[l];
+  }
+  bool first = true;
+  for (int l = 0; l < L; ++l) {
+    const int out = m.dims[l + 1], in = m.dims[l];
+    const int nside = t.a_isA[l] ? out : in;
+    const int nblk = (nside + 63) / 64;
+    const long long aimg = t.a_isA[l] ? t.aoff[l] : t.doff[l];
+    const long long bimg = t.a_isA[l] ? t.doff[l] : t.aoff[l];
+    for (int hh = 0; hh < t.nh[l]; ++hh) {
+      if (n >= tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+      tc::GemmOp& o = t.ops.op[n++];
+      o.kind = 1;
+      o.aimg = t.img + aimg + (size_t)hh * 32768;
+      o.wimg = t.img + bimg;
+      o.cta_stride = t.img_cta;
+      o.a_bytes = 32768;
+      o.a_step = (uint32_t)(t.nh[l] * 32768);
+      o.b_step = (uint32_t)(2 * nblk * 8192);
+      o.nblk_b = nblk;
+      o.npad = (nside + 15) / 16 * 16;
+      o.nchunk = 2;
+      o.first_dw = first ? 1 : 0;
+      first = false;
+    }
+  }
+  t.ops.nops = n;
+  CK(cudaEventRecord(c->ev[2], st));
+  if (launch_bwd_tc(t, grid, st)) {
+    cudaError_t e = cudaGetLastError();
+    return fail(GBNDE_ERR_CUDA, "backward (tc) launch failed: %s", cudaGetErrorString(e));
+  }
+  CK(cudaEventRecord(c->ev[3], st));
+  if (launch_reduce_mu_comp(t.b.mu_acc, t.mu_comp, grid, P, dp_d, st))
+    return fail(GBNDE_ERR_CUDA, "reduce launch failed");
+  return 0;
+}
+
 static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* dLdu0,
                          float* dLdp, bool out_host, gbnde_stats* stats) {
   if (!c) return fail(GBNDE_ERR_INVALID, "null context");
@@ -668,13 +795,18 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   a.bar = c->bsync.as<unsigned int>();
   a.status = reinterpret_cast<int*>(c->bsync.as<char>() + 16);
   a.counters = c->bcounters.as<long long>();
-  CK(cudaEventRecord(c->ev[2], st));
-  if (launch_bwd_f32(a, grid, smem, st)) {
-    cudaError_t e = cudaGetLastError();
-    return fail(GBNDE_ERR_CUDA, "backward launch failed: %s", cudaGetErrorString(e));
+  const bool tcbwd = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && c->dense_valid;
+  if (tcbwd) {
+    if (int rr = backward_tc(c, a, st, dp_d)) return rr;
+  } else {
+    CK(cudaEventRecord(c->ev[2], st));
+    if (launch_bwd_f32(a, grid, smem, st)) {
+      cudaError_t e = cudaGetLastError();
+      return fail(GBNDE_ERR_CUDA, "backward launch failed: %s", cudaGetErrorString(e));
+    }
+    CK(cudaEventRecord(c->ev[3], st));
+    if (launch_reduce_mu(a.mu_acc, grid, P, dp_d, st)) return fail(GBNDE_ERR_CUDA, "reduce launch failed");
   }
-  CK(cudaEventRecord(c->ev[3], st));
-  if (launch_reduce_mu(a.mu_acc, grid, P, dp_d, st)) return fail(GBNDE_ERR_CUDA, "reduce launch failed");
   long long cnt[CT_NSLOTS];
   int status[4];
   CK(cudaMemcpyAsync(cnt, c->bcounters.p, sizeof cnt, cudaMemcpyDeviceToHost, st));

@@ -1,0 +1,681 @@
+// bwd_tc.cu -- persistent InterpolatingAdjoint solve, BF16 tensor-core form.
+//
+// Same adjoint algorithm as bwd_f32.cu (the pullback of SciMLSensitivity's
+// rrule on `solve` for sensealg = InterpolatingAdjoint(), src/neural_de.jl:57):
+// reverse-time Tsit5 on lam with the PI controller over lam, the save points
+// as stops where lam jumps by dL/du(t_i), and the parameter quadrature mu with
+// the Tsit5 weights over accepted steps. u(t) is the free interpolant of the
+// forward's dense stage storage (one slot per accepted forward step).
+//
+// One adjoint right-hand side on a tile of 128 trajectories is a list of
+// tensor-core ops (tc_engine.cuh):
+//   forward recompute  z_l = W_l a_{l-1},          l = 1..L-1   (5 split products)
+//   VJP chain          g_l = W_l^T delta_{l+1},    l = L..1     (5 split products)
+//                      delta_l = g_l * act'(z_l), delta_L = lam, kl = g_1
+//   weight gradients   dW_l = delta_{l+1} a_l^T summed over the 128 trajectories
+//                      (K = trajectories, MN-major operands, 3 split products)
+// The epilogue writes the activations and cotangents as split-BF16
+// trajectory-major images into per-CTA scratch; the producer warp bulk-copies
+// them back as the weight-gradient operands, and the epilogue drains each
+// weight-gradient accumulator from tensor memory into the CTA's pending
+// quadrature buffer with the stage weight. Bias gradients are column sums of
+// the cotangents (warp butterfly reductions, deterministic order).
+// lam and mu use compensated (TwoSum / Kahan) sums; t, H and the controller
+// are FP64.
+#include "tc_args.h"
+
+namespace gbnde {
+
+
+namespace {
+
+struct Thr {
+  int r, ch, nmine, q, lane;
+};
+
+__device__ __forceinline__ void ld32(const float* p, int n, bool vec, float* x) {
+  if (vec) {
+#pragma unroll
+    for (int i = 0; i < 32; i += 4) {
+      const float4 v = *reinterpret_cast<const float4*>(p + i);
+      x[i] = v.x; x[i + 1] = v.y; x[i + 2] = v.z; x[i + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) x[i] = (i < n) ? p[i] : 0.f;
+  }
+}
+
+__device__ __forceinline__ void st32(float* p, int n, bool vec, const float* x) {
+  if (vec) {
+#pragma unroll
+    for (int i = 0; i < 32; i += 4)
+      *reinterpret_cast<float4*>(p + i) = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+      if (i < n) p[i] = x[i];
+  }
+}
+
+__device__ __forceinline__ bool epi_grid_barrier(const BwdArgs& a, unsigned int& gen, int* okflag) {
+  tc::epi_bar();
+  gen += 1;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(a.bar, 1u);
+    const unsigned int target = gen * gridDim.x;
+    const unsigned long long t0 = globaltimer_ns();
+    int ok = 1;
+    while (ld_acquire_u32(a.bar) < target) {
+      if (*((volatile int*)&a.status[ST_BARRIER]) != 0) { ok = 0; break; }
+      if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+        atomicExch(&a.status[ST_BARRIER], 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    *okflag = ok;
+  }
+  tc::epi_bar();
+  return *okflag != 0;
+}
+
+__device__ __forceinline__ double epi_partials_sum(const double* p, int n, tc::Shared& sh) {
+  if (threadIdx.x < 32) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) v += __ldcg(p + i);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) sh.red[15] = v;
+  }
+  tc::epi_bar();
+  const double v = sh.red[15];
+  tc::epi_bar();
+  return v;
+}
+
+// Split-BF16 pieces of 32 values -> this thread's part of a weight-gradient
+// image (2 pieces). Block c holds features [64c, 64c+64); the thread writes
+// its 16-byte groups 4*ch..4*ch+3 of trajectory row r.
+__device__ __forceinline__ void img_store(uint8_t* img, int isA, int nblk, int nh, const Thr& th,
+                                          int c, const uint4* hi, const uint4* mid) {
+  const int kc = th.r >> 6, row = th.r & 63;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t sw = tc::sw128_offset(row, 4 * th.ch + j);
+    size_t o0, o1;
+    if (isA) {
+      const int h = c >> 1, bb = c & 1;
+      o0 = ((size_t)((kc * nh + h) * 2 + 0)) * 16384 + bb * 8192 + sw;
+      o1 = ((size_t)((kc * nh + h) * 2 + 1)) * 16384 + bb * 8192 + sw;
+    } else {
+      o0 = ((size_t)((kc * 2 + 0) * nblk + c)) * 8192 + sw;
+      o1 = ((size_t)((kc * 2 + 1) * nblk + c)) * 8192 + sw;
+    }
+    *reinterpret_cast<uint4*>(img + o0) = hi[j];
+    *reinterpret_cast<uint4*>(img + o1) = mid[j];
+  }
+}
+
+// 32 values: chain A chunk (3 pieces) and/or image (2 pieces).
+__device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* aring, const Thr& th,
+                                     const float* x, bool chain, uint8_t* img, int isA, int nblk,
+                                     int nh, int c) {
+  uint4 hi[4], mid[4], lo[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) tc::split3_bf16(x + 8 * j, hi[j], mid[j], lo[j]);
+  if (chain) {
+    if (!tc::mbar_wait(&sh.a_empty[e.aslot], e.aph ^ 1, &sh.err)) return false;
+    uint8_t* base = aring + e.aslot * tc::kASlotBytes;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t off = tc::sw128_offset(th.r, 4 * th.ch + j);
+      *reinterpret_cast<uint4*>(base + off) = hi[j];
+      *reinterpret_cast<uint4*>(base + 16384 + off) = mid[j];
+      *reinterpret_cast<uint4*>(base + 32768 + off) = lo[j];
+    }
+    tc::fence_proxy_async_smem();
+    tc::mbar_arrive(&sh.a_full[e.aslot]);
+    if (++e.aslot == tc::kARing) { e.aslot = 0; e.aph ^= 1; }
+  }
+  if (img) img_store(img, isA, nblk, nh, th, c, hi, mid);
+  return true;
+}
+
+// Column sums over the warp's 32 trajectory rows: after the butterfly, lane j
+// holds the sum of value j over the 32 lanes.
+__device__ __forceinline__ float warp_colsum(float* v, int lane) {
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+#pragma unroll
+    for (int i = 0; i < s; ++i) {
+      const bool up = (lane & s) != 0;
+      const float send = up ? v[i] : v[i + s];
+      const float keep = up ? v[i + s] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+    }
+  }
+  return v[0];
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* aring = smem;
+  uint8_t* wring = smem + tc::kARing * tc::kASlotBytes;
+  __shared__ tc::Shared sh;
+  __shared__ int s_ok;
+  const BwdArgs& a = A.b;
+  const int warp = threadIdx.x >> 5;
+
+  tc::init_shared(sh);
+  if (warp == tc::kMmaWarp) tc::tmem_alloc(&sh.tmem_base, 512);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+
+  if (warp == tc::kMmaWarp) {
+    tc::mma_loop(A.ops, sh, aring, wring);
+  } else if (warp == tc::kTmaWarp) {
+    tc::tma_loop(A.ops, sh, aring, wring);
+  } else {
+    // ======================= epilogue warps =======================
+    const MlpDev& m = a.mlp;
+    const int L = m.nlayers;
+    const int S = a.S, G = gridDim.x;
+    const size_t SB = (size_t)S * a.B;
+    const double Nn = (double)SB;
+    Thr th;
+    th.lane = threadIdx.x & 31;
+    th.q = warp & 3;
+    th.r = 32 * th.q + th.lane;
+    th.ch = warp >> 2;
+    th.nmine = min(32, max(0, S - 32 * th.ch));
+    const bool vec = (S % 4 == 0) && th.nmine == 32;
+    const uint32_t lane_base = ((uint32_t)(th.q * 32)) << 16;
+    tc::EpiState es;
+    tc::epi_state_init(es);
+    unsigned int gen = 0;
+    int par = 0, cur = 0;
+    int ret = GBNDE_RET_SUCCESS;
+    long long nf_adj = 0, nacc = 0, nrej = 0, iter = 0;
+    double dt = 0.0, qold = kQoldInit;
+    bool swp = false, ok = true;
+    uint8_t* img = A.img + (size_t)blockIdx.x * A.img_cta;
+    float* hscr = A.hscr + ((size_t)blockIdx.x * tc::kEpiThreads + threadIdx.x) * A.hvals;
+    float* bpart = A.bpart + (size_t)blockIdx.x * 4 * A.nbias;
+    float* mu_acc = a.mu_acc + (size_t)blockIdx.x * a.P;
+    float* mu_comp = A.mu_comp + (size_t)blockIdx.x * a.P;
+    float* Pb[3] = {a.mu_stage + (size_t)blockIdx.x * 3 * a.P,
+                    a.mu_stage + ((size_t)blockIdx.x * 3 + 1) * a.P,
+                    a.mu_stage + ((size_t)blockIdx.x * 3 + 2) * a.P};
+    int iP1 = 0, iP7 = 2;
+    float* Pmid = Pb[1];
+    int ndw = 0;  // weight-gradient ops per evaluation (A-ring slots they use: 2 each)
+    for (int l = 0; l < L; ++l) ndw += A.nh[l];
+
+    auto klb = [&](int j) -> float* {
+      if (j == 0) return swp ? a.kl[6] : a.kl[0];
+      if (j == 6) return swp ? a.kl[0] : a.kl[6];
+      return a.kl[j];
+    };
+    auto gofs = [&](int tile) -> size_t { return ((size_t)tile * 128 + th.r) * S + 32 * th.ch; };
+    auto valid = [&](int tile) -> bool { return tile * 128 + th.r < a.B && th.nmine > 0; };
+    auto zero_cta = [&](float* p) {
+      for (size_t i = threadIdx.x; i < (size_t)a.P; i += tc::kEpiThreads) p[i] = 0.f;
+    };
+
+    // scratch images start at zero (padding rows/blocks are never written)
+    for (size_t i = threadIdx.x; i < A.img_cta / 16; i += tc::kEpiThreads)
+      reinterpret_cast<uint4*>(img)[i] = make_uint4(0, 0, 0, 0);
+    zero_cta(mu_acc);
+    zero_cta(mu_comp);
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+      if (!valid(tile)) continue;
+      float v[32], z[32];
+      for (int i = 0; i < 32; ++i) { v[i] = 0.f; z[i] = 0.f; }
+      for (int qq = 0; qq < a.nsave_last; ++qq) {
+        float d[32];
+        ld32(a.dLdu + (size_t)(a.save_last + qq) * SB + gofs(tile), th.nmine, vec, d);
+        for (int i = 0; i < 32; ++i) v[i] += d[i];
+      }
+      st32(a.lam[0] + gofs(tile), th.nmine, vec, v);
+      st32(A.lam_comp[0] + gofs(tile), th.nmine, vec, z);
+    }
+    tc::epi_bar();
+
+    // ---- adjoint right-hand side of one tile ------------------------------------------
+    // lam_in: stage input lam (own components), x: u(t) (own components).
+    // P/c: pending quadrature buffer and weight (P == nullptr: no quadrature).
+    auto adj_eval = [&](const float* lam_in, const float* x, float* P, float c, float* kl) -> bool {
+      float v[32];
+      // a_0 = x (or x^3)
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const float y = (i < th.nmine) ? x[i] : 0.f;
+        v[i] = m.cube ? y * y * y : y;
+      }
+      if (!emit(es, sh, aring, th, v, true, img + A.aoff[0], A.a_isA[0], (m.dims[0] + 63) / 64, A.nh[0], 0))
+        return false;
+      // forward recompute of the hidden layers
+      for (int l = 0; l < L - 1; ++l) {
+        const int N = m.dims[l + 1];
+        const float* b = A.bias[l];
+        uint32_t col;
+        if (!tc::epi_wait_acc(es, sh, &col)) return false;
+        for (int cc = 0; cc < (N + 63) / 64; ++cc) {
+          const int n0 = 64 * cc + 32 * th.ch;
+          tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+#pragma unroll
+          for (int i = 0; i < 32; ++i) v[i] = (n0 + i < N) ? act_apply(v[i] + __ldg(b + n0 + i), m.act[l]) : 0.f;
+          st32(hscr + A.hoff[l + 1] + 32 * cc, 32, true, v);
+          if (!emit(es, sh, aring, th, v, l + 1 <= L - 2, img + A.aoff[l + 1], A.a_isA[l + 1],
+                    (N + 63) / 64, A.nh[l + 1], cc))
+            return false;
+        }
+        tc::epi_release_acc(es, sh);
+      }
+      // delta_L = lam (identity output layer)
+      const int bbase = threadIdx.x;  // unused placeholder to keep indices readable
+      (void)bbase;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = (i < th.nmine) ? lam_in[i] : 0.f;
+      if (!emit(es, sh, aring, th, v, true, img + A.doff[L - 1], !A.a_isA[L - 1],
+                (m.dims[L] + 63) / 64, A.nh[L - 1], 0))
+        return false;
+      if (P) {
+        float w[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) w[i] = v[i];
+        const float s = warp_colsum(w, th.lane);
+        bpart[th.q * A.nbias + A.boffp[L - 1] + 32 * th.ch + th.lane] = s;
+      }
+      // VJP chain
+      for (int l = L - 1; l >= 1; --l) {
+        const int N = m.dims[l];
+        uint32_t col;
+        if (!tc::epi_wait_acc(es, sh, &col)) return false;
+        for (int cc = 0; cc < (N + 63) / 64; ++cc) {
+          const int n0 = 64 * cc + 32 * th.ch;
+          float h[32];
+          tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+          ld32(hscr + A.hoff[l] + 32 * cc, 32, true, h);
+#pragma unroll
+          for (int i = 0; i < 32; ++i) v[i] = (n0 + i < N) ? v[i] * act_deriv_from_out(h[i], m.act[l - 1]) : 0.f;
+          if (!emit(es, sh, aring, th, v, true, img + A.doff[l - 1], !A.a_isA[l - 1], (N + 63) / 64,
+                    A.nh[l - 1], cc))
+            return false;
+          if (P) {
+            const float s = warp_colsum(v, th.lane);
+            bpart[th.q * A.nbias + A.boffp[l - 1] + n0 + th.lane] = s;
+          }
+        }
+        tc::epi_release_acc(es, sh);
+      }
+      // all weight-gradient images written: hand them to the producer warp
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+      tc::mbar_arrive(&sh.img_ready);
+      // kl = W_1^T delta_1 (times 3 x^2 for the cube prefix)
+      {
+        uint32_t col;
+        if (!tc::epi_wait_acc(es, sh, &col)) return false;
+        tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)(32 * th.ch), v);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          float g = (i < th.nmine) ? v[i] : 0.f;
+          if (m.cube) g *= 3.f * x[i] * x[i];
+          kl[i] = g;
+        }
+        tc::epi_release_acc(es, sh);
+      }
+      // weight-gradient accumulators -> pending quadrature buffer
+      tc::epi_skip_a(es, 2 * ndw);
+      for (int l = 0; l < L; ++l) {
+        const int out = m.dims[l + 1], in = m.dims[l];
+        const int Nn2 = A.a_isA[l] ? out : in;  // N side of the dW op
+        const float* wbase = nullptr;
+        (void)wbase;
+        for (int hh = 0; hh < A.nh[l]; ++hh) {
+          uint32_t col;
+          if (!tc::epi_wait_acc(es, sh, &col)) return false;
+          if (P) {
+            const int mrow = 128 * hh + th.r;  // M-side feature of this lane
+            for (int cc = 0; cc < (Nn2 + 63) / 64; ++cc) {
+              const int n0 = 64 * cc + 32 * th.ch;
+              tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+#pragma unroll
+              for (int i = 0; i < 32; ++i) {
+                const int nn = n0 + i;
+                const int o = A.a_isA[l] ? nn : mrow;
+                const int ii = A.a_isA[l] ? mrow : nn;
+                if (o < out && ii < in) {
+                  float* pp = P + m.woff[l] + (size_t)ii * out + o;
+                  *pp = fmaf(c, v[i], *pp);
+                }
+              }
+            }
+          }
+          tc::epi_release_acc(es, sh);
+        }
+      }
+      if (P) {
+        tc::epi_bar();
+        for (int f = threadIdx.x; f < A.nbias; f += tc::kEpiThreads) {
+          // which layer's bias holds f
+          int l = 0;
+          while (l + 1 < L && f >= A.boffp[l + 1]) ++l;
+          const int o = f - A.boffp[l];
+          if (o < m.dims[l + 1]) {
+            const float s = ((bpart[f] + bpart[A.nbias + f]) + bpart[2 * A.nbias + f]) + bpart[3 * A.nbias + f];
+            float* pp = P + m.boff[l] + o;
+            *pp = fmaf(c, s, *pp);
+          }
+        }
+        tc::epi_bar();
+      }
+      return true;
+    };
+
+    // u(t) from the dense forward slots: step n, weights hb
+    auto dense_setup = [&](const Interval& iv, double t, int* nstep, float* hb) {
+      int n = iv.nlo;
+      while (n < iv.nhi && a.fsteps[2 * (n + 1)] <= t) ++n;
+      const double tn = a.fsteps[2 * n], h = a.fsteps[2 * n + 1];
+      float bw[7];
+      interp_weights((t - tn) / h, bw);
+      for (int j = 0; j < 7; ++j) hb[j] = (float)(h * (double)bw[j]);
+      *nstep = n;
+    };
+    auto dense_u = [&](int tile, int n, const float* hb, float* x) {
+      const float* slot = a.dense + (size_t)n * 8 * SB;
+      const size_t g = gofs(tile);
+      float acc[32];
+      ld32(slot + g, th.nmine, vec, x);
+      for (int i = 0; i < 32; ++i) acc[i] = 0.f;
+      for (int j = 0; j < 7; ++j) {
+        float kj[32];
+        ld32(slot + (size_t)(j + 1) * SB + g, th.nmine, vec, kj);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) acc[i] = fmaf(hb[j], kj[i], acc[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < 32; ++i) x[i] += acc[i];
+    };
+
+    for (int ivi = 0; ivi < a.niv && ok && ret == GBNDE_RET_SUCCESS; ++ivi) {
+      const Interval iv = a.iv[ivi];
+      double t = iv.t_hi;
+      const double t_lo = iv.t_lo;
+      // ---- FSAL stage at the interval start: kl1 and P1 = b1 * mu ----
+      {
+        zero_cta(Pb[iP1]);
+        tc::epi_bar();
+        int n;
+        float hb[7];
+        dense_setup(iv, t, &n, hb);
+        for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
+          float lam[32], x[32], kl[32];
+          const bool v = valid(tile);
+          if (v) {
+            ld32(a.lam[cur] + gofs(tile), th.nmine, vec, lam);
+            dense_u(tile, n, hb, x);
+          } else {
+            for (int i = 0; i < 32; ++i) lam[i] = x[i] = 0.f;
+          }
+          ok = adj_eval(lam, x, Pb[iP1], (float)c_tab.b[0], kl);
+          if (v) st32(klb(0) + gofs(tile), th.nmine, vec, kl);
+        }
+        ++nf_adj;
+        if (!ok) break;
+      }
+      // ---- initial step (first interval) ----
+      if (ivi == 0) {
+        double p0 = 0.0, p1 = 0.0;
+        for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+          if (!valid(tile)) continue;
+          float l[32], f[32];
+          ld32(a.lam[cur] + gofs(tile), th.nmine, vec, l);
+          ld32(klb(0) + gofs(tile), th.nmine, vec, f);
+          for (int i = 0; i < th.nmine; ++i) {
+            const float sk = (float)a.abstol + fabsf(l[i]) * (float)a.reltol;
+            const double xx = (double)(l[i] / sk), yy = (double)(f[i] / sk);
+            p0 += xx * xx;
+            p1 += yy * yy;
+          }
+        }
+        p0 = tc::epi_sum(p0, sh);
+        p1 = tc::epi_sum(p1, sh);
+        double* pp = a.partials + (size_t)par * 2 * G;
+        if (threadIdx.x == 0) {
+          pp[blockIdx.x] = p0;
+          pp[G + blockIdx.x] = p1;
+        }
+        if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
+        const double d0 = sqrt(epi_partials_sum(pp, G, sh) / Nn);
+        const double d1 = sqrt(epi_partials_sum(pp + G, G, sh) / Nn);
+        par ^= 1;
+        double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+        dt0 = fmin(dt0, a.dtmax);
+        const float hf = (float)dt0;
+        const double tp = t - dt0;
+        int n;
+        float hb[7];
+        dense_setup(iv, tp, &n, hb);
+        double p2 = 0.0;
+        for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
+          const bool v = valid(tile);
+          float l[32], f0[32], x[32], f1[32];
+          if (v) {
+            ld32(a.lam[cur] + gofs(tile), th.nmine, vec, l);
+            ld32(klb(0) + gofs(tile), th.nmine, vec, f0);
+            dense_u(tile, n, hb, x);
+          } else {
+            for (int i = 0; i < 32; ++i) l[i] = f0[i] = x[i] = 0.f;
+          }
+          float li[32];
+          for (int i = 0; i < 32; ++i) li[i] = l[i] + hf * f0[i];
+          ok = adj_eval(li, x, nullptr, 0.f, f1);
+          if (v)
+            for (int i = 0; i < th.nmine; ++i) {
+              const float sk = (float)a.abstol + fabsf(l[i]) * (float)a.reltol;
+              const double z = (double)((f1[i] - f0[i]) / sk);
+              p2 += z * z;
+            }
+        }
+        ++nf_adj;
+        if (!ok) break;
+        p2 = tc::epi_sum(p2, sh);
+        pp = a.partials + (size_t)par * 2 * G;
+        if (threadIdx.x == 0) pp[blockIdx.x] = p2;
+        if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
+        const double d2 = sqrt(epi_partials_sum(pp, G, sh) / Nn) / dt0;
+        par ^= 1;
+        const double mm = fmax(d1, d2);
+        const double dt1 = (mm <= 1e-15) ? fmax(1e-6, dt0 * 1e-3) : pow(10.0, -(2.0 + log10(mm)) / 5.0);
+        dt = fmin(100.0 * dt0, fmin(dt1, a.dtmax));
+      }
+      // ---- adaptive steps down to t_lo ----
+      while (t > t_lo && ok) {
+        if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
+        ++iter;
+        const double rem = t - t_lo;
+        const bool clipped = dt >= rem;
+        const double H = clipped ? rem : dt;
+        const float* lcur = a.lam[cur];
+        float* lnew = a.lam[cur ^ 1];
+        const float* ccur = A.lam_comp[cur];
+        float* cnew = A.lam_comp[cur ^ 1];
+        zero_cta(Pmid);
+        tc::epi_bar();
+        double perr = 0.0;
+        for (int i = 1; i < 7 && ok; ++i) {
+          const double tt = t - c_tab.c[i] * H;
+          float ha[6];
+          for (int j = 0; j < 6; ++j) ha[j] = (float)(H * c_tab.a[i][j]);
+          float* P = (i < 6) ? Pmid : Pb[iP7];
+          if (i == 6) {
+            zero_cta(P);
+            tc::epi_bar();
+          }
+          const float cw = (i < 6) ? (float)c_tab.b[i] : (float)c_tab.b[0];
+          int n;
+          float hb[7];
+          dense_setup(iv, tt, &n, hb);
+          for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
+            const bool v = valid(tile);
+            const size_t g = gofs(tile);
+            float l[32], s[32], Y[32], x[32], kl[32];
+            if (v) {
+              ld32(lcur + g, th.nmine, vec, l);
+              ld32(ccur + g, th.nmine, vec, s);
+              for (int j = 0; j < i; ++j) {
+                float kj[32];
+                ld32(klb(j) + g, th.nmine, vec, kj);
+#pragma unroll
+                for (int q = 0; q < 32; ++q) s[q] = fmaf(ha[j], kj[q], s[q]);
+              }
+#pragma unroll
+              for (int q = 0; q < 32; ++q) Y[q] = l[q] + s[q];
+              if (i == 6) {
+                float cn[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) cn[q] = s[q] - (Y[q] - l[q]);
+                st32(lnew + g, th.nmine, vec, Y);
+                st32(cnew + g, th.nmine, vec, cn);
+              }
+              dense_u(tile, n, hb, x);
+            } else {
+              for (int q = 0; q < 32; ++q) Y[q] = x[q] = l[q] = 0.f;
+            }
+            ok = adj_eval(Y, x, P, cw, kl);
+            if (v) {
+              st32(klb(i) + g, th.nmine, vec, kl);
+              if (i == 6) {
+                float lt[32];
+                for (int q = 0; q < 32; ++q) lt[q] = (float)(H * c_tab.btilde[6]) * kl[q];
+                for (int j = 0; j < 6; ++j) {
+                  float kj[32];
+                  ld32(klb(j) + g, th.nmine, vec, kj);
+                  const float hbt = (float)(H * c_tab.btilde[j]);
+#pragma unroll
+                  for (int q = 0; q < 32; ++q) lt[q] = fmaf(hbt, kj[q], lt[q]);
+                }
+                for (int q = 0; q < th.nmine; ++q) {
+                  const float sc = (float)a.abstol + fmaxf(fabsf(l[q]), fabsf(Y[q])) * (float)a.reltol;
+                  const double rr = (double)(lt[q] / sc);
+                  perr += isfinite(Y[q]) ? rr * rr : (double)INFINITY;
+                }
+              }
+            }
+          }
+          ++nf_adj;
+        }
+        if (!ok) break;
+        perr = tc::epi_sum(perr, sh);
+        double* pp = a.partials + (size_t)par * 2 * G;
+        if (threadIdx.x == 0) pp[blockIdx.x] = perr;
+        if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
+        const double eest = sqrt(epi_partials_sum(pp, G, sh) / Nn);
+        par ^= 1;
+        if (!isfinite(eest)) { ret = GBNDE_RET_UNSTABLE; break; }
+        double q11;
+        double q = pi_q(eest, qold, &q11);
+        if (eest <= 1.0) {
+          // mu += H (P1 + Pmid), Kahan-compensated per CTA
+          const float Hf = (float)H;
+          const float* P1 = Pb[iP1];
+          for (size_t k = threadIdx.x; k < (size_t)a.P; k += tc::kEpiThreads) {
+            const float y = fmaf(Hf, P1[k] + Pmid[k], -mu_comp[k]);
+            const float tsum = mu_acc[k] + y;
+            mu_comp[k] = (tsum - mu_acc[k]) - y;
+            mu_acc[k] = tsum;
+          }
+          tc::epi_bar();
+          const int tmp = iP1;
+          iP1 = iP7;
+          iP7 = tmp;
+          ++nacc;
+          cur ^= 1;
+          swp = !swp;
+          t = clipped ? t_lo : t - H;
+          if (q >= 1.0 && q <= 1.0) q = 1.0;
+          qold = fmax(eest, kQoldInit);
+          dt = fmin(H / q, a.dtmax);
+        } else {
+          ++nrej;
+          dt = H / fmin(1.0 / kQmin, q11 / kGamma);
+        }
+      }
+      if (!ok || ret != GBNDE_RET_SUCCESS) break;
+      // ---- jump at t_lo ----
+      if (iv.nsave_lo > 0) {
+        for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+          if (!valid(tile)) continue;
+          float v[32];
+          ld32(a.lam[cur] + gofs(tile), th.nmine, vec, v);
+          for (int qq = 0; qq < iv.nsave_lo; ++qq) {
+            float d[32];
+            ld32(a.dLdu + (size_t)(iv.save_lo + qq) * SB + gofs(tile), th.nmine, vec, d);
+            for (int i = 0; i < 32; ++i) v[i] += d[i];
+          }
+          st32(a.lam[cur] + gofs(tile), th.nmine, vec, v);
+        }
+      }
+    }
+    if (!ok && ret == GBNDE_RET_SUCCESS) ret = GBNDE_RET_BARRIER_TIMEOUT;
+    if (ret == GBNDE_RET_SUCCESS) {
+      for (int tile = blockIdx.x; tile < a.ntiles; tile += G)
+        if (valid(tile)) {
+          float v[32];
+          ld32(a.lam[cur] + gofs(tile), th.nmine, vec, v);
+          st32(a.dLdu0 + gofs(tile), th.nmine, vec, v);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.counters[CT_NF] = nf_adj;
+      a.counters[CT_NACCEPT] = nacc;
+      a.counters[CT_NREJECT] = nrej;
+      a.counters[CT_NRECOMP] = 0;
+      const int e = ((volatile int*)&sh.err)[0];
+      a.status[ST_RETCODE] = (a.status[ST_BARRIER] != 0 || e != 0) ? GBNDE_RET_BARRIER_TIMEOUT : ret;
+      if (e) a.status[2] = e;
+    }
+    tc::epi_bar();
+    if (threadIdx.x == 0) ((volatile int*)&sh.stop)[0] = 1;
+  }
+  __syncthreads();
+  tc::tc_fence_after();
+  if (warp == tc::kMmaWarp) tc::tmem_dealloc(sh.tmem_base, 512);
+}
+
+// dLdp[i] = sum over CTAs of (mu_acc - mu_comp), FP64 accumulation in CTA order.
+__global__ void reduce_mu_comp_kernel(const float* __restrict__ acc, const float* __restrict__ comp,
+                                      int nblk, int P, float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += (double)acc[(size_t)b * P + i] - (double)comp[(size_t)b * P + i];
+  out[i] = (float)s;
+}
+
+int launch_bwd_tc(const BwdTcArgs& a, int grid, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       tc::kSmemBytes);
+  if (e != cudaSuccess) return -1;
+  void* args[] = {(void*)&a};
+  e = cudaLaunchCooperativeKernel((const void*)bwd_tc_kernel, dim3(grid), dim3(tc::kThreads), args,
+                                  tc::kSmemBytes, st);
+  return e == cudaSuccess ? 0 : -1;
+}
+
+int launch_reduce_mu_comp(const float* acc, const float* comp, int nblk, int P, float* out, cudaStream_t st) {
+  reduce_mu_comp_kernel<<<(P + 255) / 256, 256, 0, st>>>(acc, comp, nblk, P, out);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace gbnde

@@ -16,19 +16,10 @@
 // Dense stage storage: with `dense` set, accepted step n keeps (u_n, k1..k7)
 // in slot n -- the forward dense output the InterpolatingAdjoint backward
 // interpolates, so no recompute is needed.
-#include "tc_engine.cuh"
+#include "tc_args.h"
 
 namespace gbnde {
 
-struct FwdTcArgs {
-  FwdArgs f;
-  tc::OpList ops;
-  const float* bias[GBNDE_MAX_LAYERS];
-  float* comp[2];       // compensation of the state (ping-pong with ubuf)
-  float* dense;         // slots of 8 x S*B floats: u_n, k1..k7 (or null)
-  long long dense_slots;
-  float* kring;         // 7 x S*B stage buffers when dense == null
-};
 
 namespace {
 
@@ -166,7 +157,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
   if (warp == tc::kMmaWarp) {
     tc::mma_loop(A.ops, sh, aring, wring);
   } else if (warp == tc::kTmaWarp) {
-    tc::tma_loop(A.ops, sh, wring);
+    tc::tma_loop(A.ops, sh, aring, wring);
   } else {
     // ======================= epilogue warps =======================
     const int S = a.S, G = gridDim.x;

@@ -1,0 +1,43 @@
+// tc_args.h -- launch descriptors of the tensor-core (BF16-form) solver kernels,
+// shared by the kernels and the host API.
+#pragma once
+#include "tc_engine.cuh"
+
+namespace gbnde {
+
+struct FwdTcArgs {
+  FwdArgs f;
+  tc::OpList ops;
+  const float* bias[GBNDE_MAX_LAYERS];
+  float* comp[2];       // compensation of the state (ping-pong with ubuf)
+  float* dense;         // slots of 8 x S*B floats: u_n, k1..k7 (or null)
+  long long dense_slots;
+  float* kring;         // 7 x S*B stage buffers when dense == null
+};
+
+
+struct BwdTcArgs {
+  BwdArgs b;
+  tc::OpList ops;
+  const float* bias[GBNDE_MAX_LAYERS];
+  float* lam_comp[2];           // compensation of lam
+  float* mu_comp;               // [grid][P] Kahan compensation of mu_acc
+  float* hscr;                  // [grid][256][hvals] hidden activations (fp32), thread-private
+  int hvals;                    // values per thread in hscr
+  int hoff[GBNDE_MAX_LAYERS];   // offset of hidden layer l (1..L-1) inside a thread's hscr
+  uint8_t* img;                 // [grid][img_cta] weight-gradient operand images
+  size_t img_cta;
+  long long aoff[GBNDE_MAX_LAYERS];  // image offset of a_l (l = 0..L-1)
+  long long doff[GBNDE_MAX_LAYERS];  // image offset of delta_{l+1} (l = 0..L-1)
+  int a_isA[GBNDE_MAX_LAYERS];       // 1: a_l is the A operand (rows = in) of layer l's dW
+  int nh[GBNDE_MAX_LAYERS];          // M halves (128 rows) of layer l's dW
+  float* bpart;                 // [grid][4][nbias] bias partial sums
+  int nbias;
+  int boffp[GBNDE_MAX_LAYERS];  // offset of layer l's bias inside bpart rows
+};
+
+
+int launch_bwd_tc(const BwdTcArgs& a, int grid, cudaStream_t st);
+int launch_reduce_mu_comp(const float* acc, const float* comp, int nblk, int P, float* out, cudaStream_t st);
+
+}  // namespace gbnde

@@ -29,12 +29,25 @@ constexpr int kWSlotBytes = 2 * 32768;   // 2 pieces x 256 rows x 128 B
 constexpr int kARing = 2;
 constexpr int kWRing = 2;
 constexpr int kSmemBytes = 1024 + kARing * kASlotBytes + kWRing * kWSlotBytes;
-constexpr int kMaxOps = 8;
+constexpr int kMaxOps = 40;
 
+// kind 0 (chain GEMM): A chunks written by the epilogue (3 pieces, K-major),
+//   B = weight image chunks (2 pieces, K-major), five split products.
+// kind 1 (weight-gradient GEMM, K = trajectories): A and B both bulk-copied
+//   from per-CTA images (2 pieces, MN-major 64-column blocks), three products
+//   hi.hi + hi.lo + lo.hi.
 struct GemmOp {
-  const uint8_t* wimg;  // weight image: nchunk x 2 pieces x npad rows x 128 B
+  const uint8_t* wimg;  // kind 0: weight image; kind 1: B image base of CTA 0
+  const uint8_t* aimg;  // kind 1: A image base of CTA 0
+  size_t cta_stride;    // kind 1: bytes between consecutive CTAs' images
+  uint32_t a_bytes;     // kind 1: bytes of one A chunk
+  uint32_t a_step;      // kind 1: bytes between consecutive A chunks
+  uint32_t b_step;      // kind 1: bytes between consecutive B chunks
   int npad;             // N rounded up to 16 (<= 256)
   int nchunk;           // K / 64 (rounded up)
+  int kind;
+  int nblk_b;           // kind 1: 64-column blocks in a B chunk
+  int first_dw;         // kind 1: first weight-gradient op of an evaluation (waits for images)
 };
 
 struct OpList {
@@ -46,6 +59,7 @@ struct Shared {
   uint64_t a_full[kARing], a_empty[kARing];
   uint64_t w_full[kWRing], w_empty[kWRing];
   uint64_t acc_full[2], acc_empty[2];
+  uint64_t img_ready;
   uint32_t tmem_base;
   int stop;
   int err;
@@ -82,6 +96,7 @@ __device__ __forceinline__ void init_shared(Shared& sh) {
       mbar_init(&sh.acc_full[i], 1);
       mbar_init(&sh.acc_empty[i], kEpiThreads);
     }
+    mbar_init(&sh.img_ready, kEpiThreads);
     sh.stop = 0;
     sh.err = 0;
     fence_mbar_init();
@@ -113,8 +128,8 @@ __device__ __forceinline__ void mma_loop(const OpList& ops, Shared& sh, uint8_t*
       }
     }
     const uint32_t d = sh.tmem_base + (uint32_t)(reg * 256);
-    const uint32_t idesc = idesc_bf16(128, op.npad);
-    const uint32_t wpiece = (uint32_t)op.npad * 128;
+    const uint32_t idesc = op.kind == 0 ? idesc_bf16(128, op.npad) : idesc_bf16_mn(128, op.npad);
+    const uint32_t wpiece = op.kind == 0 ? (uint32_t)op.npad * 128 : (uint32_t)op.nblk_b * 8192;
     for (int c = 0; c < op.nchunk; ++c) {
       // A chunk ready? (bounded by the stop flag: the epilogue may be done)
       {
@@ -130,13 +145,28 @@ __device__ __forceinline__ void mma_loop(const OpList& ops, Shared& sh, uint8_t*
       if (leader) {
         const uint32_t a0 = smem_u32(aring + aslot * kASlotBytes);
         const uint32_t b0 = smem_u32(wring + wslot * kWSlotBytes);
+        if (op.kind == 0) {
 #pragma unroll
-        for (int pr = 0; pr < 5; ++pr) {
+          for (int pr = 0; pr < 5; ++pr) {
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            const uint64_t ad = sdesc_sw128(a0 + pa[pr] * 16384 + kk * 32);
-            const uint64_t bd = sdesc_sw128(b0 + pb[pr] * wpiece + kk * 32);
-            mma_bf16(d, ad, bd, idesc, (c > 0 || pr > 0 || kk > 0) ? 1u : 0u);
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint64_t ad = sdesc_sw128(a0 + pa[pr] * 16384 + kk * 32);
+              const uint64_t bd = sdesc_sw128(b0 + pb[pr] * wpiece + kk * 32);
+              mma_bf16(d, ad, bd, idesc, (c > 0 || pr > 0 || kk > 0) ? 1u : 0u);
+            }
+          }
+        } else {
+          // A chunk: 2 pieces x 2 blocks x 8 KB; B chunk: 2 pieces x nblk x 8 KB.
+          // Products hi.hi, hi.lo, lo.hi; K step of 16 trajectories = 2048 bytes.
+#pragma unroll
+          for (int pr = 0; pr < 3; ++pr) {
+            const int qa = (pr == 2) ? 1 : 0, qb = (pr == 1) ? 1 : 0;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint64_t ad = sdesc_sw128_mn(a0 + qa * 16384 + kk * 2048, 8192);
+              const uint64_t bd = sdesc_sw128_mn(b0 + qb * wpiece + kk * 2048, 8192);
+              mma_bf16(d, ad, bd, idesc, (c > 0 || pr > 0 || kk > 0) ? 1u : 0u);
+            }
           }
         }
         mma_commit(&sh.a_empty[aslot]);
@@ -152,43 +182,71 @@ __device__ __forceinline__ void mma_loop(const OpList& ops, Shared& sh, uint8_t*
   }
 }
 
-// ---- weight producer warp -------------------------------------------------------------
-__device__ __forceinline__ void tma_loop(const OpList& ops, Shared& sh, uint8_t* wring) {
+// ---- producer warp ---------------------------------------------------------------------
+// Streams the B chunks of every op (weight images, or weight-gradient B
+// images) into the W ring and, for weight-gradient ops, their A chunks into
+// the A ring (those slots are completed by one arrive of 256 counts plus the
+// transaction bytes, so the ring keeps one protocol with the epilogue).
+// The A ring position advances over the epilogue-written chunks as well.
+__device__ __forceinline__ void tma_loop(const OpList& ops, Shared& sh, uint8_t* aring,
+                                         uint8_t* wring) {
   volatile int* verr = &sh.err;
   volatile int* vstop = &sh.stop;
   const bool leader = (threadIdx.x & 31) == 0;
-  int wslot = 0;
-  uint32_t wph = 0;
+  int wslot = 0, aslot = 0;
+  uint32_t wph = 0, aph = 0, img_phase = 0;
   long long g = 0;
-  uint32_t issued[kWRing] = {0, 0};  // copies issued per slot
-  while (!*vstop && !*verr) {
+  uint32_t issued_w[kWRing] = {0, 0};
+  uint32_t issued_a[kARing] = {0, 0};
+  auto wait_or_stop = [&](uint64_t* bar, uint32_t par) -> bool {
+    while (true) {
+      if (mbar_try_wait(bar, par)) return true;
+      if (*vstop || *verr) return false;
+    }
+  };
+  bool run = true;
+  while (run && !*vstop && !*verr) {
     const GemmOp& op = ops.op[g % ops.nops];
-    const uint32_t bytes = 2u * (uint32_t)op.npad * 128u;
+    const uint32_t bbytes = op.kind == 0 ? 2u * (uint32_t)op.npad * 128u : 2u * (uint32_t)op.nblk_b * 8192u;
+    const uint8_t* bbase = op.kind == 0 ? op.wimg : op.wimg + (size_t)blockIdx.x * op.cta_stride;
+    const uint8_t* abase = op.kind == 0 ? nullptr : op.aimg + (size_t)blockIdx.x * op.cta_stride;
+    if (op.kind == 1 && op.first_dw) {
+      if (!wait_or_stop(&sh.img_ready, img_phase)) break;
+      img_phase ^= 1;
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+    }
     for (int c = 0; c < op.nchunk; ++c) {
-      // wait for the slot to be consumed (phase parity of its previous use)
-      const uint32_t par = wph ^ 1;
-      bool go = false;
-      while (true) {
-        if (mbar_try_wait(&sh.w_empty[wslot], par)) { go = true; break; }
-        if (*vstop || *verr) break;
+      if (op.kind == 1) {
+        if (!wait_or_stop(&sh.a_empty[aslot], aph ^ 1)) { run = false; break; }
+        if (leader) {
+          mbar_arrive_expect_tx(&sh.a_full[aslot], op.a_bytes);
+          asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                           smem_u32(&sh.a_full[aslot])),
+                       "r"(kEpiThreads - 1)
+                       : "memory");
+          bulk_g2s(aring + aslot * kASlotBytes, abase + (size_t)c * op.a_step, op.a_bytes, &sh.a_full[aslot]);
+        }
+        __syncwarp();
+        issued_a[aslot] += 1;
       }
-      if (!go) break;
+      if (++aslot == kARing) { aslot = 0; aph ^= 1; }
+      if (!wait_or_stop(&sh.w_empty[wslot], wph ^ 1)) { run = false; break; }
       if (leader) {
-        mbar_arrive_expect_tx(&sh.w_full[wslot], bytes);
-        bulk_g2s(wring + wslot * kWSlotBytes, op.wimg + (size_t)c * bytes, bytes, &sh.w_full[wslot]);
+        mbar_arrive_expect_tx(&sh.w_full[wslot], bbytes);
+        const uint8_t* src = op.kind == 0 ? bbase + (size_t)c * bbytes : bbase + (size_t)c * op.b_step;
+        bulk_g2s(wring + wslot * kWSlotBytes, src, bbytes, &sh.w_full[wslot]);
       }
       __syncwarp();
-      issued[wslot] += 1;
+      issued_w[wslot] += 1;
       if (++wslot == kWRing) { wslot = 0; wph ^= 1; }
     }
     ++g;
   }
   // drain: every issued copy must have landed before the CTA exits
   for (int s = 0; s < kWRing; ++s) {
-    if (issued[s] == 0) continue;
-    const uint32_t last_par = (issued[s] - 1) & 1;
+    if (issued_w[s] == 0) continue;
     const unsigned long long t0 = globaltimer_ns();
-    while (!mbar_try_wait(&sh.w_full[s], last_par)) {
+    while (!mbar_try_wait(&sh.w_full[s], (issued_w[s] - 1) & 1)) {
       if (globaltimer_ns() - t0 > kWaitTimeoutNs) { *verr = 3; break; }
     }
   }
@@ -230,6 +288,12 @@ __device__ __forceinline__ bool epi_write_a(EpiState& e, Shared& sh, uint8_t* ar
   mbar_arrive(&sh.a_full[e.aslot]);
   if (++e.aslot == kARing) { e.aslot = 0; e.aph ^= 1; }
   return true;
+}
+
+// Skip A-ring slots that the producer warp fills (weight-gradient ops).
+__device__ __forceinline__ void epi_skip_a(EpiState& e, int n) {
+  for (int i = 0; i < n; ++i)
+    if (++e.aslot == kARing) { e.aslot = 0; e.aph ^= 1; }
 }
 
 // Wait for the accumulator of the next op; returns its TMEM column base.

@@ -144,12 +144,105 @@ __global__ void __launch_bounds__(256, 1) tc_selftest_kernel(const float* __rest
   if (tid == 0) *err = s_err;
 }
 
+// ---- self-test of MN-major operands (the weight-gradient products) -----------------
+// D[128 x N] = G^T A where G is [128 (K) x 128 (M)] and A is [128 (K) x N],
+// both stored trajectory-major: per 64-wide K chunk, per piece, MN blocks of
+// 64 columns (64 rows x 128 B each, SW128). Products: hi.hi + hi.lo + lo.hi.
+__global__ void __launch_bounds__(256, 1) tc_selftest_mn_kernel(const float* __restrict__ G,
+                                                                const float* __restrict__ A, int N,
+                                                                float* __restrict__ D, int* err) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int nbA = 2, nbB = N / 64;
+  uint8_t* sA = smem;                       // 2 pieces x nbA blocks x 8 KB
+  uint8_t* sB = smem + 2 * nbA * 8192;      // 2 pieces x nbB blocks x 8 KB
+  __shared__ uint64_t bar_mma;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_err;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    s_err = 0;
+    tc::mbar_init(&bar_mma, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, 256);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  volatile int* verr = &s_err;
+  for (int kc = 0; kc < 2; ++kc) {
+    // rows k in [64kc, 64kc+64): thread -> (row, 16-byte group)
+    for (int idx = tid; idx < 64 * (128 / 8); idx += 256) {
+      const int r = idx / 16, j = idx % 16;  // j: 16-byte group across 128 columns
+      float x[8];
+      for (int e = 0; e < 8; ++e) x[e] = G[(size_t)(64 * kc + r) * 128 + 8 * j + e];
+      uint4 hi = tc::pack8_bf16(x);
+      const __nv_bfloat16* hb = reinterpret_cast<const __nv_bfloat16*>(&hi);
+      float rr[8];
+      for (int e = 0; e < 8; ++e) rr[e] = x[e] - __bfloat162float(hb[e]);
+      uint4 lo = tc::pack8_bf16(rr);
+      const int blk = j / 8, jj = j % 8;
+      const uint32_t off = blk * 8192 + tc::sw128_offset(r, jj);
+      *reinterpret_cast<uint4*>(sA + off) = hi;
+      *reinterpret_cast<uint4*>(sA + nbA * 8192 + off) = lo;
+    }
+    for (int idx = tid; idx < 64 * (N / 8); idx += 256) {
+      const int r = idx / (N / 8), j = idx % (N / 8);
+      float x[8];
+      for (int e = 0; e < 8; ++e) x[e] = A[(size_t)(64 * kc + r) * N + 8 * j + e];
+      uint4 hi = tc::pack8_bf16(x);
+      const __nv_bfloat16* hb = reinterpret_cast<const __nv_bfloat16*>(&hi);
+      float rr[8];
+      for (int e = 0; e < 8; ++e) rr[e] = x[e] - __bfloat162float(hb[e]);
+      uint4 lo = tc::pack8_bf16(rr);
+      const int blk = j / 8, jj = j % 8;
+      const uint32_t off = blk * 8192 + tc::sw128_offset(r, jj);
+      *reinterpret_cast<uint4*>(sB + off) = hi;
+      *reinterpret_cast<uint4*>(sB + nbB * 8192 + off) = lo;
+    }
+    tc::fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::tc_fence_after();
+      const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB);
+      const uint32_t idesc = tc::idesc_bf16_mn(128, N);
+      const int pa[3] = {0, 0, 1};
+      const int pb[3] = {0, 1, 0};
+      for (int pr = 0; pr < 3; ++pr)
+        for (int kk = 0; kk < 4; ++kk) {
+          const uint64_t ad = tc::sdesc_sw128_mn(a0 + pa[pr] * nbA * 8192 + kk * 2048, 8192);
+          const uint64_t bd = tc::sdesc_sw128_mn(b0 + pb[pr] * nbB * 8192 + kk * 2048, 8192);
+          tc::mma_bf16(tmem, ad, bd, idesc, (kc > 0 || pr > 0 || kk > 0) ? 1u : 0u);
+        }
+      tc::mma_commit(&bar_mma);
+    }
+    __syncthreads();
+    tc::mbar_wait(&bar_mma, kc & 1, verr);
+    tc::tc_fence_after();
+    __syncthreads();
+  }
+  if (warp < 4 && !*verr) {
+    for (int cb = 0; cb < N; cb += 32) {
+      float v[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb, v);
+      const int r = warp * 32 + lane;
+      for (int i = 0; i < 32; ++i) D[(size_t)r * N + cb + i] = v[i];
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 256);
+  if (tid == 0) *err = s_err;
+}
+
 }  // namespace gbnde
 
 extern "C" int gbnde_tc_selftest(const float* A, const float* W, int N, int K, int mode, float* D) {
   using namespace gbnde;
-  if (!A || !W || !D || (N != 64 && N != 128 && N != 256) || K < 1 || K > 1024 || (mode != 0 && mode != 1))
+  if (!A || !W || !D || (N != 64 && N != 128 && N != 256) || K < 1 || K > 1024 || mode < 0 || mode > 2)
     return GBNDE_ERR_INVALID;
+  if (mode == 2 && K != 128) return GBNDE_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
@@ -170,9 +263,16 @@ extern "C" int gbnde_tc_selftest(const float* A, const float* W, int N, int K, i
     cudaMemcpy(dW, W, (size_t)N * K * 4, cudaMemcpyHostToDevice);
     cudaMemset(derr, 0, 4);
     cudaMemset(dD, 0, 128 * (size_t)N * 4);
-    launch_prep_weight_image(dW, N, K, N, img, 0);
-    cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    tc_selftest_kernel<<<1, 256, smem>>>(dA, img, N, K, mode, dD, derr);
+    if (mode == 2) {
+      // A: K x 128 (rows k, columns m), W: K x N
+      const size_t smem2 = 1024 + 2 * 2 * 8192 + 2 * (size_t)(N / 64) * 8192;
+      cudaFuncSetAttribute(tc_selftest_mn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+      tc_selftest_mn_kernel<<<1, 256, smem2>>>(dA, dW, N, dD, derr);
+    } else {
+      launch_prep_weight_image(dW, N, K, N, img, 0);
+      cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      tc_selftest_kernel<<<1, 256, smem>>>(dA, img, N, K, mode, dD, derr);
+    }
     int herr = 0;
     if (cudaDeviceSynchronize() != cudaSuccess) {
       rc = GBNDE_ERR_CUDA;

@@ -117,12 +117,31 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   return d;
 }
 
+// Shared-memory matrix descriptor: MN-major, SWIZZLE_128B. The operand is
+// stored as blocks of 64 MN-elements (128-byte rows, one row per K index,
+// 8-row swizzle atoms 1024 bytes apart = SBO); consecutive 64-element MN
+// blocks are `lbo` bytes apart.
+__device__ __forceinline__ uint64_t sdesc_sw128_mn(uint32_t saddr, uint32_t lbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;    // leading byte offset: next 64-element MN block
+  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset: next 8 K-rows
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
 // Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4)                 // D format F32
          | (1u << 7)               // A format BF16
          | (1u << 10)              // B format BF16
          | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Same with both operands MN-major (transpose bits for A and B).
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int M, int N) {
+  return idesc_bf16(M, N) | (1u << 15) | (1u << 16);
 }
 
 // ---- MMA --------------------------------------------------------------------------

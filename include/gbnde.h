@@ -177,7 +177,9 @@ int gbnde_last_kernel_ms(gbnde_ctx* ctx, double* fwd_ms, double* bwd_ms);
  * D[128 x N] = A[128 x K] * W[N x K]^T (host arrays, row-major) through bulk
  * copied SW128 weight images, tcgen05.mma into tensor memory and tcgen05.ld.
  * mode 0: one BF16 product; mode 1: the five split-BF16 products of the BF16
- * form. N in {64, 128, 256}, K <= 1024. No reference counterpart (diagnostic). */
+ * form. N in {64, 128, 256}, K <= 1024. mode 2: the MN-major weight-gradient
+ * form, D = A^T W with A of K x 128 and W of K x N (K = 128), three products.
+ * No reference counterpart (diagnostic). */
 int gbnde_tc_selftest(const float* A, const float* W, int N, int K, int mode, float* D);
 
 const char* gbnde_strerror(int code);

@@ -42,3 +42,22 @@ def test_tc_gemm_single_and_split(lib, N, K):
     assert np.abs(D1 - emul).max() / scale < 1e-5
     # and within the 16-bit weight truncation of the FP64 product
     assert np.abs(D1 - ref).max() / scale < 2e-5
+
+
+@pytest.mark.parametrize("N", [64, 256])
+def test_tc_gemm_mn_major_weight_gradient_form(lib, N):
+    """D = G^T A with both operands stored trajectory-major (MN-major for the MMA),
+    the layout of the weight-gradient products of the adjoint."""
+    rng = np.random.default_rng(N)
+    G = rng.standard_normal((128, 128)).astype(np.float32)
+    A = rng.standard_normal((128, N)).astype(np.float32)
+    fp = C.POINTER(C.c_float)
+    D = np.zeros((128, N), np.float32)
+    assert lib.gbnde_tc_selftest(G.ctypes.data_as(fp), A.ctypes.data_as(fp), N, 128, 2, D.ctypes.data_as(fp)) == 0
+    Gh = _bf16(G); Gl = _bf16(G - Gh)
+    Ah = _bf16(A); Al = _bf16(A - Ah)
+    emul = Gh.T @ Ah + Gh.T @ Al + Gl.T @ Ah
+    ref = G.astype(np.float64).T @ A.astype(np.float64)
+    scale = np.abs(ref).max()
+    assert np.abs(D - emul).max() / scale < 1e-5
+    assert np.abs(D - ref).max() / scale < 3e-5
