@@ -335,7 +335,7 @@ def run_gpu(args):
                    "sensealg": "InterpolatingAdjoint", "loss": "MSE", "precision": args.precision,
                    "l2": "flushed between steps (256 MB write)", "parallelism": "replicas"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": args.steps * 5,
+        "gpu_launches": args.steps * 4,
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk,

@@ -103,6 +103,8 @@ struct gbnde_ctx {
   std::vector<int> ckstep;
   long long naccept = 0;
   long long nattempt = 0;
+  long long last_naccept = 0;
+  bool rerun_guard = false;
   int final_cur = 0;
   int fwd_retcode = 0;
   const float* usave_dev = nullptr;  // saved states of the last forward (device)
@@ -379,26 +381,29 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   int r = 0;
   // dense stage storage: one slot (u_n, k1..k7) per accepted step, within a
   // quarter of the free device memory
-  {
-    size_t freeb = 0, totb = 0;
-    cudaMemGetInfo(&freeb, &totb);
-    const size_t slot = 8 * SB * sizeof(float);
-    long long want = std::min<long long>(maxiters + 1, 4096);
+  // dense stage storage: one slot (u_n, k1..k7) per accepted step. Sized from
+  // the step count of the previous solve (at least 64 slots), within a
+  // quarter of the free device memory; grows only when a solve needs more.
+  const size_t slot = 8 * SB * sizeof(float);
+  auto size_dense = [&](long long want) {
+    want = std::min<long long>(std::max<long long>(want, 64), maxiters + 1);
     const long long have_now = (long long)(c->dense.n / slot);
-    const long long budget = (long long)((freeb / 4) / slot) + have_now;
-    long long ns = std::min(want, budget);
-    if (ns < 2) ns = 0;
-    if (ns > have_now && have_now < std::min<long long>(want, 64)) {
-      // grow to the smaller of what is wanted and a first chunk of 64 steps,
-      // then on later calls by doubling
-      ns = std::min(ns, std::max<long long>(64, 2 * have_now));
+    if (want > have_now) {
+      size_t freeb = 0, totb = 0;
+      cudaMemGetInfo(&freeb, &totb);
+      const long long budget = (long long)((freeb / 4) / slot) + have_now;
+      long long ns = std::min(want, budget);
+      if (ns > have_now) {
+        c->dense.release();
+        if (ns >= 2 && c->dense.ensure((size_t)ns * slot)) {
+          cudaGetLastError();
+          c->dense.release();
+        }
+      }
     }
-    if (ns > 0 && (r = c->dense.ensure((size_t)ns * slot))) {
-      cudaGetLastError();
-      ns = 0;
-    }
-    c->dense_slots = ns > 0 ? (long long)(c->dense.n / slot) : 0;
-  }
+    c->dense_slots = (long long)(c->dense.n / slot);
+  };
+  size_dense(2 * c->last_naccept + 8);
   if (tcform && (r = c->comp.ensure(2 * SB * 4))) return r;
   if (u0_host && (r = c->u0.ensure(SB * 4))) return r;
   if ((r = c->ubuf.ensure(2 * SB * 4)) || (r = c->kbuf.ensure(7 * SB * 4))) return r;
@@ -533,6 +538,15 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   c->saveat.assign(d->saveat, d->saveat + nsave);
   c->have_fwd = (status[ST_RETCODE] == GBNDE_RET_SUCCESS) && nacc <= maxsteps;
   c->dense_valid = c->dense_slots > 0 && nacc < c->dense_slots;
+  c->last_naccept = nacc;
+  if (c->have_fwd && !c->dense_valid && !c->rerun_guard) {
+    // the solve outgrew the dense stage storage: grow it and solve again once
+    // (the backward then interpolates the stored stages instead of recomputing)
+    c->rerun_guard = true;
+    const int rr = forward_impl(c, d, S, B, u0, u0_host, usave, usave_host, stats);
+    c->rerun_guard = false;
+    return rr;
+  }
   c->usave_dev = usd;
   return 0;
 }
@@ -639,6 +653,12 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
       (r = c->tmucomp.ensure((size_t)grid * P * 4)) || (r = c->tlamcomp.ensure(2 * SB * 4)) ||
       (r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4)))
     return r;
+  // per-CTA quadrature slots padded to a multiple of 4 floats (float4 sweeps)
+  const int Ppad = (P + 3) / 4 * 4;
+  t.b.P = Ppad;
+  if ((r = c->mu_acc.ensure((size_t)grid * Ppad * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * Ppad * 4)) ||
+      (r = c->tmucomp.ensure((size_t)grid * Ppad * 4)))
+    return r;
   t.b.mu_acc = c->mu_acc.as<float>();
   t.b.mu_stage = c->mu_stage.as<float>();
   t.img = c->timg.as<uint8_t>();
@@ -696,7 +716,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
     return fail(GBNDE_ERR_CUDA, "backward (tc) launch failed: %s", cudaGetErrorString(e));
   }
   CK(cudaEventRecord(c->ev[3], st));
-  if (launch_reduce_mu_comp(t.b.mu_acc, t.mu_comp, grid, P, dp_d, st))
+  if (launch_reduce_mu_comp(t.b.mu_acc, t.mu_comp, grid, Ppad, P, dp_d, st))
     return fail(GBNDE_ERR_CUDA, "reduce launch failed");
   return 0;
 }

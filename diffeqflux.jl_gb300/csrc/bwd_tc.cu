@@ -226,8 +226,10 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     };
     auto gofs = [&](int tile) -> size_t { return ((size_t)tile * 128 + th.r) * S + 32 * th.ch; };
     auto valid = [&](int tile) -> bool { return tile * 128 + th.r < a.B && th.nmine > 0; };
+    // P is a multiple of 4 floats per CTA slot (the host pads it)
     auto zero_cta = [&](float* p) {
-      for (size_t i = threadIdx.x; i < (size_t)a.P; i += tc::kEpiThreads) p[i] = 0.f;
+      float4* p4 = reinterpret_cast<float4*>(p);
+      for (size_t i = threadIdx.x; i < (size_t)a.P / 4; i += tc::kEpiThreads) p4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     };
 
     // scratch images start at zero (padding rows/blocks are never written)
@@ -345,18 +347,43 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           if (!tc::epi_wait_acc(es, sh, &col)) return false;
           if (P) {
             const int mrow = 128 * hh + th.r;  // M-side feature of this lane
+            const int isA = A.a_isA[l];
+            float* __restrict__ Pw = P + m.woff[l];
             for (int cc = 0; cc < (Nn2 + 63) / 64; ++cc) {
               const int n0 = 64 * cc + 32 * th.ch;
               tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+              // all loads first, then the stores (independent addresses)
+              float pv[32];
+              if (isA) {
+                // row mrow = in feature; 32 consecutive out features
+                const bool full = mrow < in && n0 + 32 <= out && (out % 4 == 0);
+                float* rowp = Pw + (size_t)mrow * out + n0;
+                if (full) {
 #pragma unroll
-              for (int i = 0; i < 32; ++i) {
-                const int nn = n0 + i;
-                const int o = A.a_isA[l] ? nn : mrow;
-                const int ii = A.a_isA[l] ? mrow : nn;
-                if (o < out && ii < in) {
-                  float* pp = P + m.woff[l] + (size_t)ii * out + o;
-                  *pp = fmaf(c, v[i], *pp);
+                  for (int i = 0; i < 32; i += 4) {
+                    const float4 q4 = *reinterpret_cast<const float4*>(rowp + i);
+                    pv[i] = q4.x; pv[i + 1] = q4.y; pv[i + 2] = q4.z; pv[i + 3] = q4.w;
+                  }
+#pragma unroll
+                  for (int i = 0; i < 32; i += 4)
+                    *reinterpret_cast<float4*>(rowp + i) =
+                        make_float4(fmaf(c, v[i], pv[i]), fmaf(c, v[i + 1], pv[i + 1]),
+                                    fmaf(c, v[i + 2], pv[i + 2]), fmaf(c, v[i + 3], pv[i + 3]));
+                } else if (mrow < in) {
+#pragma unroll
+                  for (int i = 0; i < 32; ++i) pv[i] = (n0 + i < out) ? rowp[i] : 0.f;
+#pragma unroll
+                  for (int i = 0; i < 32; ++i)
+                    if (n0 + i < out) rowp[i] = fmaf(c, v[i], pv[i]);
                 }
+              } else if (mrow < out) {
+                // row mrow = out feature; in features n0.. at stride `out`
+                float* colp = Pw + (size_t)n0 * out + mrow;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) pv[i] = (n0 + i < in) ? colp[(size_t)i * out] : 0.f;
+#pragma unroll
+                for (int i = 0; i < 32; ++i)
+                  if (n0 + i < in) colp[(size_t)i * out] = fmaf(c, v[i], pv[i]);
               }
             }
           }
@@ -588,12 +615,25 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         if (eest <= 1.0) {
           // mu += H (P1 + Pmid), Kahan-compensated per CTA
           const float Hf = (float)H;
-          const float* P1 = Pb[iP1];
-          for (size_t k = threadIdx.x; k < (size_t)a.P; k += tc::kEpiThreads) {
-            const float y = fmaf(Hf, P1[k] + Pmid[k], -mu_comp[k]);
-            const float tsum = mu_acc[k] + y;
-            mu_comp[k] = (tsum - mu_acc[k]) - y;
-            mu_acc[k] = tsum;
+          const float4* P1 = reinterpret_cast<const float4*>(Pb[iP1]);
+          const float4* Pm = reinterpret_cast<const float4*>(Pmid);
+          float4* acc4 = reinterpret_cast<float4*>(mu_acc);
+          float4* cmp4 = reinterpret_cast<float4*>(mu_comp);
+          for (size_t k = threadIdx.x; k < (size_t)a.P / 4; k += tc::kEpiThreads) {
+            const float4 p1 = P1[k], pm = Pm[k], cm = cmp4[k], ac = acc4[k];
+            float4 na, nc;
+            auto kahan = [&](float p1v, float pmv, float cmv, float acv, float& nav, float& ncv) {
+              const float y = fmaf(Hf, p1v + pmv, -cmv);
+              const float tsum = acv + y;
+              ncv = (tsum - acv) - y;
+              nav = tsum;
+            };
+            kahan(p1.x, pm.x, cm.x, ac.x, na.x, nc.x);
+            kahan(p1.y, pm.y, cm.y, ac.y, na.y, nc.y);
+            kahan(p1.z, pm.z, cm.z, ac.z, na.z, nc.z);
+            kahan(p1.w, pm.w, cm.w, ac.w, na.w, nc.w);
+            acc4[k] = na;
+            cmp4[k] = nc;
           }
           tc::epi_bar();
           const int tmp = iP1;
@@ -654,12 +694,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
 }
 
 // dLdp[i] = sum over CTAs of (mu_acc - mu_comp), FP64 accumulation in CTA order.
+// Per-CTA slots are `stride` floats apart; `P` parameters are written.
 __global__ void reduce_mu_comp_kernel(const float* __restrict__ acc, const float* __restrict__ comp,
-                                      int nblk, int P, float* __restrict__ out) {
+                                      int nblk, int stride, int P, float* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P) return;
   double s = 0.0;
-  for (int b = 0; b < nblk; ++b) s += (double)acc[(size_t)b * P + i] - (double)comp[(size_t)b * P + i];
+  for (int b = 0; b < nblk; ++b)
+    s += (double)acc[(size_t)b * stride + i] - (double)comp[(size_t)b * stride + i];
   out[i] = (float)s;
 }
 
@@ -673,8 +715,9 @@ int launch_bwd_tc(const BwdTcArgs& a, int grid, cudaStream_t st) {
   return e == cudaSuccess ? 0 : -1;
 }
 
-int launch_reduce_mu_comp(const float* acc, const float* comp, int nblk, int P, float* out, cudaStream_t st) {
-  reduce_mu_comp_kernel<<<(P + 255) / 256, 256, 0, st>>>(acc, comp, nblk, P, out);
+int launch_reduce_mu_comp(const float* acc, const float* comp, int nblk, int stride, int P, float* out,
+                          cudaStream_t st) {
+  reduce_mu_comp_kernel<<<(P + 255) / 256, 256, 0, st>>>(acc, comp, nblk, stride, P, out);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

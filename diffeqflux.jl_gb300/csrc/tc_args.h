@@ -38,6 +38,7 @@ struct BwdTcArgs {
 
 
 int launch_bwd_tc(const BwdTcArgs& a, int grid, cudaStream_t st);
-int launch_reduce_mu_comp(const float* acc, const float* comp, int nblk, int P, float* out, cudaStream_t st);
+int launch_reduce_mu_comp(const float* acc, const float* comp, int nblk, int stride, int P, float* out,
+                          cudaStream_t st);
 
 }  // namespace gbnde
