@@ -81,6 +81,7 @@ _SIGS = {
     "gbnde_backward": (C.c_int, [_P, _P, _P, _P, C.POINTER(Stats)]),
     "gbnde_backward_device": (C.c_int, [_P, _P, _P, _P, C.POINTER(Stats)]),
     "gbnde_loss_device": (C.c_int, [_P, _P, _P, C.c_int, _P, C.POINTER(C.c_double)]),
+    "gbnde_loss_noalloc": (C.c_int, [_P, _P, C.c_size_t, C.c_int, _P, C.POINTER(C.c_double), _P]),
     "gbnde_forward_steps": (C.c_longlong, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong]),
     "gbnde_forward_trace": (C.c_longlong, [_P, C.POINTER(C.c_double), C.c_longlong]),
     "gbnde_stream": (C.c_void_p, [_P]),

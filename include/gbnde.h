@@ -154,6 +154,25 @@ int gbnde_backward_device(gbnde_ctx* ctx, const float* dL_dusave_dev, float* dL_
 int gbnde_loss_device(gbnde_ctx* ctx, const float* usave_dev, const float* target_dev,
                       int kind, float* dL_dusave_dev, double* loss);
 
+/* ---- fused loss without any device allocation ----------------------------------
+ * No counterpart in the reference. Same loss and cotangent as
+ * gbnde_loss_device (kind 0: sum of squared errors, kind 1: their mean) on n
+ * floats of caller-owned device memory, for callers that must not allocate:
+ * host functions run by cudaLaunchHostFunc (no CUDA calls that may allocate),
+ * real-time loops that cannot take the device-wide synchronisation of
+ * cudaMalloc/cudaFree, and hosts whose own pool owns every device byte. It
+ * needs no context: its scratch is a 32 KB array compiled into the library
+ * (held on every device that loads it, until the process exits).
+ * n <= GBNDE_LOSS_NOALLOC_MAX_N, else GBNDE_ERR_UNSUPPORTED. The first call on a
+ * device looks up the scratch address for that device; make that first call
+ * before any stream capture. All calls on a device share the scratch: calls
+ * whose kernels overlap on the GPU (other streams or host threads) race and
+ * may return wrong losses. stream: a cudaStream_t, or NULL for the default
+ * stream; the call returns after the loss is on the host. */
+#define GBNDE_LOSS_NOALLOC_MAX_N (4096LL * 65536LL)
+int gbnde_loss_noalloc(const float* usave_dev, const float* target_dev, size_t n, int kind,
+                       float* dL_dusave_dev, double* loss, void* stream);
+
 /* Accepted steps (t_n, h_n) of the last forward solve; returns the count
  * (may exceed cap; only cap entries are written). */
 long long gbnde_forward_steps(gbnde_ctx* ctx, double* t, double* h, long long cap);
