@@ -20,6 +20,33 @@
 
 namespace gbnde {
 int launch_reduce_mu(const float* mu_acc, int nblk, int P, float* out, cudaStream_t st);
+struct MsSeg {
+  double t0, t1;
+  int save_off, nsave;
+};
+struct MsArgs {
+  MlpDev mlp;
+  int S, nseg, TM, LD, ntiles;
+  double abstol, reltol;
+  long long maxiters;
+  int MS;
+  const MsSeg* segs;
+  const double* saveat;
+  const float* u0;
+  float* usave;
+  float* dense;
+  double* steplog;
+  int* nacc;
+  int* retcode;
+  long long* counters;
+  const float* dLdu;
+  float* dLdu0;
+  float* bar;
+  float* mu_acc;
+  int P;
+};
+int launch_ms_fwd(const MsArgs& a, int grid, size_t smem, cudaStream_t st);
+int launch_ms_bwd(const MsArgs& a, int grid, size_t smem, cudaStream_t st);
 
 int launch_transpose_params(const MlpDev& m, const float* p, float* wtr, cudaStream_t st);
 int launch_loss(const float* usave, const float* target, size_t n, int kind, float* dL,
@@ -118,6 +145,11 @@ struct gbnde_ctx {
   bool tc_shape_ok = false;
   bool tc_bwd_ok = false;  // tensor-core adjoint covers this model
   DBuf timg, thscr, tbpart, tmucomp, tlamcomp;
+  // multiple shooting workspace
+  DBuf ms_segs, ms_saveat, ms_u0, ms_usave, ms_dense, ms_steplog, ms_nacc, ms_ret, ms_cnt, ms_dldu,
+      ms_dldu0, ms_bar, ms_mu, ms_dldp;
+  bool ms_have = false;
+  int ms_S = 0, ms_nseg = 0, ms_nsave = 0, ms_MS = 0;
   // dense stage storage of the last forward
   DBuf comp, dense;
   long long dense_slots = 0;
@@ -250,7 +282,9 @@ void gbnde_destroy(gbnde_ctx* c) {
                   &c->bnd_d, &c->dldu, &c->dldu0, &c->dldp, &c->lam, &c->ub, &c->kl, &c->ku,
                   &c->ibuf, &c->mu_acc, &c->mu_stage, &c->iv_d, &c->bsync, &c->bcounters,
                   &c->loss_part, &c->wimg, &c->comp, &c->dense, &c->timg, &c->thscr,
-                  &c->tbpart, &c->tmucomp, &c->tlamcomp};
+                  &c->tbpart, &c->tmucomp, &c->tlamcomp, &c->ms_segs, &c->ms_saveat, &c->ms_u0,
+                  &c->ms_usave, &c->ms_dense, &c->ms_steplog, &c->ms_nacc, &c->ms_ret, &c->ms_cnt,
+                  &c->ms_dldu, &c->ms_dldu0, &c->ms_bar, &c->ms_mu, &c->ms_dldp};
   for (DBuf* b : bufs) b->release();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -849,6 +883,155 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
     stats->retcode_adj = status[ST_RETCODE];
   }
   if (status[ST_BARRIER]) return fail(GBNDE_ERR_TIMEOUT, "backward grid barrier timed out");
+  return 0;
+}
+
+static MsArgs ms_args(gbnde_ctx* c, int TM) {
+  MsArgs m{};
+  m.mlp = c->mlp;
+  m.S = c->ms_S;
+  m.nseg = c->ms_nseg;
+  m.TM = TM;
+  m.LD = TM + 4;
+  m.ntiles = (c->ms_nseg + TM - 1) / TM;
+  m.MS = c->ms_MS;
+  m.segs = c->ms_segs.as<MsSeg>();
+  m.saveat = c->ms_saveat.as<double>();
+  m.u0 = c->ms_u0.as<float>();
+  m.usave = c->ms_usave.as<float>();
+  m.dense = c->ms_dense.as<float>();
+  m.steplog = c->ms_steplog.as<double>();
+  m.nacc = c->ms_nacc.as<int>();
+  m.retcode = c->ms_ret.as<int>();
+  m.counters = c->ms_cnt.as<long long>();
+  return m;
+}
+
+static int ms_grid(int ntiles) {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return std::max(1, std::min(ntiles, nsm));
+}
+
+int gbnde_multishoot_forward(gbnde_ctx* c, int S, int nseg, const gbnde_segment* segs,
+                             const double* saveat, int nsave_total, const float* u0, double abstol,
+                             double reltol, long long maxiters, float* usave, int* retcodes,
+                             gbnde_stats* stats) {
+  if (!c || !segs || !saveat || !u0 || !usave) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (!c->have_params) return fail(GBNDE_ERR_STATE, "parameters not set");
+  if (S != c->S || nseg < 1 || nsave_total < 1) return fail(GBNDE_ERR_INVALID, "bad sizes");
+  if (c->mlp.timein) return fail(GBNDE_ERR_UNSUPPORTED, "multiple shooting with a time input");
+  if (!(abstol > 0) || !(reltol >= 0)) return fail(GBNDE_ERR_INVALID, "tolerances must be positive");
+  for (int i = 0; i < nseg; ++i) {
+    const gbnde_segment& g = segs[i];
+    if (!(g.t1 >= g.t0) || g.nsave < 1 || g.save_off < 0 || g.save_off + g.nsave > nsave_total)
+      return fail(GBNDE_ERR_INVALID, "segment %d is malformed", i);
+    for (int q = 0; q < g.nsave; ++q) {
+      const double s = saveat[g.save_off + q];
+      if (!(s >= g.t0 && s <= g.t1) || (q > 0 && s < saveat[g.save_off + q - 1]))
+        return fail(GBNDE_ERR_INVALID, "segment %d: save times must be increasing inside [t0, t1]", i);
+    }
+  }
+  if (int r = set_device(c)) return r;
+  c->ms_have = false;
+  c->ms_S = S;
+  c->ms_nseg = nseg;
+  c->ms_nsave = nsave_total;
+  c->ms_MS = 256;
+  const size_t SN = (size_t)S * nseg;
+  int TM = 0;
+  if (choose_tm(2 * c->mlp.maxdim, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "layer too wide");
+  TM = std::min(TM, 64);
+  const size_t smem = (size_t)2 * c->mlp.maxdim * (TM + 4) * sizeof(float);
+  int r = 0;
+  if ((r = c->ms_segs.ensure(nseg * sizeof(MsSeg))) || (r = c->ms_saveat.ensure(nsave_total * sizeof(double))) ||
+      (r = c->ms_u0.ensure(SN * 4)) || (r = c->ms_usave.ensure((size_t)S * nsave_total * 4)) ||
+      (r = c->ms_dense.ensure((size_t)nseg * (c->ms_MS + 1) * 8 * S * 4)) ||
+      (r = c->ms_steplog.ensure((size_t)nseg * c->ms_MS * 2 * sizeof(double))) ||
+      (r = c->ms_nacc.ensure(nseg * sizeof(int))) || (r = c->ms_ret.ensure(nseg * sizeof(int))) ||
+      (r = c->ms_cnt.ensure(8 * sizeof(long long))))
+    return r;
+  cudaStream_t st = c->stream;
+  static_assert(sizeof(MsSeg) == sizeof(gbnde_segment), "segment layout");
+  CK(cudaMemcpyAsync(c->ms_segs.p, segs, nseg * sizeof(MsSeg), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->ms_saveat.p, saveat, nsave_total * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->ms_u0.p, u0, SN * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(c->ms_usave.p, 0, (size_t)S * nsave_total * 4, st));
+  CK(cudaMemsetAsync(c->ms_cnt.p, 0, 8 * sizeof(long long), st));
+  MsArgs m = ms_args(c, TM);
+  m.abstol = abstol;
+  m.reltol = reltol;
+  m.maxiters = maxiters > 0 ? maxiters : 100000;
+  const int grid = ms_grid(m.ntiles);
+  CK(cudaEventRecord(c->ev[0], st));
+  if (launch_ms_fwd(m, grid, smem, st)) return fail(GBNDE_ERR_CUDA, "multishoot forward launch failed");
+  CK(cudaEventRecord(c->ev[1], st));
+  long long cnt[8];
+  CK(cudaMemcpyAsync(cnt, c->ms_cnt.p, sizeof cnt, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(usave, c->ms_usave.p, (size_t)S * nsave_total * 4, cudaMemcpyDeviceToHost, st));
+  std::vector<int> ret(nseg);
+  CK(cudaMemcpyAsync(ret.data(), c->ms_ret.p, nseg * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+  c->fwd_ms = ms;
+  int worst = GBNDE_RET_SUCCESS;
+  for (int i = 0; i < nseg; ++i) {
+    if (retcodes) retcodes[i] = ret[i];
+    if (ret[i] != GBNDE_RET_SUCCESS) worst = ret[i];
+  }
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    stats->nf = cnt[0];
+    stats->naccept = cnt[1];
+    stats->nreject = cnt[2];
+    stats->retcode = worst;
+  }
+  c->ms_have = (worst == GBNDE_RET_SUCCESS);
+  return 0;
+}
+
+int gbnde_multishoot_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, float* dLdp,
+                              gbnde_stats* stats) {
+  if (!c || !dLdu || !dLdu0 || !dLdp) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (!c->ms_have) return fail(GBNDE_ERR_STATE, "backward needs a successful multishoot forward first");
+  if (int r = set_device(c)) return r;
+  const int S = c->ms_S, nseg = c->ms_nseg;
+  const size_t SN = (size_t)S * nseg;
+  const int P = (int)c->P;
+  int rows = 0;
+  for (int l = 0; l <= c->mlp.nlayers; ++l) rows += c->mlp.dims[l];
+  rows += 2 * c->mlp.maxdim + S;
+  int TM = 0;
+  if (choose_tm(rows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "network too wide");
+  TM = std::min(TM, 64);
+  const size_t smem = (size_t)rows * (TM + 4) * sizeof(float);
+  MsArgs m = ms_args(c, TM);
+  const int grid = ms_grid(m.ntiles);
+  int r = 0;
+  if ((r = c->ms_dldu.ensure((size_t)S * c->ms_nsave * 4)) || (r = c->ms_dldu0.ensure(SN * 4)) ||
+      (r = c->ms_bar.ensure(SN * 9 * 4)) || (r = c->ms_mu.ensure((size_t)grid * P * 4)) ||
+      (r = c->ms_dldp.ensure((size_t)P * 4)))
+    return r;
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(c->ms_dldu.p, dLdu, (size_t)S * c->ms_nsave * 4, cudaMemcpyHostToDevice, st));
+  m.dLdu = c->ms_dldu.as<float>();
+  m.dLdu0 = c->ms_dldu0.as<float>();
+  m.bar = c->ms_bar.as<float>();
+  m.mu_acc = c->ms_mu.as<float>();
+  m.P = P;
+  CK(cudaEventRecord(c->ev[2], st));
+  if (launch_ms_bwd(m, grid, smem, st)) return fail(GBNDE_ERR_CUDA, "multishoot backward launch failed");
+  if (launch_reduce_mu(m.mu_acc, grid, P, c->ms_dldp.as<float>(), st)) return fail(GBNDE_ERR_CUDA, "reduce failed");
+  CK(cudaEventRecord(c->ev[3], st));
+  CK(cudaMemcpyAsync(dLdu0, c->ms_dldu0.p, SN * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(dLdp, c->ms_dldp.p, (size_t)P * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]));
+  c->bwd_ms = ms;
+  if (stats) stats->retcode_adj = GBNDE_RET_SUCCESS;
   return 0;
 }
 

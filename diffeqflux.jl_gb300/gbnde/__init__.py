@@ -10,3 +10,4 @@ from .layers import (  # noqa: F401
     Array, BacksolveAdjoint, Chain, Dense, GB300Tsit5, InterpolatingAdjoint, NeuralODE,
     ODESolution, Solver, Tsit5, WrappedFunction, ZygoteVJP, cube,
 )
+from .multiple_shooting import group_ranges, multiple_shoot, multiple_shoot_batch  # noqa: F401

@@ -54,6 +54,10 @@ class SolveDesc(C.Structure):
     ]
 
 
+class Segment(C.Structure):
+    _fields_ = [("t0", C.c_double), ("t1", C.c_double), ("save_off", C.c_int), ("nsave", C.c_int)]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("nf", C.c_longlong), ("naccept", C.c_longlong), ("nreject", C.c_longlong),
@@ -81,6 +85,10 @@ _SIGS = {
     "gbnde_backward": (C.c_int, [_P, _P, _P, _P, C.POINTER(Stats)]),
     "gbnde_backward_device": (C.c_int, [_P, _P, _P, _P, C.POINTER(Stats)]),
     "gbnde_loss_device": (C.c_int, [_P, _P, _P, C.c_int, _P, C.POINTER(C.c_double)]),
+    "gbnde_multishoot_forward": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Segment), C.POINTER(C.c_double),
+                                          C.c_int, _P, C.c_double, C.c_double, C.c_longlong, _P,
+                                          C.POINTER(C.c_int), C.POINTER(Stats)]),
+    "gbnde_multishoot_backward": (C.c_int, [_P, _P, _P, _P, C.POINTER(Stats)]),
     "gbnde_loss_noalloc": (C.c_int, [_P, _P, C.c_size_t, C.c_int, _P, C.POINTER(C.c_double), _P]),
     "gbnde_forward_steps": (C.c_longlong, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong]),
     "gbnde_forward_trace": (C.c_longlong, [_P, C.POINTER(C.c_double), C.c_longlong]),

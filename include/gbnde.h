@@ -148,6 +148,30 @@ int gbnde_backward(gbnde_ctx* ctx, const float* dL_dusave, float* dL_du0, float*
 int gbnde_backward_device(gbnde_ctx* ctx, const float* dL_dusave_dev, float* dL_du0_dev,
                           float* dL_dp_dev, gbnde_stats* stats);
 
+/* ---- multiple shooting -------------------------------------------------------------
+ * Replaces the per-group solves of multiple_shoot (src/multiple_shooting.jl:52-62):
+ * segment i solves from u0[:, i] over [t0, t1] with its own adaptive Tsit5
+ * step-size control and saves at saveat[save_off .. save_off + nsave - 1]
+ * (times inside [t0, t1], increasing). All segments run in one launch.
+ * FP32 arithmetic in both precisions. usave: S x nsave_total (column j = save
+ * time j). retcodes[i] is segment i's gbnde_retcode (the reference turns any
+ * failure into an Inf loss, src/multiple_shooting.jl:66-67). */
+typedef struct {
+  double t0, t1;
+  int save_off;
+  int nsave;
+} gbnde_segment;
+
+int gbnde_multishoot_forward(gbnde_ctx* ctx, int S, int nseg, const gbnde_segment* segs,
+                             const double* saveat, int nsave_total, const float* u0,
+                             double abstol, double reltol, long long maxiters, float* usave,
+                             int* retcodes, gbnde_stats* stats);
+/* Gradient of a loss of the saved states of the last multiple-shooting forward:
+ * the discrete adjoint of its accepted steps (exact gradient of the computed
+ * solution). dL_dusave: S x nsave_total; outputs dL/du0 (S x nseg), dL/dp. */
+int gbnde_multishoot_backward(gbnde_ctx* ctx, const float* dL_dusave, float* dL_du0,
+                              float* dL_dp, gbnde_stats* stats);
+
 /* ---- fused loss at the save points (device pointers) -------------------------
  * kind 0: sum(abs2, target .- usave) (docs/src/examples/neural_ode.md:41);
  * kind 1: mean(abs2, ...). Writes dL/dusave and the loss (FP64, host). */

@@ -13,8 +13,9 @@ HEADER = os.path.join(ROOT, "include", "gbnde.h")
 
 
 def _declared():
-    txt = open(HEADER).read()
-    return sorted(set(re.findall(r"\b(gbnde_[a-z_]+)\s*\(", txt)))
+    txt = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)  # drop comments
+    pat = r"^\s*(?:const\s+)?(?:int|void|size_t|long\s+long|char)\s*\**\s*(gbnde_[a-z_]+)\s*\("
+    return sorted(set(re.findall(pat, txt, flags=re.M)))
 
 
 def test_exports_every_declared_symbol(lib):
