@@ -149,6 +149,10 @@ struct gbnde_ctx {
   DBuf ms_segs, ms_saveat, ms_u0, ms_usave, ms_dense, ms_steplog, ms_nacc, ms_ret, ms_cnt, ms_dldu,
       ms_dldu0, ms_bar, ms_mu, ms_dldp;
   bool ms_have = false;
+  // FFJORD
+  DBuf ffnoise, ffu0, ffus;
+  int fS = 0;          // state dim of the last forward (d + 1 for FFJORD)
+  int ff_on = 0, ff_d = 0, ff_exact = 0;
   int ms_S = 0, ms_nseg = 0, ms_nsave = 0, ms_MS = 0;
   // dense stage storage of the last forward
   DBuf comp, dense;
@@ -284,7 +288,8 @@ void gbnde_destroy(gbnde_ctx* c) {
                   &c->loss_part, &c->wimg, &c->comp, &c->dense, &c->timg, &c->thscr,
                   &c->tbpart, &c->tmucomp, &c->tlamcomp, &c->ms_segs, &c->ms_saveat, &c->ms_u0,
                   &c->ms_usave, &c->ms_dense, &c->ms_steplog, &c->ms_nacc, &c->ms_ret, &c->ms_cnt,
-                  &c->ms_dldu, &c->ms_dldu0, &c->ms_bar, &c->ms_mu, &c->ms_dldp};
+                  &c->ms_dldu, &c->ms_dldu0, &c->ms_bar, &c->ms_mu, &c->ms_dldp, &c->ffnoise,
+                  &c->ffu0, &c->ffus};
   for (DBuf* b : bufs) b->release();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -363,7 +368,8 @@ int gbnde_set_params_device(gbnde_ctx* c, const float* p, size_t n) {
 
 static int validate_desc(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B) {
   if (!d) return fail(GBNDE_ERR_INVALID, "null solve descriptor");
-  if (S != c->S) return fail(GBNDE_ERR_INVALID, "state dim %d does not match the model (%d)", S, c->S);
+  if (S != c->S + (c->ff_on ? 1 : 0))
+    return fail(GBNDE_ERR_INVALID, "state dim %d does not match the model (%d)", S, c->S);
   if (B < 1) return fail(GBNDE_ERR_INVALID, "batch must be >= 1");
   if (!(d->t1 > d->t0)) return fail(GBNDE_ERR_UNSUPPORTED, "tspan must satisfy t1 > t0");
   if (!(d->abstol > 0) || !(d->reltol >= 0)) return fail(GBNDE_ERR_INVALID, "tolerances must be positive");
@@ -398,11 +404,14 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
     if (d->saveat[i] > d->t0) bnd.push_back(d->saveat[i]);
   const int nb = (int)bnd.size();
 
+  int sumdims = 0;
+  for (int l = 0; l <= c->mlp.nlayers; ++l) sumdims += c->mlp.dims[l];
+  const int frows = c->ff_on ? 2 * sumdims + c->mlp.maxdim + 1 : 2 * c->mlp.maxdim;
   int TM = 0;
-  if (choose_tm(2 * c->mlp.maxdim, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "layer too wide");
+  if (choose_tm(frows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "layer too wide");
   const int LD = TM + 4;
-  const size_t smem = (size_t)2 * c->mlp.maxdim * LD * sizeof(float);
-  const bool tcform = c->precision == GBNDE_PREC_BF16;
+  const size_t smem = (size_t)frows * LD * sizeof(float);
+  const bool tcform = c->precision == GBNDE_PREC_BF16 && !c->ff_on;
   const int ntiles = tcform ? (B + 127) / 128 : (B + TM - 1) / TM;
   int gmax = 0;
   if (tcform) {
@@ -499,6 +508,10 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   a.tfinal = reinterpret_cast<double*>(c->counters.as<char>() + CT_NSLOTS * sizeof(long long));
   a.dense = c->dense_slots > 0 ? c->dense.as<float>() : nullptr;
   a.dense_slots = c->dense_slots;
+  a.ffj = c->ff_on;
+  a.ffd = c->ff_d;
+  a.exact = c->ff_exact;
+  a.noise = c->ff_on ? c->ffnoise.as<float>() : nullptr;
   CK(cudaEventRecord(c->ev[0], st));
   if (tcform) {
     FwdTcArgs ta{};
@@ -573,6 +586,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   c->have_fwd = (status[ST_RETCODE] == GBNDE_RET_SUCCESS) && nacc <= maxsteps;
   c->dense_valid = c->dense_slots > 0 && nacc < c->dense_slots;
   c->last_naccept = nacc;
+  c->fS = S;
   if (c->have_fwd && !c->dense_valid && !c->rerun_guard) {
     // the solve outgrew the dense stage storage: grow it and solve again once
     // (the backward then interpolates the stored stages instead of recomputing)
@@ -761,9 +775,11 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   if (!c->have_fwd) return fail(GBNDE_ERR_STATE, "backward needs a successful forward solve first");
   if (!dLdu || !dLdu0 || !dLdp) return fail(GBNDE_ERR_INVALID, "null argument");
   if (int r = set_device(c)) return r;
-  const int S = c->S, B = c->B, nsave = c->nsave;
+  const int S = c->fS, B = c->B, nsave = c->nsave;
   const size_t SB = (size_t)S * B;
   const int P = (int)c->P;
+  if (c->ff_on && (c->sensealg != GBNDE_SENSE_INTERPOLATING || !c->dense_valid))
+    return fail(GBNDE_ERR_UNSUPPORTED, "FFJORD gradients use InterpolatingAdjoint with stored stages");
   std::vector<Interval> ivs;
   int max_slots = 1, save_last = 0, nsave_last = 0;
   if (int r = build_intervals(c, ivs, &max_slots, &save_last, &nsave_last)) return r;
@@ -771,7 +787,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
 
   int rows = 0;
   for (int l = 0; l <= c->mlp.nlayers; ++l) rows += c->mlp.dims[l];
-  rows += 2 * c->mlp.maxdim + S;
+  rows = c->ff_on ? 2 * rows + 4 * c->mlp.maxdim + 1 : rows + 2 * c->mlp.maxdim + S;
   int TM = 0;
   if (choose_tm(rows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "network too wide");
   const int LD = TM + 4;
@@ -849,7 +865,11 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   a.bar = c->bsync.as<unsigned int>();
   a.status = reinterpret_cast<int*>(c->bsync.as<char>() + 16);
   a.counters = c->bcounters.as<long long>();
-  const bool tcbwd = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && c->dense_valid;
+  a.ffj = c->ff_on;
+  a.ffd = c->ff_d;
+  a.exact = c->ff_exact;
+  a.noise = c->ff_on ? c->ffnoise.as<float>() : nullptr;
+  const bool tcbwd = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && c->dense_valid && !c->ff_on;
   if (tcbwd) {
     if (int rr = backward_tc(c, a, st, dp_d)) return rr;
   } else {
@@ -1002,7 +1022,7 @@ int gbnde_multishoot_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, flo
   const int P = (int)c->P;
   int rows = 0;
   for (int l = 0; l <= c->mlp.nlayers; ++l) rows += c->mlp.dims[l];
-  rows += 2 * c->mlp.maxdim + S;
+  rows = c->ff_on ? 2 * rows + 4 * c->mlp.maxdim + 1 : rows + 2 * c->mlp.maxdim + S;
   int TM = 0;
   if (choose_tm(rows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "network too wide");
   TM = std::min(TM, 64);
@@ -1037,14 +1057,80 @@ int gbnde_multishoot_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, flo
 
 int gbnde_forward(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, const float* u0,
                   float* usave, gbnde_stats* stats) {
-  if (!u0 || !usave) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (!c || !u0 || !usave) return fail(GBNDE_ERR_INVALID, "null argument");
+  c->ff_on = 0;
   return forward_impl(c, d, S, B, u0, true, usave, true, stats);
 }
 
 int gbnde_forward_device(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, const float* u0,
                          float* usave, gbnde_stats* stats) {
-  if (!u0 || !usave) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (!c || !u0 || !usave) return fail(GBNDE_ERR_INVALID, "null argument");
+  c->ff_on = 0;
   return forward_impl(c, d, S, B, u0, false, usave, false, stats);
+}
+
+int gbnde_ffjord_forward(gbnde_ctx* c, const gbnde_solve_desc* desc, int d, int B, const float* x,
+                         const float* noise, float* logpx, float* zT, gbnde_stats* stats) {
+  if (!c || !desc || !x || !logpx) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (d != c->S) return fail(GBNDE_ERR_INVALID, "data dim %d does not match the model (%d)", d, c->S);
+  if (c->mlp.cube) return fail(GBNDE_ERR_UNSUPPORTED, "FFJORD with a cube prefix");
+  if (int r = set_device(c)) return r;
+  const int S = d + 1;
+  const size_t SB = (size_t)S * B;
+  int r = 0;
+  if ((r = c->ffu0.ensure(SB * 4)) || (r = c->ffus.ensure(SB * 4)) ||
+      (noise && (r = c->ffnoise.ensure((size_t)d * B * 4))))
+    return r;
+  std::vector<float> y0(SB, 0.f);
+  for (int b = 0; b < B; ++b)
+    for (int s = 0; s < d; ++s) y0[(size_t)b * S + s] = x[(size_t)b * d + s];
+  CK(cudaMemcpy(c->ffu0.p, y0.data(), SB * 4, cudaMemcpyHostToDevice));
+  if (noise) CK(cudaMemcpy(c->ffnoise.p, noise, (size_t)d * B * 4, cudaMemcpyHostToDevice));
+  gbnde_solve_desc dd = *desc;
+  const double tend = desc->t1;
+  dd.saveat = &tend;
+  dd.nsave = 1;
+  dd.sensealg = GBNDE_SENSE_INTERPOLATING;
+  c->ff_on = 1;
+  c->ff_d = d;
+  c->ff_exact = noise ? 0 : 1;
+  r = forward_impl(c, &dd, S, B, c->ffu0.as<float>(), false, c->ffus.as<float>(), false, stats);
+  if (r) return r;
+  std::vector<float> yT(SB);
+  CK(cudaMemcpy(yT.data(), c->ffus.p, SB * 4, cudaMemcpyDeviceToHost));
+  const double lognorm = 0.5 * d * std::log(6.283185307179586);  // log(2 pi)
+  for (int b = 0; b < B; ++b) {
+    double q = 0.0;
+    for (int s = 0; s < d; ++s) {
+      const double z = yT[(size_t)b * S + s];
+      q += z * z;
+      if (zT) zT[(size_t)b * d + s] = (float)z;
+    }
+    logpx[b] = (float)(-0.5 * q - lognorm - (double)yT[(size_t)b * S + d]);
+  }
+  return 0;
+}
+
+int gbnde_ffjord_backward(gbnde_ctx* c, const float* dLdlogpx, const float* dLdzT, float* dLdx, float* dLdp,
+                          gbnde_stats* stats) {
+  if (!c || !dLdlogpx || !dLdx || !dLdp) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (!c->ff_on || !c->have_fwd) return fail(GBNDE_ERR_STATE, "backward needs a successful FFJORD forward");
+  if (int r = set_device(c)) return r;
+  const int d = c->ff_d, S = d + 1, B = c->B;
+  const size_t SB = (size_t)S * B;
+  std::vector<float> yT(SB), g(SB), du0(SB);
+  CK(cudaMemcpy(yT.data(), c->ffus.p, SB * 4, cudaMemcpyDeviceToHost));
+  for (int b = 0; b < B; ++b) {
+    const float gl = dLdlogpx[b];
+    for (int s = 0; s < d; ++s)
+      g[(size_t)b * S + s] = -yT[(size_t)b * S + s] * gl + (dLdzT ? dLdzT[(size_t)b * d + s] : 0.f);
+    g[(size_t)b * S + d] = -gl;
+  }
+  const int r = backward_impl(c, g.data(), true, du0.data(), dLdp, true, stats);
+  if (r) return r;
+  for (int b = 0; b < B; ++b)
+    for (int s = 0; s < d; ++s) dLdx[(size_t)b * d + s] = du0[(size_t)b * S + s];
+  return 0;
 }
 
 int gbnde_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, float* dLdp, gbnde_stats* stats) {

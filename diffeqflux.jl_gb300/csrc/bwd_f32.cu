@@ -131,9 +131,82 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
   // Adjoint RHS on a tile at time `tt`: lam stage from `lamv`, u from `uval`
   // (Interpolating: dense forward output; Backsolve: stage of co-integrated u).
   // Writes kl (J^T lam) and, for Backsolve, ku (-f(u)); accumulates mu into P*c.
+  // FFJORD layout: act[0..L], zd[0..L] (sum(dims) rows each), 4 cotangent
+  // buffers (maxdim rows each), tmp (maxdim rows).
+  float* fact[GBNDE_MAX_LAYERS + 1];
+  float* fzd[GBNDE_MAX_LAYERS + 1];
+  float* fcot[4];
+  float* ftmp = nullptr;
+  float* flam = nullptr;  // lam_l per trajectory of the tile
+  if (a.ffj) {
+    float* p = smem;
+    for (int l = 0; l <= a.mlp.nlayers; ++l) { fact[l] = p; p += (size_t)a.mlp.dims[l] * LD; }
+    for (int l = 0; l <= a.mlp.nlayers; ++l) { fzd[l] = p; p += (size_t)a.mlp.dims[l] * LD; }
+    for (int q = 0; q < 4; ++q) { fcot[q] = p; p += (size_t)a.mlp.maxdim * LD; }
+    ftmp = fcot[3];  // the tangent pass runs before fcot[3] is used as a cotangent
+    flam = p;
+  }
+  // FFJORD adjoint right-hand side: cotangent [lam_z; lam_l] of [f; -trace];
+  // writes kl = lam_z^T df/dz - lam_l d(trace)/dz (z rows; 0 for the logp row).
+  auto ffj_eval = [&](int tile, double tt, auto&& lamv, auto&& uval, float* kl_out, float* P, float c,
+                      float* lam_store) {
+    const MlpDev& m = a.mlp;
+    const int d = a.ffd, L = m.nlayers;
+    const size_t base = (size_t)tile * TM * S;
+    const int nv = nvalid_of(a, tile);
+    for (int e = threadIdx.x; e < TM * S; e += blockDim.x) {
+      const int mm = e / S, s = e - mm * S;
+      float u = 0.f, l = 0.f;
+      if (mm < nv) {
+        u = uval(base + e);
+        l = lamv(base + e);
+        if (lam_store) lam_store[base + e] = l;
+      }
+      if (s < d) {
+        fact[0][s * LD + mm] = u;
+        fcot[0][s * LD + mm] = l;     // cotangent of f (primal output), rows < d
+      } else {
+        flam[mm] = l;
+      }
+    }
+    if (m.timein)
+      for (int mm = threadIdx.x; mm < TM; mm += blockDim.x) fact[0][d * LD + mm] = (float)tt;
+    __syncthreads();
+    mlp_fwd_tile(m, fact[0], nullptr, LD, TM, fact + 1);
+    const int ndir = a.exact ? d : 1;
+    for (int k = 0; k < ndir; ++k) {
+      for (int e = threadIdx.x; e < m.dims[0] * TM; e += blockDim.x) {
+        const int s = e / TM, mm = e - s * TM;
+        float v = 0.f;
+        if (s < d && mm < nv) v = a.exact ? (s == k ? 1.f : 0.f) : a.noise[((size_t)tile * TM + mm) * d + s];
+        fzd[0][s * LD + mm] = v;
+      }
+      __syncthreads();
+      mlp_tangent_tile(m, fact, fzd, ftmp, LD, TM);
+      // cotangents: primal (first direction only) and tangent output -lam_l e
+      for (int e = threadIdx.x; e < d * TM; e += blockDim.x) {
+        const int s = e / TM, mm = e - s * TM;
+        fcot[2][s * LD + mm] = -flam[mm] * fzd[0][s * LD + mm];
+        if (k > 0) fcot[0][s * LD + mm] = 0.f;
+      }
+      __syncthreads();
+      const float* gi = ffjord_vjp_tile(m, fact, fzd, fcot[0], fcot[1], fcot[2], fcot[3], LD, TM, P, c);
+      for (int e = threadIdx.x; e < nv * S; e += blockDim.x) {
+        const int mm = e / S, s = e - mm * S;
+        const float g = s < d ? gi[s * LD + mm] : 0.f;
+        kl_out[base + e] = (k == 0) ? g : kl_out[base + e] + g;
+      }
+      __syncthreads();
+    }
+  };
+
   auto adj_eval = [&](int tile, double tt, const Interval& iv, auto&& lamv, auto&& uval,
                       float* kl_out, float* ku_out, float* P, float c, float* lam_store,
                       float* u_store) {
+    if (a.ffj) {
+      ffj_eval(tile, tt, lamv, uval, kl_out, P, c, lam_store);
+      return;
+    }
     const size_t base = (size_t)tile * TM * S;
     const int nv = nvalid_of(a, tile);
     // chain input

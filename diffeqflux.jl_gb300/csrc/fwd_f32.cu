@@ -70,13 +70,81 @@ __device__ __forceinline__ size_t tile_elems(const FwdArgs& a, int tile) {
   return (size_t)min(a.TM, a.B - tile * a.TM) * a.S;
 }
 
+// FFJORD right-hand side of a tile: [f(z, t); -trace(df/dz)], the trace as
+// e^T (J e) along the sample's noise e (Hutchinson) or summed over the unit
+// directions (exact). smem: act[0..L], zd[0..L] (sum(dims) rows each), tmp
+// (maxdim rows), trace sums (TM).
+template <class Fn, class Sink>
+__device__ __forceinline__ void ffjord_rhs_tile(const FwdArgs& a, int tile, float* smem, double tstage,
+                                                Fn&& val, Sink&& sink) {
+  const MlpDev& m = a.mlp;
+  const int S = a.S, d = a.ffd, TM = a.TM, LD = a.LD;
+  float* act[GBNDE_MAX_LAYERS + 1];
+  float* zd[GBNDE_MAX_LAYERS + 1];
+  float* p = smem;
+  for (int l = 0; l <= m.nlayers; ++l) { act[l] = p; p += (size_t)m.dims[l] * LD; }
+  for (int l = 0; l <= m.nlayers; ++l) { zd[l] = p; p += (size_t)m.dims[l] * LD; }
+  float* tmp = p;
+  p += (size_t)m.maxdim * LD;
+  float* tr = p;
+  const size_t base = (size_t)tile * TM * S;
+  const int nvalid = min(TM, a.B - tile * TM);
+  for (int e = threadIdx.x; e < TM * S; e += blockDim.x) {
+    const int mm = e / S, s = e - mm * S;
+    const float v = (mm < nvalid) ? val(base + e) : 0.f;
+    if (s < d) act[0][s * LD + mm] = v;
+  }
+  if (m.timein)
+    for (int mm = threadIdx.x; mm < TM; mm += blockDim.x) act[0][d * LD + mm] = (float)tstage;
+  for (int mm = threadIdx.x; mm < TM; mm += blockDim.x) tr[mm] = 0.f;
+  __syncthreads();
+  mlp_fwd_tile(m, act[0], nullptr, LD, TM, act + 1);
+  const int ndir = a.exact ? d : 1;
+  const int L = m.nlayers;
+  for (int k = 0; k < ndir; ++k) {
+    for (int e = threadIdx.x; e < m.dims[0] * TM; e += blockDim.x) {
+      const int s = e / TM, mm = e - s * TM;
+      float v = 0.f;
+      if (s < d && mm < nvalid) v = a.exact ? (s == k ? 1.f : 0.f) : a.noise[((size_t)tile * TM + mm) * d + s];
+      zd[0][s * LD + mm] = v;
+    }
+    __syncthreads();
+    mlp_tangent_tile(m, act, zd, tmp, LD, TM);
+    for (int mm = threadIdx.x; mm < TM; mm += blockDim.x) {
+      float s_ = 0.f;
+      for (int s = 0; s < d; ++s)
+        s_ = fmaf(zd[0][s * LD + mm], act_deriv_from_out(act[L][s * LD + mm], m.act[L - 1]) * zd[L][s * LD + mm], s_);
+      tr[mm] += s_;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < nvalid * S; e += blockDim.x) {
+    const int mm = e / S, s = e - mm * S;
+    sink(base + e, s < d ? act[L][s * LD + mm] : -tr[mm]);
+  }
+  __syncthreads();
+}
+
+// One right-hand side of a tile: the NeuralODE chain or the FFJORD system.
+template <class Fn, class Sink>
+__device__ __forceinline__ void rhs_tile(const FwdArgs& a, int tile, float* smem, double tstage, Fn&& val,
+                                         Sink&& sink) {
+  if (a.ffj) {
+    ffjord_rhs_tile(a, tile, smem, tstage, val, sink);
+    return;
+  }
+  float* bufA = smem;
+  float* bufB = smem + (size_t)a.mlp.maxdim * a.LD;
+  load_tile_input(a, tile, bufA, tstage, val);
+  const float* out = mlp_fwd_tile(a.mlp, bufA, bufB, a.LD, a.TM, nullptr);
+  store_tile_output(a, tile, out, sink);
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
   extern __shared__ __align__(16) float smem[];
   __shared__ double red[40];
-  float* bufA = smem;
-  float* bufB = smem + (size_t)a.mlp.maxdim * a.LD;
   const int G = gridDim.x;
   const double N = (double)a.S * (double)a.B;
   const double tdir = a.t1 >= a.t0 ? 1.0 : -1.0;
@@ -89,15 +157,15 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
 
   // ---- k1 = f(u0, t0); ubuf[0] = u0 --------------------------------------
   for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
-    load_tile_input(a, tile, bufA, a.t0, [&](size_t g) {
-      const float v = a.u0[g];
-      a.ubuf[0][g] = v;
-      if (a.dense) a.dense[g] = v;
-      return v;
-    });
-    const float* out = mlp_fwd_tile(a.mlp, bufA, bufB, a.LD, a.TM, nullptr);
     float* k1 = kb(a, 0, swp);
-    store_tile_output(a, tile, out, [&](size_t g, float v) { k1[g] = v; });
+    rhs_tile(a, tile, smem, a.t0,
+             [&](size_t g) {
+               const float v = a.u0[g];
+               a.ubuf[0][g] = v;
+               if (a.dense) a.dense[g] = v;
+               return v;
+             },
+             [&](size_t g, float v) { k1[g] = v; });
   }
   nf = 1;
 
@@ -148,10 +216,8 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
       float* f1b = kb(a, 1, swp);
       double p2 = 0.0;
       for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
-        load_tile_input(a, tile, bufA, a.t0 + tdir * dt0,
-                        [&](size_t g) { return a.u0[g] + hf * k1[g]; });
-        const float* out = mlp_fwd_tile(a.mlp, bufA, bufB, a.LD, a.TM, nullptr);
-        store_tile_output(a, tile, out, [&](size_t g, float v) {
+        rhs_tile(a, tile, smem, a.t0 + tdir * dt0, [&](size_t g) { return a.u0[g] + hf * k1[g]; },
+                 [&](size_t g, float v) {
           f1b[g] = v;
           const float sk = (float)a.abstol + fabsf(a.u0[g]) * (float)a.reltol;
           const double z = (double)((v - k1[g]) / sk);
@@ -198,18 +264,17 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
 #pragma unroll
         for (int j = 0; j < 7; ++j) hbt[j] = (float)(h * c_tab.btilde[j]);
         for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
-          load_tile_input(a, tile, bufA, t + c_tab.c[i] * h, [&](size_t g) {
+          auto stage_in = [&](size_t g) {
             float s = 0.f;
             for (int j = 0; j < i; ++j) s = fmaf(ha[j], kj[j][g], s);
             const float y = ucur[g] + s;
             if (i == 6) unew[g] = y;
             return y;
-          });
-          const float* out = mlp_fwd_tile(a.mlp, bufA, bufB, a.LD, a.TM, nullptr);
+          };
           if (i < 6) {
-            store_tile_output(a, tile, out, [&](size_t g, float v) { ki[g] = v; });
+            rhs_tile(a, tile, smem, t + c_tab.c[i] * h, stage_in, [&](size_t g, float v) { ki[g] = v; });
           } else {
-            store_tile_output(a, tile, out, [&](size_t g, float v) {
+            rhs_tile(a, tile, smem, t + c_tab.c[i] * h, stage_in, [&](size_t g, float v) {
               ki[g] = v;
               float ut = hbt[6] * v;
 #pragma unroll

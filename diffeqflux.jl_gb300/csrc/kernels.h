@@ -45,6 +45,9 @@ struct FwdArgs {
   int* status;
   long long* counters;
   double* tfinal;
+  // FFJORD mode: state = [z (ffd rows); delta_logp], RHS = [f(z); -trace]
+  int ffj, ffd, exact;
+  const float* noise;    // ffd x B (Hutchinson directions)
 };
 
 // One backward interval of InterpolatingAdjoint: forward steps [nlo, nhi]
@@ -91,6 +94,8 @@ struct BwdArgs {
   unsigned int* bar;
   int* status;
   long long* counters;
+  int ffj, ffd, exact;    // FFJORD mode (see FwdArgs)
+  const float* noise;
 };
 
 int launch_fwd_f32(const FwdArgs& a, int grid, size_t smem, cudaStream_t st);

@@ -215,4 +215,121 @@ __device__ __forceinline__ float* mlp_vjp_tile(const MlpDev& m, float* const* ac
   return g;
 }
 
+
+// ---- FFJORD: directional derivative and its reverse pass ------------------------------
+//
+// act'' from the output y: tanh -> -2 y (1 - y^2); softplus -> s (1 - s) with
+// s = 1 - exp(-y); identity -> 0.
+__device__ __forceinline__ float act_deriv2_from_out(float y, int act) {
+  if (act == GBNDE_ACT_TANH) return -2.f * y * (1.f - y * y);
+  if (act == GBNDE_ACT_SOFTPLUS) {
+    const float sg = -expm1f(-y);
+    return sg * (1.f - sg);
+  }
+  return 0.f;
+}
+
+// Tangent of the chain along the input direction held in zd[0] (feature-major,
+// rows [0, dims[0])): zd[l+1] = W_l adot_l with adot_0 = zd[0] and
+// adot_l = act'(act[l]) * zd[l] for l >= 1. act[0..L] must hold the primal
+// activations. tmp: one buffer of maxdim rows.
+__device__ __forceinline__ void mlp_tangent_tile(const MlpDev& m, float* const* act, float* const* zd,
+                                                 float* tmp, int LD, int TM) {
+  for (int l = 0; l < m.nlayers; ++l) {
+    const int K = m.dims[l];
+    const float* in = zd[0];
+    if (l > 0) {
+      for (int e = threadIdx.x; e < K * TM; e += blockDim.x) {
+        const int k = e / TM, mm = e - k * TM;
+        tmp[k * LD + mm] = act_deriv_from_out(act[l][k * LD + mm], m.act[l - 1]) * zd[l][k * LD + mm];
+      }
+      __syncthreads();
+      in = tmp;
+    }
+    dense_fwd(m.Wt[l], nullptr, K, m.dims[l + 1], GBNDE_ACT_IDENTITY, in, zd[l + 1], LD, TM);
+    __syncthreads();
+  }
+}
+
+// P[k*N + n] += c * sum_m g[n][m] * (act'(y[k][m]) * x[k][m]) : the weight
+// gradient of the tangent chain (operand adot = act'(y) * zdot).
+__device__ __forceinline__ void dw_accum_scaled(float* __restrict__ P, const float* g, const float* x,
+                                                const float* y, int actcode, int N, int K, int LD,
+                                                int TM, float c) {
+  const int tnc = (N + 7) >> 3, tkc = (K + 7) >> 3;
+  for (int mt = threadIdx.x; mt < tnc * tkc; mt += blockDim.x) {
+    const int n0 = (mt % tnc) * 8, k0 = (mt / tnc) * 8;
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    for (int mm = 0; mm < TM; ++mm) {
+      float gv[8], av[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        gv[i] = g[min(n0 + i, N - 1) * LD + mm];
+        const int kk = min(k0 + i, K - 1) * LD + mm;
+        av[i] = (y ? act_deriv_from_out(y[kk], actcode) : 1.f) * x[kk];
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(gv[i], av[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      if (k0 + j >= K) continue;
+      float* row = P + (size_t)(k0 + j) * N;
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (n0 + i < N) row[n0 + i] += c * acc[i][j];
+    }
+  }
+}
+
+// Reverse pass through the primal chain and its tangent (reverse over forward).
+// Inputs: act[0..L] primal activations, zd[0..L] tangents (zd[0] = input
+// direction), abar (rows dims[L]) cotangent of the primal output, tbar (rows
+// dims[L]) cotangent of the tangent output. Buffers abar/abar2 and tbar/tbar2
+// are ping-pong pairs of maxdim rows. Accumulates the parameter cotangent
+// into P scaled by c (when P != null). Returns the buffer with the cotangent
+// of the primal input (rows dims[0]).
+__device__ __forceinline__ float* ffjord_vjp_tile(const MlpDev& m, float* const* act, float* const* zd,
+                                                  float* abar, float* abar2, float* tbar, float* tbar2,
+                                                  int LD, int TM, float* P, float c) {
+  for (int l = m.nlayers - 1; l >= 0; --l) {
+    const int N = m.dims[l + 1], K = m.dims[l];
+    const int code = m.act[l];
+    const float* y = act[l + 1];
+    const float* zl = zd[l + 1];
+    // tbar <- tbar * act'(y) (= zdot bar); abar <- tbar_in * act''(y) * zdot + abar * act'(y) (= z bar)
+    for (int e = threadIdx.x; e < N * TM; e += blockDim.x) {
+      const int n = e / TM, mm = e - n * TM, o = n * LD + mm;
+      const float d1 = act_deriv_from_out(y[o], code), d2 = act_deriv2_from_out(y[o], code);
+      const float tb = tbar[o];
+      abar[o] = fmaf(tb * d2, zl[o], abar[o] * d1);
+      tbar[o] = tb * d1;
+    }
+    __syncthreads();
+    if (P) {
+      dw_accum(P + m.woff[l], abar, act[l], N, K, LD, TM, c);
+      dw_accum_scaled(P + m.woff[l], tbar, zd[l], l > 0 ? act[l] : nullptr, l > 0 ? m.act[l - 1] : 0, N, K,
+                      LD, TM, c);
+      db_accum(P + m.boff[l], abar, N, LD, TM, c);
+    }
+    __syncthreads();
+    dense_fwd(m.W[l], nullptr, N, K, GBNDE_ACT_IDENTITY, abar, abar2, LD, TM);
+    dense_fwd(m.W[l], nullptr, N, K, GBNDE_ACT_IDENTITY, tbar, tbar2, LD, TM);
+    __syncthreads();
+    float* t1 = abar;
+    abar = abar2;
+    abar2 = t1;
+    float* t2 = tbar;
+    tbar = tbar2;
+    tbar2 = t2;
+  }
+  return abar;
+}
+
 }  // namespace gbnde

@@ -10,4 +10,5 @@ from .layers import (  # noqa: F401
     Array, BacksolveAdjoint, Chain, Dense, GB300Tsit5, InterpolatingAdjoint, NeuralODE,
     ODESolution, Solver, Tsit5, WrappedFunction, ZygoteVJP, cube,
 )
+from .ffjord import FFJORD  # noqa: F401
 from .multiple_shooting import group_ranges, multiple_shoot, multiple_shoot_batch  # noqa: F401

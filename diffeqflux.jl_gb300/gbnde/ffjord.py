@@ -1,0 +1,126 @@
+"""Host-side mirror of DiffEqFlux's FFJORD layer on the GB300 solver.
+
+`FFJORD(model, tspan, input_dims, alg; basedist=None, kwargs...)` and
+`(f)(x, ps, st) -> ((logpx, lambda1, lambda2), st)` as in src/ffjord.jl:51-178:
+the augmented system [z; delta_logp] with right-hand side
+[f(z [, t]); -trace(df/dz)] is solved from (x, 0), keeping only the end state,
+and logpx = logpz(z(t1)) - delta_logp(t1) with the standard-normal base.
+`st` carries the reference's flags: monte_carlo (Hutchinson trace, the
+default) or the exact trace; regularize=True is not offered. The Hutchinson
+noise is drawn once per sample per solve (Rademacher by default, Gaussian on
+request) from `st["rng"]` -- the reference draws fresh Gaussian noise on every
+right-hand-side call, which makes its ODE stochastic. With torch tensors the
+returned logpx is differentiable through the library's InterpolatingAdjoint.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .layers import Chain, Solver, Tsit5
+
+
+class FFJORD:
+    def __init__(self, model, tspan, input_dims, alg=None, *, basedist=None, abstol=1e-6, reltol=1e-3,
+                 maxiters=100000, time_input=False, noise="rademacher", device=0):
+        if not isinstance(model, Chain):
+            raise TypeError("model must be a Chain of Dense layers")
+        if basedist is not None:
+            raise NotImplementedError("only the standard-normal base distribution is offered")
+        if model.cube_input:
+            raise ValueError("FFJORD models take no cube prefix")
+        d = int(np.prod(input_dims))
+        if model.dims[-1] != d or model.dims[0] != d + (1 if time_input else 0):
+            raise ValueError("model must map the data dim (plus t when time_input) to the data dim")
+        self.model, self.d = model, d
+        self.tspan = (float(tspan[0]), float(tspan[1]))
+        self.alg = alg if alg is not None else Tsit5()
+        self.abstol, self.reltol, self.maxiters = float(abstol), float(reltol), int(maxiters)
+        self.time_input = bool(time_input)
+        self.noise = noise
+        self.device = device
+        self._solver = None
+
+    # Lux.initialstates (src/ffjord.jl:61-66)
+    def setup(self, rng):
+        return self.model.init_params(rng), {"regularize": False, "monte_carlo": True,
+                                             "rng": np.random.default_rng(int(rng.integers(1 << 31)))}
+
+    @property
+    def solver(self):
+        if self._solver is None:
+            self._solver = Solver(self.model, self.alg.precision, self.device, time_input=self.time_input)
+        return self._solver
+
+    def desc(self):
+        return Solver.solve_desc(self.tspan[0], self.tspan[1], [self.tspan[1]], self.abstol, self.reltol,
+                                 0, 0.0, 0.0, self.maxiters)
+
+    def draw_noise(self, rng, B):
+        if self.noise == "gaussian":
+            return rng.standard_normal((B, self.d)).astype(np.float32)
+        return rng.choice(np.array([-1.0, 1.0], np.float32), size=(B, self.d))
+
+    # numpy core --------------------------------------------------------------------
+    def forward_np(self, x, p, noise):
+        """x: d x B. noise: B x d (row-major per sample) or None (exact trace)."""
+        s = self.solver
+        s.set_params(p)
+        x = np.ascontiguousarray(np.asarray(x, np.float32).T)  # B x d = column-major d x B
+        B = x.shape[0]
+        logpx = np.empty(B, np.float32)
+        zT = np.empty((B, self.d), np.float32)
+        st = _lib.Stats()
+        nz = None if noise is None else np.ascontiguousarray(noise, np.float32)
+        _lib.check(s.lib.gbnde_ffjord_forward(s.h, C.byref(self.desc()), self.d, B, x.ctypes.data,
+                                              None if nz is None else nz.ctypes.data, logpx.ctypes.data,
+                                              zT.ctypes.data, C.byref(st)))
+        self._keep = nz
+        return logpx, zT.T, st
+
+    def backward_np(self, dlogpx, dzT=None):
+        s = self.solver
+        g = np.ascontiguousarray(dlogpx, np.float32)
+        B = g.size
+        gz = None if dzT is None else np.ascontiguousarray(np.asarray(dzT, np.float32).T)
+        dx = np.empty((B, self.d), np.float32)
+        dp = np.empty(s.nparams, np.float32)
+        st = _lib.Stats()
+        _lib.check(s.lib.gbnde_ffjord_backward(s.h, g.ctypes.data, None if gz is None else gz.ctypes.data,
+                                               dx.ctypes.data, dp.ctypes.data, C.byref(st)))
+        return dx.T, dp, st
+
+    def __call__(self, x, ps, st):
+        if st.get("regularize", False):
+            raise NotImplementedError("regularize=True is not offered by the GB300 FFJORD")
+        mc = st.get("monte_carlo", True)
+        rng = st.get("rng") or np.random.default_rng(0)
+        B = np.asarray(x.shape)[-1]
+        noise = self.draw_noise(rng, int(B)) if mc else None
+        try:
+            import torch
+            is_torch = isinstance(x, torch.Tensor) or isinstance(ps, torch.Tensor)
+        except ImportError:  # pragma: no cover
+            is_torch = False
+        if not is_torch:
+            logpx, zT, _ = self.forward_np(x, ps, noise)
+            out = logpx.reshape(1, -1)
+            return (out, out, out), st
+        import torch
+        layer = self
+
+        class _Fn(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, xt, pt):
+                lp, _, _ = layer.forward_np(xt.detach().cpu().numpy(), pt.detach().cpu().numpy(), noise)
+                return torch.from_numpy(lp).to(pt.device)
+
+            @staticmethod
+            def backward(ctx, g):
+                dx, dp, _ = layer.backward_np(g.detach().cpu().numpy())
+                return torch.from_numpy(np.ascontiguousarray(dx)).to(g.device), torch.from_numpy(dp).to(g.device)
+
+        xt = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x, np.float32))
+        pt = ps if isinstance(ps, torch.Tensor) else torch.as_tensor(np.asarray(ps, np.float32))
+        lp = _Fn.apply(xt, pt).reshape(1, -1)
+        return (lp, lp, lp), st

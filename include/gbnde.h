@@ -148,6 +148,23 @@ int gbnde_backward(gbnde_ctx* ctx, const float* dL_dusave, float* dL_du0, float*
 int gbnde_backward_device(gbnde_ctx* ctx, const float* dL_dusave_dev, float* dL_du0_dev,
                           float* dL_dp_dev, gbnde_stats* stats);
 
+/* ---- FFJORD (continuous normalizing flow) ------------------------------------------
+ * Replaces __forward_ffjord (src/ffjord.jl:140-178): solves the augmented
+ * system [z; delta_logp] with right-hand side [f(z [, t]); -trace(df/dz)] from
+ * (x, 0) over [t0, t1], keeping only the end state (:154-157), and returns
+ * logpx = logpz(z(t1)) - delta_logp(t1) for the standard-normal base
+ * (:171-176). The model is the context's chain with state dim d (time_input
+ * appends t to its input). noise: d x B Hutchinson directions, fixed for the
+ * solve (monte_carlo = true), or NULL for the exact trace (monte_carlo =
+ * false). FP32 arithmetic in both precisions; desc->saveat is ignored. */
+int gbnde_ffjord_forward(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int d, int B, const float* x,
+                         const float* noise, float* logpx, float* zT, gbnde_stats* stats);
+/* Gradient of a loss of logpx (and optionally of z(t1)) through the
+ * InterpolatingAdjoint of the last gbnde_ffjord_forward (sensealg at
+ * src/ffjord.jl:143). dL_dzT may be NULL. Outputs dL/dx (d x B) and dL/dp. */
+int gbnde_ffjord_backward(gbnde_ctx* ctx, const float* dL_dlogpx, const float* dL_dzT, float* dL_dx,
+                          float* dL_dp, gbnde_stats* stats);
+
 /* ---- multiple shooting -------------------------------------------------------------
  * Replaces the per-group solves of multiple_shoot (src/multiple_shooting.jl:52-62):
  * segment i solves from u0[:, i] over [t0, t1] with its own adaptive Tsit5

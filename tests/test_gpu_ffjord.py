@@ -1,0 +1,72 @@
+"""FFJORD (FP32 form) against the FP64 oracle through the C ABI: logpx with the
+Hutchinson and the exact trace, and the InterpolatingAdjoint gradient of the
+mean negative log-likelihood.
+
+Tolerances: logpx 1e-4 relative to max|logpx| (adaptive FP32 vs FP64 at
+1e-7); gradients 1e-3 relative (norm)."""
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="no CUDA GPU")]
+
+
+def _case(d, H, B, act, exact, seed, tol=1e-7):
+    import gbnde
+    from oracle import ffjord as off
+    from oracle import mlp as omlp
+    from oracle import tsit5 as ots
+    rng = np.random.default_rng(seed)
+    model = gbnde.Chain(gbnde.Dense(d + 1, H, act), gbnde.Dense(H, H, act), gbnde.Dense(H, d))
+    p = model.init_params(rng)
+    x = rng.standard_normal((d, B)).astype(np.float32)
+    fj = gbnde.FFJORD(model, (0.0, 1.0), (d,), gbnde.Tsit5(), abstol=tol, reltol=tol, time_input=True)
+    noise = None if exact else fj.draw_noise(rng, B)
+    logpx, zT, st = fj.forward_np(x, p, noise)
+    assert st.retcode == 0
+    om = omlp.MLP(model.dims, model.acts, time_input=True)
+    rhs = off.FFJORDRHS(om, p.astype(np.float64), noise=None if exact else noise.T.astype(np.float64),
+                        exact=exact)
+    y0 = np.vstack([x.astype(np.float64), np.zeros((1, B))])
+    ys, fwd = ots.solve_forward(rhs, y0, 0.0, 1.0, [1.0], tol, tol)
+    ref = off.logpx_from_final(ys[..., 0], d)
+    assert np.abs(logpx - ref).max() < 1e-4 * np.abs(ref).max()
+    assert np.abs(zT - ys[:d, :, 0]).max() < 1e-4 * np.abs(ys[:d]).max()
+    # gradient of the mean negative log-likelihood
+    g = -np.ones(B) / B
+    dx, dp, sta = fj.backward_np(g.astype(np.float32))
+    assert sta.retcode_adj == 0
+    dy = np.vstack([-ys[:d, :, 0] * g, -g[None, :]])
+    gu, gp, _ = ots.adjoint_interpolating(rhs, fwd, [1.0], dy[..., None], 0.0, tol, tol)
+    rel = lambda a, b: np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b)  # noqa: E731
+    assert rel(dp, gp) < 1e-3
+    assert rel(dx, gu[:d]) < 1e-3
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_ffjord_small(exact):
+    _case(2, 16, 64, "tanh", exact, 0)
+
+
+def test_ffjord_config3_structure():
+    """d = 16, (16+1) -> 512 -> 512 -> 16 softplus with time concatenated."""
+    _case(16, 512, 96, "softplus", False, 1, tol=1e-5)
+
+
+def test_ffjord_layer_torch_autograd():
+    import torch
+
+    import gbnde
+    d, H, B = 2, 12, 32
+    rng = np.random.default_rng(3)
+    model = gbnde.Chain(gbnde.Dense(d + 1, H, "tanh"), gbnde.Dense(H, d))
+    fj = gbnde.FFJORD(model, (0.0, 1.0), (d,), gbnde.Tsit5(), abstol=1e-6, reltol=1e-6, time_input=True)
+    p, st = fj.setup(rng)
+    x = torch.tensor(rng.standard_normal((d, B)).astype(np.float32), requires_grad=True)
+    pt = torch.tensor(p, requires_grad=True)
+    (logpx, _, _), st = fj(x, pt, st)
+    loss = -logpx.mean()
+    loss.backward()
+    assert torch.isfinite(pt.grad).all() and torch.count_nonzero(pt.grad) > 0
+    assert x.grad.shape == x.shape and torch.isfinite(x.grad).all()
