@@ -371,14 +371,19 @@ static int validate_desc(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B) 
   if (S != c->S + (c->ff_on ? 1 : 0))
     return fail(GBNDE_ERR_INVALID, "state dim %d does not match the model (%d)", S, c->S);
   if (B < 1) return fail(GBNDE_ERR_INVALID, "batch must be >= 1");
-  if (!(d->t1 > d->t0)) return fail(GBNDE_ERR_UNSUPPORTED, "tspan must satisfy t1 > t0");
+  if (!(d->t1 != d->t0)) return fail(GBNDE_ERR_INVALID, "tspan must satisfy t1 != t0");
   if (!(d->abstol > 0) || !(d->reltol >= 0)) return fail(GBNDE_ERR_INVALID, "tolerances must be positive");
   if (d->nsave < 1 || !d->saveat) return fail(GBNDE_ERR_INVALID, "saveat must hold >= 1 time");
+  const double tdir = d->t1 > d->t0 ? 1.0 : -1.0;
   for (int i = 0; i < d->nsave; ++i) {
     const double s = d->saveat[i];
-    if (!(s >= d->t0 && s <= d->t1)) return fail(GBNDE_ERR_INVALID, "saveat[%d] = %g outside tspan", i, s);
-    if (i > 0 && s < d->saveat[i - 1]) return fail(GBNDE_ERR_INVALID, "saveat must be non-decreasing");
+    if (!(tdir * (s - d->t0) >= 0 && tdir * (d->t1 - s) >= 0))
+      return fail(GBNDE_ERR_INVALID, "saveat[%d] = %g outside tspan", i, s);
+    if (i > 0 && tdir * (s - d->saveat[i - 1]) < 0)
+      return fail(GBNDE_ERR_INVALID, "saveat must be ordered from t0 to t1");
   }
+  if (tdir < 0 && c->precision == GBNDE_PREC_BF16 && !c->ff_on)
+    return fail(GBNDE_ERR_UNSUPPORTED, "reverse time spans run in the FP32 form");
   if (d->sensealg != GBNDE_SENSE_INTERPOLATING && d->sensealg != GBNDE_SENSE_BACKSOLVE)
     return fail(GBNDE_ERR_INVALID, "unknown sensealg %d", d->sensealg);
   if ((long long)B * S > (1LL << 31)) return fail(GBNDE_ERR_UNSUPPORTED, "S*B too large");
@@ -484,7 +489,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   a.reltol = d->reltol;
   a.dt0 = d->dt0;
   a.dtmin = d->dtmin > 0 ? d->dtmin : 0.0;
-  a.dtmax = d->t1 - d->t0;
+  a.dtmax = std::fabs(d->t1 - d->t0);
   a.maxiters = maxiters;
   a.saveat = c->saveat_d.as<double>();
   a.nsave = nsave;
@@ -773,6 +778,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
                          float* dLdp, bool out_host, gbnde_stats* stats) {
   if (!c) return fail(GBNDE_ERR_INVALID, "null context");
   if (!c->have_fwd) return fail(GBNDE_ERR_STATE, "backward needs a successful forward solve first");
+  if (!(c->t1 > c->t0)) return fail(GBNDE_ERR_UNSUPPORTED, "gradients of reverse time spans");
   if (!dLdu || !dLdu0 || !dLdp) return fail(GBNDE_ERR_INVALID, "null argument");
   if (int r = set_device(c)) return r;
   const int S = c->fS, B = c->B, nsave = c->nsave;

@@ -10,5 +10,6 @@ from .layers import (  # noqa: F401
     Array, BacksolveAdjoint, Chain, Dense, GB300Tsit5, InterpolatingAdjoint, NeuralODE,
     ODESolution, Solver, Tsit5, WrappedFunction, ZygoteVJP, cube,
 )
-from .ffjord import FFJORD  # noqa: F401
+from .ffjord import FFJORD, FFJORDDistribution  # noqa: F401
+from .layers import AugmentedNDELayer, DimMover  # noqa: F401
 from .multiple_shooting import group_ranges, multiple_shoot, multiple_shoot_batch  # noqa: F401

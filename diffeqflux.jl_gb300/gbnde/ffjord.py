@@ -124,3 +124,36 @@ class FFJORD:
         pt = ps if isinstance(ps, torch.Tensor) else torch.as_tensor(np.asarray(ps, np.float32))
         lp = _Fn.apply(xt, pt).reshape(1, -1)
         return (lp, lp, lp), st
+
+
+class FFJORDDistribution:
+    """``FFJORDDistribution(model, ps, st)`` (src/ffjord.jl:217-246): `rand` solves
+    the flow backwards in time from base samples (``reverse(tspan)``, :183-214)
+    and returns z; `logpdf` is the forward logpx."""
+
+    def __init__(self, model, ps, st):
+        self.model, self.ps, self.st = model, ps, st
+        self._rev = FFJORD(model.model, (model.tspan[1], model.tspan[0]), (model.d,), model.alg,
+                           abstol=model.abstol, reltol=model.reltol, maxiters=model.maxiters,
+                           time_input=model.time_input, noise=model.noise, device=model.device)
+
+    def __len__(self):
+        return self.model.d
+
+    def logpdf(self, x):
+        x = np.asarray(x, np.float32)
+        x2 = x.reshape(-1, 1) if x.ndim == 1 else x
+        (lp, _, _), _ = self.model(x2, self.ps, self.st)
+        out = np.asarray(lp).reshape(-1)
+        return out[0] if x.ndim == 1 else out
+
+    def pdf(self, x):
+        return np.exp(self.logpdf(x))
+
+    def rand(self, n, rng=None):
+        rng = rng or self.st.get("rng") or np.random.default_rng(0)
+        x = rng.standard_normal((self.model.d, n)).astype(np.float32)
+        noise = self._rev.draw_noise(rng, n)
+        _, zT, st = self._rev.forward_np(x, self.ps, noise)
+        _lib.check(0 if st.retcode == 0 else _lib.ERR_INVALID)
+        return zT

@@ -392,3 +392,49 @@ class NeuralODE:
             if one:
                 arr = arr[:, 0, :]
         return ODESolution(self.saveat, arr, stats.retcode, stats.as_dict()), st
+
+
+class AugmentedNDELayer:
+    """``AugmentedNDELayer(node, adim)`` (src/neural_de.jl:356-386): the state is
+    padded with `adim` zero rows before the wrapped NeuralODE solves it."""
+
+    def __init__(self, node, adim):
+        self.node = node
+        self.adim = int(adim)
+
+    def setup(self, rng):
+        return self.node.setup(rng)
+
+    def augment(self, x):
+        try:
+            import torch
+            if isinstance(x, torch.Tensor):
+                z = x.new_zeros((self.adim,) + tuple(x.shape[1:]))
+                return torch.cat([x, z], dim=0)
+        except ImportError:  # pragma: no cover
+            pass
+        x = np.asarray(x, dtype=np.float32)
+        return np.concatenate([x, np.zeros((self.adim,) + x.shape[1:], np.float32)], axis=0)
+
+    def __call__(self, x, p, st=None):
+        return self.node(self.augment(x), p, st)
+
+
+class DimMover:
+    """``DimMover(from_dim, to_dim)`` (src/neural_de.jl:397-412): moves an array
+    axis (1-based, negative counts from the end), e.g. the time axis of a solution."""
+
+    def __init__(self, from_dim=-2, to_dim=-1):
+        self.from_dim, self.to_dim = from_dim, to_dim
+
+    def __call__(self, x, p=None, st=None):
+        nd = np.ndim(x)
+        f = self.from_dim - 1 if self.from_dim > 0 else nd + self.from_dim
+        t = self.to_dim - 1 if self.to_dim > 0 else nd + self.to_dim
+        try:
+            import torch
+            if isinstance(x, torch.Tensor):
+                return torch.movedim(x, f, t), st
+        except ImportError:  # pragma: no cover
+            pass
+        return np.moveaxis(np.asarray(x), f, t), st

@@ -70,3 +70,37 @@ def test_ffjord_layer_torch_autograd():
     loss.backward()
     assert torch.isfinite(pt.grad).all() and torch.count_nonzero(pt.grad) > 0
     assert x.grad.shape == x.shape and torch.isfinite(x.grad).all()
+
+
+def test_ffjord_distribution_sampling_inverts_the_flow():
+    """rand() solves the flow backwards (reverse tspan); pushing the samples
+    forward again must return the base draws (src/ffjord.jl:183-246)."""
+    import gbnde
+    d, H, n = 2, 16, 64
+    rng = np.random.default_rng(4)
+    model = gbnde.Chain(gbnde.Dense(d + 1, H, "tanh"), gbnde.Dense(H, d))
+    fj = gbnde.FFJORD(model, (0.0, 1.0), (d,), gbnde.Tsit5(), abstol=1e-8, reltol=1e-8, time_input=True)
+    p, st = fj.setup(rng)
+    st["rng"] = np.random.default_rng(9)
+    dist = gbnde.FFJORDDistribution(fj, p, st)
+    z = dist.rand(n)
+    assert z.shape == (d, n) and np.all(np.isfinite(z))
+    base = np.random.default_rng(9).standard_normal((d, n)).astype(np.float32)
+    _, zT, _ = fj.forward_np(z, p, fj.draw_noise(np.random.default_rng(1), n))
+    assert np.abs(zT - base).max() < 1e-4 * max(1.0, np.abs(base).max())
+    lp = dist.logpdf(z)
+    assert lp.shape == (n,) and np.all(np.isfinite(lp))
+
+
+def test_augmented_layer_pads_the_state():
+    import gbnde
+    S, a = 2, 2
+    model = gbnde.Chain(gbnde.Dense(S + a, 8, "tanh"), gbnde.Dense(8, S + a))
+    node = gbnde.NeuralODE(model, (0.0, 1.0), gbnde.Tsit5(), saveat=[0.0, 1.0])
+    anode = gbnde.AugmentedNDELayer(node, a)
+    p, st = anode.setup(np.random.default_rng(0))
+    x = np.array([[1.0, 0.5], [0.0, -0.5]], np.float32)
+    sol, _ = anode(x, p, st)
+    arr = np.asarray(sol)
+    assert arr.shape == (S + a, 2, 2)
+    assert np.allclose(arr[S:, :, 0], 0.0)
