@@ -43,6 +43,10 @@ METRIC = "NeuralODE grad evals/sec, BF16-TC vs plain FP32 GPU, at <=1e-3 rel err
 UNIT = "grad_evals/s"
 
 
+def workload_name(B):
+    return f"neuralode_b{B}_s64_h256x2_tanh_nsave20"
+
+
 def workload(S=64, H=256, B=16384, nsave=20, seed=1):
     from scipy.linalg import expm
     rng = np.random.default_rng(seed)
@@ -167,7 +171,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": "neuralode_b16384_s64_h256x2_tanh_nsave20", "batch": wl["B"],
+        "config": {"workload": workload_name(wl["B"]), "batch": wl["B"],
                    "state": wl["S"], "hidden": wl["H"], "nsave": 20, "abstol": 1e-7, "reltol": 1e-5,
                    "sensealg": "InterpolatingAdjoint"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -180,13 +184,87 @@ def run_reference(args):
     return 0
 
 
+class Form:
+    """One precision form of the solver with its device buffers; ``grad_eval``
+    is one training-step gradient: forward solve, fused MSE at the save
+    points, adjoint solve (four kernel launches)."""
+
+    LAUNCHES_PER_EVAL = 4   # forward, loss, adjoint, quadrature reduction
+
+    def __init__(self, wl, precision, local, dev, u0_d, tg_d, p_d):
+        import ctypes as C
+
+        import torch
+
+        import gbnde
+        from gbnde import _lib
+        S, B, H = wl["S"], wl["B"], wl["H"]
+        model = gbnde.Chain(gbnde.Dense(S, H, "tanh"), gbnde.Dense(H, H, "tanh"), gbnde.Dense(H, S))
+        self.solver = gbnde.Solver(model, precision, local)
+        self.lib = self.solver.lib
+        self.desc = gbnde.Solver.solve_desc(0.0, 1.0, wl["ts"], wl["abstol"], wl["reltol"], 0)
+        ns = len(wl["ts"])
+        self.u0_d, self.tg_d = u0_d, tg_d
+        self.us_d = torch.empty((ns, B, S), dtype=torch.float32, device=dev)
+        self.dl_d = torch.empty_like(self.us_d)
+        self.du0_d = torch.empty((B, S), dtype=torch.float32, device=dev)
+        self.dp_d = torch.empty(self.solver.nparams, dtype=torch.float32, device=dev)
+        self.solver.set_params_device(p_d)
+        torch.cuda.synchronize()
+        # The library launches on a torch-owned stream: pinned-memory copies
+        # issued on it stay valid however the objects are torn down (torch's
+        # host allocator records events on every stream a pinned block was
+        # used on, also when the block is freed).
+        self.lstream = torch.cuda.Stream(device=dev)
+        _lib.check(self.lib.gbnde_set_stream(self.solver.h, C.c_void_p(self.lstream.cuda_stream)))
+        self.st_f, self.st_b, self.loss = _lib.Stats(), _lib.Stats(), C.c_double()
+        self._C, self._check, self.S, self.B = C, _lib.check, S, B
+
+    def grad_eval(self):
+        C, lib, h = self._C, self.lib, self.solver.h
+        self._check(lib.gbnde_forward_device(h, C.byref(self.desc), self.S, self.B,
+                                             self.u0_d.data_ptr(), self.us_d.data_ptr(),
+                                             C.byref(self.st_f)))
+        self._check(lib.gbnde_loss_device(h, self.us_d.data_ptr(), self.tg_d.data_ptr(), 1,
+                                          self.dl_d.data_ptr(), C.byref(self.loss)))
+        self._check(lib.gbnde_backward_device(h, self.dl_d.data_ptr(), self.du0_d.data_ptr(),
+                                              self.dp_d.data_ptr(), C.byref(self.st_b)))
+
+    def timed(self, steps, flush):
+        """Device time (ms) of `steps` gradient evaluations, L2 flushed before each."""
+        import torch
+        tot = 0.0
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(self.lstream)
+            self.grad_eval()
+            e1.record(self.lstream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot
+
+
+def profiled_traffic(kernel, workload_name):
+    """DRAM bytes per launch of `kernel` on `workload_name` from the committed
+    ncu summaries: a line `traffic_bytes_per_launch <kernel> <workload> = N`."""
+    import glob
+    import re
+    pat = re.compile(r"traffic_bytes_per_launch\s+(\S+)\s+(\S+)\s*=\s*([0-9.eE+]+)")
+    for fn in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        for ln in open(fn):
+            m = pat.search(ln)
+            if m and m.group(1) == kernel and m.group(2) == workload_name:
+                return float(m.group(3)), os.path.relpath(fn, ROOT)
+    return None, None
+
+
 def run_gpu(args):
     import ctypes as C
 
     import torch
-
-    import gbnde
-    from gbnde import _lib
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -199,37 +277,18 @@ def run_gpu(args):
 
     wl = workload(B=args.batch)
     S, B = wl["S"], wl["B"]
-    model = gbnde.Chain(gbnde.Dense(S, wl["H"], "tanh"), gbnde.Dense(wl["H"], wl["H"], "tanh"),
-                        gbnde.Dense(wl["H"], S))
-    solver = gbnde.Solver(model, args.precision, local)
-    lib = solver.lib
-    desc = gbnde.Solver.solve_desc(0.0, 1.0, wl["ts"], wl["abstol"], wl["reltol"], 0)
-    ns = len(wl["ts"])
     dev = torch.device("cuda", local)
+    ns = len(wl["ts"])
     # column-major device buffers
     u0_d = torch.from_numpy(np.ascontiguousarray(wl["u0"].T)).to(dev)
     tg_d = torch.from_numpy(np.ascontiguousarray(np.transpose(wl["target"], (2, 1, 0)))).to(dev)
     p_d = torch.from_numpy(wl["p"]).to(dev)
-    us_d = torch.empty((ns, B, S), dtype=torch.float32, device=dev)
-    dl_d = torch.empty_like(us_d)
-    du0_d = torch.empty((B, S), dtype=torch.float32, device=dev)
-    dp_d = torch.empty(solver.nparams, dtype=torch.float32, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    solver.set_params_device(p_d)
-    torch.cuda.synchronize()
-    lstream = torch.cuda.ExternalStream(lib.gbnde_stream(solver.h), device=dev)
-
-    st_f = _lib.Stats()
-    st_b = _lib.Stats()
-    loss = C.c_double()
-
-    def grad_eval():
-        _lib.check(lib.gbnde_forward_device(solver.h, C.byref(desc), S, B, u0_d.data_ptr(),
-                                            us_d.data_ptr(), C.byref(st_f)))
-        _lib.check(lib.gbnde_loss_device(solver.h, us_d.data_ptr(), tg_d.data_ptr(), 1,
-                                         dl_d.data_ptr(), C.byref(loss)))
-        _lib.check(lib.gbnde_backward_device(solver.h, dl_d.data_ptr(), du0_d.data_ptr(),
-                                             dp_d.data_ptr(), C.byref(st_b)))
+    form = Form(wl, args.precision, local, dev, u0_d, tg_d, p_d)
+    solver, lib, lstream = form.solver, form.lib, form.lstream
+    st_f, st_b, loss = form.st_f, form.st_b, form.loss
+    du0_d, dp_d = form.du0_d, form.dp_d
+    grad_eval = form.grad_eval
 
     for _ in range(args.warmup):
         grad_eval()
@@ -311,12 +370,33 @@ def run_gpu(args):
     peak_tf = peaks.get("bf16_tflops", 1900.0)
     peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
     bwd_ms_avg = k_bwd / args.steps
+    kname = "bwd_tc_kernel" if args.precision == "bf16" else "bwd_f32_kernel"
+    traffic, traffic_src = profiled_traffic(kname, workload_name(B))
     achieved_tf = (flops / args.steps) / (bwd_ms_avg / 1000.0) / 1e12
-    roof = {"kernel": "bwd_%s_kernel" % args.precision.replace("fp32", "f32"),
+    roof = {"kernel": kname,
             "bound": "tensor", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
             "frac": achieved_tf / peak_tf, "peak_source": peak_src,
-            "traffic": None,
+            "traffic": traffic, "traffic_source": traffic_src,
             "basis": "GEMM FLOPs of the adjoint launch: F*nf_recompute + 3F*nf_adj, F = 2*B*sum(in*out)"}
+
+    # ---- the plain FP32 form on the same inputs: speed ratio and agreement ------
+    fp32 = None
+    if args.precision == "bf16" and not args.no_fp32_form:
+        g_tc = dp_d.double().cpu().numpy()
+        loss_tc = loss.value
+        f32 = Form(wl, "fp32", local, dev, u0_d, tg_d, p_d)
+        f32.grad_eval()
+        torch.cuda.synchronize()
+        n32 = max(1, min(args.steps, 3))
+        ms32 = f32.timed(n32, flush) / n32
+        g32 = f32.dp_d.double().cpu().numpy()
+        fp32 = {"value": 1000.0 / ms32, "ms_per_step": ms32, "steps": n32,
+                "speedup_of_bf16_form": (value / world) * ms32 / 1000.0,
+                "loss_rel_diff": abs(loss_tc - f32.loss.value) / abs(f32.loss.value),
+                "grad_rel_diff": float(np.linalg.norm(g_tc - g32) / np.linalg.norm(g32)),
+                "note": "plain FP32 kernels, same inputs; the FP32 form agrees with the FP64 "
+                        "oracle to ~1e-6, so the differences bound the BF16 form's error"}
+        del f32
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -330,12 +410,13 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
         "data": "synthetic (seeded)",
-        "config": {"workload": "neuralode_b16384_s64_h256x2_tanh_nsave20", "batch": B, "state": S,
+        "config": {"workload": workload_name(B), "batch": B, "state": S,
                    "hidden": wl["H"], "nsave": ns, "abstol": 1e-7, "reltol": 1e-5,
                    "sensealg": "InterpolatingAdjoint", "loss": "MSE", "precision": args.precision,
                    "l2": "flushed between steps (256 MB write)", "parallelism": "replicas"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": args.steps * 4,
+        "gpu_launches": args.steps * Form.LAUNCHES_PER_EVAL,
+        "fp32_form": fp32,
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk,
@@ -355,14 +436,15 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16"])
+    ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16"])
     ap.add_argument("--batch", type=int, default=16384)
     ap.add_argument("--cpu-sample", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp32-form", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

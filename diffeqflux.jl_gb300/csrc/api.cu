@@ -692,7 +692,9 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
     t.hoff[l] = hv;
     hv += 32 * ((m.dims[l] + 63) / 64);
   }
-  t.hvals = std::max(hv, 4);
+  t.hx = hv;
+  hv += 32;
+  t.hvals = hv;
   int nb = 0;
   for (int l = 0; l < L; ++l) {
     t.boffp[l] = nb;

@@ -58,6 +58,22 @@ __device__ __forceinline__ void st32(float* p, int n, bool vec, const float* x) 
   }
 }
 
+// Thread-private FP32 scratch in slot-major layout: float4 slot k of thread t
+// at hs4[k * 256 + t], so the 32 lanes of a warp touch 512 contiguous bytes.
+__device__ __forceinline__ void hs_ld32(const float4* hs4, int k0, float* x) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float4 q = hs4[(size_t)(k0 + j) * tc::kEpiThreads + threadIdx.x];
+    x[4 * j] = q.x; x[4 * j + 1] = q.y; x[4 * j + 2] = q.z; x[4 * j + 3] = q.w;
+  }
+}
+__device__ __forceinline__ void hs_st32(float4* hs4, int k0, const float* x) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    hs4[(size_t)(k0 + j) * tc::kEpiThreads + threadIdx.x] =
+        make_float4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
+}
+
 __device__ __forceinline__ bool epi_grid_barrier(const BwdArgs& a, unsigned int& gen, int* okflag) {
   tc::epi_bar();
   gen += 1;
@@ -179,11 +195,12 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
   __syncthreads();
   tc::tc_fence_after();
 
-  if (warp == tc::kMmaWarp) {
-    tc::mma_loop(A.ops, sh, aring, wring);
-  } else if (warp == tc::kTmaWarp) {
-    tc::tma_loop(A.ops, sh, aring, wring);
+  if (warp >= tc::kMmaWarp) {
+    tc::regs_give_ctl();
+    if (warp == tc::kMmaWarp) tc::mma_loop(A.ops, sh, aring, wring);
+    else if (warp == tc::kTmaWarp) tc::tma_loop(A.ops, sh, aring, wring);
   } else {
+    tc::regs_take_epi();
     // ======================= epilogue warps =======================
     const MlpDev& m = a.mlp;
     const int L = m.nlayers;
@@ -207,7 +224,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     double dt = 0.0, qold = kQoldInit;
     bool swp = false, ok = true;
     uint8_t* img = A.img + (size_t)blockIdx.x * A.img_cta;
-    float* hscr = A.hscr + ((size_t)blockIdx.x * tc::kEpiThreads + threadIdx.x) * A.hvals;
+    float4* hs4 = reinterpret_cast<float4*>(A.hscr + (size_t)blockIdx.x * tc::kEpiThreads * A.hvals);
     float* bpart = A.bpart + (size_t)blockIdx.x * 4 * A.nbias;
     float* mu_acc = a.mu_acc + (size_t)blockIdx.x * a.P;
     float* mu_comp = A.mu_comp + (size_t)blockIdx.x * a.P;
@@ -262,6 +279,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         const float y = (i < th.nmine) ? x[i] : 0.f;
         v[i] = m.cube ? y * y * y : y;
       }
+      if (m.cube) hs_st32(hs4, A.hx / 4, x);  // for the chain rule through x^3 at the end
       if (!emit(es, sh, aring, th, v, true, img + A.aoff[0], A.a_isA[0], (m.dims[0] + 63) / 64, A.nh[0], 0))
         return false;
       // forward recompute of the hidden layers
@@ -270,12 +288,18 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         const float* b = A.bias[l];
         uint32_t col;
         if (!tc::epi_wait_acc(es, sh, &col)) return false;
-        for (int cc = 0; cc < (N + 63) / 64; ++cc) {
+        const int nch = (N + 63) / 64;
+        float bnext[32];
+        tc::load_bias32(b, 32 * th.ch, N, bnext);
+        for (int cc = 0; cc < nch; ++cc) {
           const int n0 = 64 * cc + 32 * th.ch;
-          tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+          float bc[32];
 #pragma unroll
-          for (int i = 0; i < 32; ++i) v[i] = (n0 + i < N) ? act_apply(v[i] + __ldg(b + n0 + i), m.act[l]) : 0.f;
-          st32(hscr + A.hoff[l + 1] + 32 * cc, 32, true, v);
+          for (int i = 0; i < 32; ++i) bc[i] = bnext[i];
+          if (cc + 1 < nch) tc::load_bias32(b, n0 + 64, N, bnext);
+          tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+          tc::bias_act32(v, bc, m.act[l], n0, N);
+          hs_st32(hs4, (A.hoff[l + 1] + 32 * cc) / 4, v);
           if (!emit(es, sh, aring, th, v, l + 1 <= L - 2, img + A.aoff[l + 1], A.a_isA[l + 1],
                     (N + 63) / 64, A.nh[l + 1], cc))
             return false;
@@ -300,13 +324,20 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       // VJP chain
       for (int l = L - 1; l >= 1; --l) {
         const int N = m.dims[l];
+        const int nch = (N + 63) / 64;
+        // the stored activations of this layer are known before the
+        // accumulator: fetch chunk 0 now and chunk cc+1 while working on cc
+        float hnext[32];
+        hs_ld32(hs4, A.hoff[l] / 4, hnext);
         uint32_t col;
         if (!tc::epi_wait_acc(es, sh, &col)) return false;
-        for (int cc = 0; cc < (N + 63) / 64; ++cc) {
+        for (int cc = 0; cc < nch; ++cc) {
           const int n0 = 64 * cc + 32 * th.ch;
           float h[32];
+#pragma unroll
+          for (int i = 0; i < 32; ++i) h[i] = hnext[i];
+          if (cc + 1 < nch) hs_ld32(hs4, (A.hoff[l] + 32 * (cc + 1)) / 4, hnext);
           tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
-          ld32(hscr + A.hoff[l] + 32 * cc, 32, true, h);
 #pragma unroll
           for (int i = 0; i < 32; ++i) v[i] = (n0 + i < N) ? v[i] * act_deriv_from_out(h[i], m.act[l - 1]) : 0.f;
           if (!emit(es, sh, aring, th, v, true, img + A.doff[l - 1], !A.a_isA[l - 1], (N + 63) / 64,
@@ -328,10 +359,12 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         if (!tc::epi_wait_acc(es, sh, &col)) return false;
         tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)(32 * th.ch), v);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          float g = (i < th.nmine) ? v[i] : 0.f;
-          if (m.cube) g *= 3.f * x[i] * x[i];
-          kl[i] = g;
+        for (int i = 0; i < 32; ++i) kl[i] = (i < th.nmine) ? v[i] : 0.f;
+        if (m.cube) {
+          float xc[32];
+          hs_ld32(hs4, A.hx / 4, xc);
+#pragma unroll
+          for (int i = 0; i < 32; ++i) kl[i] *= 3.f * xc[i] * xc[i];
         }
         tc::epi_release_acc(es, sh);
       }
@@ -340,8 +373,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       for (int l = 0; l < L; ++l) {
         const int out = m.dims[l + 1], in = m.dims[l];
         const int Nn2 = A.a_isA[l] ? out : in;  // N side of the dW op
-        const float* wbase = nullptr;
-        (void)wbase;
         for (int hh = 0; hh < A.nh[l]; ++hh) {
           uint32_t col;
           if (!tc::epi_wait_acc(es, sh, &col)) return false;
@@ -352,38 +383,25 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             for (int cc = 0; cc < (Nn2 + 63) / 64; ++cc) {
               const int n0 = 64 * cc + 32 * th.ch;
               tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
-              // all loads first, then the stores (independent addresses)
-              float pv[32];
               if (isA) {
                 // row mrow = in feature; 32 consecutive out features
-                const bool full = mrow < in && n0 + 32 <= out && (out % 4 == 0);
                 float* rowp = Pw + (size_t)mrow * out + n0;
+                const bool full = mrow < in && n0 + 32 <= out && (reinterpret_cast<uintptr_t>(rowp) & 15) == 0;
                 if (full) {
 #pragma unroll
-                  for (int i = 0; i < 32; i += 4) {
-                    const float4 q4 = *reinterpret_cast<const float4*>(rowp + i);
-                    pv[i] = q4.x; pv[i + 1] = q4.y; pv[i + 2] = q4.z; pv[i + 3] = q4.w;
-                  }
-#pragma unroll
                   for (int i = 0; i < 32; i += 4)
-                    *reinterpret_cast<float4*>(rowp + i) =
-                        make_float4(fmaf(c, v[i], pv[i]), fmaf(c, v[i + 1], pv[i + 1]),
-                                    fmaf(c, v[i + 2], pv[i + 2]), fmaf(c, v[i + 3], pv[i + 3]));
+                    tc::red_add_v4(rowp + i, c * v[i], c * v[i + 1], c * v[i + 2], c * v[i + 3]);
                 } else if (mrow < in) {
 #pragma unroll
-                  for (int i = 0; i < 32; ++i) pv[i] = (n0 + i < out) ? rowp[i] : 0.f;
-#pragma unroll
                   for (int i = 0; i < 32; ++i)
-                    if (n0 + i < out) rowp[i] = fmaf(c, v[i], pv[i]);
+                    if (n0 + i < out) tc::red_add(rowp + i, c * v[i]);
                 }
               } else if (mrow < out) {
                 // row mrow = out feature; in features n0.. at stride `out`
                 float* colp = Pw + (size_t)n0 * out + mrow;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) pv[i] = (n0 + i < in) ? colp[(size_t)i * out] : 0.f;
-#pragma unroll
                 for (int i = 0; i < 32; ++i)
-                  if (n0 + i < in) colp[(size_t)i * out] = fmaf(c, v[i], pv[i]);
+                  if (n0 + i < in) tc::red_add(colp + (size_t)i * out, c * v[i]);
               }
             }
           }
@@ -399,8 +417,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           const int o = f - A.boffp[l];
           if (o < m.dims[l + 1]) {
             const float s = ((bpart[f] + bpart[A.nbias + f]) + bpart[2 * A.nbias + f]) + bpart[3 * A.nbias + f];
-            float* pp = P + m.boff[l] + o;
-            *pp = fmaf(c, s, *pp);
+            tc::red_add(P + m.boff[l] + o, c * s);
           }
         }
         tc::epi_bar();
@@ -423,7 +440,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       const size_t g = gofs(tile);
       float acc[32];
       ld32(slot + g, th.nmine, vec, x);
+#pragma unroll
       for (int i = 0; i < 32; ++i) acc[i] = 0.f;
+#pragma unroll
       for (int j = 0; j < 7; ++j) {
         float kj[32];
         ld32(slot + (size_t)(j + 1) * SB + g, th.nmine, vec, kj);
@@ -468,7 +487,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           float l[32], f[32];
           ld32(a.lam[cur] + gofs(tile), th.nmine, vec, l);
           ld32(klb(0) + gofs(tile), th.nmine, vec, f);
-          for (int i = 0; i < th.nmine; ++i) {
+          #pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            if (i >= th.nmine) continue;
             const float sk = (float)a.abstol + fabsf(l[i]) * (float)a.reltol;
             const double xx = (double)(l[i] / sk), yy = (double)(f[i] / sk);
             p0 += xx * xx;
@@ -507,12 +528,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           float li[32];
           for (int i = 0; i < 32; ++i) li[i] = l[i] + hf * f0[i];
           ok = adj_eval(li, x, nullptr, 0.f, f1);
-          if (v)
-            for (int i = 0; i < th.nmine; ++i) {
+          if (v) {
+            #pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              if (i >= th.nmine) continue;
               const float sk = (float)a.abstol + fabsf(l[i]) * (float)a.reltol;
               const double z = (double)((f1[i] - f0[i]) / sk);
               p2 += z * z;
             }
+          }
         }
         ++nf_adj;
         if (!ok) break;
@@ -560,7 +584,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             if (v) {
               ld32(lcur + g, th.nmine, vec, l);
               ld32(ccur + g, th.nmine, vec, s);
-              for (int j = 0; j < i; ++j) {
+#pragma unroll
+              for (int j = 0; j < 6; ++j) {
+                if (j >= i) break;
                 float kj[32];
                 ld32(klb(j) + g, th.nmine, vec, kj);
 #pragma unroll
@@ -583,8 +609,13 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             if (v) {
               st32(klb(i) + g, th.nmine, vec, kl);
               if (i == 6) {
+                // lam and the stage value again (stored above): nothing of
+                // the stage arithmetic stays in registers across adj_eval
+                ld32(lcur + g, th.nmine, vec, l);
+                ld32(lnew + g, th.nmine, vec, Y);
                 float lt[32];
                 for (int q = 0; q < 32; ++q) lt[q] = (float)(H * c_tab.btilde[6]) * kl[q];
+#pragma unroll
                 for (int j = 0; j < 6; ++j) {
                   float kj[32];
                   ld32(klb(j) + g, th.nmine, vec, kj);
@@ -592,7 +623,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
 #pragma unroll
                   for (int q = 0; q < 32; ++q) lt[q] = fmaf(hbt, kj[q], lt[q]);
                 }
-                for (int q = 0; q < th.nmine; ++q) {
+                #pragma unroll
+                for (int q = 0; q < 32; ++q) {
+                  if (q >= th.nmine) continue;
                   const float sc = (float)a.abstol + fmaxf(fabsf(l[q]), fabsf(Y[q])) * (float)a.reltol;
                   const double rr = (double)(lt[q] / sc);
                   perr += isfinite(Y[q]) ? rr * rr : (double)INFINITY;
@@ -619,8 +652,10 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           const float4* Pm = reinterpret_cast<const float4*>(Pmid);
           float4* acc4 = reinterpret_cast<float4*>(mu_acc);
           float4* cmp4 = reinterpret_cast<float4*>(mu_comp);
+#pragma unroll 4
           for (size_t k = threadIdx.x; k < (size_t)a.P / 4; k += tc::kEpiThreads) {
-            const float4 p1 = P1[k], pm = Pm[k], cm = cmp4[k], ac = acc4[k];
+            // pending buffers were summed by L2 adds: read them from L2
+            const float4 p1 = __ldcg(P1 + k), pm = __ldcg(Pm + k), cm = cmp4[k], ac = acc4[k];
             float4 na, nc;
             auto kahan = [&](float p1v, float pmv, float cmv, float acv, float& nav, float& ncv) {
               const float y = fmaf(Hf, p1v + pmv, -cmv);
@@ -706,6 +741,7 @@ __global__ void reduce_mu_comp_kernel(const float* __restrict__ acc, const float
 }
 
 int launch_bwd_tc(const BwdTcArgs& a, int grid, cudaStream_t st) {
+  if (tc_check_regs((const void*)bwd_tc_kernel)) return -1;
   cudaError_t e = cudaFuncSetAttribute(bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        tc::kSmemBytes);
   if (e != cudaSuccess) return -1;

@@ -113,12 +113,17 @@ __device__ __forceinline__ bool epi_rhs(const FwdTcArgs& A, tc::EpiState& e, tc:
     const float* b = A.bias[l];
     uint32_t col;
     if (!tc::epi_wait_acc(e, sh, &col)) return false;
-    for (int c = 0; c < (N + 63) / 64; ++c) {
-      float v[32];
+    const int nch = (N + 63) / 64;
+    float bnext[32];
+    tc::load_bias32(b, 32 * th.ch, N, bnext);
+    for (int c = 0; c < nch; ++c) {
+      float v[32], bc[32];
       const int n0 = 64 * c + 32 * th.ch;
-      tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = (n0 + i < N) ? act_apply(v[i] + __ldg(b + n0 + i), act) : 0.f;
+      for (int i = 0; i < 32; ++i) bc[i] = bnext[i];
+      if (c + 1 < nch) tc::load_bias32(b, n0 + 64, N, bnext);
+      tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+      tc::bias_act32(v, bc, act, n0, N);
       if (!tc::epi_write_a(e, sh, aring, th.r, th.ch, v)) return false;
     }
     tc::epi_release_acc(e, sh);
@@ -127,10 +132,11 @@ __device__ __forceinline__ bool epi_rhs(const FwdTcArgs& A, tc::EpiState& e, tc:
     const float* b = A.bias[m.nlayers - 1];
     uint32_t col;
     if (!tc::epi_wait_acc(e, sh, &col)) return false;
-    float v[32];
+    float v[32], bc[32];
+    tc::load_bias32(b, 32 * th.ch, m.dims[m.nlayers], bc);
     tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)(32 * th.ch), v);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) kout[i] = (i < th.nmine) ? v[i] + __ldg(b + 32 * th.ch + i) : 0.f;
+    for (int i = 0; i < 32; ++i) kout[i] = (i < th.nmine) ? v[i] + bc[i] : 0.f;
     tc::epi_release_acc(e, sh);
   }
   return true;
@@ -154,11 +160,12 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
   __syncthreads();
   tc::tc_fence_after();
 
-  if (warp == tc::kMmaWarp) {
-    tc::mma_loop(A.ops, sh, aring, wring);
-  } else if (warp == tc::kTmaWarp) {
-    tc::tma_loop(A.ops, sh, aring, wring);
+  if (warp >= tc::kMmaWarp) {
+    tc::regs_give_ctl();
+    if (warp == tc::kMmaWarp) tc::mma_loop(A.ops, sh, aring, wring);
+    else if (warp == tc::kTmaWarp) tc::tma_loop(A.ops, sh, aring, wring);
   } else {
+    tc::regs_take_epi();
     // ======================= epilogue warps =======================
     const int S = a.S, G = gridDim.x;
     const size_t SB = (size_t)S * a.B;
@@ -227,7 +234,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
         float u[32], f[32];
         ld32(a.u0 + gofs(tile), th.nmine, vec, u);
         ld32(kptr(0) + gofs(tile), th.nmine, vec, f);
-        for (int i = 0; i < th.nmine; ++i) {
+        #pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          if (i >= th.nmine) continue;
           const float sk = (float)a.abstol + fabsf(u[i]) * (float)a.reltol;
           const double x = (double)(u[i] / sk), y = (double)(f[i] / sk);
           p0 += x * x;
@@ -260,12 +269,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
         }
         for (int i = 0; i < 32; ++i) Y[i] = u[i] + hf * f0[i];
         ok = epi_rhs(A, es, sh, aring, th, Y, f1);
-        if (v)
-          for (int i = 0; i < th.nmine; ++i) {
+        if (v) {
+          #pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            if (i >= th.nmine) continue;
             const float sk = (float)a.abstol + fabsf(u[i]) * (float)a.reltol;
             const double z = (double)((f1[i] - f0[i]) / sk);
             p2 += z * z;
           }
+        }
       }
       nf += 1;
       if (!ok) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto epi_done; }
@@ -310,7 +322,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
             if (v) {
               ld32(ucur + g, th.nmine, vec, u);
               ld32(ccur + g, th.nmine, vec, s);
-              for (int j = 0; j < i; ++j) {
+#pragma unroll
+              for (int j = 0; j < 6; ++j) {
+                if (j >= i) break;
                 float kj[32];
                 ld32(kptr(j) + g, th.nmine, vec, kj);
 #pragma unroll
@@ -333,16 +347,23 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
             if (v) {
               st32(kptr(i) + g, th.nmine, vec, k);
               if (i == 6) {
+                // u and the stage value again (stored above): nothing of the
+                // stage arithmetic stays in registers across epi_rhs
+                ld32(ucur + g, th.nmine, vec, u);
+                ld32(unew + g, th.nmine, vec, Y);
                 float ut[32];
 #pragma unroll
                 for (int q = 0; q < 32; ++q) ut[q] = hbt[6] * k[q];
+#pragma unroll
                 for (int j = 0; j < 6; ++j) {
                   float kj[32];
                   ld32(kptr(j) + g, th.nmine, vec, kj);
 #pragma unroll
                   for (int q = 0; q < 32; ++q) ut[q] = fmaf(hbt[j], kj[q], ut[q]);
                 }
-                for (int q = 0; q < th.nmine; ++q) {
+                #pragma unroll
+                for (int q = 0; q < 32; ++q) {
+                  if (q >= th.nmine) continue;
                   const float sc = (float)a.abstol + fmaxf(fabsf(u[q]), fabsf(Y[q])) * (float)a.reltol;
                   const double rr = (double)(ut[q] / sc);
                   perr += isfinite(Y[q]) ? rr * rr : (double)INFINITY;
@@ -390,6 +411,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
                 float u[32];
                 ld32(ucur + g, th.nmine, vec, u);
                 ld32(ccur + g, th.nmine, vec, o);
+#pragma unroll
                 for (int j = 0; j < 7; ++j) {
                   float kj[32];
                   ld32(kptr(j) + g, th.nmine, vec, kj);
@@ -470,7 +492,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
   if (warp == tc::kMmaWarp) tc::tmem_dealloc(sh.tmem_base, 512);
 }
 
+int tc_check_regs(const void* kernel) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return -1;
+  return fa.numRegs == tc::kLaunchRegs ? 0 : -1;
+}
+
 int max_grid_fwd_tc(int* grid) {
+  if (tc_check_regs((const void*)fwd_tc_kernel)) return -1;
   cudaError_t e = cudaFuncSetAttribute(fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        tc::kSmemBytes);
   if (e != cudaSuccess) return -1;
@@ -484,6 +513,7 @@ int max_grid_fwd_tc(int* grid) {
 }
 
 int launch_fwd_tc(const FwdTcArgs& a, int grid, cudaStream_t st) {
+  if (tc_check_regs((const void*)fwd_tc_kernel)) return -1;
   void* args[] = {(void*)&a};
   cudaError_t e = cudaLaunchCooperativeKernel((const void*)fwd_tc_kernel, dim3(grid), dim3(tc::kThreads),
                                               args, tc::kSmemBytes, st);

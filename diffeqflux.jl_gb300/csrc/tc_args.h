@@ -22,9 +22,11 @@ struct BwdTcArgs {
   const float* bias[GBNDE_MAX_LAYERS];
   float* lam_comp[2];           // compensation of lam
   float* mu_comp;               // [grid][P] Kahan compensation of mu_acc
-  float* hscr;                  // [grid][256][hvals] hidden activations (fp32), thread-private
+  float* hscr;                  // per CTA hvals/4 float4 slots x 256 threads (slot-major, so a
+                                //   warp's accesses to one slot are contiguous), fp32 activations
   int hvals;                    // values per thread in hscr
   int hoff[GBNDE_MAX_LAYERS];   // offset of hidden layer l (1..L-1) inside a thread's hscr
+  int hx;                       // offset of the 32 state values kept for the cube prefix
   uint8_t* img;                 // [grid][img_cta] weight-gradient operand images
   size_t img_cta;
   long long aoff[GBNDE_MAX_LAYERS];  // image offset of a_l (l = 0..L-1)
@@ -38,6 +40,12 @@ struct BwdTcArgs {
 
 
 int launch_bwd_tc(const BwdTcArgs& a, int grid, cudaStream_t st);
+
+// 0 if `kernel` was compiled with exactly tc::kLaunchRegs registers per
+// thread, the count the warpgroup register split is sized for; -1 otherwise
+// (the kernel must then not be launched: its register split would wait for
+// registers that the launch never had).
+int tc_check_regs(const void* kernel);
 int launch_reduce_mu_comp(const float* acc, const float* comp, int nblk, int stride, int P, float* out,
                           cudaStream_t st);
 

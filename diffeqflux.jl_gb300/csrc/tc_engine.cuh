@@ -10,9 +10,15 @@
 // warp with bulk copies. Ops alternate between two 256-column accumulator
 // regions so that the epilogue can drain one while the next op accumulates.
 //
-// Warp roles (320 threads): warps 0-7 epilogue (EPI), warp 8 MMA issuer,
-// warp 9 weight producer. The MMA and producer warps run the op list
-// cyclically until the epilogue raises the stop flag.
+// Warp roles (384 threads, three warpgroups): warps 0-7 epilogue (EPI),
+// warp 8 MMA issuer, warp 9 weight producer, warps 10-11 idle. The MMA and
+// producer warps run the op list cyclically until the epilogue raises the
+// stop flag. The kernel is launched with kLaunchRegs registers per thread;
+// the control warpgroup then gives registers back (setmaxnreg.dec to
+// kCtlRegs) and the two epilogue warpgroups take them (setmaxnreg.inc to
+// kEpiRegs): 256 * kEpiRegs + 128 * kCtlRegs == 384 * kLaunchRegs, checked at
+// compile time here and against the compiled kernel's register count before
+// every launch (a split above the launch's registers would never complete).
 #pragma once
 #include "kernels.h"
 #include "tc_ptx.cuh"
@@ -21,9 +27,15 @@ namespace gbnde {
 namespace tc {
 
 constexpr int kEpiThreads = 256;
-constexpr int kThreads = 320;
+constexpr int kThreads = 384;
 constexpr int kMmaWarp = 8;
 constexpr int kTmaWarp = 9;
+constexpr int kLaunchRegs = 168;   // 65536 / 384, rounded down to a multiple of 8
+constexpr int kEpiRegs = 224;
+constexpr int kCtlRegs = 56;
+static_assert(kEpiThreads * kEpiRegs + (kThreads - kEpiThreads) * kCtlRegs == kThreads * kLaunchRegs,
+              "register split must equal the launch's registers");
+static_assert(kThreads * kLaunchRegs <= 65536, "launch registers exceed the register file");
 constexpr int kASlotBytes = 3 * 16384;   // 3 pieces x 128 rows x 128 B
 constexpr int kWSlotBytes = 2 * 32768;   // 2 pieces x 256 rows x 128 B
 constexpr int kARing = 2;
@@ -67,6 +79,15 @@ struct Shared {
 };
 
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// Register split between the warpgroups (all four warps of a warpgroup
+// execute the same instruction).
+__device__ __forceinline__ void regs_take_epi() {
+  asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kEpiRegs));
+}
+__device__ __forceinline__ void regs_give_ctl() {
+  asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kCtlRegs));
+}
 
 // Deterministic sum of a double over the 256 epilogue threads.
 __device__ __forceinline__ double epi_sum(double v, Shared& sh) {
@@ -288,6 +309,45 @@ __device__ __forceinline__ bool epi_write_a(EpiState& e, Shared& sh, uint8_t* ar
   mbar_arrive(&sh.a_full[e.aslot]);
   if (++e.aslot == kARing) { e.aslot = 0; e.aph ^= 1; }
   return true;
+}
+
+// Bias values of columns [n0, n0 + 32) of a layer with N outputs (zero past
+// N), loaded together (vector loads where aligned) so that a single memory
+// round trip covers them; callers issue the next chunk's load before working
+// on the current one.
+__device__ __forceinline__ void load_bias32(const float* __restrict__ b, int n0, int N, float* out) {
+  const float* p = b + n0;
+  if (n0 + 32 <= N && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const float4 q = __ldg(reinterpret_cast<const float4*>(p) + i);
+      out[4 * i] = q.x; out[4 * i + 1] = q.y; out[4 * i + 2] = q.z; out[4 * i + 3] = q.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) out[i] = (n0 + i < N) ? __ldg(p + i) : 0.f;
+  }
+}
+
+// v <- act(v + bias) on 32 columns starting at n0 (columns at or past N -> 0,
+// the zero padding of the next GEMM's K dimension). The activation branch is
+// taken once per chunk, not per element.
+__device__ __forceinline__ void bias_act32(float* v, const float* bias, int act, int n0, int N) {
+  if (act == GBNDE_ACT_TANH) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = tanh_tc(v[i] + bias[i]);
+  } else if (act == GBNDE_ACT_SOFTPLUS) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = act_apply_tc(v[i] + bias[i], GBNDE_ACT_SOFTPLUS);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] += bias[i];
+  }
+  if (n0 + 32 > N) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+      if (n0 + i >= N) v[i] = 0.f;
+  }
 }
 
 // Skip A-ring slots that the producer warp fills (weight-gradient ops).

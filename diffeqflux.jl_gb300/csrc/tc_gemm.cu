@@ -289,3 +289,45 @@ extern "C" int gbnde_tc_selftest(const float* A, const float* W, int N, int K, i
   cudaFree(derr);
   return rc;
 }
+
+// ---- activation self-test: the tensor-core epilogue's activation beside the
+// library's (tanhf / log1pf(expf)) on the same inputs ------------------------
+namespace gbnde {
+__global__ void act_selftest_kernel(const float* __restrict__ x, int n, int act, float* __restrict__ ytc,
+                                    float* __restrict__ ylib) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  ytc[i] = act_apply_tc(x[i], act);
+  ylib[i] = act_apply(x[i], act);
+}
+}  // namespace gbnde
+
+extern "C" int gbnde_act_selftest(const float* x, int n, int act, float* y_tc, float* y_lib) {
+  using namespace gbnde;
+  if (!x || !y_tc || !y_lib || n < 1 || act < GBNDE_ACT_IDENTITY || act > GBNDE_ACT_SOFTPLUS)
+    return GBNDE_ERR_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return GBNDE_ERR_CUDA;
+  }
+  float *dx = nullptr, *d1 = nullptr, *d2 = nullptr;
+  const size_t bytes = (size_t)n * 4;
+  int rc = GBNDE_OK;
+  if (cudaMalloc(&dx, bytes) || cudaMalloc(&d1, bytes) || cudaMalloc(&d2, bytes)) {
+    rc = GBNDE_ERR_NOMEM;
+  } else if (cudaMemcpy(dx, x, bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    rc = GBNDE_ERR_CUDA;
+  } else {
+    act_selftest_kernel<<<(n + 255) / 256, 256>>>(dx, n, act, d1, d2);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(y_tc, d1, bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(y_lib, d2, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = GBNDE_ERR_CUDA;
+  }
+  cudaFree(dx);
+  cudaFree(d1);
+  cudaFree(d2);
+  cudaGetLastError();
+  return rc;
+}

@@ -225,7 +225,11 @@ long long gbnde_forward_trace(gbnde_ctx* ctx, double* out4, long long cap);
 
 /* The CUDA stream (cudaStream_t) the context launches on, and a way to use
  * the caller's stream instead (e.g. CUDA.jl's task stream); NULL restores the
- * context's own stream. No reference counterpart (stream plumbing of the host). */
+ * context's own stream. No reference counterpart (stream plumbing of the host).
+ * The context's own stream is destroyed with the context: a host whose
+ * allocator keeps per-stream records (torch's pinned-memory allocator records
+ * events on every stream a block was used on, also when the block is freed)
+ * should hand its own stream to gbnde_set_stream rather than use this one. */
 void* gbnde_stream(gbnde_ctx* ctx);
 int gbnde_set_stream(gbnde_ctx* ctx, void* stream);
 
@@ -241,6 +245,13 @@ int gbnde_last_kernel_ms(gbnde_ctx* ctx, double* fwd_ms, double* bwd_ms);
  * form, D = A^T W with A of K x 128 and W of K x N (K = 128), three products.
  * No reference counterpart (diagnostic). */
 int gbnde_tc_selftest(const float* A, const float* W, int N, int K, int mode, float* D);
+
+/* Self-test of the activation the tensor-core epilogues evaluate (a tanh
+ * built from its Maclaurin series and the exponential identity on the
+ * ex2/rcp instructions) beside the library functions the plain FP32 form
+ * uses, on n host inputs: y_tc = epilogue activation, y_lib = library
+ * activation. act: gbnde_act. No reference counterpart (diagnostic). */
+int gbnde_act_selftest(const float* x, int n, int act, float* y_tc, float* y_lib);
 
 const char* gbnde_strerror(int code);
 const char* gbnde_last_error(void);

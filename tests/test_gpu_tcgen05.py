@@ -61,3 +61,28 @@ def test_tc_gemm_mn_major_weight_gradient_form(lib, N):
     scale = np.abs(ref).max()
     assert np.abs(D - emul).max() / scale < 1e-5
     assert np.abs(D - ref).max() / scale < 3e-5
+
+
+def test_epilogue_tanh_against_library_tanhf(lib):
+    """The tensor-core epilogue's tanh (Maclaurin series below 0.6, the
+    exponential identity on ex2/rcp above) stays within a few 2^-24 of the
+    library tanhf, absolutely, and keeps NaN, signs and the saturation."""
+    fp = C.POINTER(C.c_float)
+    x = np.concatenate([np.linspace(-12.0, 12.0, 1 << 21), np.linspace(-0.7, 0.7, 1 << 20),
+                        np.array([0.0, -0.0, 1e-30, -1e-30, 0.6, -0.6, np.nextafter(0.6, 0),
+                                  20.0, -20.0, 1e30, -1e30, np.inf, -np.inf])]).astype(np.float32)
+    ytc = np.empty_like(x)
+    ylib = np.empty_like(x)
+    assert lib.gbnde_act_selftest(x.ctypes.data_as(fp), x.size, 1, ytc.ctypes.data_as(fp),
+                                  ylib.ctypes.data_as(fp)) == 0
+    err = np.abs(ytc.astype(np.float64) - ylib.astype(np.float64))
+    assert err.max() <= 4.0 * 2.0 ** -24, err.max()
+    small = np.abs(x) < 0.6
+    rel = err[small] / np.maximum(np.abs(ylib[small].astype(np.float64)), 1e-38)
+    assert rel[np.abs(x[small]) > 1e-30].max() <= 4.0 * 2.0 ** -24
+    assert np.all(np.sign(ytc) == np.sign(ylib))
+    assert np.all(np.abs(ytc) <= 1.0)
+    xn = np.array([np.nan], np.float32)
+    yn, yl = np.empty_like(xn), np.empty_like(xn)
+    assert lib.gbnde_act_selftest(xn.ctypes.data_as(fp), 1, 1, yn.ctypes.data_as(fp), yl.ctypes.data_as(fp)) == 0
+    assert np.isnan(yn[0])
