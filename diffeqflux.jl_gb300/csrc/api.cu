@@ -702,7 +702,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   }
   t.nbias = nb;
   int r = 0;
-  if ((r = c->timg.ensure((size_t)grid * t.img_cta)) ||
+  if ((r = c->timg.ensure((size_t)grid * tc::kImgSlots * t.img_cta)) ||
       (r = c->thscr.ensure((size_t)grid * tc::kEpiThreads * t.hvals * 4)) ||
       (r = c->tbpart.ensure((size_t)grid * 4 * t.nbias * 4)) ||
       (r = c->tmucomp.ensure((size_t)grid * P * 4)) || (r = c->tlamcomp.ensure(2 * SB * 4)) ||
@@ -711,11 +711,12 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   // per-CTA quadrature slots padded to a multiple of 4 floats (float4 sweeps)
   const int Ppad = (P + 3) / 4 * 4;
   t.b.P = Ppad;
-  if ((r = c->mu_acc.ensure((size_t)grid * Ppad * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * Ppad * 4)) ||
+  if ((r = c->mu_acc.ensure((size_t)grid * Ppad * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * t.nbias * 4)) ||
       (r = c->tmucomp.ensure((size_t)grid * Ppad * 4)))
     return r;
   t.b.mu_acc = c->mu_acc.as<float>();
   t.b.mu_stage = c->mu_stage.as<float>();
+  t.pbias = c->mu_stage.as<float>();
   t.img = c->timg.as<uint8_t>();
   t.hscr = c->thscr.as<float>();
   t.bpart = c->tbpart.as<float>();
@@ -724,7 +725,8 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   t.lam_comp[1] = c->tlamcomp.as<float>() + SB;
   t.b.dense = c->dense.as<float>();
   for (int l = 0; l < L; ++l) t.bias[l] = m.bias[l];
-  // op list: forward recompute, VJP chain, weight gradients
+  // op lists: forward recompute + VJP chain (per evaluation), and the
+  // stage-stacked weight gradients (per accepted step: K = 6 stages x 128)
   int n = 0;
   for (int l = 0; l + 1 < L; ++l) {
     tc::GemmOp& o = t.ops.op[n++];
@@ -740,7 +742,9 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
     o.npad = c->npadT[l];
     o.nchunk = c->nchunkT[l];
   }
-  bool first = true;
+  t.ops.nops = n;
+  n = 0;
+  t.dw_chunks = 0;
   for (int l = 0; l < L; ++l) {
     const int out = m.dims[l + 1], in = m.dims[l];
     const int nside = t.a_isA[l] ? out : in;
@@ -749,22 +753,23 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
     const long long bimg = t.a_isA[l] ? t.doff[l] : t.aoff[l];
     for (int hh = 0; hh < t.nh[l]; ++hh) {
       if (n >= tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
-      tc::GemmOp& o = t.ops.op[n++];
+      tc::GemmOp& o = t.dwops.op[n++];
       o.kind = 1;
       o.aimg = t.img + aimg + (size_t)hh * 32768;
       o.wimg = t.img + bimg;
-      o.cta_stride = t.img_cta;
+      o.cta_stride = tc::kImgSlots * t.img_cta;
+      o.slot_stride = t.img_cta;
       o.a_bytes = 32768;
       o.a_step = (uint32_t)(t.nh[l] * 32768);
       o.b_step = (uint32_t)(2 * nblk * 8192);
       o.nblk_b = nblk;
       o.npad = (nside + 15) / 16 * 16;
-      o.nchunk = 2;
-      o.first_dw = first ? 1 : 0;
-      first = false;
+      o.nchunk = 2 * 6;
+      o.first_dw = 0;
+      t.dw_chunks += o.nchunk;
     }
   }
-  t.ops.nops = n;
+  t.dwops.nops = n;
   CK(cudaEventRecord(c->ev[2], st));
   if (launch_bwd_tc(t, grid, st)) {
     cudaError_t e = cudaGetLastError();

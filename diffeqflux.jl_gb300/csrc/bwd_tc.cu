@@ -8,20 +8,25 @@
 // forward's dense stage storage (one slot per accepted forward step).
 //
 // One adjoint right-hand side on a tile of 128 trajectories is a list of
-// tensor-core ops (tc_engine.cuh):
+// tensor-core ops (tc_engine.cuh, command mode):
 //   forward recompute  z_l = W_l a_{l-1},          l = 1..L-1   (5 split products)
 //   VJP chain          g_l = W_l^T delta_{l+1},    l = L..1     (5 split products)
 //                      delta_l = g_l * act'(z_l), delta_L = lam, kl = g_1
-//   weight gradients   dW_l = delta_{l+1} a_l^T summed over the 128 trajectories
-//                      (K = trajectories, MN-major operands, 3 split products)
-// The epilogue writes the activations and cotangents as split-BF16
-// trajectory-major images into per-CTA scratch; the producer warp bulk-copies
-// them back as the weight-gradient operands, and the epilogue drains each
-// weight-gradient accumulator from tensor memory into the CTA's pending
-// quadrature buffer with the stage weight. Bias gradients are column sums of
-// the cotangents (warp butterfly reductions, deterministic order).
-// lam and mu use compensated (TwoSum / Kahan) sums; t, H and the controller
-// are FP64.
+// The epilogue also writes the activations a_l and the cotangents
+// b_s delta_{l+1} (b_s: the stage's quadrature weight) as split-BF16
+// trajectory-major images into the image slot of the stage. Once a step is
+// accepted, one weight-gradient op per layer (and 128-row half) runs over
+// the six stages' images stacked along K (K = 6 x 128 trajectories, MN-major
+// operands, 3 split products),
+//   sum_s b_s dW_l(s) = sum_s b_s delta_{l+1}(s) a_l(s)^T,
+// and the epilogue adds H times that accumulator to the CTA's mu with L2
+// reductions: one drain per accepted step instead of one per stage, and no
+// weight-gradient work at all for rejected steps. Stage 7 of a step is stage
+// 1 of the next (FSAL): its images go to the second of two stage-1 slots,
+// already weighted by b_1. Bias gradients are column sums of the cotangents
+// (warp butterfly reductions, deterministic order) kept in small per-CTA
+// pending buffers. lam uses compensated (TwoSum) sums; t, H and the
+// controller are FP64.
 #include "tc_args.h"
 
 namespace gbnde {
@@ -136,10 +141,11 @@ __device__ __forceinline__ void img_store(uint8_t* img, int isA, int nblk, int n
   }
 }
 
-// 32 values: chain A chunk (3 pieces) and/or image (2 pieces).
+// 32 values: chain A chunk (3 pieces, the values themselves) and/or image
+// (2 pieces of the values times `scale`).
 __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* aring, const Thr& th,
                                      const float* x, bool chain, uint8_t* img, int isA, int nblk,
-                                     int nh, int c) {
+                                     int nh, int c, float scale = 1.f) {
   uint4 hi[4], mid[4], lo[4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) tc::split3_bf16(x + 8 * j, hi[j], mid[j], lo[j]);
@@ -157,7 +163,20 @@ __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* a
     tc::mbar_arrive(&sh.a_full[e.aslot]);
     if (++e.aslot == tc::kARing) { e.aslot = 0; e.aph ^= 1; }
   }
-  if (img) img_store(img, isA, nblk, nh, th, c, hi, mid);
+  if (img) {
+    if (scale == 1.f) {
+      img_store(img, isA, nblk, nh, th, c, hi, mid);
+    } else {
+      float xs[8];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) xs[q] = scale * x[8 * j + q];
+        tc::split3_bf16(xs, hi[j], mid[j], lo[j]);
+      }
+      img_store(img, isA, nblk, nh, th, c, hi, mid);
+    }
+  }
   return true;
 }
 
@@ -197,8 +216,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
 
   if (warp >= tc::kMmaWarp) {
     tc::regs_give_ctl();
-    if (warp == tc::kMmaWarp) tc::mma_loop(A.ops, sh, aring, wring);
-    else if (warp == tc::kTmaWarp) tc::tma_loop(A.ops, sh, aring, wring);
+    if (warp == tc::kMmaWarp) tc::mma_loop_cmd(A.ops, A.dwops, sh, aring, wring);
+    else if (warp == tc::kTmaWarp) tc::tma_loop_cmd(A.ops, A.dwops, sh, aring, wring);
   } else {
     tc::regs_take_epi();
     // ======================= epilogue warps =======================
@@ -223,18 +242,20 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     long long nf_adj = 0, nacc = 0, nrej = 0, iter = 0;
     double dt = 0.0, qold = kQoldInit;
     bool swp = false, ok = true;
-    uint8_t* img = A.img + (size_t)blockIdx.x * A.img_cta;
+    // image slots of this CTA: stage 1 in slot fs (0 or 6), stages 2..6 in
+    // slots 1..5, stage 7 in slot 6 - fs (stage 1 of the next step)
+    uint8_t* img = A.img + (size_t)blockIdx.x * tc::kImgSlots * A.img_cta;
+    int fs = 0;
     float4* hs4 = reinterpret_cast<float4*>(A.hscr + (size_t)blockIdx.x * tc::kEpiThreads * A.hvals);
     float* bpart = A.bpart + (size_t)blockIdx.x * 4 * A.nbias;
     float* mu_acc = a.mu_acc + (size_t)blockIdx.x * a.P;
     float* mu_comp = A.mu_comp + (size_t)blockIdx.x * a.P;
-    float* Pb[3] = {a.mu_stage + (size_t)blockIdx.x * 3 * a.P,
-                    a.mu_stage + ((size_t)blockIdx.x * 3 + 1) * a.P,
-                    a.mu_stage + ((size_t)blockIdx.x * 3 + 2) * a.P};
+    // pending bias quadrature (nbias floats each): stage 1, stages 2..6, stage 7
+    float* Pb[3] = {A.pbias + (size_t)blockIdx.x * 3 * A.nbias, A.pbias + ((size_t)blockIdx.x * 3 + 1) * A.nbias,
+                    A.pbias + ((size_t)blockIdx.x * 3 + 2) * A.nbias};
     int iP1 = 0, iP7 = 2;
     float* Pmid = Pb[1];
-    int ndw = 0;  // weight-gradient ops per evaluation (A-ring slots they use: 2 each)
-    for (int l = 0; l < L; ++l) ndw += A.nh[l];
+    tc::CmdPoster cmdp;
 
     auto klb = [&](int j) -> float* {
       if (j == 0) return swp ? a.kl[6] : a.kl[0];
@@ -248,12 +269,17 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       float4* p4 = reinterpret_cast<float4*>(p);
       for (size_t i = threadIdx.x; i < (size_t)a.P / 4; i += tc::kEpiThreads) p4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     };
+    auto zero_bias = [&](float* p) {
+      for (int i = threadIdx.x; i < A.nbias; i += tc::kEpiThreads) p[i] = 0.f;
+    };
 
     // scratch images start at zero (padding rows/blocks are never written)
-    for (size_t i = threadIdx.x; i < A.img_cta / 16; i += tc::kEpiThreads)
+    for (size_t i = threadIdx.x; i < tc::kImgSlots * A.img_cta / 16; i += tc::kEpiThreads)
       reinterpret_cast<uint4*>(img)[i] = make_uint4(0, 0, 0, 0);
     zero_cta(mu_acc);
     zero_cta(mu_comp);
+    // the weight-gradient images are read by the producer warp (async proxy)
+    asm volatile("fence.proxy.async.global;" ::: "memory");
     for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
       if (!valid(tile)) continue;
       float v[32], z[32];
@@ -270,8 +296,12 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
 
     // ---- adjoint right-hand side of one tile ------------------------------------------
     // lam_in: stage input lam (own components), x: u(t) (own components).
-    // P/c: pending quadrature buffer and weight (P == nullptr: no quadrature).
-    auto adj_eval = [&](const float* lam_in, const float* x, float* P, float c, float* kl) -> bool {
+    // slot: image slot of the stage's weight-gradient operands (-1: none);
+    // P/c: pending bias quadrature buffer and the stage weight (P == nullptr:
+    // no quadrature). The cotangent images carry the weight c.
+    auto adj_eval = [&](const float* lam_in, const float* x, int slot, float* P, float c, float* kl) -> bool {
+      if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_EVAL)) return false;
+      uint8_t* im = slot >= 0 ? img + (size_t)slot * A.img_cta : nullptr;
       float v[32];
       // a_0 = x (or x^3)
 #pragma unroll
@@ -280,7 +310,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         v[i] = m.cube ? y * y * y : y;
       }
       if (m.cube) hs_st32(hs4, A.hx / 4, x);  // for the chain rule through x^3 at the end
-      if (!emit(es, sh, aring, th, v, true, img + A.aoff[0], A.a_isA[0], (m.dims[0] + 63) / 64, A.nh[0], 0))
+      if (!emit(es, sh, aring, th, v, true, im ? im + A.aoff[0] : nullptr, A.a_isA[0], (m.dims[0] + 63) / 64,
+                A.nh[0], 0))
         return false;
       // forward recompute of the hidden layers
       for (int l = 0; l < L - 1; ++l) {
@@ -300,7 +331,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
           tc::bias_act32(v, bc, m.act[l], n0, N);
           hs_st32(hs4, (A.hoff[l + 1] + 32 * cc) / 4, v);
-          if (!emit(es, sh, aring, th, v, l + 1 <= L - 2, img + A.aoff[l + 1], A.a_isA[l + 1],
+          if (!emit(es, sh, aring, th, v, l + 1 <= L - 2, im ? im + A.aoff[l + 1] : nullptr, A.a_isA[l + 1],
                     (N + 63) / 64, A.nh[l + 1], cc))
             return false;
         }
@@ -311,8 +342,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       (void)bbase;
 #pragma unroll
       for (int i = 0; i < 32; ++i) v[i] = (i < th.nmine) ? lam_in[i] : 0.f;
-      if (!emit(es, sh, aring, th, v, true, img + A.doff[L - 1], !A.a_isA[L - 1],
-                (m.dims[L] + 63) / 64, A.nh[L - 1], 0))
+      if (!emit(es, sh, aring, th, v, true, im ? im + A.doff[L - 1] : nullptr, !A.a_isA[L - 1],
+                (m.dims[L] + 63) / 64, A.nh[L - 1], 0, c))
         return false;
       if (P) {
         float w[32];
@@ -340,8 +371,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
 #pragma unroll
           for (int i = 0; i < 32; ++i) v[i] = (n0 + i < N) ? v[i] * act_deriv_from_out(h[i], m.act[l - 1]) : 0.f;
-          if (!emit(es, sh, aring, th, v, true, img + A.doff[l - 1], !A.a_isA[l - 1], (N + 63) / 64,
-                    A.nh[l - 1], cc))
+          if (!emit(es, sh, aring, th, v, true, im ? im + A.doff[l - 1] : nullptr, !A.a_isA[l - 1],
+                    (N + 63) / 64, A.nh[l - 1], cc, c))
             return false;
           if (P) {
             const float s = warp_colsum(v, th.lane);
@@ -350,9 +381,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         }
         tc::epi_release_acc(es, sh);
       }
-      // all weight-gradient images written: hand them to the producer warp
-      asm volatile("fence.proxy.async.global;" ::: "memory");
-      tc::mbar_arrive(&sh.img_ready);
       // kl = W_1^T delta_1 (times 3 x^2 for the cube prefix)
       {
         uint32_t col;
@@ -368,60 +396,73 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         }
         tc::epi_release_acc(es, sh);
       }
-      // weight-gradient accumulators -> pending quadrature buffer
-      tc::epi_skip_a(es, 2 * ndw);
+      if (P) {
+        tc::epi_bar();
+        for (int f = threadIdx.x; f < A.nbias; f += tc::kEpiThreads) {
+          const float s = ((bpart[f] + bpart[A.nbias + f]) + bpart[2 * A.nbias + f]) + bpart[3 * A.nbias + f];
+          tc::red_add(P + f, c * s);
+        }
+        tc::epi_bar();
+      }
+      return true;
+    };
+
+    // ---- weight gradients of an accepted step -------------------------------------
+    // One stage-stacked op per layer and 128-row half; mu += H * accumulator
+    // (L2 reductions: each mu element has one writing thread per CTA). Then the
+    // bias quadrature mu_b += H (P1 + Pmid).
+    auto commit_step = [&](float Hf) -> bool {
+      // images of the step (generic-proxy stores) -> producer warp (async proxy)
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+      tc::epi_bar();
+      if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_DW | ((uint32_t)fs << 8))) return false;
+      tc::epi_skip_a(es, A.dw_chunks);
+      float v[32];
       for (int l = 0; l < L; ++l) {
         const int out = m.dims[l + 1], in = m.dims[l];
-        const int Nn2 = A.a_isA[l] ? out : in;  // N side of the dW op
+        const int isA = A.a_isA[l];
+        const int Nn2 = isA ? out : in;  // N side of the dW op
+        float* __restrict__ Pw = mu_acc + m.woff[l];
         for (int hh = 0; hh < A.nh[l]; ++hh) {
           uint32_t col;
           if (!tc::epi_wait_acc(es, sh, &col)) return false;
-          if (P) {
-            const int mrow = 128 * hh + th.r;  // M-side feature of this lane
-            const int isA = A.a_isA[l];
-            float* __restrict__ Pw = P + m.woff[l];
-            for (int cc = 0; cc < (Nn2 + 63) / 64; ++cc) {
-              const int n0 = 64 * cc + 32 * th.ch;
-              tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
-              if (isA) {
-                // row mrow = in feature; 32 consecutive out features
-                float* rowp = Pw + (size_t)mrow * out + n0;
-                const bool full = mrow < in && n0 + 32 <= out && (reinterpret_cast<uintptr_t>(rowp) & 15) == 0;
-                if (full) {
+          const int mrow = 128 * hh + th.r;  // M-side feature of this lane
+          for (int cc = 0; cc < (Nn2 + 63) / 64; ++cc) {
+            const int n0 = 64 * cc + 32 * th.ch;
+            tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+            if (isA) {
+              // row mrow = in feature; 32 consecutive out features
+              float* rowp = Pw + (size_t)mrow * out + n0;
+              const bool full = mrow < in && n0 + 32 <= out && (reinterpret_cast<uintptr_t>(rowp) & 15) == 0;
+              if (full) {
 #pragma unroll
-                  for (int i = 0; i < 32; i += 4)
-                    tc::red_add_v4(rowp + i, c * v[i], c * v[i + 1], c * v[i + 2], c * v[i + 3]);
-                } else if (mrow < in) {
-#pragma unroll
-                  for (int i = 0; i < 32; ++i)
-                    if (n0 + i < out) tc::red_add(rowp + i, c * v[i]);
-                }
-              } else if (mrow < out) {
-                // row mrow = out feature; in features n0.. at stride `out`
-                float* colp = Pw + (size_t)n0 * out + mrow;
+                for (int i = 0; i < 32; i += 4)
+                  tc::red_add_v4(rowp + i, Hf * v[i], Hf * v[i + 1], Hf * v[i + 2], Hf * v[i + 3]);
+              } else if (mrow < in) {
 #pragma unroll
                 for (int i = 0; i < 32; ++i)
-                  if (n0 + i < in) tc::red_add(colp + (size_t)i * out, c * v[i]);
+                  if (n0 + i < out) tc::red_add(rowp + i, Hf * v[i]);
               }
+            } else if (mrow < out) {
+              // row mrow = out feature; in features n0.. at stride `out`
+              float* colp = Pw + (size_t)n0 * out + mrow;
+#pragma unroll
+              for (int i = 0; i < 32; ++i)
+                if (n0 + i < in) tc::red_add(colp + (size_t)i * out, Hf * v[i]);
             }
           }
           tc::epi_release_acc(es, sh);
         }
       }
-      if (P) {
-        tc::epi_bar();
-        for (int f = threadIdx.x; f < A.nbias; f += tc::kEpiThreads) {
-          // which layer's bias holds f
-          int l = 0;
-          while (l + 1 < L && f >= A.boffp[l + 1]) ++l;
-          const int o = f - A.boffp[l];
-          if (o < m.dims[l + 1]) {
-            const float s = ((bpart[f] + bpart[A.nbias + f]) + bpart[2 * A.nbias + f]) + bpart[3 * A.nbias + f];
-            tc::red_add(P + m.boff[l] + o, c * s);
-          }
-        }
-        tc::epi_bar();
+      // bias quadrature (pending buffers were summed by L2 adds: read them from L2)
+      const float* P1 = Pb[iP1];
+      for (int f = threadIdx.x; f < A.nbias; f += tc::kEpiThreads) {
+        int l = 0;
+        while (l + 1 < L && f >= A.boffp[l + 1]) ++l;
+        const int o = f - A.boffp[l];
+        if (o < m.dims[l + 1]) tc::red_add(mu_acc + m.boff[l] + o, Hf * (__ldcg(P1 + f) + __ldcg(Pmid + f)));
       }
+      tc::epi_bar();
       return true;
     };
 
@@ -459,7 +500,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       const double t_lo = iv.t_lo;
       // ---- FSAL stage at the interval start: kl1 and P1 = b1 * mu ----
       {
-        zero_cta(Pb[iP1]);
+        zero_bias(Pb[iP1]);
         tc::epi_bar();
         int n;
         float hb[7];
@@ -473,7 +514,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           } else {
             for (int i = 0; i < 32; ++i) lam[i] = x[i] = 0.f;
           }
-          ok = adj_eval(lam, x, Pb[iP1], (float)c_tab.b[0], kl);
+          ok = adj_eval(lam, x, fs, Pb[iP1], (float)c_tab.b[0], kl);
           if (v) st32(klb(0) + gofs(tile), th.nmine, vec, kl);
         }
         ++nf_adj;
@@ -527,7 +568,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           }
           float li[32];
           for (int i = 0; i < 32; ++i) li[i] = l[i] + hf * f0[i];
-          ok = adj_eval(li, x, nullptr, 0.f, f1);
+          ok = adj_eval(li, x, -1, nullptr, 0.f, f1);
           if (v) {
             #pragma unroll
             for (int i = 0; i < 32; ++i) {
@@ -561,7 +602,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         float* lnew = a.lam[cur ^ 1];
         const float* ccur = A.lam_comp[cur];
         float* cnew = A.lam_comp[cur ^ 1];
-        zero_cta(Pmid);
+        zero_bias(Pmid);
         tc::epi_bar();
         double perr = 0.0;
         for (int i = 1; i < 7 && ok; ++i) {
@@ -569,8 +610,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           float ha[6];
           for (int j = 0; j < 6; ++j) ha[j] = (float)(H * c_tab.a[i][j]);
           float* P = (i < 6) ? Pmid : Pb[iP7];
+          const int slot = (i < 6) ? i : tc::kImgSlots - 1 - fs;
           if (i == 6) {
-            zero_cta(P);
+            zero_bias(P);
             tc::epi_bar();
           }
           const float cw = (i < 6) ? (float)c_tab.b[i] : (float)c_tab.b[0];
@@ -605,7 +647,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             } else {
               for (int q = 0; q < 32; ++q) Y[q] = x[q] = l[q] = 0.f;
             }
-            ok = adj_eval(Y, x, P, cw, kl);
+            ok = adj_eval(Y, x, slot, P, cw, kl);
             if (v) {
               st32(klb(i) + g, th.nmine, vec, kl);
               if (i == 6) {
@@ -646,34 +688,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         double q11;
         double q = pi_q(eest, qold, &q11);
         if (eest <= 1.0) {
-          // mu += H (P1 + Pmid), Kahan-compensated per CTA
-          const float Hf = (float)H;
-          const float4* P1 = reinterpret_cast<const float4*>(Pb[iP1]);
-          const float4* Pm = reinterpret_cast<const float4*>(Pmid);
-          float4* acc4 = reinterpret_cast<float4*>(mu_acc);
-          float4* cmp4 = reinterpret_cast<float4*>(mu_comp);
-#pragma unroll 4
-          for (size_t k = threadIdx.x; k < (size_t)a.P / 4; k += tc::kEpiThreads) {
-            // pending buffers were summed by L2 adds: read them from L2
-            const float4 p1 = __ldcg(P1 + k), pm = __ldcg(Pm + k), cm = cmp4[k], ac = acc4[k];
-            float4 na, nc;
-            auto kahan = [&](float p1v, float pmv, float cmv, float acv, float& nav, float& ncv) {
-              const float y = fmaf(Hf, p1v + pmv, -cmv);
-              const float tsum = acv + y;
-              ncv = (tsum - acv) - y;
-              nav = tsum;
-            };
-            kahan(p1.x, pm.x, cm.x, ac.x, na.x, nc.x);
-            kahan(p1.y, pm.y, cm.y, ac.y, na.y, nc.y);
-            kahan(p1.z, pm.z, cm.z, ac.z, na.z, nc.z);
-            kahan(p1.w, pm.w, cm.w, ac.w, na.w, nc.w);
-            acc4[k] = na;
-            cmp4[k] = nc;
-          }
-          tc::epi_bar();
+          if (!commit_step((float)H)) { ok = false; break; }
           const int tmp = iP1;
           iP1 = iP7;
           iP7 = tmp;
+          fs = tc::kImgSlots - 1 - fs;
           ++nacc;
           cur ^= 1;
           swp = !swp;

@@ -165,29 +165,17 @@ __device__ __forceinline__ float act_apply(float z, int act) {
   return z;
 }
 
-// tanh for the tensor-core epilogues, built from two identities:
-//   |x| <  0.6: the Maclaurin series x + sum_{n=2..10} c_n x^(2n-1),
-//               c_n = 2^(2n) (2^(2n) - 1) B_(2n) / (2n)!  (B: Bernoulli numbers);
-//               the first omitted term is below 4e-9 relative at 0.6;
-//   |x| >= 0.6: tanh|x| = 1 - 2 / (exp(2|x|) + 1), with exp(2|x|) = 2^(2|x|/ln 2)
-//               from the ex2.approx instruction and 1/(e+1) from rcp.approx
-//               refined by one Newton step (q <- q (2 - d q)).
-// Absolute error within a few units of 2^-24 of the library tanhf (tested
-// against it over [-12, 12]), at a fraction of its instruction count: the
-// epilogue evaluates 32 of these per thread and chunk between tensor-core ops.
+// tanh for the tensor-core epilogues from the identity
+//   tanh x = sign(x) (1 - 2 / (exp(2|x|) + 1)),
+// with exp(2|x|) = 2^(2|x| / ln 2) from the ex2.approx instruction and
+// 1/(e + 1) from rcp.approx refined by one Newton step (q <- q (2 - d q)).
+// Branch-free: 8 instructions, 2 of them on the special-function unit.
+// Its error is absolute, a few units of 2^-24 (largest near 0, where the
+// relative error grows like 2^-24/|x|): the size of the FP32 rounding of
+// O(1) activations, which is what the next layer's GEMM sees. Tested against
+// the library tanhf over [-12, 12].
 __device__ __forceinline__ float tanh_tc(float x) {
   const float ax = fabsf(x);
-  const float x2 = x * x;
-  float p = -2.3912911424355248e-04f;           // x^19
-  p = fmaf(p, x2, 5.9002744094558600e-04f);     // x^17
-  p = fmaf(p, x2, -1.4558343870513183e-03f);    // x^15
-  p = fmaf(p, x2, 3.5921280365724810e-03f);     // x^13
-  p = fmaf(p, x2, -8.8632355299021970e-03f);    // x^11
-  p = fmaf(p, x2, 2.1869488536155203e-02f);     // x^9
-  p = fmaf(p, x2, -5.3968253968253970e-02f);    // x^7
-  p = fmaf(p, x2, 1.3333333333333333e-01f);     // x^5
-  p = fmaf(p, x2, -3.3333333333333333e-01f);    // x^3
-  const float small = fmaf(x * x2, p, x);
   // clamp keeps exp finite (tanh(10) rounds to 1) and lets NaN through
   const float axc = ax > 10.f ? 10.f : ax;
   float e, q;
@@ -195,8 +183,7 @@ __device__ __forceinline__ float tanh_tc(float x) {
   const float d = e + 1.f;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(q) : "f"(d));
   q = q * fmaf(-d, q, 2.f);
-  const float big = copysignf(fmaf(-2.f, q, 1.f), x);
-  return ax < 0.6f ? small : big;
+  return copysignf(fmaf(-2.f, q, 1.f), x);
 }
 
 __device__ __forceinline__ float act_apply_tc(float z, int act) {

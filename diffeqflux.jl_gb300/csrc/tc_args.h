@@ -18,7 +18,10 @@ struct FwdTcArgs {
 
 struct BwdTcArgs {
   BwdArgs b;
-  tc::OpList ops;
+  tc::OpList ops;               // one adjoint evaluation: forward recompute + VJP chain
+  tc::OpList dwops;             // one accepted step: stage-stacked weight-gradient ops
+  int dw_chunks;                // K chunks of all dwops (A-ring slots the producer fills)
+  float* pbias;                 // [grid][3][nbias] pending bias quadrature: stage 1, 2..6, 7
   const float* bias[GBNDE_MAX_LAYERS];
   float* lam_comp[2];           // compensation of lam
   float* mu_comp;               // [grid][P] Kahan compensation of mu_acc
@@ -27,8 +30,8 @@ struct BwdTcArgs {
   int hvals;                    // values per thread in hscr
   int hoff[GBNDE_MAX_LAYERS];   // offset of hidden layer l (1..L-1) inside a thread's hscr
   int hx;                       // offset of the 32 state values kept for the cube prefix
-  uint8_t* img;                 // [grid][img_cta] weight-gradient operand images
-  size_t img_cta;
+  uint8_t* img;                 // [grid][kImgSlots][img_cta] weight-gradient operand images
+  size_t img_cta;               // bytes of one stage's images
   long long aoff[GBNDE_MAX_LAYERS];  // image offset of a_l (l = 0..L-1)
   long long doff[GBNDE_MAX_LAYERS];  // image offset of delta_{l+1} (l = 0..L-1)
   int a_isA[GBNDE_MAX_LAYERS];       // 1: a_l is the A operand (rows = in) of layer l's dW

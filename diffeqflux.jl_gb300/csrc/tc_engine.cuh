@@ -41,7 +41,9 @@ constexpr int kWSlotBytes = 2 * 32768;   // 2 pieces x 256 rows x 128 B
 constexpr int kARing = 2;
 constexpr int kWRing = 2;
 constexpr int kSmemBytes = 1024 + kARing * kASlotBytes + kWRing * kWSlotBytes;
-constexpr int kMaxOps = 40;
+constexpr int kMaxOps = 20;
+constexpr int kCmdRing = 4;
+constexpr int kImgSlots = 7;    // weight-gradient image slots per CTA: stages 1..6 + the next stage 1
 
 // kind 0 (chain GEMM): A chunks written by the epilogue (3 pieces, K-major),
 //   B = weight image chunks (2 pieces, K-major), five split products.
@@ -60,6 +62,7 @@ struct GemmOp {
   int kind;
   int nblk_b;           // kind 1: 64-column blocks in a B chunk
   int first_dw;         // kind 1: first weight-gradient op of an evaluation (waits for images)
+  size_t slot_stride;   // kind 1: bytes between the image slots of consecutive stages
 };
 
 struct OpList {
@@ -72,6 +75,8 @@ struct Shared {
   uint64_t w_full[kWRing], w_empty[kWRing];
   uint64_t acc_full[2], acc_empty[2];
   uint64_t img_ready;
+  uint64_t cmd_full[kCmdRing], cmd_empty[kCmdRing];
+  uint32_t cmd[kCmdRing];
   uint32_t tmem_base;
   int stop;
   int err;
@@ -118,88 +123,139 @@ __device__ __forceinline__ void init_shared(Shared& sh) {
       mbar_init(&sh.acc_empty[i], kEpiThreads);
     }
     mbar_init(&sh.img_ready, kEpiThreads);
+    for (int i = 0; i < kCmdRing; ++i) {
+      mbar_init(&sh.cmd_full[i], 1);
+      mbar_init(&sh.cmd_empty[i], 2);
+    }
     sh.stop = 0;
     sh.err = 0;
     fence_mbar_init();
   }
 }
 
+// ---- command ring (command mode) -------------------------------------------------
+// In command mode the epilogue decides, round by round, which op list the MMA
+// and producer warps run next: CMD_EVAL (the evaluation list, once) or CMD_DW
+// (the weight-gradient list, once; bits 8.. carry the image slot of stage 1).
+// Thread 0 of the epilogue posts; the MMA and producer leaders both release
+// the slot.
+enum : uint32_t { CMD_EVAL = 1, CMD_DW = 2 };
+
+// Image slot of stacked stage s (0-based) when stage 1 lives in slot f.
+__device__ __forceinline__ int stage_slot(int s, int f) { return s == 0 ? f : s; }
+
 // ---- MMA warp ------------------------------------------------------------------------
-// Executes the op list cyclically. Returns when the stop flag is raised (or on
-// a wait timeout, which also raises sh.err).
-__device__ __forceinline__ void mma_loop(const OpList& ops, Shared& sh, uint8_t* aring,
-                                         uint8_t* wring) {
-  volatile int* verr = &sh.err;
-  volatile int* vstop = &sh.stop;
-  const bool leader = (threadIdx.x & 31) == 0;
+struct MmaState {
   int aslot = 0, wslot = 0;
   uint32_t aph = 0, wph = 0;
   uint32_t use[2] = {0, 0};
   long long g = 0;
+};
+
+// One op: waits for its accumulator region, then for every K chunk for the A
+// chunk and the W chunk, and issues the products. Returns false when the
+// loop must end (stop flag, error or wait limit).
+__device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh, uint8_t* aring,
+                                       uint8_t* wring) {
+  volatile int* verr = &sh.err;
+  volatile int* vstop = &sh.stop;
+  const bool leader = (threadIdx.x & 31) == 0;
   const int pa[5] = {0, 1, 0, 2, 1};
   const int pb[5] = {0, 0, 1, 0, 1};
-  while (true) {
-    const GemmOp& op = ops.op[g % ops.nops];
-    const int reg = (int)(g & 1);
-    // accumulator region free?
+  const int reg = (int)(m.g & 1);
+  {
+    const uint32_t par = (m.use[reg] & 1) ^ 1;
+    while (!mbar_try_wait(&sh.acc_empty[reg], par)) {
+      if (*vstop || *verr) return false;
+    }
+  }
+  const uint32_t d = sh.tmem_base + (uint32_t)(reg * 256);
+  const uint32_t idesc = op.kind == 0 ? idesc_bf16(128, op.npad) : idesc_bf16_mn(128, op.npad);
+  const uint32_t wpiece = op.kind == 0 ? (uint32_t)op.npad * 128 : (uint32_t)op.nblk_b * 8192;
+  for (int c = 0; c < op.nchunk; ++c) {
+    // A chunk ready? (bounded by the stop flag: the epilogue may be done)
     {
-      const uint32_t par = (use[reg] & 1) ^ 1;
-      while (!mbar_try_wait(&sh.acc_empty[reg], par)) {
-        if (*vstop || *verr) return;
+      unsigned long long t0 = 0;
+      while (!mbar_try_wait(&sh.a_full[m.aslot], m.aph)) {
+        if (*vstop || *verr) return false;
+        if (t0 == 0) t0 = globaltimer_ns();
+        else if (globaltimer_ns() - t0 > 4 * kWaitTimeoutNs) { *verr = 2; return false; }
       }
     }
-    const uint32_t d = sh.tmem_base + (uint32_t)(reg * 256);
-    const uint32_t idesc = op.kind == 0 ? idesc_bf16(128, op.npad) : idesc_bf16_mn(128, op.npad);
-    const uint32_t wpiece = op.kind == 0 ? (uint32_t)op.npad * 128 : (uint32_t)op.nblk_b * 8192;
-    for (int c = 0; c < op.nchunk; ++c) {
-      // A chunk ready? (bounded by the stop flag: the epilogue may be done)
-      {
-        unsigned long long t0 = 0;
-        while (!mbar_try_wait(&sh.a_full[aslot], aph)) {
-          if (*vstop || *verr) return;
-          if (t0 == 0) t0 = globaltimer_ns();
-          else if (globaltimer_ns() - t0 > 4 * kWaitTimeoutNs) { *verr = 2; return; }
-        }
-      }
-      if (!mbar_wait(&sh.w_full[wslot], wph, verr)) return;
-      tc_fence_after();
-      if (leader) {
-        const uint32_t a0 = smem_u32(aring + aslot * kASlotBytes);
-        const uint32_t b0 = smem_u32(wring + wslot * kWSlotBytes);
-        if (op.kind == 0) {
+    if (!mbar_wait(&sh.w_full[m.wslot], m.wph, verr)) return false;
+    tc_fence_after();
+    if (leader) {
+      const uint32_t a0 = smem_u32(aring + m.aslot * kASlotBytes);
+      const uint32_t b0 = smem_u32(wring + m.wslot * kWSlotBytes);
+      if (op.kind == 0) {
 #pragma unroll
-          for (int pr = 0; pr < 5; ++pr) {
+        for (int pr = 0; pr < 5; ++pr) {
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-              const uint64_t ad = sdesc_sw128(a0 + pa[pr] * 16384 + kk * 32);
-              const uint64_t bd = sdesc_sw128(b0 + pb[pr] * wpiece + kk * 32);
-              mma_bf16(d, ad, bd, idesc, (c > 0 || pr > 0 || kk > 0) ? 1u : 0u);
-            }
-          }
-        } else {
-          // A chunk: 2 pieces x 2 blocks x 8 KB; B chunk: 2 pieces x nblk x 8 KB.
-          // Products hi.hi, hi.lo, lo.hi; K step of 16 trajectories = 2048 bytes.
-#pragma unroll
-          for (int pr = 0; pr < 3; ++pr) {
-            const int qa = (pr == 2) ? 1 : 0, qb = (pr == 1) ? 1 : 0;
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-              const uint64_t ad = sdesc_sw128_mn(a0 + qa * 16384 + kk * 2048, 8192);
-              const uint64_t bd = sdesc_sw128_mn(b0 + qb * wpiece + kk * 2048, 8192);
-              mma_bf16(d, ad, bd, idesc, (c > 0 || pr > 0 || kk > 0) ? 1u : 0u);
-            }
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint64_t ad = sdesc_sw128(a0 + pa[pr] * 16384 + kk * 32);
+            const uint64_t bd = sdesc_sw128(b0 + pb[pr] * wpiece + kk * 32);
+            mma_bf16(d, ad, bd, idesc, (c > 0 || pr > 0 || kk > 0) ? 1u : 0u);
           }
         }
-        mma_commit(&sh.a_empty[aslot]);
-        mma_commit(&sh.w_empty[wslot]);
-        if (c == op.nchunk - 1) mma_commit(&sh.acc_full[reg]);
+      } else {
+        // A chunk: 2 pieces x 2 blocks x 8 KB; B chunk: 2 pieces x nblk x 8 KB.
+        // Products hi.hi, hi.lo, lo.hi; K step of 16 trajectories = 2048 bytes.
+#pragma unroll
+        for (int pr = 0; pr < 3; ++pr) {
+          const int qa = (pr == 2) ? 1 : 0, qb = (pr == 1) ? 1 : 0;
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint64_t ad = sdesc_sw128_mn(a0 + qa * 16384 + kk * 2048, 8192);
+            const uint64_t bd = sdesc_sw128_mn(b0 + qb * wpiece + kk * 2048, 8192);
+            mma_bf16(d, ad, bd, idesc, (c > 0 || pr > 0 || kk > 0) ? 1u : 0u);
+          }
+        }
       }
-      __syncwarp();
-      if (++aslot == kARing) { aslot = 0; aph ^= 1; }
-      if (++wslot == kWRing) { wslot = 0; wph ^= 1; }
+      mma_commit(&sh.a_empty[m.aslot]);
+      mma_commit(&sh.w_empty[m.wslot]);
+      if (c == op.nchunk - 1) mma_commit(&sh.acc_full[reg]);
     }
-    use[reg] += 1;
-    ++g;
+    __syncwarp();
+    if (++m.aslot == kARing) { m.aslot = 0; m.aph ^= 1; }
+    if (++m.wslot == kWRing) { m.wslot = 0; m.wph ^= 1; }
+  }
+  m.use[reg] += 1;
+  ++m.g;
+  return true;
+}
+
+// Cyclic mode: runs the op list over and over until the stop flag is raised
+// (or a wait gives up, which also raises sh.err).
+__device__ __forceinline__ void mma_loop(const OpList& ops, Shared& sh, uint8_t* aring, uint8_t* wring) {
+  MmaState m;
+  while (mma_op(ops.op[m.g % ops.nops], m, sh, aring, wring)) {
+  }
+}
+
+// Waits for the next command of the ring; false when the loop must end.
+__device__ __forceinline__ bool cmd_take(Shared& sh, int& cs, uint32_t& cph, uint32_t* cmd) {
+  volatile int* verr = &sh.err;
+  volatile int* vstop = &sh.stop;
+  while (!mbar_try_wait(&sh.cmd_full[cs], cph)) {
+    if (*vstop || *verr) return false;
+  }
+  *cmd = ((volatile uint32_t*)sh.cmd)[cs];
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(&sh.cmd_empty[cs]);
+  if (++cs == kCmdRing) { cs = 0; cph ^= 1; }
+  return true;
+}
+
+// Command mode: one op list per command.
+__device__ __forceinline__ void mma_loop_cmd(const OpList& ev, const OpList& dw, Shared& sh, uint8_t* aring,
+                                             uint8_t* wring) {
+  MmaState m;
+  int cs = 0;
+  uint32_t cph = 0, cmd = 0;
+  while (cmd_take(sh, cs, cph, &cmd)) {
+    const OpList& L = (cmd & 0xffu) == CMD_DW ? dw : ev;
+    for (int i = 0; i < L.nops; ++i)
+      if (!mma_op(L.op[i], m, sh, aring, wring)) return;
   }
 }
 
@@ -209,68 +265,122 @@ __device__ __forceinline__ void mma_loop(const OpList& ops, Shared& sh, uint8_t*
 // the A ring (those slots are completed by one arrive of 256 counts plus the
 // transaction bytes, so the ring keeps one protocol with the epilogue).
 // The A ring position advances over the epilogue-written chunks as well.
-__device__ __forceinline__ void tma_loop(const OpList& ops, Shared& sh, uint8_t* aring,
-                                         uint8_t* wring) {
-  volatile int* verr = &sh.err;
-  volatile int* vstop = &sh.stop;
-  const bool leader = (threadIdx.x & 31) == 0;
+struct TmaState {
   int wslot = 0, aslot = 0;
   uint32_t wph = 0, aph = 0, img_phase = 0;
   long long g = 0;
   uint32_t issued_w[kWRing] = {0, 0};
-  uint32_t issued_a[kARing] = {0, 0};
-  auto wait_or_stop = [&](uint64_t* bar, uint32_t par) -> bool {
-    while (true) {
-      if (mbar_try_wait(bar, par)) return true;
-      if (*vstop || *verr) return false;
-    }
-  };
-  bool run = true;
-  while (run && !*vstop && !*verr) {
-    const GemmOp& op = ops.op[g % ops.nops];
-    const uint32_t bbytes = op.kind == 0 ? 2u * (uint32_t)op.npad * 128u : 2u * (uint32_t)op.nblk_b * 8192u;
-    const uint8_t* bbase = op.kind == 0 ? op.wimg : op.wimg + (size_t)blockIdx.x * op.cta_stride;
-    const uint8_t* abase = op.kind == 0 ? nullptr : op.aimg + (size_t)blockIdx.x * op.cta_stride;
-    if (op.kind == 1 && op.first_dw) {
-      if (!wait_or_stop(&sh.img_ready, img_phase)) break;
-      img_phase ^= 1;
-      asm volatile("fence.proxy.async.global;" ::: "memory");
-    }
-    for (int c = 0; c < op.nchunk; ++c) {
-      if (op.kind == 1) {
-        if (!wait_or_stop(&sh.a_empty[aslot], aph ^ 1)) { run = false; break; }
-        if (leader) {
-          mbar_arrive_expect_tx(&sh.a_full[aslot], op.a_bytes);
-          asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
-                           smem_u32(&sh.a_full[aslot])),
-                       "r"(kEpiThreads - 1)
-                       : "memory");
-          bulk_g2s(aring + aslot * kASlotBytes, abase + (size_t)c * op.a_step, op.a_bytes, &sh.a_full[aslot]);
-        }
-        __syncwarp();
-        issued_a[aslot] += 1;
-      }
-      if (++aslot == kARing) { aslot = 0; aph ^= 1; }
-      if (!wait_or_stop(&sh.w_empty[wslot], wph ^ 1)) { run = false; break; }
+  int a_pending[kARing] = {0, 0};     // a producer-filled A slot whose copy may be in flight
+  uint32_t a_par[kARing] = {0, 0};    // ... and the phase parity of that fill
+};
+
+__device__ __forceinline__ bool tma_wait_or_stop(Shared& sh, uint64_t* bar, uint32_t par) {
+  volatile int* verr = &sh.err;
+  volatile int* vstop = &sh.stop;
+  while (true) {
+    if (mbar_try_wait(bar, par)) return true;
+    if (*vstop || *verr) return false;
+  }
+}
+
+// One op's copies; `f` is the image slot of stage 1 for stage-stacked
+// weight-gradient ops (K chunk c: stage c / 2, trajectory block c % 2).
+__device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh, uint8_t* aring,
+                                       uint8_t* wring, int f) {
+  const bool leader = (threadIdx.x & 31) == 0;
+  const uint32_t bbytes = op.kind == 0 ? 2u * (uint32_t)op.npad * 128u : 2u * (uint32_t)op.nblk_b * 8192u;
+  const uint8_t* bbase = op.kind == 0 ? op.wimg : op.wimg + (size_t)blockIdx.x * op.cta_stride;
+  const uint8_t* abase = op.kind == 0 ? nullptr : op.aimg + (size_t)blockIdx.x * op.cta_stride;
+  if (op.kind == 1 && op.first_dw) {
+    if (!tma_wait_or_stop(sh, &sh.img_ready, t.img_phase)) return false;
+    t.img_phase ^= 1;
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+  for (int c = 0; c < op.nchunk; ++c) {
+    size_t aoff = 0, boff = 0;
+    if (op.kind == 1) {
+      const int s = c >> 1, kb = c & 1;
+      const size_t slot = (size_t)stage_slot(s, f) * op.slot_stride;
+      aoff = slot + (size_t)kb * op.a_step;
+      boff = slot + (size_t)kb * op.b_step;
+      if (!tma_wait_or_stop(sh, &sh.a_empty[t.aslot], t.aph ^ 1)) return false;
       if (leader) {
-        mbar_arrive_expect_tx(&sh.w_full[wslot], bbytes);
-        const uint8_t* src = op.kind == 0 ? bbase + (size_t)c * bbytes : bbase + (size_t)c * op.b_step;
-        bulk_g2s(wring + wslot * kWSlotBytes, src, bbytes, &sh.w_full[wslot]);
+        mbar_arrive_expect_tx(&sh.a_full[t.aslot], op.a_bytes);
+        asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                         smem_u32(&sh.a_full[t.aslot])),
+                     "r"(kEpiThreads - 1)
+                     : "memory");
+        bulk_g2s(aring + t.aslot * kASlotBytes, abase + aoff, op.a_bytes, &sh.a_full[t.aslot]);
       }
       __syncwarp();
-      issued_w[wslot] += 1;
-      if (++wslot == kWRing) { wslot = 0; wph ^= 1; }
+      t.a_pending[t.aslot] = 1;
+      t.a_par[t.aslot] = t.aph;
+    } else {
+      t.a_pending[t.aslot] = 0;  // an epilogue chunk follows the earlier copy into this slot
     }
-    ++g;
+    if (++t.aslot == kARing) { t.aslot = 0; t.aph ^= 1; }
+    if (!tma_wait_or_stop(sh, &sh.w_empty[t.wslot], t.wph ^ 1)) return false;
+    if (leader) {
+      mbar_arrive_expect_tx(&sh.w_full[t.wslot], bbytes);
+      const uint8_t* src = op.kind == 0 ? bbase + (size_t)c * bbytes : bbase + boff;
+      bulk_g2s(wring + t.wslot * kWSlotBytes, src, bbytes, &sh.w_full[t.wslot]);
+    }
+    __syncwarp();
+    t.issued_w[t.wslot] += 1;
+    if (++t.wslot == kWRing) { t.wslot = 0; t.wph ^= 1; }
   }
-  // drain: every issued copy must have landed before the CTA exits
-  for (int s = 0; s < kWRing; ++s) {
-    if (issued_w[s] == 0) continue;
+  ++t.g;
+  return true;
+}
+
+// Every issued copy must have landed before the CTA exits.
+__device__ __forceinline__ void tma_drain(TmaState& t, Shared& sh) {
+  volatile int* verr = &sh.err;
+  // A slot whose last fill was a producer copy: normally the MMA consumed it
+  // long ago (the epilogue drains every op). After an early exit the copy may
+  // still be in flight; then the slot's phase is that fill's, and the wait
+  // below ends when the bytes land. A phase that moved on twice since reads
+  // like an unfinished one, so the wait is short and sets no error.
+  for (int s = 0; s < kARing; ++s) {
+    if (!t.a_pending[s]) continue;
     const unsigned long long t0 = globaltimer_ns();
-    while (!mbar_try_wait(&sh.w_full[s], (issued_w[s] - 1) & 1)) {
+    while (!mbar_try_wait(&sh.a_full[s], t.a_par[s])) {
+      if (globaltimer_ns() - t0 > 20000ull) break;
+    }
+  }
+  for (int s = 0; s < kWRing; ++s) {
+    if (t.issued_w[s] == 0) continue;
+    const unsigned long long t0 = globaltimer_ns();
+    while (!mbar_try_wait(&sh.w_full[s], (t.issued_w[s] - 1) & 1)) {
       if (globaltimer_ns() - t0 > kWaitTimeoutNs) { *verr = 3; break; }
     }
   }
+}
+
+__device__ __forceinline__ void tma_loop(const OpList& ops, Shared& sh, uint8_t* aring, uint8_t* wring) {
+  TmaState t;
+  volatile int* verr = &sh.err;
+  volatile int* vstop = &sh.stop;
+  while (!*vstop && !*verr && tma_op(ops.op[t.g % ops.nops], t, sh, aring, wring, 0)) {
+  }
+  tma_drain(t, sh);
+}
+
+__device__ __forceinline__ void tma_loop_cmd(const OpList& ev, const OpList& dw, Shared& sh, uint8_t* aring,
+                                             uint8_t* wring) {
+  TmaState t;
+  int cs = 0;
+  uint32_t cph = 0, cmd = 0;
+  bool run = true;
+  while (run && cmd_take(sh, cs, cph, &cmd)) {
+    const bool isdw = (cmd & 0xffu) == CMD_DW;
+    const OpList& L = isdw ? dw : ev;
+    // weight-gradient images were written by the epilogue (generic proxy)
+    // before it posted the command
+    if (isdw) asm volatile("fence.proxy.async.global;" ::: "memory");
+    for (int i = 0; i < L.nops && run; ++i) run = tma_op(L.op[i], t, sh, aring, wring, (int)(cmd >> 8));
+  }
+  tma_drain(t, sh);
 }
 
 // ---- epilogue helpers --------------------------------------------------------------------
@@ -362,6 +472,20 @@ __device__ __forceinline__ bool epi_wait_acc(EpiState& e, Shared& sh, uint32_t* 
   if (!mbar_wait(&sh.acc_full[reg], e.use[reg] & 1, &sh.err)) return false;
   tc_fence_after();
   *col = (uint32_t)(reg * 256);
+  return true;
+}
+
+// Posts a command (thread 0 of the epilogue only). Returns false if the ring
+// slot did not come free within the wait limit.
+struct CmdPoster {
+  int cs = 0;
+  uint32_t cph = 0;
+};
+__device__ __forceinline__ bool epi_post(CmdPoster& p, Shared& sh, uint32_t cmd) {
+  if (!mbar_wait(&sh.cmd_empty[p.cs], p.cph ^ 1, &sh.err)) return false;
+  ((volatile uint32_t*)sh.cmd)[p.cs] = cmd;
+  mbar_arrive(&sh.cmd_full[p.cs]);
+  if (++p.cs == kCmdRing) { p.cs = 0; p.cph ^= 1; }
   return true;
 }
 
