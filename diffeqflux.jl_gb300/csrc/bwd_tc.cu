@@ -66,17 +66,24 @@ __device__ __forceinline__ void st32(float* p, int n, bool vec, const float* x) 
 // Thread-private FP32 scratch in slot-major layout: float4 slot k of thread t
 // at hs4[k * 256 + t], so the 32 lanes of a warp touch 512 contiguous bytes.
 __device__ __forceinline__ void hs_ld32(const float4* hs4, int k0, float* x) {
+  const uint64_t pol = tc::policy_evict_first();  // last use
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const float4 q = hs4[(size_t)(k0 + j) * tc::kEpiThreads + threadIdx.x];
+    const float4 q = tc::ld_v4f_hint(hs4 + (size_t)(k0 + j) * tc::kEpiThreads + threadIdx.x, pol);
     x[4 * j] = q.x; x[4 * j + 1] = q.y; x[4 * j + 2] = q.z; x[4 * j + 3] = q.w;
   }
 }
 __device__ __forceinline__ void hs_st32(float4* hs4, int k0, const float* x) {
+  const uint64_t pol = tc::policy_evict_last();  // read back within the evaluation
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
-    hs4[(size_t)(k0 + j) * tc::kEpiThreads + threadIdx.x] =
-        make_float4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
+  for (int j = 0; j < 8; ++j) {
+    uint4 u;
+    u.x = __float_as_uint(x[4 * j]);
+    u.y = __float_as_uint(x[4 * j + 1]);
+    u.z = __float_as_uint(x[4 * j + 2]);
+    u.w = __float_as_uint(x[4 * j + 3]);
+    tc::st_v4_hint(hs4 + (size_t)(k0 + j) * tc::kEpiThreads + threadIdx.x, u, pol);
+  }
 }
 
 __device__ __forceinline__ bool epi_grid_barrier(const BwdArgs& a, unsigned int& gen, int* okflag) {
@@ -124,6 +131,7 @@ __device__ __forceinline__ double epi_partials_sum(const double* p, int n, tc::S
 __device__ __forceinline__ void img_store(uint8_t* img, int isA, int nblk, int nh, const Thr& th,
                                           int c, const uint4* hi, const uint4* mid) {
   const int kc = th.r >> 6, row = th.r & 63;
+  const uint64_t pol = tc::policy_evict_first();  // read once, at the step's commit
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const uint32_t sw = tc::sw128_offset(row, 4 * th.ch + j);
@@ -136,8 +144,8 @@ __device__ __forceinline__ void img_store(uint8_t* img, int isA, int nblk, int n
       o0 = ((size_t)((kc * 2 + 0) * nblk + c)) * 8192 + sw;
       o1 = ((size_t)((kc * 2 + 1) * nblk + c)) * 8192 + sw;
     }
-    *reinterpret_cast<uint4*>(img + o0) = hi[j];
-    *reinterpret_cast<uint4*>(img + o1) = mid[j];
+    tc::st_v4_hint(img + o0, hi[j], pol);
+    tc::st_v4_hint(img + o1, mid[j], pol);
   }
 }
 
@@ -369,8 +377,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           for (int i = 0; i < 32; ++i) h[i] = hnext[i];
           if (cc + 1 < nch) hs_ld32(hs4, (A.hoff[l] + 32 * (cc + 1)) / 4, hnext);
           tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
-#pragma unroll
-          for (int i = 0; i < 32; ++i) v[i] = (n0 + i < N) ? v[i] * act_deriv_from_out(h[i], m.act[l - 1]) : 0.f;
+          tc::deriv_mul32(v, h, m.act[l - 1], n0, N);
           if (!emit(es, sh, aring, th, v, true, im ? im + A.doff[l - 1] : nullptr, !A.a_isA[l - 1],
                     (N + 63) / 64, A.nh[l - 1], cc, c))
             return false;
@@ -626,13 +633,33 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             if (v) {
               ld32(lcur + g, th.nmine, vec, l);
               ld32(ccur + g, th.nmine, vec, s);
+              if (i < 6) {
 #pragma unroll
-              for (int j = 0; j < 6; ++j) {
-                if (j >= i) break;
-                float kj[32];
-                ld32(klb(j) + g, th.nmine, vec, kj);
+                for (int j = 0; j < 5; ++j) {
+                  if (j >= i) break;
+                  float kj[32];
+                  ld32(klb(j) + g, th.nmine, vec, kj);
 #pragma unroll
-                for (int q = 0; q < 32; ++q) s[q] = fmaf(ha[j], kj[q], s[q]);
+                  for (int q = 0; q < 32; ++q) s[q] = fmaf(ha[j], kj[q], s[q]);
+                }
+              } else {
+                // stage 7 reads k1..k6 anyway: the embedded error estimate's
+                // sum over them is formed here and parked in the k7 slot
+                float lt[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) lt[q] = 0.f;
+#pragma unroll
+                for (int j = 0; j < 6; ++j) {
+                  float kj[32];
+                  ld32(klb(j) + g, th.nmine, vec, kj);
+                  const float hbt = (float)(H * c_tab.btilde[j]);
+#pragma unroll
+                  for (int q = 0; q < 32; ++q) {
+                    s[q] = fmaf(ha[j], kj[q], s[q]);
+                    lt[q] = fmaf(hbt, kj[q], lt[q]);
+                  }
+                }
+                st32(klb(6) + g, th.nmine, vec, lt);
               }
 #pragma unroll
               for (int q = 0; q < 32; ++q) Y[q] = l[q] + s[q];
@@ -649,22 +676,18 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             }
             ok = adj_eval(Y, x, slot, P, cw, kl);
             if (v) {
-              st32(klb(i) + g, th.nmine, vec, kl);
               if (i == 6) {
-                // lam and the stage value again (stored above): nothing of
-                // the stage arithmetic stays in registers across adj_eval
+                // lam, the stage value and the error sum over k1..k6 again
+                // (stored above): nothing of the stage arithmetic stays in
+                // registers across adj_eval
+                float lt[32];
+                ld32(klb(6) + g, th.nmine, vec, lt);
                 ld32(lcur + g, th.nmine, vec, l);
                 ld32(lnew + g, th.nmine, vec, Y);
-                float lt[32];
-                for (int q = 0; q < 32; ++q) lt[q] = (float)(H * c_tab.btilde[6]) * kl[q];
+                const float hbt6 = (float)(H * c_tab.btilde[6]);
 #pragma unroll
-                for (int j = 0; j < 6; ++j) {
-                  float kj[32];
-                  ld32(klb(j) + g, th.nmine, vec, kj);
-                  const float hbt = (float)(H * c_tab.btilde[j]);
-#pragma unroll
-                  for (int q = 0; q < 32; ++q) lt[q] = fmaf(hbt, kj[q], lt[q]);
-                }
+                for (int q = 0; q < 32; ++q) lt[q] = fmaf(hbt6, kl[q], lt[q]);
+                st32(klb(i) + g, th.nmine, vec, kl);
                 #pragma unroll
                 for (int q = 0; q < 32; ++q) {
                   if (q >= th.nmine) continue;
@@ -672,6 +695,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
                   const double rr = (double)(lt[q] / sc);
                   perr += isfinite(Y[q]) ? rr * rr : (double)INFINITY;
                 }
+              } else {
+                st32(klb(i) + g, th.nmine, vec, kl);
               }
             }
           }

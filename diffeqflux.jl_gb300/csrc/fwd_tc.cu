@@ -322,13 +322,32 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
             if (v) {
               ld32(ucur + g, th.nmine, vec, u);
               ld32(ccur + g, th.nmine, vec, s);
+              if (i < 6) {
 #pragma unroll
-              for (int j = 0; j < 6; ++j) {
-                if (j >= i) break;
-                float kj[32];
-                ld32(kptr(j) + g, th.nmine, vec, kj);
+                for (int j = 0; j < 5; ++j) {
+                  if (j >= i) break;
+                  float kj[32];
+                  ld32(kptr(j) + g, th.nmine, vec, kj);
 #pragma unroll
-                for (int q = 0; q < 32; ++q) s[q] = fmaf(ha[j], kj[q], s[q]);
+                  for (int q = 0; q < 32; ++q) s[q] = fmaf(ha[j], kj[q], s[q]);
+                }
+              } else {
+                // stage 7 reads k1..k6 anyway: the embedded error estimate's
+                // sum over them is formed here and parked in the k7 slot
+                float ut[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) ut[q] = 0.f;
+#pragma unroll
+                for (int j = 0; j < 6; ++j) {
+                  float kj[32];
+                  ld32(kptr(j) + g, th.nmine, vec, kj);
+#pragma unroll
+                  for (int q = 0; q < 32; ++q) {
+                    s[q] = fmaf(ha[j], kj[q], s[q]);
+                    ut[q] = fmaf(hbt[j], kj[q], ut[q]);
+                  }
+                }
+                st32(kptr(6) + g, th.nmine, vec, ut);
               }
 #pragma unroll
               for (int q = 0; q < 32; ++q) Y[q] = u[q] + s[q];
@@ -345,22 +364,17 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
             }
             ok = epi_rhs(A, es, sh, aring, th, Y, k);
             if (v) {
-              st32(kptr(i) + g, th.nmine, vec, k);
               if (i == 6) {
-                // u and the stage value again (stored above): nothing of the
-                // stage arithmetic stays in registers across epi_rhs
+                // u, the stage value and the error sum over k1..k6 again
+                // (stored above): nothing of the stage arithmetic stays in
+                // registers across epi_rhs
+                float ut[32];
+                ld32(kptr(6) + g, th.nmine, vec, ut);
                 ld32(ucur + g, th.nmine, vec, u);
                 ld32(unew + g, th.nmine, vec, Y);
-                float ut[32];
 #pragma unroll
-                for (int q = 0; q < 32; ++q) ut[q] = hbt[6] * k[q];
-#pragma unroll
-                for (int j = 0; j < 6; ++j) {
-                  float kj[32];
-                  ld32(kptr(j) + g, th.nmine, vec, kj);
-#pragma unroll
-                  for (int q = 0; q < 32; ++q) ut[q] = fmaf(hbt[j], kj[q], ut[q]);
-                }
+                for (int q = 0; q < 32; ++q) ut[q] = fmaf(hbt[6], k[q], ut[q]);
+                st32(kptr(i) + g, th.nmine, vec, k);
                 #pragma unroll
                 for (int q = 0; q < 32; ++q) {
                   if (q >= th.nmine) continue;
@@ -368,6 +382,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
                   const double rr = (double)(ut[q] / sc);
                   perr += isfinite(Y[q]) ? rr * rr : (double)INFINITY;
                 }
+              } else {
+                st32(kptr(i) + g, th.nmine, vec, k);
               }
             }
           }

@@ -460,6 +460,24 @@ __device__ __forceinline__ void bias_act32(float* v, const float* bias, int act,
   }
 }
 
+// v <- v * act'(z) on 32 columns starting at n0, with act' taken from the
+// stored activation outputs y (tanh: 1 - y^2; softplus: 1 - exp(-y));
+// columns at or past N -> 0. The activation branch is taken once per chunk.
+__device__ __forceinline__ void deriv_mul32(float* v, const float* y, int act, int n0, int N) {
+  if (act == GBNDE_ACT_TANH) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] *= fmaf(-y[i], y[i], 1.f);
+  } else if (act == GBNDE_ACT_SOFTPLUS) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] *= -expm1f(-y[i]);
+  }
+  if (n0 + 32 > N) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+      if (n0 + i >= N) v[i] = 0.f;
+  }
+}
+
 // Skip A-ring slots that the producer warp fills (weight-gradient ops).
 __device__ __forceinline__ void epi_skip_a(EpiState& e, int n) {
   for (int i = 0; i < n; ++i)

@@ -220,6 +220,34 @@ __device__ __forceinline__ void split3_bf16(const float* x, uint4& hi, uint4& mi
   lo = pack8_bf16(r);
 }
 
+// ---- L2 eviction priority ----------------------------------------------------------
+// Cache policies for accesses whose reuse distance is known: data read once
+// much later (weight-gradient images) is marked evict-first so that it does
+// not push out data read back soon (activation scratch, marked evict-last).
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void st_v4_hint(void* ptr, uint4 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(ptr), "r"(v.x), "r"(v.y),
+               "r"(v.z), "r"(v.w), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ float4 ld_v4f_hint(const void* ptr, uint64_t pol) {
+  float4 v;
+  asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(ptr), "l"(pol)
+               : "memory");
+  return v;
+}
+
 // Fire-and-forget global adds (performed at L2; no value returned, so the
 // issuing thread does not wait for the memory round trip). Each address of a
 // pending quadrature buffer has one writing thread, so the adds to an address
