@@ -192,6 +192,37 @@ __device__ __forceinline__ float act_apply_tc(float z, int act) {
   return z;
 }
 
+// Activations as types, so that a loop over elements can be compiled for one
+// activation: `with_act(code, [&](auto A) { ... A.f(z) ... A.d(y) ... })`
+// takes the branch on the (uniform) activation code once, outside the loop.
+// With the code tested per element, the compiler evaluates every
+// activation's formula for every element and selects.
+// f: the activation; d: act'(z) from the output y; d2: act''(z) from y.
+struct ActIdentity {
+  __device__ __forceinline__ float f(float z) const { return z; }
+  __device__ __forceinline__ float d(float) const { return 1.f; }
+  __device__ __forceinline__ float d2(float) const { return 0.f; }
+};
+struct ActTanh {
+  __device__ __forceinline__ float f(float z) const { return tanhf(z); }
+  __device__ __forceinline__ float d(float y) const { return 1.f - y * y; }
+  __device__ __forceinline__ float d2(float y) const { return -2.f * y * (1.f - y * y); }
+};
+struct ActSoftplus {
+  __device__ __forceinline__ float f(float z) const { return fmaxf(z, 0.f) + log1pf(expf(-fabsf(z))); }
+  __device__ __forceinline__ float d(float y) const { return -expm1f(-y); }
+  __device__ __forceinline__ float d2(float y) const {
+    const float sg = -expm1f(-y);
+    return sg * (1.f - sg);
+  }
+};
+template <class F>
+__device__ __forceinline__ void with_act(int act, F&& fn) {
+  if (act == GBNDE_ACT_TANH) fn(ActTanh{});
+  else if (act == GBNDE_ACT_SOFTPLUS) fn(ActSoftplus{});
+  else fn(ActIdentity{});
+}
+
 // act'(z) from the activation output y (tanh: 1 - y^2; softplus: 1 - exp(-y)).
 __device__ __forceinline__ float act_deriv_from_out(float y, int act) {
   if (act == GBNDE_ACT_TANH) return 1.f - y * y;

@@ -110,12 +110,14 @@ __device__ __forceinline__ void ffjord_rhs_tile(const FwdArgs& a, int tile, floa
     }
     __syncthreads();
     mlp_tangent_tile(m, act, zd, tmp, LD, TM);
-    for (int mm = threadIdx.x; mm < TM; mm += blockDim.x) {
-      float s_ = 0.f;
-      for (int s = 0; s < d; ++s)
-        s_ = fmaf(zd[0][s * LD + mm], act_deriv_from_out(act[L][s * LD + mm], m.act[L - 1]) * zd[L][s * LD + mm], s_);
-      tr[mm] += s_;
-    }
+    with_act(m.act[L - 1], [&](auto A) {
+      for (int mm = threadIdx.x; mm < TM; mm += blockDim.x) {
+        float s_ = 0.f;
+        for (int s = 0; s < d; ++s)
+          s_ = fmaf(zd[0][s * LD + mm], A.d(act[L][s * LD + mm]) * zd[L][s * LD + mm], s_);
+        tr[mm] += s_;
+      }
+    });
     __syncthreads();
   }
   for (int e = threadIdx.x; e < nvalid * S; e += blockDim.x) {

@@ -71,22 +71,24 @@ __device__ __forceinline__ void dense_fwd_tile(const float* __restrict__ Wt,
 #pragma unroll
         for (int j = 0; j < RN; ++j) acc[i][j] = fmaf(a[i], w[j], acc[i][j]);
     }
+    with_act(act, [&](auto A) {
 #pragma unroll
-    for (int j = 0; j < RN; ++j) {
-      if (n0 + j < N) {
-        const float bb = bias ? __ldg(bias + n0 + j) : 0.f;
-        float* op = out_s + (n0 + j) * LD + m0;
+      for (int j = 0; j < RN; ++j) {
+        if (n0 + j < N) {
+          const float bb = bias ? __ldg(bias + n0 + j) : 0.f;
+          float* op = out_s + (n0 + j) * LD + m0;
 #pragma unroll
-        for (int i = 0; i < RM; i += 4) {
-          float4 v;
-          v.x = act_apply(acc[i][j] + bb, act);
-          v.y = act_apply(acc[i + 1][j] + bb, act);
-          v.z = act_apply(acc[i + 2][j] + bb, act);
-          v.w = act_apply(acc[i + 3][j] + bb, act);
-          *reinterpret_cast<float4*>(op + i) = v;
+          for (int i = 0; i < RM; i += 4) {
+            float4 v;
+            v.x = A.f(acc[i][j] + bb);
+            v.y = A.f(acc[i + 1][j] + bb);
+            v.z = A.f(acc[i + 2][j] + bb);
+            v.w = A.f(acc[i + 3][j] + bb);
+            *reinterpret_cast<float4*>(op + i) = v;
+          }
         }
       }
-    }
+    });
   }
 }
 
@@ -195,10 +197,12 @@ __device__ __forceinline__ float* mlp_vjp_tile(const MlpDev& m, float* const* ac
     const int N = m.dims[l + 1], K = m.dims[l];
     if (m.act[l] != GBNDE_ACT_IDENTITY) {
       const float* y = act[l + 1];
-      for (int e = threadIdx.x; e < N * TM; e += blockDim.x) {
-        const int n = e / TM, mm = e - n * TM;
-        g[n * LD + mm] *= act_deriv_from_out(y[n * LD + mm], m.act[l]);
-      }
+      with_act(m.act[l], [&](auto A) {
+        for (int e = threadIdx.x; e < N * TM; e += blockDim.x) {
+          const int n = e / TM, mm = e - n * TM;
+          g[n * LD + mm] *= A.d(y[n * LD + mm]);
+        }
+      });
       __syncthreads();
     }
     if (P) {
@@ -239,10 +243,12 @@ __device__ __forceinline__ void mlp_tangent_tile(const MlpDev& m, float* const* 
     const int K = m.dims[l];
     const float* in = zd[0];
     if (l > 0) {
-      for (int e = threadIdx.x; e < K * TM; e += blockDim.x) {
-        const int k = e / TM, mm = e - k * TM;
-        tmp[k * LD + mm] = act_deriv_from_out(act[l][k * LD + mm], m.act[l - 1]) * zd[l][k * LD + mm];
-      }
+      with_act(m.act[l - 1], [&](auto A) {
+        for (int e = threadIdx.x; e < K * TM; e += blockDim.x) {
+          const int k = e / TM, mm = e - k * TM;
+          tmp[k * LD + mm] = A.d(act[l][k * LD + mm]) * zd[l][k * LD + mm];
+        }
+      });
       __syncthreads();
       in = tmp;
     }
@@ -257,6 +263,7 @@ __device__ __forceinline__ void dw_accum_scaled(float* __restrict__ P, const flo
                                                 const float* y, int actcode, int N, int K, int LD,
                                                 int TM, float c) {
   const int tnc = (N + 7) >> 3, tkc = (K + 7) >> 3;
+  with_act(y ? actcode : GBNDE_ACT_IDENTITY, [&](auto A) {
   for (int mt = threadIdx.x; mt < tnc * tkc; mt += blockDim.x) {
     const int n0 = (mt % tnc) * 8, k0 = (mt / tnc) * 8;
     float acc[8][8];
@@ -270,7 +277,7 @@ __device__ __forceinline__ void dw_accum_scaled(float* __restrict__ P, const flo
       for (int i = 0; i < 8; ++i) {
         gv[i] = g[min(n0 + i, N - 1) * LD + mm];
         const int kk = min(k0 + i, K - 1) * LD + mm;
-        av[i] = (y ? act_deriv_from_out(y[kk], actcode) : 1.f) * x[kk];
+        av[i] = (y ? A.d(y[kk]) : 1.f) * x[kk];
       }
 #pragma unroll
       for (int i = 0; i < 8; ++i)
@@ -286,6 +293,7 @@ __device__ __forceinline__ void dw_accum_scaled(float* __restrict__ P, const flo
         if (n0 + i < N) row[n0 + i] += c * acc[i][j];
     }
   }
+  });
 }
 
 // Reverse pass through the primal chain and its tangent (reverse over forward).
@@ -304,13 +312,15 @@ __device__ __forceinline__ float* ffjord_vjp_tile(const MlpDev& m, float* const*
     const float* y = act[l + 1];
     const float* zl = zd[l + 1];
     // tbar <- tbar * act'(y) (= zdot bar); abar <- tbar_in * act''(y) * zdot + abar * act'(y) (= z bar)
-    for (int e = threadIdx.x; e < N * TM; e += blockDim.x) {
-      const int n = e / TM, mm = e - n * TM, o = n * LD + mm;
-      const float d1 = act_deriv_from_out(y[o], code), d2 = act_deriv2_from_out(y[o], code);
-      const float tb = tbar[o];
-      abar[o] = fmaf(tb * d2, zl[o], abar[o] * d1);
-      tbar[o] = tb * d1;
-    }
+    with_act(code, [&](auto A) {
+      for (int e = threadIdx.x; e < N * TM; e += blockDim.x) {
+        const int n = e / TM, mm = e - n * TM, o = n * LD + mm;
+        const float d1 = A.d(y[o]), d2 = A.d2(y[o]);
+        const float tb = tbar[o];
+        abar[o] = fmaf(tb * d2, zl[o], abar[o] * d1);
+        tbar[o] = tb * d1;
+      }
+    });
     __syncthreads();
     if (P) {
       dw_accum(P + m.woff[l], abar, act[l], N, K, LD, TM, c);
