@@ -12,8 +12,9 @@
 //   forward recompute  z_l = W_l a_{l-1},          l = 1..L-1   (5 split products)
 //   VJP chain          g_l = W_l^T delta_{l+1},    l = L..1     (5 split products)
 //                      delta_l = g_l * act'(z_l), delta_L = lam, kl = g_1
-// The epilogue also writes the activations a_l and the cotangents
-// b_s delta_{l+1} (b_s: the stage's quadrature weight) as split-BF16
+// The VJP chain runs on b_s lam (b_s: the stage's quadrature weight; it is
+// linear, so kl is divided by b_s at the end), and the epilogue writes the
+// activations a_l and the weighted cotangents b_s delta_{l+1} as split-BF16
 // trajectory-major images into the image slot of the stage. Once a step is
 // accepted, one weight-gradient op per layer (and 128-row half) runs over
 // the six stages' images stacked along K (K = 6 x 128 trajectories, MN-major
@@ -149,11 +150,10 @@ __device__ __forceinline__ void img_store(uint8_t* img, int isA, int nblk, int n
   }
 }
 
-// 32 values: chain A chunk (3 pieces, the values themselves) and/or image
-// (2 pieces of the values times `scale`).
+// 32 values: chain A chunk (3 pieces) and/or image (the first 2 pieces).
 __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* aring, const Thr& th,
                                      const float* x, bool chain, uint8_t* img, int isA, int nblk,
-                                     int nh, int c, float scale = 1.f) {
+                                     int nh, int c) {
   uint4 hi[4], mid[4], lo[4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) tc::split3_bf16(x + 8 * j, hi[j], mid[j], lo[j]);
@@ -171,20 +171,7 @@ __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* a
     tc::mbar_arrive(&sh.a_full[e.aslot]);
     if (++e.aslot == tc::kARing) { e.aslot = 0; e.aph ^= 1; }
   }
-  if (img) {
-    if (scale == 1.f) {
-      img_store(img, isA, nblk, nh, th, c, hi, mid);
-    } else {
-      float xs[8];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) xs[q] = scale * x[8 * j + q];
-        tc::split3_bf16(xs, hi[j], mid[j], lo[j]);
-      }
-      img_store(img, isA, nblk, nh, th, c, hi, mid);
-    }
-  }
+  if (img) img_store(img, isA, nblk, nh, th, c, hi, mid);
   return true;
 }
 
@@ -345,13 +332,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         }
         tc::epi_release_acc(es, sh);
       }
-      // delta_L = lam (identity output layer)
-      const int bbase = threadIdx.x;  // unused placeholder to keep indices readable
-      (void)bbase;
+      // delta_L = c lam (identity output layer). The VJP chain is linear in
+      // its input, so every cotangent below carries the stage weight c: the
+      // chain chunks double as the weight-gradient images, and kl is divided
+      // by c at the end.
+      const float cs = P ? c : 1.f;
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = (i < th.nmine) ? lam_in[i] : 0.f;
+      for (int i = 0; i < 32; ++i) v[i] = (i < th.nmine) ? cs * lam_in[i] : 0.f;
       if (!emit(es, sh, aring, th, v, true, im ? im + A.doff[L - 1] : nullptr, !A.a_isA[L - 1],
-                (m.dims[L] + 63) / 64, A.nh[L - 1], 0, c))
+                (m.dims[L] + 63) / 64, A.nh[L - 1], 0))
         return false;
       if (P) {
         float w[32];
@@ -379,7 +368,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
           tc::deriv_mul32(v, h, m.act[l - 1], n0, N);
           if (!emit(es, sh, aring, th, v, true, im ? im + A.doff[l - 1] : nullptr, !A.a_isA[l - 1],
-                    (N + 63) / 64, A.nh[l - 1], cc, c))
+                    (N + 63) / 64, A.nh[l - 1], cc))
             return false;
           if (P) {
             const float s = warp_colsum(v, th.lane);
@@ -393,8 +382,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         uint32_t col;
         if (!tc::epi_wait_acc(es, sh, &col)) return false;
         tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)(32 * th.ch), v);
+        const float inv = 1.f / cs;
 #pragma unroll
-        for (int i = 0; i < 32; ++i) kl[i] = (i < th.nmine) ? v[i] : 0.f;
+        for (int i = 0; i < 32; ++i) kl[i] = (i < th.nmine) ? v[i] * inv : 0.f;
         if (m.cube) {
           float xc[32];
           hs_ld32(hs4, A.hx / 4, xc);
@@ -406,8 +396,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       if (P) {
         tc::epi_bar();
         for (int f = threadIdx.x; f < A.nbias; f += tc::kEpiThreads) {
+          // the column sums already carry the stage weight
           const float s = ((bpart[f] + bpart[A.nbias + f]) + bpart[2 * A.nbias + f]) + bpart[3 * A.nbias + f];
-          tc::red_add(P + f, c * s);
+          tc::red_add(P + f, s);
         }
         tc::epi_bar();
       }
