@@ -727,13 +727,22 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   for (int l = 0; l < L; ++l) t.bias[l] = m.bias[l];
   // op lists: forward recompute + VJP chain (per evaluation), and the
   // stage-stacked weight gradients (per accepted step: K = 6 stages x 128)
+  // Every chain operand is also a weight-gradient image: forward op l's A is
+  // a_l (image aoff[l]), VJP op l's A is delta_{l+1} (image doff[l]); the MMA
+  // warp copies the chunks to the stage's slot. The output layer's forward
+  // product is computed only to pass a_{L-1} through the ring.
   int n = 0;
-  for (int l = 0; l + 1 < L; ++l) {
+  if (2 * L > tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+  for (int l = 0; l < L; ++l) {
     tc::GemmOp& o = t.ops.op[n++];
     o.kind = 0;
     o.wimg = c->wimg.as<uint8_t>() + c->wimg_off[l];
     o.npad = c->npad[l];
     o.nchunk = c->nchunk[l];
+    o.img_off = (int)t.aoff[l];
+    o.img_isA = (uint8_t)t.a_isA[l];
+    o.img_nblk = (uint8_t)((m.dims[l] + 63) / 64);
+    o.img_nh = (uint16_t)t.nh[l];
   }
   for (int l = L - 1; l >= 0; --l) {
     tc::GemmOp& o = t.ops.op[n++];
@@ -741,6 +750,10 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
     o.wimg = c->wimg.as<uint8_t>() + c->wtimg_off[l];
     o.npad = c->npadT[l];
     o.nchunk = c->nchunkT[l];
+    o.img_off = (int)t.doff[l];
+    o.img_isA = (uint8_t)(!t.a_isA[l]);
+    o.img_nblk = (uint8_t)((m.dims[l + 1] + 63) / 64);
+    o.img_nh = (uint16_t)t.nh[l];
   }
   t.ops.nops = n;
   n = 0;
@@ -766,6 +779,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
       o.npad = (nside + 15) / 16 * 16;
       o.nchunk = 2 * 6;
       o.first_dw = 0;
+      o.img_off = -1;
       t.dw_chunks += o.nchunk;
     }
   }

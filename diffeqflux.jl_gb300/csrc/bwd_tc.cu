@@ -64,6 +64,34 @@ __device__ __forceinline__ void st32(float* p, int n, bool vec, const float* x) 
   }
 }
 
+// Half (16 values) of a thread's 32 components: p already offset to the half,
+// n = valid values in it. All loads of a half are issued before any is used,
+// so several vectors cost one memory round trip.
+__device__ __forceinline__ void ld16(const float* p, int n, bool vec, float* x) {
+  if (vec) {
+#pragma unroll
+    for (int i = 0; i < 16; i += 4) {
+      const float4 v = *reinterpret_cast<const float4*>(p + i);
+      x[i] = v.x; x[i + 1] = v.y; x[i + 2] = v.z; x[i + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) x[i] = (i < n) ? p[i] : 0.f;
+  }
+}
+
+__device__ __forceinline__ void st16(float* p, int n, bool vec, const float* x) {
+  if (vec) {
+#pragma unroll
+    for (int i = 0; i < 16; i += 4)
+      *reinterpret_cast<float4*>(p + i) = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+      if (i < n) p[i] = x[i];
+  }
+}
+
 // Thread-private FP32 scratch in slot-major layout: float4 slot k of thread t
 // at hs4[k * 256 + t], so the 32 lanes of a warp touch 512 contiguous bytes.
 __device__ __forceinline__ void hs_ld32(const float4* hs4, int k0, float* x) {
@@ -126,38 +154,15 @@ __device__ __forceinline__ double epi_partials_sum(const double* p, int n, tc::S
   return v;
 }
 
-// Split-BF16 pieces of 32 values -> this thread's part of a weight-gradient
-// image (2 pieces). Block c holds features [64c, 64c+64); the thread writes
-// its 16-byte groups 4*ch..4*ch+3 of trajectory row r.
-__device__ __forceinline__ void img_store(uint8_t* img, int isA, int nblk, int nh, const Thr& th,
-                                          int c, const uint4* hi, const uint4* mid) {
-  const int kc = th.r >> 6, row = th.r & 63;
-  const uint64_t pol = tc::policy_evict_first();  // read once, at the step's commit
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const uint32_t sw = tc::sw128_offset(row, 4 * th.ch + j);
-    size_t o0, o1;
-    if (isA) {
-      const int h = c >> 1, bb = c & 1;
-      o0 = ((size_t)((kc * nh + h) * 2 + 0)) * 16384 + bb * 8192 + sw;
-      o1 = ((size_t)((kc * nh + h) * 2 + 1)) * 16384 + bb * 8192 + sw;
-    } else {
-      o0 = ((size_t)((kc * 2 + 0) * nblk + c)) * 8192 + sw;
-      o1 = ((size_t)((kc * 2 + 1) * nblk + c)) * 8192 + sw;
-    }
-    tc::st_v4_hint(img + o0, hi[j], pol);
-    tc::st_v4_hint(img + o1, mid[j], pol);
-  }
-}
-
-// 32 values: chain A chunk (3 pieces) and/or image (the first 2 pieces).
+// 32 values of this thread's row into the next chain A chunk (3 split
+// pieces). The MMA warp also copies the chunk's first two pieces to the
+// stage's weight-gradient image when the op asks for it.
 __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* aring, const Thr& th,
-                                     const float* x, bool chain, uint8_t* img, int isA, int nblk,
-                                     int nh, int c) {
+                                     const float* x) {
   uint4 hi[4], mid[4], lo[4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) tc::split3_bf16(x + 8 * j, hi[j], mid[j], lo[j]);
-  if (chain) {
+  {
     if (!tc::mbar_wait(&sh.a_empty[e.aslot], e.aph ^ 1, &sh.err)) return false;
     uint8_t* base = aring + e.aslot * tc::kASlotBytes;
 #pragma unroll
@@ -171,7 +176,6 @@ __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* a
     tc::mbar_arrive(&sh.a_full[e.aslot]);
     if (++e.aslot == tc::kARing) { e.aslot = 0; e.aph ^= 1; }
   }
-  if (img) img_store(img, isA, nblk, nh, th, c, hi, mid);
   return true;
 }
 
@@ -200,6 +204,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
   uint8_t* wring = smem + tc::kARing * tc::kASlotBytes;
   __shared__ tc::Shared sh;
   __shared__ int s_ok;
+  // per-step scalars of stages 2..7, computed once by one warp: h a_ij, the
+  // interpolation weights h b_j(theta) and forward slot of each stage time,
+  // and the error weights h btilde_j
+  __shared__ float s_ha[6][6], s_hb[6][7], s_hbt[7];
+  __shared__ int s_n[6];
   const BwdArgs& a = A.b;
   const int warp = threadIdx.x >> 5;
 
@@ -211,7 +220,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
 
   if (warp >= tc::kMmaWarp) {
     tc::regs_give_ctl();
-    if (warp == tc::kMmaWarp) tc::mma_loop_cmd(A.ops, A.dwops, sh, aring, wring);
+    if (warp == tc::kMmaWarp)
+      tc::mma_loop_cmd(A.ops, A.dwops, sh, aring, wring, A.img + (size_t)blockIdx.x * tc::kImgSlots * A.img_cta,
+                       A.img_cta);
     else if (warp == tc::kTmaWarp) tc::tma_loop_cmd(A.ops, A.dwops, sh, aring, wring);
   } else {
     tc::regs_take_epi();
@@ -295,8 +306,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // P/c: pending bias quadrature buffer and the stage weight (P == nullptr:
     // no quadrature). The cotangent images carry the weight c.
     auto adj_eval = [&](const float* lam_in, const float* x, int slot, float* P, float c, float* kl) -> bool {
-      if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_EVAL)) return false;
-      uint8_t* im = slot >= 0 ? img + (size_t)slot * A.img_cta : nullptr;
+      if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_EVAL | ((uint32_t)(slot + 1) << 8))) return false;
       float v[32];
       // a_0 = x (or x^3)
 #pragma unroll
@@ -305,9 +315,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         v[i] = m.cube ? y * y * y : y;
       }
       if (m.cube) hs_st32(hs4, A.hx / 4, x);  // for the chain rule through x^3 at the end
-      if (!emit(es, sh, aring, th, v, true, im ? im + A.aoff[0] : nullptr, A.a_isA[0], (m.dims[0] + 63) / 64,
-                A.nh[0], 0))
-        return false;
+      if (!emit(es, sh, aring, th, v)) return false;
       // forward recompute of the hidden layers
       for (int l = 0; l < L - 1; ++l) {
         const int N = m.dims[l + 1];
@@ -326,10 +334,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
           tc::bias_act32(v, bc, m.act[l], n0, N);
           hs_st32(hs4, (A.hoff[l + 1] + 32 * cc) / 4, v);
-          if (!emit(es, sh, aring, th, v, l + 1 <= L - 2, im ? im + A.aoff[l + 1] : nullptr, A.a_isA[l + 1],
-                    (N + 63) / 64, A.nh[l + 1], cc))
-            return false;
+          if (!emit(es, sh, aring, th, v)) return false;
         }
+        tc::epi_release_acc(es, sh);
+      }
+      // the output layer's product runs only so that a_{L-1} passes through
+      // the ring (and into its image); its accumulator is not needed
+      {
+        uint32_t col;
+        if (!tc::epi_wait_acc(es, sh, &col)) return false;
         tc::epi_release_acc(es, sh);
       }
       // delta_L = c lam (identity output layer). The VJP chain is linear in
@@ -339,9 +352,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       const float cs = P ? c : 1.f;
 #pragma unroll
       for (int i = 0; i < 32; ++i) v[i] = (i < th.nmine) ? cs * lam_in[i] : 0.f;
-      if (!emit(es, sh, aring, th, v, true, im ? im + A.doff[L - 1] : nullptr, !A.a_isA[L - 1],
-                (m.dims[L] + 63) / 64, A.nh[L - 1], 0))
-        return false;
+      if (!emit(es, sh, aring, th, v)) return false;
       if (P) {
         float w[32];
 #pragma unroll
@@ -367,9 +378,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           if (cc + 1 < nch) hs_ld32(hs4, (A.hoff[l] + 32 * (cc + 1)) / 4, hnext);
           tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
           tc::deriv_mul32(v, h, m.act[l - 1], n0, N);
-          if (!emit(es, sh, aring, th, v, true, im ? im + A.doff[l - 1] : nullptr, !A.a_isA[l - 1],
-                    (N + 63) / 64, A.nh[l - 1], cc))
-            return false;
+          if (!emit(es, sh, aring, th, v)) return false;
           if (P) {
             const float s = warp_colsum(v, th.lane);
             bpart[th.q * A.nbias + A.boffp[l - 1] + n0 + th.lane] = s;
@@ -410,8 +419,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // (L2 reductions: each mu element has one writing thread per CTA). Then the
     // bias quadrature mu_b += H (P1 + Pmid).
     auto commit_step = [&](float Hf) -> bool {
-      // images of the step (generic-proxy stores) -> producer warp (async proxy)
-      asm volatile("fence.proxy.async.global;" ::: "memory");
       tc::epi_bar();
       if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_DW | ((uint32_t)fs << 8))) return false;
       tc::epi_skip_a(es, A.dw_chunks);
@@ -477,19 +484,33 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     auto dense_u = [&](int tile, int n, const float* hb, float* x) {
       const float* slot = a.dense + (size_t)n * 8 * SB;
       const size_t g = gofs(tile);
-      float acc[32];
-      ld32(slot + g, th.nmine, vec, x);
+      // u_n + sum_j hb_j k_j, in halves of 16 components and batches of
+      // four vectors (u_n, k1..k3 then k4..k7), each batch in flight together
 #pragma unroll
-      for (int i = 0; i < 32; ++i) acc[i] = 0.f;
+      for (int hf = 0; hf < 2; ++hf) {
+        const int nn = min(16, max(0, th.nmine - 16 * hf));
+        const float* sp = slot + g + 16 * hf;
+        float v4[4][16], acc[16];
 #pragma unroll
-      for (int j = 0; j < 7; ++j) {
-        float kj[32];
-        ld32(slot + (size_t)(j + 1) * SB + g, th.nmine, vec, kj);
+        for (int j = 0; j < 4; ++j) ld16(sp + (size_t)j * SB, nn, vec, v4[j]);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) acc[i] = fmaf(hb[j], kj[i], acc[i]);
+        for (int q = 0; q < 16; ++q) {
+          float e = 0.f;
+#pragma unroll
+          for (int j = 0; j < 3; ++j) e = fmaf(hb[j], v4[j + 1][q], e);
+          acc[q] = e;
+          x[16 * hf + q] = v4[0][q];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ld16(sp + (size_t)(j + 4) * SB, nn, vec, v4[j]);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          float e = acc[q];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) e = fmaf(hb[j + 3], v4[j][q], e);
+          x[16 * hf + q] += e;
+        }
       }
-#pragma unroll
-      for (int i = 0; i < 32; ++i) x[i] += acc[i];
     };
 
     for (int ivi = 0; ivi < a.niv && ok && ret == GBNDE_RET_SUCCESS; ++ivi) {
@@ -601,12 +622,19 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         const float* ccur = A.lam_comp[cur];
         float* cnew = A.lam_comp[cur ^ 1];
         zero_bias(Pmid);
+        if (threadIdx.x < 6) {
+          const int i = threadIdx.x + 1;
+          for (int j = 0; j < 6; ++j) s_ha[i - 1][j] = (float)(H * c_tab.a[i][j]);
+          dense_setup(iv, t - c_tab.c[i] * H, &s_n[i - 1], s_hb[i - 1]);
+        } else if (threadIdx.x == 32) {
+          for (int j = 0; j < 7; ++j) s_hbt[j] = (float)(H * c_tab.btilde[j]);
+        }
         tc::epi_bar();
         double perr = 0.0;
         for (int i = 1; i < 7 && ok; ++i) {
-          const double tt = t - c_tab.c[i] * H;
           float ha[6];
-          for (int j = 0; j < 6; ++j) ha[j] = (float)(H * c_tab.a[i][j]);
+#pragma unroll
+          for (int j = 0; j < 6; ++j) ha[j] = s_ha[i - 1][j];
           float* P = (i < 6) ? Pmid : Pb[iP7];
           const int slot = (i < 6) ? i : tc::kImgSlots - 1 - fs;
           if (i == 6) {
@@ -614,56 +642,57 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             tc::epi_bar();
           }
           const float cw = (i < 6) ? (float)c_tab.b[i] : (float)c_tab.b[0];
-          int n;
+          const int n = s_n[i - 1];
           float hb[7];
-          dense_setup(iv, tt, &n, hb);
+#pragma unroll
+          for (int j = 0; j < 7; ++j) hb[j] = s_hb[i - 1][j];
           for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
             const bool v = valid(tile);
             const size_t g = gofs(tile);
-            float l[32], s[32], Y[32], x[32], kl[32];
+            float Y[32], x[32], kl[32];
             if (v) {
-              ld32(lcur + g, th.nmine, vec, l);
-              ld32(ccur + g, th.nmine, vec, s);
-              if (i < 6) {
+              // Y = lam + (comp + sum_j h a_ij k_j), in two halves of 16
+              // components whose loads are all in flight together
 #pragma unroll
-                for (int j = 0; j < 5; ++j) {
-                  if (j >= i) break;
-                  float kj[32];
-                  ld32(klb(j) + g, th.nmine, vec, kj);
+              for (int hf = 0; hf < 2; ++hf) {
+                const int nn = min(16, max(0, th.nmine - 16 * hf));
+                const size_t gh = g + 16 * hf;
+                float lv[16], sv[16], kv[6][16];
+                ld16(lcur + gh, nn, vec, lv);
+                ld16(ccur + gh, nn, vec, sv);
 #pragma unroll
-                  for (int q = 0; q < 32; ++q) s[q] = fmaf(ha[j], kj[q], s[q]);
+                for (int j = 0; j < 6; ++j)
+                  if (j < i) ld16(klb(j) + gh, nn, vec, kv[j]);
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                  float sq = sv[q];
+#pragma unroll
+                  for (int j = 0; j < 6; ++j)
+                    if (j < i) sq = fmaf(ha[j], kv[j][q], sq);
+                  sv[q] = sq;
+                  Y[16 * hf + q] = lv[q] + sq;
                 }
-              } else {
-                // stage 7 reads k1..k6 anyway: the embedded error estimate's
-                // sum over them is formed here and parked in the k7 slot
-                float lt[32];
+                if (i == 6) {
+                  // stage 7 reads k1..k6 anyway: the embedded error
+                  // estimate's sum over them is formed here and parked in
+                  // the k7 slot; the new lam and its compensation are stored
+                  float lt[16], cn[16];
 #pragma unroll
-                for (int q = 0; q < 32; ++q) lt[q] = 0.f;
+                  for (int q = 0; q < 16; ++q) {
+                    float e = 0.f;
 #pragma unroll
-                for (int j = 0; j < 6; ++j) {
-                  float kj[32];
-                  ld32(klb(j) + g, th.nmine, vec, kj);
-                  const float hbt = (float)(H * c_tab.btilde[j]);
-#pragma unroll
-                  for (int q = 0; q < 32; ++q) {
-                    s[q] = fmaf(ha[j], kj[q], s[q]);
-                    lt[q] = fmaf(hbt, kj[q], lt[q]);
+                    for (int j = 0; j < 6; ++j) e = fmaf(s_hbt[j], kv[j][q], e);
+                    lt[q] = e;
+                    cn[q] = sv[q] - (Y[16 * hf + q] - lv[q]);
                   }
+                  st16(klb(6) + gh, nn, vec, lt);
+                  st16(lnew + gh, nn, vec, Y + 16 * hf);
+                  st16(cnew + gh, nn, vec, cn);
                 }
-                st32(klb(6) + g, th.nmine, vec, lt);
-              }
-#pragma unroll
-              for (int q = 0; q < 32; ++q) Y[q] = l[q] + s[q];
-              if (i == 6) {
-                float cn[32];
-#pragma unroll
-                for (int q = 0; q < 32; ++q) cn[q] = s[q] - (Y[q] - l[q]);
-                st32(lnew + g, th.nmine, vec, Y);
-                st32(cnew + g, th.nmine, vec, cn);
               }
               dense_u(tile, n, hb, x);
             } else {
-              for (int q = 0; q < 32; ++q) Y[q] = x[q] = l[q] = 0.f;
+              for (int q = 0; q < 32; ++q) Y[q] = x[q] = 0.f;
             }
             ok = adj_eval(Y, x, slot, P, cw, kl);
             if (v) {
@@ -671,21 +700,25 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
                 // lam, the stage value and the error sum over k1..k6 again
                 // (stored above): nothing of the stage arithmetic stays in
                 // registers across adj_eval
-                float lt[32];
-                ld32(klb(6) + g, th.nmine, vec, lt);
-                ld32(lcur + g, th.nmine, vec, l);
-                ld32(lnew + g, th.nmine, vec, Y);
-                const float hbt6 = (float)(H * c_tab.btilde[6]);
+                const float hbt6 = s_hbt[6];
 #pragma unroll
-                for (int q = 0; q < 32; ++q) lt[q] = fmaf(hbt6, kl[q], lt[q]);
-                st32(klb(i) + g, th.nmine, vec, kl);
-                #pragma unroll
-                for (int q = 0; q < 32; ++q) {
-                  if (q >= th.nmine) continue;
-                  const float sc = (float)a.abstol + fmaxf(fabsf(l[q]), fabsf(Y[q])) * (float)a.reltol;
-                  const double rr = (double)(lt[q] / sc);
-                  perr += isfinite(Y[q]) ? rr * rr : (double)INFINITY;
+                for (int hf = 0; hf < 2; ++hf) {
+                  const int nn = min(16, max(0, th.nmine - 16 * hf));
+                  const size_t gh = g + 16 * hf;
+                  float lt[16], lv[16], yv[16];
+                  ld16(klb(6) + gh, nn, vec, lt);
+                  ld16(lcur + gh, nn, vec, lv);
+                  ld16(lnew + gh, nn, vec, yv);
+#pragma unroll
+                  for (int q = 0; q < 16; ++q) {
+                    if (16 * hf + q >= th.nmine) continue;
+                    const float e = fmaf(hbt6, kl[16 * hf + q], lt[q]);
+                    const float sc = (float)a.abstol + fmaxf(fabsf(lv[q]), fabsf(yv[q])) * (float)a.reltol;
+                    const double rr = (double)(e / sc);
+                    perr += isfinite(yv[q]) ? rr * rr : (double)INFINITY;
+                  }
                 }
+                st32(klb(i) + g, th.nmine, vec, kl);
               } else {
                 st32(klb(i) + g, th.nmine, vec, kl);
               }

@@ -41,7 +41,7 @@ constexpr int kWSlotBytes = 2 * 32768;   // 2 pieces x 256 rows x 128 B
 constexpr int kARing = 2;
 constexpr int kWRing = 2;
 constexpr int kSmemBytes = 1024 + kARing * kASlotBytes + kWRing * kWSlotBytes;
-constexpr int kMaxOps = 20;
+constexpr int kMaxOps = 18;
 constexpr int kCmdRing = 4;
 constexpr int kImgSlots = 7;    // weight-gradient image slots per CTA: stages 1..6 + the next stage 1
 
@@ -63,6 +63,14 @@ struct GemmOp {
   int nblk_b;           // kind 1: 64-column blocks in a B chunk
   int first_dw;         // kind 1: first weight-gradient op of an evaluation (waits for images)
   size_t slot_stride;   // kind 1: bytes between the image slots of consecutive stages
+  // kind 0 in command mode: the A chunks are also the weight-gradient image
+  // of this operand (first two split pieces), bulk-copied by the MMA warp to
+  // the stage's image slot at byte offset img_off (< 0: no image). Layout:
+  // img_isA (rows = M-side features, img_nh 128-row halves) or img_nblk
+  // 64-feature blocks.
+  int img_off;
+  uint8_t img_isA, img_nblk;
+  uint16_t img_nh;
 };
 
 struct OpList {
@@ -75,6 +83,7 @@ struct Shared {
   uint64_t w_full[kWRing], w_empty[kWRing];
   uint64_t acc_full[2], acc_empty[2];
   uint64_t img_ready;
+  uint64_t img_done;  // command mode: the MMA warp's image copies of the step have landed
   uint64_t cmd_full[kCmdRing], cmd_empty[kCmdRing];
   uint32_t cmd[kCmdRing];
   uint32_t tmem_base;
@@ -123,6 +132,7 @@ __device__ __forceinline__ void init_shared(Shared& sh) {
       mbar_init(&sh.acc_empty[i], kEpiThreads);
     }
     mbar_init(&sh.img_ready, kEpiThreads);
+    mbar_init(&sh.img_done, 1);
     for (int i = 0; i < kCmdRing; ++i) {
       mbar_init(&sh.cmd_full[i], 1);
       mbar_init(&sh.cmd_empty[i], 2);
@@ -152,11 +162,31 @@ struct MmaState {
   long long g = 0;
 };
 
+// Bulk copies of A chunk c (pieces hi and mid, rows 0-63 and 64-127) of a
+// kind-0 op to its weight-gradient image (same SW128 arrangement as the
+// image's 8 KB blocks). Issued by the elected lane.
+__device__ __forceinline__ void copy_a_image(const GemmOp& op, int c, const uint8_t* achunk, uint8_t* img_base) {
+  const uint64_t pol = policy_evict_first();  // read once, at the step's commit
+  uint8_t* dst0 = img_base + op.img_off;
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+#pragma unroll
+    for (int kc = 0; kc < 2; ++kc) {
+      const size_t o = op.img_isA ? ((size_t)((kc * op.img_nh + (c >> 1)) * 2 + p)) * 16384 + (size_t)(c & 1) * 8192
+                                  : ((size_t)((kc * 2 + p) * op.img_nblk + c)) * 8192;
+      bulk_s2g(dst0 + o, achunk + p * 16384 + kc * 8192, 8192, pol);
+    }
+  }
+  bulk_commit();
+}
+
 // One op: waits for its accumulator region, then for every K chunk for the A
-// chunk and the W chunk, and issues the products. Returns false when the
-// loop must end (stop flag, error or wait limit).
+// chunk and the W chunk, and issues the products (and, with img_base, the
+// image copies of the A chunks, which must have read the slot before it is
+// released). Returns false when the loop must end (stop flag, error or wait
+// limit).
 __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh, uint8_t* aring,
-                                       uint8_t* wring) {
+                                       uint8_t* wring, uint8_t* img_base = nullptr) {
   volatile int* verr = &sh.err;
   volatile int* vstop = &sh.stop;
   const bool leader = (threadIdx.x & 31) == 0;
@@ -187,6 +217,8 @@ __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh
     if (leader) {
       const uint32_t a0 = smem_u32(aring + m.aslot * kASlotBytes);
       const uint32_t b0 = smem_u32(wring + m.wslot * kWSlotBytes);
+      const bool copy = op.kind == 0 && img_base != nullptr && op.img_off >= 0;
+      if (copy) copy_a_image(op, c, aring + m.aslot * kASlotBytes, img_base);
       if (op.kind == 0) {
 #pragma unroll
         for (int pr = 0; pr < 5; ++pr) {
@@ -211,6 +243,7 @@ __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh
           }
         }
       }
+      if (copy) bulk_wait_read_all();
       mma_commit(&sh.a_empty[m.aslot]);
       mma_commit(&sh.w_empty[m.wslot]);
       if (c == op.nchunk - 1) mma_commit(&sh.acc_full[reg]);
@@ -246,17 +279,33 @@ __device__ __forceinline__ bool cmd_take(Shared& sh, int& cs, uint32_t& cph, uin
   return true;
 }
 
-// Command mode: one op list per command.
+// Command mode: one op list per command. CMD_EVAL carries slot + 1 in bits
+// 8.. (0: no images); `imgs` is this CTA's image region, `img_cta` the bytes
+// of one slot. Before a CMD_DW round the image copies must have landed: the
+// elected lane waits for its bulk groups and signals the producer.
 __device__ __forceinline__ void mma_loop_cmd(const OpList& ev, const OpList& dw, Shared& sh, uint8_t* aring,
-                                             uint8_t* wring) {
+                                             uint8_t* wring, uint8_t* imgs, size_t img_cta) {
   MmaState m;
   int cs = 0;
   uint32_t cph = 0, cmd = 0;
-  while (cmd_take(sh, cs, cph, &cmd)) {
-    const OpList& L = (cmd & 0xffu) == CMD_DW ? dw : ev;
-    for (int i = 0; i < L.nops; ++i)
-      if (!mma_op(L.op[i], m, sh, aring, wring)) return;
+  const bool leader = (threadIdx.x & 31) == 0;
+  bool ok = true;
+  while (ok && cmd_take(sh, cs, cph, &cmd)) {
+    const bool isdw = (cmd & 0xffu) == CMD_DW;
+    uint8_t* img_base = nullptr;
+    if (isdw) {
+      if (leader) {
+        bulk_wait_all();
+        mbar_arrive(&sh.img_done);
+      }
+      __syncwarp();
+    } else if ((cmd >> 8) != 0) {
+      img_base = imgs + (size_t)((cmd >> 8) - 1) * img_cta;
+    }
+    const OpList& L = isdw ? dw : ev;
+    for (int i = 0; i < L.nops && ok; ++i) ok = mma_op(L.op[i], m, sh, aring, wring, img_base);
   }
+  if (leader) bulk_wait_all();
 }
 
 // ---- producer warp ---------------------------------------------------------------------
@@ -370,14 +419,17 @@ __device__ __forceinline__ void tma_loop_cmd(const OpList& ev, const OpList& dw,
                                              uint8_t* wring) {
   TmaState t;
   int cs = 0;
-  uint32_t cph = 0, cmd = 0;
+  uint32_t cph = 0, cmd = 0, dph = 0;
   bool run = true;
   while (run && cmd_take(sh, cs, cph, &cmd)) {
     const bool isdw = (cmd & 0xffu) == CMD_DW;
     const OpList& L = isdw ? dw : ev;
-    // weight-gradient images were written by the epilogue (generic proxy)
-    // before it posted the command
-    if (isdw) asm volatile("fence.proxy.async.global;" ::: "memory");
+    if (isdw) {
+      // the stage images (bulk-copied by the MMA warp) must have landed
+      if (!tma_wait_or_stop(sh, &sh.img_done, dph)) break;
+      dph ^= 1;
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+    }
     for (int i = 0; i < L.nops && run; ++i) run = tma_op(L.op[i], t, sh, aring, wring, (int)(cmd >> 8));
   }
   tma_drain(t, sh);
