@@ -133,6 +133,7 @@ struct gbnde_ctx {
   long long last_naccept = 0;
   bool rerun_guard = false;
   int final_cur = 0;
+  bool dense_tl = false;  // the last forward kept its dense slots in the tile layout (BF16 form)
   int fwd_retcode = 0;
   const float* usave_dev = nullptr;  // saved states of the last forward (device)
   cudaStream_t own_stream = nullptr;
@@ -432,7 +433,10 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   // dense stage storage: one slot (u_n, k1..k7) per accepted step. Sized from
   // the step count of the previous solve (at least 64 slots), within a
   // quarter of the free device memory; grows only when a solve needs more.
-  const size_t slot = 8 * SB * sizeof(float);
+  // the BF16 form keeps its internal vectors (state, stages, dense slots) in
+  // the tile layout: ntiles * 128 rows x 64 components each
+  const size_t SBv = tcform ? (size_t)ntiles * tc::kTileVec : SB;
+  const size_t slot = 8 * SBv * sizeof(float);
   auto size_dense = [&](long long want) {
     want = std::min<long long>(std::max<long long>(want, 64), maxiters + 1);
     const long long have_now = (long long)(c->dense.n / slot);
@@ -452,9 +456,9 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
     c->dense_slots = (long long)(c->dense.n / slot);
   };
   size_dense(2 * c->last_naccept + 8);
-  if (tcform && (r = c->comp.ensure(2 * SB * 4))) return r;
+  if (tcform && (r = c->comp.ensure(2 * SBv * 4))) return r;
   if (u0_host && (r = c->u0.ensure(SB * 4))) return r;
-  if ((r = c->ubuf.ensure(2 * SB * 4)) || (r = c->kbuf.ensure(7 * SB * 4))) return r;
+  if ((r = c->ubuf.ensure(2 * SBv * 4)) || (r = c->kbuf.ensure(7 * SBv * 4))) return r;
   if (usave_host && (r = c->usave.ensure(SB * nsave * 4))) return r;
   if ((r = c->ckpt.ensure(SB * nb * 4)) || (r = c->ckpt_step.ensure(nb * sizeof(int)))) return r;
   const long long maxsteps = std::min<long long>(maxiters, 1LL << 22);
@@ -497,8 +501,8 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   a.nbnd = nb;
   a.u0 = u0d;
   a.ubuf[0] = c->ubuf.as<float>();
-  a.ubuf[1] = c->ubuf.as<float>() + SB;
-  for (int j = 0; j < 7; ++j) a.kbuf[j] = c->kbuf.as<float>() + j * SB;
+  a.ubuf[1] = c->ubuf.as<float>() + SBv;
+  for (int j = 0; j < 7; ++j) a.kbuf[j] = c->kbuf.as<float>() + j * SBv;
   a.usave = usd;
   a.ckpt = c->ckpt.as<float>();
   a.max_ckpt = nb;
@@ -532,7 +536,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
       ta.bias[l] = c->mlp.bias[l];
     }
     ta.comp[0] = c->comp.as<float>();
-    ta.comp[1] = c->comp.as<float>() + SB;
+    ta.comp[1] = c->comp.as<float>() + SBv;
     ta.dense = a.dense;
     ta.dense_slots = a.dense_slots;
     ta.kring = c->kbuf.as<float>();
@@ -590,6 +594,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   c->saveat.assign(d->saveat, d->saveat + nsave);
   c->have_fwd = (status[ST_RETCODE] == GBNDE_RET_SUCCESS) && nacc <= maxsteps;
   c->dense_valid = c->dense_slots > 0 && nacc < c->dense_slots;
+  c->dense_tl = tcform;
   c->last_naccept = nacc;
   c->fS = S;
   if (c->have_fwd && !c->dense_valid && !c->rerun_guard) {
@@ -660,13 +665,13 @@ static int build_intervals(gbnde_ctx* c, std::vector<Interval>& ivs, int* max_sl
 static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float* dp_d) {
   const MlpDev& m = c->mlp;
   const int L = m.nlayers;
-  const int S = c->S, B = c->B;
-  const size_t SB = (size_t)S * B;
+  const int B = c->B;
   const int P = (int)c->P;
   int gmax = 0;
   if (max_grid_fwd_tc(&gmax)) return fail(GBNDE_ERR_CUDA, "occupancy query failed (tc)");
   const int ntiles = (B + 127) / 128;
   const int grid = std::min(gmax, ntiles);
+  const size_t SBt = (size_t)ntiles * tc::kTileVec;  // tile-layout vectors
   BwdTcArgs t{};
   t.b = base;
   t.b.ntiles = ntiles;
@@ -705,7 +710,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   if ((r = c->timg.ensure((size_t)grid * tc::kImgSlots * t.img_cta)) ||
       (r = c->thscr.ensure((size_t)grid * tc::kEpiThreads * t.hvals * 4)) ||
       (r = c->tbpart.ensure((size_t)grid * 4 * t.nbias * 4)) ||
-      (r = c->tmucomp.ensure((size_t)grid * P * 4)) || (r = c->tlamcomp.ensure(2 * SB * 4)) ||
+      (r = c->tmucomp.ensure((size_t)grid * P * 4)) || (r = c->tlamcomp.ensure(2 * SBt * 4)) ||
       (r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4)))
     return r;
   // per-CTA quadrature slots padded to a multiple of 4 floats (float4 sweeps)
@@ -722,7 +727,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   t.bpart = c->tbpart.as<float>();
   t.mu_comp = c->tmucomp.as<float>();
   t.lam_comp[0] = c->tlamcomp.as<float>();
-  t.lam_comp[1] = c->tlamcomp.as<float>() + SB;
+  t.lam_comp[1] = c->tlamcomp.as<float>() + SBt;
   t.b.dense = c->dense.as<float>();
   for (int l = 0; l < L; ++l) t.bias[l] = m.bias[l];
   // op lists: forward recompute + VJP chain (per evaluation), and the
@@ -811,6 +816,11 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   int max_slots = 1, save_last = 0, nsave_last = 0;
   if (int r = build_intervals(c, ivs, &max_slots, &save_last, &nsave_last)) return r;
   const bool backsolve = c->sensealg == GBNDE_SENSE_BACKSOLVE;
+  const bool tcbwd = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && c->dense_valid && !c->ff_on;
+  // the FP32 adjoint reads dense slots only in its own layout; after a
+  // tensor-core forward it recomputes each interval from the checkpoints
+  const bool dense_f32 = c->dense_valid && !backsolve && !c->dense_tl;
+  const size_t SBv = tcbwd ? (size_t)((B + 127) / 128) * tc::kTileVec : SB;
 
   int rows = 0;
   for (int l = 0; l <= c->mlp.nlayers; ++l) rows += c->mlp.dims[l];
@@ -827,9 +837,9 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   int r = 0;
   if (in_host && (r = c->dldu.ensure(SB * nsave * 4))) return r;
   if (out_host && ((r = c->dldu0.ensure(SB * 4)) || (r = c->dldp.ensure((size_t)P * 4)))) return r;
-  if ((r = c->lam.ensure(2 * SB * 4)) || (r = c->kl.ensure(7 * SB * 4))) return r;
+  if ((r = c->lam.ensure(2 * SBv * 4)) || (r = c->kl.ensure(7 * SBv * 4))) return r;
   if (backsolve && ((r = c->ub.ensure(2 * SB * 4)) || (r = c->ku.ensure(7 * SB * 4)))) return r;
-  if (!backsolve && !c->dense_valid && (r = c->ibuf.ensure((size_t)max_slots * 8 * SB * 4))) return r;
+  if (!tcbwd && !backsolve && !dense_f32 && (r = c->ibuf.ensure((size_t)max_slots * 8 * SB * 4))) return r;
   if ((r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4))) return r;
   if ((r = c->iv_d.ensure(std::max<size_t>(1, ivs.size()) * sizeof(Interval)))) return r;
   if ((r = c->bsync.ensure(64)) || (r = c->bcounters.ensure(CT_NSLOTS * sizeof(long long)))) return r;
@@ -875,13 +885,13 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   a.nsave_last = nsave_last;
   a.ibuf = c->ibuf.as<float>();
   a.ibuf_slots = max_slots;
-  a.dense = (c->dense_valid && !backsolve) ? c->dense.as<float>() : nullptr;
+  a.dense = tcbwd || dense_f32 ? c->dense.as<float>() : nullptr;
   a.lam[0] = c->lam.as<float>();
-  a.lam[1] = c->lam.as<float>() + SB;
+  a.lam[1] = c->lam.as<float>() + SBv;
   a.ub[0] = backsolve ? c->ub.as<float>() : nullptr;
   a.ub[1] = backsolve ? c->ub.as<float>() + SB : nullptr;
   for (int j = 0; j < 7; ++j) {
-    a.kl[j] = c->kl.as<float>() + j * SB;
+    a.kl[j] = c->kl.as<float>() + j * SBv;
     a.ku[j] = backsolve ? c->ku.as<float>() + j * SB : nullptr;
     a.kf[j] = nullptr;
   }
@@ -896,7 +906,6 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   a.ffd = c->ff_d;
   a.exact = c->ff_exact;
   a.noise = c->ff_on ? c->ffnoise.as<float>() : nullptr;
-  const bool tcbwd = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && c->dense_valid && !c->ff_on;
   if (tcbwd) {
     if (int rr = backward_tc(c, a, st, dp_d)) return rr;
   } else {

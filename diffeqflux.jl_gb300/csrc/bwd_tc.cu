@@ -64,34 +64,6 @@ __device__ __forceinline__ void st32(float* p, int n, bool vec, const float* x) 
   }
 }
 
-// Half (16 values) of a thread's 32 components: p already offset to the half,
-// n = valid values in it. All loads of a half are issued before any is used,
-// so several vectors cost one memory round trip.
-__device__ __forceinline__ void ld16(const float* p, int n, bool vec, float* x) {
-  if (vec) {
-#pragma unroll
-    for (int i = 0; i < 16; i += 4) {
-      const float4 v = *reinterpret_cast<const float4*>(p + i);
-      x[i] = v.x; x[i + 1] = v.y; x[i + 2] = v.z; x[i + 3] = v.w;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < 16; ++i) x[i] = (i < n) ? p[i] : 0.f;
-  }
-}
-
-__device__ __forceinline__ void st16(float* p, int n, bool vec, const float* x) {
-  if (vec) {
-#pragma unroll
-    for (int i = 0; i < 16; i += 4)
-      *reinterpret_cast<float4*>(p + i) = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
-  } else {
-#pragma unroll
-    for (int i = 0; i < 16; ++i)
-      if (i < n) p[i] = x[i];
-  }
-}
-
 // Thread-private FP32 scratch in slot-major layout: float4 slot k of thread t
 // at hs4[k * 256 + t], so the 32 lanes of a warp touch 512 contiguous bytes.
 __device__ __forceinline__ void hs_ld32(const float4* hs4, int k0, float* x) {
@@ -268,7 +240,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       if (j == 6) return swp ? a.kl[0] : a.kl[6];
       return a.kl[j];
     };
+    // lam, its compensation, the stages and the dense forward slots use the
+    // tile layout; the cotangents dL/du(t_i) and dL/du0 the API layout
+    const size_t SBt = (size_t)a.ntiles * tc::kTileVec;
     auto gofs = [&](int tile) -> size_t { return ((size_t)tile * 128 + th.r) * S + 32 * th.ch; };
+    auto tofs = [&](int tile) -> size_t { return tc::tl_offset(tile, th.ch, th.r); };
     auto valid = [&](int tile) -> bool { return tile * 128 + th.r < a.B && th.nmine > 0; };
     // P is a multiple of 4 floats per CTA slot (the host pads it)
     auto zero_cta = [&](float* p) {
@@ -295,8 +271,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         ld32(a.dLdu + (size_t)(a.save_last + qq) * SB + gofs(tile), th.nmine, vec, d);
         for (int i = 0; i < 32; ++i) v[i] += d[i];
       }
-      st32(a.lam[0] + gofs(tile), th.nmine, vec, v);
-      st32(A.lam_comp[0] + gofs(tile), th.nmine, vec, z);
+      tc::tl_st32(a.lam[0] + tofs(tile), v);
+      tc::tl_st32(A.lam_comp[0] + tofs(tile), z);
     }
     tc::epi_bar();
 
@@ -482,17 +458,16 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       *nstep = n;
     };
     auto dense_u = [&](int tile, int n, const float* hb, float* x) {
-      const float* slot = a.dense + (size_t)n * 8 * SB;
-      const size_t g = gofs(tile);
+      const float* slot = a.dense + (size_t)n * 8 * SBt;
+      const size_t g = tofs(tile);
       // u_n + sum_j hb_j k_j, in halves of 16 components and batches of
       // four vectors (u_n, k1..k3 then k4..k7), each batch in flight together
 #pragma unroll
       for (int hf = 0; hf < 2; ++hf) {
-        const int nn = min(16, max(0, th.nmine - 16 * hf));
-        const float* sp = slot + g + 16 * hf;
+        const float* sp = slot + g;
         float v4[4][16], acc[16];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) ld16(sp + (size_t)j * SB, nn, vec, v4[j]);
+        for (int j = 0; j < 4; ++j) tc::tl_ld16(sp + (size_t)j * SBt, hf, v4[j]);
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
           float e = 0.f;
@@ -502,7 +477,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           x[16 * hf + q] = v4[0][q];
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) ld16(sp + (size_t)(j + 4) * SB, nn, vec, v4[j]);
+        for (int j = 0; j < 4; ++j) tc::tl_ld16(sp + (size_t)(j + 4) * SBt, hf, v4[j]);
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
           float e = acc[q];
@@ -528,13 +503,13 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           float lam[32], x[32], kl[32];
           const bool v = valid(tile);
           if (v) {
-            ld32(a.lam[cur] + gofs(tile), th.nmine, vec, lam);
+            tc::tl_ld32(a.lam[cur] + tofs(tile), lam);
             dense_u(tile, n, hb, x);
           } else {
             for (int i = 0; i < 32; ++i) lam[i] = x[i] = 0.f;
           }
           ok = adj_eval(lam, x, fs, Pb[iP1], (float)c_tab.b[0], kl);
-          if (v) st32(klb(0) + gofs(tile), th.nmine, vec, kl);
+          if (v) tc::tl_st32(klb(0) + tofs(tile), kl);
         }
         ++nf_adj;
         if (!ok) break;
@@ -545,8 +520,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
           if (!valid(tile)) continue;
           float l[32], f[32];
-          ld32(a.lam[cur] + gofs(tile), th.nmine, vec, l);
-          ld32(klb(0) + gofs(tile), th.nmine, vec, f);
+          tc::tl_ld32(a.lam[cur] + tofs(tile), l);
+          tc::tl_ld32(klb(0) + tofs(tile), f);
           #pragma unroll
           for (int i = 0; i < 32; ++i) {
             if (i >= th.nmine) continue;
@@ -579,8 +554,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           const bool v = valid(tile);
           float l[32], f0[32], x[32], f1[32];
           if (v) {
-            ld32(a.lam[cur] + gofs(tile), th.nmine, vec, l);
-            ld32(klb(0) + gofs(tile), th.nmine, vec, f0);
+            tc::tl_ld32(a.lam[cur] + tofs(tile), l);
+            tc::tl_ld32(klb(0) + tofs(tile), f0);
             dense_u(tile, n, hb, x);
           } else {
             for (int i = 0; i < 32; ++i) l[i] = f0[i] = x[i] = 0.f;
@@ -648,21 +623,19 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           for (int j = 0; j < 7; ++j) hb[j] = s_hb[i - 1][j];
           for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
             const bool v = valid(tile);
-            const size_t g = gofs(tile);
+            const size_t g = tofs(tile);  // tile layout
             float Y[32], x[32], kl[32];
             if (v) {
               // Y = lam + (comp + sum_j h a_ij k_j), in two halves of 16
               // components whose loads are all in flight together
 #pragma unroll
               for (int hf = 0; hf < 2; ++hf) {
-                const int nn = min(16, max(0, th.nmine - 16 * hf));
-                const size_t gh = g + 16 * hf;
                 float lv[16], sv[16], kv[6][16];
-                ld16(lcur + gh, nn, vec, lv);
-                ld16(ccur + gh, nn, vec, sv);
+                tc::tl_ld16(lcur + g, hf, lv);
+                tc::tl_ld16(ccur + g, hf, sv);
 #pragma unroll
                 for (int j = 0; j < 6; ++j)
-                  if (j < i) ld16(klb(j) + gh, nn, vec, kv[j]);
+                  if (j < i) tc::tl_ld16(klb(j) + g, hf, kv[j]);
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
                   float sq = sv[q];
@@ -685,9 +658,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
                     lt[q] = e;
                     cn[q] = sv[q] - (Y[16 * hf + q] - lv[q]);
                   }
-                  st16(klb(6) + gh, nn, vec, lt);
-                  st16(lnew + gh, nn, vec, Y + 16 * hf);
-                  st16(cnew + gh, nn, vec, cn);
+                  tc::tl_st16(klb(6) + g, hf, lt);
+                  tc::tl_st16(lnew + g, hf, Y + 16 * hf);
+                  tc::tl_st16(cnew + g, hf, cn);
                 }
               }
               dense_u(tile, n, hb, x);
@@ -703,12 +676,10 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
                 const float hbt6 = s_hbt[6];
 #pragma unroll
                 for (int hf = 0; hf < 2; ++hf) {
-                  const int nn = min(16, max(0, th.nmine - 16 * hf));
-                  const size_t gh = g + 16 * hf;
                   float lt[16], lv[16], yv[16];
-                  ld16(klb(6) + gh, nn, vec, lt);
-                  ld16(lcur + gh, nn, vec, lv);
-                  ld16(lnew + gh, nn, vec, yv);
+                  tc::tl_ld16(klb(6) + g, hf, lt);
+                  tc::tl_ld16(lcur + g, hf, lv);
+                  tc::tl_ld16(lnew + g, hf, yv);
 #pragma unroll
                   for (int q = 0; q < 16; ++q) {
                     if (16 * hf + q >= th.nmine) continue;
@@ -718,9 +689,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
                     perr += isfinite(yv[q]) ? rr * rr : (double)INFINITY;
                   }
                 }
-                st32(klb(i) + g, th.nmine, vec, kl);
+                tc::tl_st32(klb(i) + g, kl);
               } else {
-                st32(klb(i) + g, th.nmine, vec, kl);
+                tc::tl_st32(klb(i) + g, kl);
               }
             }
           }
@@ -760,13 +731,13 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
           if (!valid(tile)) continue;
           float v[32];
-          ld32(a.lam[cur] + gofs(tile), th.nmine, vec, v);
+          tc::tl_ld32(a.lam[cur] + tofs(tile), v);
           for (int qq = 0; qq < iv.nsave_lo; ++qq) {
             float d[32];
             ld32(a.dLdu + (size_t)(iv.save_lo + qq) * SB + gofs(tile), th.nmine, vec, d);
             for (int i = 0; i < 32; ++i) v[i] += d[i];
           }
-          st32(a.lam[cur] + gofs(tile), th.nmine, vec, v);
+          tc::tl_st32(a.lam[cur] + tofs(tile), v);
         }
       }
     }
@@ -775,7 +746,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       for (int tile = blockIdx.x; tile < a.ntiles; tile += G)
         if (valid(tile)) {
           float v[32];
-          ld32(a.lam[cur] + gofs(tile), th.nmine, vec, v);
+          tc::tl_ld32(a.lam[cur] + tofs(tile), v);
           st32(a.dLdu0 + gofs(tile), th.nmine, vec, v);
         }
     }

@@ -135,8 +135,10 @@ __device__ __forceinline__ bool epi_rhs(const FwdTcArgs& A, tc::EpiState& e, tc:
     float v[32], bc[32];
     tc::load_bias32(b, 32 * th.ch, m.dims[m.nlayers], bc);
     tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)(32 * th.ch), v);
+    // output layer: bias and its activation (identity for most models)
+    tc::bias_act32(v, bc, m.act[m.nlayers - 1], 32 * th.ch, m.dims[m.nlayers]);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) kout[i] = (i < th.nmine) ? v[i] + bc[i] : 0.f;
+    for (int i = 0; i < 32; ++i) kout[i] = (i < th.nmine) ? v[i] : 0.f;
     tc::epi_release_acc(e, sh);
   }
   return true;
@@ -184,11 +186,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
     long long nf = 0, naccept = 0, nreject = 0, iter = 0;
     const bool dense = A.dense != nullptr;
     // stage buffer j of the current attempt (slot = accepted-step index)
+    // internal vectors (state, compensation, stages, dense slots) use the
+    // tile layout; u0, the saved states and the checkpoints the API layout
+    const size_t SBt = (size_t)a.ntiles * tc::kTileVec;
     auto kptr = [&](int j) -> float* {
-      if (dense) return A.dense + ((size_t)min(naccept, A.dense_slots - 1) * 8 + 1 + j) * SB;
-      return A.kring + (size_t)j * SB;
+      if (dense) return A.dense + ((size_t)min(naccept, A.dense_slots - 1) * 8 + 1 + j) * SBt;
+      return A.kring + (size_t)j * SBt;
     };
     auto gofs = [&](int tile) -> size_t { return ((size_t)tile * 128 + th.r) * S + 32 * th.ch; };
+    auto tofs = [&](int tile) -> size_t { return tc::tl_offset(tile, th.ch, th.r); };
     auto valid = [&](int tile) -> bool { return tile * 128 + th.r < a.B && th.nmine > 0; };
     bool ok = true;
 
@@ -204,10 +210,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
       if (v) {
         float z[32];
         for (int i = 0; i < 32; ++i) z[i] = 0.f;
-        st32(a.ubuf[0] + g, th.nmine, vec, Y);
-        st32(A.comp[0] + g, th.nmine, vec, z);
-        if (dense) st32(A.dense + g, th.nmine, vec, Y);
-        st32(kptr(0) + g, th.nmine, vec, k);
+        const size_t tg = tofs(tile);
+        tc::tl_st32(a.ubuf[0] + tg, Y);
+        tc::tl_st32(A.comp[0] + tg, z);
+        if (dense) tc::tl_st32(A.dense + tg, Y);
+        tc::tl_st32(kptr(0) + tg, k);
       }
     }
     nf = 1;
@@ -233,7 +240,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
         if (!valid(tile)) continue;
         float u[32], f[32];
         ld32(a.u0 + gofs(tile), th.nmine, vec, u);
-        ld32(kptr(0) + gofs(tile), th.nmine, vec, f);
+        tc::tl_ld32(kptr(0) + tofs(tile), f);
         #pragma unroll
         for (int i = 0; i < 32; ++i) {
           if (i >= th.nmine) continue;
@@ -263,7 +270,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
         float u[32], f0[32], Y[32], f1[32];
         if (v) {
           ld32(a.u0 + gofs(tile), th.nmine, vec, u);
-          ld32(kptr(0) + gofs(tile), th.nmine, vec, f0);
+          tc::tl_ld32(kptr(0) + tofs(tile), f0);
         } else {
           for (int i = 0; i < 32; ++i) u[i] = f0[i] = 0.f;
         }
@@ -317,17 +324,17 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
           for (int j = 0; j < 7; ++j) hbt[j] = (float)(h * c_tab.btilde[j]);
           for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
             const bool v = valid(tile);
-            const size_t g = gofs(tile);
+            const size_t g = tofs(tile);  // tile layout
             float u[32], s[32], Y[32], k[32];
             if (v) {
-              ld32(ucur + g, th.nmine, vec, u);
-              ld32(ccur + g, th.nmine, vec, s);
+              tc::tl_ld32(ucur + g, u);
+              tc::tl_ld32(ccur + g, s);
               if (i < 6) {
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
                   if (j >= i) break;
                   float kj[32];
-                  ld32(kptr(j) + g, th.nmine, vec, kj);
+                  tc::tl_ld32(kptr(j) + g, kj);
 #pragma unroll
                   for (int q = 0; q < 32; ++q) s[q] = fmaf(ha[j], kj[q], s[q]);
                 }
@@ -340,14 +347,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
 #pragma unroll
                 for (int j = 0; j < 6; ++j) {
                   float kj[32];
-                  ld32(kptr(j) + g, th.nmine, vec, kj);
+                  tc::tl_ld32(kptr(j) + g, kj);
 #pragma unroll
                   for (int q = 0; q < 32; ++q) {
                     s[q] = fmaf(ha[j], kj[q], s[q]);
                     ut[q] = fmaf(hbt[j], kj[q], ut[q]);
                   }
                 }
-                st32(kptr(6) + g, th.nmine, vec, ut);
+                tc::tl_st32(kptr(6) + g, ut);
               }
 #pragma unroll
               for (int q = 0; q < 32; ++q) Y[q] = u[q] + s[q];
@@ -355,8 +362,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
                 float cn[32];
 #pragma unroll
                 for (int q = 0; q < 32; ++q) cn[q] = s[q] - (Y[q] - u[q]);
-                st32(unew + g, th.nmine, vec, Y);
-                st32(cnew + g, th.nmine, vec, cn);
+                tc::tl_st32(unew + g, Y);
+                tc::tl_st32(cnew + g, cn);
               }
             } else {
 #pragma unroll
@@ -369,12 +376,12 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
                 // (stored above): nothing of the stage arithmetic stays in
                 // registers across epi_rhs
                 float ut[32];
-                ld32(kptr(6) + g, th.nmine, vec, ut);
-                ld32(ucur + g, th.nmine, vec, u);
-                ld32(unew + g, th.nmine, vec, Y);
+                tc::tl_ld32(kptr(6) + g, ut);
+                tc::tl_ld32(ucur + g, u);
+                tc::tl_ld32(unew + g, Y);
 #pragma unroll
                 for (int q = 0; q < 32; ++q) ut[q] = fmaf(hbt[6], k[q], ut[q]);
-                st32(kptr(i) + g, th.nmine, vec, k);
+                tc::tl_st32(kptr(i) + g, k);
                 #pragma unroll
                 for (int q = 0; q < 32; ++q) {
                   if (q >= th.nmine) continue;
@@ -383,7 +390,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
                   perr += isfinite(Y[q]) ? rr * rr : (double)INFINITY;
                 }
               } else {
-                st32(kptr(i) + g, th.nmine, vec, k);
+                tc::tl_st32(kptr(i) + g, k);
               }
             }
           }
@@ -419,18 +426,18 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
             }
             for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
               if (!valid(tile)) continue;
-              const size_t g = gofs(tile);
+              const size_t g = gofs(tile), tg = tofs(tile);
               float o[32];
               if (sv == tnew) {
-                ld32(unew + g, th.nmine, vec, o);
+                tc::tl_ld32(unew + tg, o);
               } else {
                 float u[32];
-                ld32(ucur + g, th.nmine, vec, u);
-                ld32(ccur + g, th.nmine, vec, o);
+                tc::tl_ld32(ucur + tg, u);
+                tc::tl_ld32(ccur + tg, o);
 #pragma unroll
                 for (int j = 0; j < 7; ++j) {
                   float kj[32];
-                  ld32(kptr(j) + g, th.nmine, vec, kj);
+                  tc::tl_ld32(kptr(j) + tg, kj);
 #pragma unroll
                   for (int q = 0; q < 32; ++q) o[q] = fmaf(hb[j], kj[q], o[q]);
                 }
@@ -448,7 +455,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
             for (int tile = blockIdx.x; tile < a.ntiles; tile += G)
               if (valid(tile)) {
                 float u[32];
-                ld32(ucur + gofs(tile), th.nmine, vec, u);
+                tc::tl_ld32(ucur + tofs(tile), u);
                 st32(dst + gofs(tile), th.nmine, vec, u);
               }
             if (blockIdx.x == 0 && threadIdx.x == 0) a.ckpt_step[nck] = (int)naccept;
@@ -463,14 +470,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
           ++naccept;
           for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
             if (!valid(tile)) continue;
-            const size_t g = gofs(tile);
+            const size_t g = tofs(tile);  // tile layout
             float kk[32];
-            ld32(k7 + g, th.nmine, vec, kk);
-            st32(kptr(0) + g, th.nmine, vec, kk);
+            tc::tl_ld32(k7 + g, kk);
+            tc::tl_st32(kptr(0) + g, kk);
             if (dense && naccept < A.dense_slots) {
               float un[32];
-              ld32(unew + g, th.nmine, vec, un);
-              st32(A.dense + (size_t)naccept * 8 * SB + g, th.nmine, vec, un);
+              tc::tl_ld32(unew + g, un);
+              tc::tl_st32(A.dense + (size_t)naccept * 8 * SBt + g, un);
             }
           }
           cur ^= 1;

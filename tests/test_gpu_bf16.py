@@ -91,3 +91,60 @@ def test_bf16_small_shapes(S, H, cube):
     ous, _ = ots.solve_forward(_oracle(model, p), u0.astype(np.float64), 0.0, 1.0, ts, 1e-6, 1e-4,
                                steps=s.forward_steps())
     assert _rel(us, ous) < 2e-5
+
+
+@pytest.mark.parametrize("S,H,cube,B", [(2, 50, True, 200), (32, 128, False, 300), (48, 96, False, 130)])
+def test_bf16_small_shapes_gradient(S, H, cube, B):
+    """Tensor-core adjoint at padded shapes (state below 64 and not a multiple
+    of 32, hidden widths not multiples of 64, a partial last tile), against
+    the FP64 oracle's InterpolatingAdjoint."""
+    from oracle import tsit5 as ots
+    model, p, rng = _setup([S, H, S], ["tanh", "identity"], cube, B, 5)
+    u0 = rng.standard_normal((S, B)).astype(np.float32) * (0.5 if cube else 1.0)
+    ts = np.linspace(0.0, 1.0, 6)
+    node = _node(model, ts, "bf16", 1e-6, 1e-4)
+    s = node.solver
+    s.set_params(p)
+    us, st = s.forward(u0, node.desc())
+    assert st.retcode == 0
+    rhs = _oracle(model, p)
+    ous, fwd = ots.solve_forward(rhs, u0.astype(np.float64), 0.0, 1.0, ts, 1e-6, 1e-4)
+    g = (2.0 * us.astype(np.float64) / us.size).astype(np.float32)
+    du0, dp, sta = s.backward(g)
+    assert sta.retcode_adj == 0
+    gu, gp, _ = ots.adjoint_interpolating(rhs, fwd, ts, 2.0 * ous / ous.size, 0.0, 1e-6, 1e-4)
+    assert _rel(du0, gu) < 1e-3
+    assert _rel(dp, gp) < 1e-3
+
+
+@pytest.mark.parametrize("case", ["tanh_output", "backsolve"])
+def test_bf16_forward_with_fp32_adjoint(case):
+    """Models the tensor-core adjoint does not cover (a non-identity output
+    layer) and BacksolveAdjoint run the BF16 forward with the FP32 adjoint:
+    it must not read the forward's tile-layout stage storage, and the
+    gradient still matches the FP64 oracle."""
+    import gbnde
+    from oracle import tsit5 as ots
+    S, H, B = 16, 64, 256
+    acts = ["tanh", "tanh"] if case == "tanh_output" else ["tanh", "identity"]
+    model, p, rng = _setup([S, H, S], acts, False, B, 7)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    ts = np.linspace(0.0, 1.0, 6)
+    sense = gbnde.BacksolveAdjoint() if case == "backsolve" else gbnde.InterpolatingAdjoint()
+    node = _node(model, ts, "bf16", 1e-6, 1e-4, sensealg=sense)
+    s = node.solver
+    s.set_params(p)
+    us, st = s.forward(u0, node.desc())
+    assert st.retcode == 0
+    rhs = _oracle(model, p)
+    ous, fwd = ots.solve_forward(rhs, u0.astype(np.float64), 0.0, 1.0, ts, 1e-6, 1e-4)
+    g = (2.0 * us.astype(np.float64) / us.size).astype(np.float32)
+    du0, dp, sta = s.backward(g)
+    assert sta.retcode_adj == 0
+    dl = 2.0 * ous / ous.size
+    if case == "backsolve":
+        gu, gp, _ = ots.adjoint_backsolve(rhs, ous, ts, dl, 0.0, 1e-6, 1e-4)
+    else:
+        gu, gp, _ = ots.adjoint_interpolating(rhs, fwd, ts, dl, 0.0, 1e-6, 1e-4)
+    assert _rel(du0, gu) < 2e-3
+    assert _rel(dp, gp) < 2e-3
