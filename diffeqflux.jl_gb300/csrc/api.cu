@@ -51,6 +51,8 @@ int launch_ms_bwd(const MsArgs& a, int grid, size_t smem, cudaStream_t st);
 int launch_transpose_params(const MlpDev& m, const float* p, float* wtr, cudaStream_t st);
 int launch_loss(const float* usave, const float* target, size_t n, int kind, float* dL,
                 double* partial, int nblk, cudaStream_t st);
+int launch_adam(float* p, float* m, float* v, const float* g, size_t n, double lr, double b1, double b2,
+                double eps, long long step, cudaStream_t st);
 }  // namespace gbnde
 
 using namespace gbnde;
@@ -146,6 +148,7 @@ struct gbnde_ctx {
   bool tc_shape_ok = false;
   bool tc_bwd_ok = false;  // tensor-core adjoint covers this model
   DBuf timg, thscr, tbpart, tmucomp, tlamcomp;
+  DBuf tr_us, tr_dl, tr_du0, tr_dp;  // training-step scratch
   // multiple shooting workspace
   DBuf ms_segs, ms_saveat, ms_u0, ms_usave, ms_dense, ms_steplog, ms_nacc, ms_ret, ms_cnt, ms_dldu,
       ms_dldu0, ms_bar, ms_mu, ms_dldp;
@@ -290,7 +293,7 @@ void gbnde_destroy(gbnde_ctx* c) {
                   &c->tbpart, &c->tmucomp, &c->tlamcomp, &c->ms_segs, &c->ms_saveat, &c->ms_u0,
                   &c->ms_usave, &c->ms_dense, &c->ms_steplog, &c->ms_nacc, &c->ms_ret, &c->ms_cnt,
                   &c->ms_dldu, &c->ms_dldu0, &c->ms_bar, &c->ms_mu, &c->ms_dldp, &c->ffnoise,
-                  &c->ffu0, &c->ffus};
+                  &c->ffu0, &c->ffus, &c->tr_us, &c->tr_dl, &c->tr_du0, &c->tr_dp};
   for (DBuf* b : bufs) b->release();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -1195,6 +1198,51 @@ int gbnde_loss_device(gbnde_ctx* c, const float* usave, const float* target, int
   double s = 0.0;
   for (double v : part) s += v;
   *loss = (kind == 1) ? s / (double)n : s;
+  return 0;
+}
+
+int gbnde_train_step(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, const float* u0,
+                     const float* target, int kind, const gbnde_adam* opt, long long step, float* p,
+                     float* m, float* v, double* loss, gbnde_stats* stats) {
+  if (!c || !d || !u0 || !target || !opt || !p || !m || !v || !loss)
+    return fail(GBNDE_ERR_INVALID, "null argument");
+  if (step < 1) return fail(GBNDE_ERR_INVALID, "step counts from 1");
+  if (!(opt->lr > 0) || !(opt->beta1 >= 0 && opt->beta1 < 1) || !(opt->beta2 >= 0 && opt->beta2 < 1) ||
+      !(opt->eps > 0))
+    return fail(GBNDE_ERR_INVALID, "Adam needs lr > 0, 0 <= beta1, beta2 < 1 and eps > 0");
+  if (kind != 0 && kind != 1) return fail(GBNDE_ERR_INVALID, "unknown loss kind %d", kind);
+  if (int r = set_device(c)) return r;
+  if (d->nsave < 1 || B < 1 || S < 1) return fail(GBNDE_ERR_INVALID, "empty problem");
+  const size_t SB = (size_t)S * B, nsv = (size_t)SB * d->nsave;
+  int r = 0;
+  if ((r = c->tr_us.ensure(nsv * 4)) || (r = c->tr_dl.ensure(nsv * 4)) || (r = c->tr_du0.ensure(SB * 4)) ||
+      (r = c->tr_dp.ensure(c->P * 4)))
+    return r;
+  if ((r = gbnde_set_params_device(c, p, c->P))) return r;
+  gbnde_stats sf{}, sb{};
+  if ((r = gbnde_forward_device(c, d, S, B, u0, c->tr_us.as<float>(), &sf))) return r;
+  *loss = INFINITY;
+  if (sf.retcode == GBNDE_RET_SUCCESS) {
+    if ((r = gbnde_loss_device(c, c->tr_us.as<float>(), target, kind, c->tr_dl.as<float>(), loss))) return r;
+    if ((r = gbnde_backward_device(c, c->tr_dl.as<float>(), c->tr_du0.as<float>(), c->tr_dp.as<float>(), &sb)))
+      return r;
+    sf.nf_recompute = sb.nf_recompute;
+    sf.nf_adj = sb.nf_adj;
+    sf.naccept_adj = sb.naccept_adj;
+    sf.nreject_adj = sb.nreject_adj;
+    sf.retcode_adj = sb.retcode_adj;
+    // a failed solve leaves the parameters unchanged (its loss is Inf)
+    if (sb.retcode_adj == GBNDE_RET_SUCCESS) {
+      if (launch_adam(p, m, v, c->tr_dp.as<float>(), c->P, opt->lr, opt->beta1, opt->beta2, opt->eps, step,
+                      c->stream))
+        return fail(GBNDE_ERR_CUDA, "Adam launch failed");
+      if ((r = gbnde_set_params_device(c, p, c->P))) return r;
+      CK(cudaStreamSynchronize(c->stream));
+    } else {
+      *loss = INFINITY;
+    }
+  }
+  if (stats) *stats = sf;
   return 0;
 }
 

@@ -1,5 +1,8 @@
 // aux.cu -- small helper kernels: transposed weight copy for the VJPs and the
 // fused save-point loss with its cotangent.
+#include <algorithm>
+#include <cmath>
+
 #include "kernels.h"
 
 namespace gbnde {
@@ -59,6 +62,30 @@ __global__ void loss_kernel(const float* __restrict__ u, const float* __restrict
 int launch_loss(const float* usave, const float* target, size_t n, int kind, float* dL,
                 double* partial, int nblk, cudaStream_t st) {
   loss_kernel<<<nblk, 256, 0, st>>>(usave, target, n, kind, dL, partial);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// Adam on n parameters: moments in FP32, the update in FP32 with the bias
+// corrections c1 = 1 / (1 - b1^t), c2 = 1 / (1 - b2^t) computed on the host.
+__global__ void adam_kernel(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,
+                            const float* __restrict__ g, size_t n, float lr, float b1, float b2, float eps,
+                            float c1, float c2) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = fmaf(b1, m[i], (1.f - b1) * gi);
+    const float vi = fmaf(b2, v[i], (1.f - b2) * gi * gi);
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  }
+}
+
+int launch_adam(float* p, float* m, float* v, const float* g, size_t n, double lr, double b1, double b2,
+                double eps, long long step, cudaStream_t st) {
+  const double c1 = 1.0 / (1.0 - pow(b1, (double)step)), c2 = 1.0 / (1.0 - pow(b2, (double)step));
+  const int blocks = (int)std::min<size_t>((n + 255) / 256, 1216);
+  adam_kernel<<<blocks, 256, 0, st>>>(p, m, v, g, n, (float)lr, (float)b1, (float)b2, (float)eps, (float)c1,
+                                      (float)c2);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -58,6 +58,10 @@ class Segment(C.Structure):
     _fields_ = [("t0", C.c_double), ("t1", C.c_double), ("save_off", C.c_int), ("nsave", C.c_int)]
 
 
+class Adam(C.Structure):
+    _fields_ = [("lr", C.c_double), ("beta1", C.c_double), ("beta2", C.c_double), ("eps", C.c_double)]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("nf", C.c_longlong), ("naccept", C.c_longlong), ("nreject", C.c_longlong),
@@ -93,6 +97,9 @@ _SIGS = {
                                           C.POINTER(C.c_int), C.POINTER(Stats)]),
     "gbnde_multishoot_backward": (C.c_int, [_P, _P, _P, _P, C.POINTER(Stats)]),
     "gbnde_loss_noalloc": (C.c_int, [_P, _P, C.c_size_t, C.c_int, _P, C.POINTER(C.c_double), _P]),
+    "gbnde_train_step": (C.c_int, [_P, C.POINTER(SolveDesc), C.c_int, C.c_int, _P, _P, C.c_int,
+                                   C.POINTER(Adam), C.c_longlong, _P, _P, _P, C.POINTER(C.c_double),
+                                   C.POINTER(Stats)]),
     "gbnde_forward_steps": (C.c_longlong, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong]),
     "gbnde_forward_trace": (C.c_longlong, [_P, C.POINTER(C.c_double), C.c_longlong]),
     "gbnde_stream": (C.c_void_p, [_P]),

@@ -251,6 +251,19 @@ class Solver:
                                               int(kind), dl_cm.data_ptr(), C.byref(out)))
         return out.value
 
+    def train_step(self, u0_cm, target_cm, desc, S, B, p, m, v, step, lr=1e-3, beta1=0.9, beta2=0.999,
+                   eps=1e-8, kind=1):
+        """One Adam iteration on device tensors (gbnde_train_step): p, m, v are
+        updated in place; returns (loss, stats)."""
+        opt = _lib.Adam(float(lr), float(beta1), float(beta2), float(eps))
+        out = C.c_double()
+        st = _lib.Stats()
+        _lib.check(self.lib.gbnde_train_step(self.h, C.byref(desc), S, B, u0_cm.data_ptr(),
+                                             target_cm.data_ptr(), int(kind), C.byref(opt), int(step),
+                                             p.data_ptr(), m.data_ptr(), v.data_ptr(), C.byref(out),
+                                             C.byref(st)))
+        return out.value, st
+
 
 # ---------------------------------------------------------------------------
 # solution type

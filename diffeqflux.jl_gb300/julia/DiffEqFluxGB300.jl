@@ -24,7 +24,7 @@ module DiffEqFluxGB300
 
 using ChainRulesCore, ComponentArrays, DiffEqFlux, Lux, SciMLBase, SciMLSensitivity
 
-export GB300Tsit5, gb300
+export GB300Tsit5, gb300, gb300_train_step!
 
 const libgbnde = joinpath(@__DIR__, "..", "gbnde", "libgbnde.so")
 
@@ -166,6 +166,41 @@ function (n::NeuralODE)(x, p, st, alg::GB300Tsit5)
     us = [x isa AbstractVector ? out[:, 1, i] : out[:, :, i] for i in axes(out, 3)]
     sol = SciMLBase.build_solution(prob, alg, saveat, us; retcode = RETCODES[stats.retcode + 1])
     sol, st
+end
+
+# ---- one Adam training iteration on the device (gbnde_train_step) ------------------------
+struct AdamDesc
+    lr::Cdouble
+    beta1::Cdouble
+    beta2::Cdouble
+    eps::Cdouble
+end
+
+"""
+    gb300_train_step!(ctx, tspan, saveat, abstol, reltol, u0, target, p, m, v, step;
+                      lr = 1e-3, beta1 = 0.9, beta2 = 0.999, eps = 1e-8, loss = :mse) -> (loss, stats)
+
+One iteration of `Optimization.solve(optprob, OptimizationOptimisers.Adam(lr))`
+(docs/src/examples/neural_ode.md:66-70) for a NeuralODE with an MSE/SSE loss at
+the save points, entirely on the GPU: `u0`, `target`, `p`, `m`, `v` are
+`CuArray{Float32}` (CUDA.jl), `p`, `m`, `v` updated in place.
+"""
+function gb300_train_step!(ctx::Ctx, tspan, saveat::Vector{Float64}, abstol, reltol, u0, target, p, m, v,
+                           step::Integer; lr = 1e-3, beta1 = 0.9, beta2 = 0.999, eps = 1e-8, loss = :mse)
+    S, B = size(u0)
+    opt = Ref(AdamDesc(lr, beta1, beta2, eps))
+    l = Ref{Cdouble}(0)
+    st = Stats()
+    GC.@preserve saveat begin
+        d = Ref(SolveDesc(tspan[1], tspan[2], abstol, reltol, 0, 0, 100000, pointer(saveat),
+                          length(saveat), 0, 0))
+        check(ccall((:gbnde_train_step, libgbnde), Cint,
+                    (Ptr{Cvoid}, Ref{SolveDesc}, Cint, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ref{AdamDesc},
+                     Clonglong, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Cdouble}, Ref{Stats}),
+                    ctx.h, d, S, B, pointer(u0), pointer(target), loss === :mse ? 1 : 0, opt, step,
+                    pointer(p), pointer(m), pointer(v), l, st))
+    end
+    l[], st
 end
 
 # A layer routed to the GB300 kernels keeps the reference's `(layer)(x, p, st)`

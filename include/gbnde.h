@@ -195,6 +195,27 @@ int gbnde_multishoot_backward(gbnde_ctx* ctx, const float* dL_dusave, float* dL_
 int gbnde_loss_device(gbnde_ctx* ctx, const float* usave_dev, const float* target_dev,
                       int kind, float* dL_dusave_dev, double* loss);
 
+/* ---- one training iteration (Adam) ------------------------------------------------
+ * One iteration of the reference's training loop (Optimization.solve with
+ * OptimizationOptimisers.Adam around the loss, docs/src/examples/neural_ode.md:66-70)
+ * on device buffers: forward solve from u0_dev, the fused save-point loss
+ * against target_dev (loss_kind 0: sum of squares, 1: mean), the adjoint
+ * gradient, then Adam on the parameters in p_dev (nparams floats, updated in
+ * place and loaded into the context for the next solve). m_dev and v_dev are
+ * the Adam moments (zero before the first step); step is the 1-based
+ * iteration count used for the bias corrections:
+ *   m = b1 m + (1 - b1) g;  v = b2 v + (1 - b2) g^2;
+ *   p -= lr (m / (1 - b1^step)) / (sqrt(v / (1 - b2^step)) + eps).
+ * All launches are on the context's stream. Not capturable as one CUDA graph:
+ * the host reads the forward's step log to plan the adjoint intervals. */
+typedef struct {
+  double lr, beta1, beta2, eps;
+} gbnde_adam;
+
+int gbnde_train_step(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int S, int B, const float* u0_dev,
+                     const float* target_dev, int loss_kind, const gbnde_adam* opt, long long step,
+                     float* p_dev, float* m_dev, float* v_dev, double* loss, gbnde_stats* stats);
+
 /* ---- fused loss without any device allocation ----------------------------------
  * No counterpart in the reference. Same loss and cotangent as
  * gbnde_loss_device (kind 0: sum of squared errors, kind 1: their mean) on n

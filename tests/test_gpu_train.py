@@ -1,0 +1,92 @@
+"""One training iteration through gbnde_train_step (forward, fused loss,
+adjoint gradient, Adam on the device parameters) against the same pieces
+called one by one with a numpy Adam, and a short training run whose loss
+goes down. Both precision forms."""
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+from test_gpu_neural_ode import _setup
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="no CUDA GPU")]
+
+
+def _problem(prec, S=16, H=64, B=256, nsave=8, seed=11):
+    import torch
+
+    import gbnde
+    model, p, rng = _setup([S, H, H, S], ["tanh", "tanh", "identity"], False, B, seed, bias=0.01)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    ts = np.linspace(0.0, 1.0, nsave)
+    M = -0.5 * np.eye(S) + 0.1 * rng.standard_normal((S, S))
+    from scipy.linalg import expm
+    tgt = np.stack([expm(M * t) @ u0.astype(np.float64) for t in ts], axis=-1).astype(np.float32)
+    solver = gbnde.Solver(model, prec, 0)
+    desc = gbnde.Solver.solve_desc(0.0, 1.0, ts, 1e-6, 1e-4, 0)
+    dev = torch.device("cuda", 0)
+    u0_d = torch.from_numpy(np.ascontiguousarray(u0.T)).to(dev)                     # column-major S x B
+    tg_d = torch.from_numpy(np.ascontiguousarray(np.transpose(tgt, (2, 1, 0)))).to(dev)
+    return solver, desc, u0_d, tg_d, torch.from_numpy(p.copy()).to(dev), S, B, nsave
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_train_step_matches_pieces_and_numpy_adam(prec):
+    import torch
+    solver, desc, u0_d, tg_d, p_d, S, B, ns = _problem(prec)
+    dev = p_d.device
+    lr, b1, b2, eps = 1e-3, 0.9, 0.999, 1e-8
+    # reference: the library's own gradient, then Adam in FP64 numpy
+    solver.set_params_device(p_d)
+    us = torch.empty((ns, B, S), dtype=torch.float32, device=dev)
+    dl = torch.empty_like(us)
+    du0 = torch.empty((B, S), dtype=torch.float32, device=dev)
+    dp = torch.empty_like(p_d)
+    st = solver.forward_device(u0_d, us, desc, S, B)
+    assert st.retcode == 0
+    loss_ref = solver.loss_device(us, tg_d, 1, dl)
+    sb = solver.backward_device(dl, du0, dp)
+    assert sb.retcode_adj == 0
+    g = dp.double().cpu().numpy()
+    p0 = p_d.double().cpu().numpy()
+    m = np.zeros_like(g)
+    v = np.zeros_like(g)
+    p_ref = p0.copy()
+    for step in (1, 2):
+        m = b1 * m + (1 - b1) * g
+        v = b2 * v + (1 - b2) * g * g
+        mh = m / (1 - b1 ** step)
+        vh = v / (1 - b2 ** step)
+        p_ref = p_ref - lr * mh / (np.sqrt(vh) + eps)
+        if step == 1:
+            p_ref1 = p_ref.copy()
+    # the fused step, twice on the same data (the second uses the new params)
+    pt = p_d.clone()
+    mt = torch.zeros_like(pt)
+    vt = torch.zeros_like(pt)
+    loss1, st1 = solver.train_step(u0_d, tg_d, desc, S, B, pt, mt, vt, 1, lr, b1, b2, eps, kind=1)
+    assert st1.retcode == 0 and st1.retcode_adj == 0
+    assert abs(loss1 - loss_ref) <= 1e-12 * max(1.0, abs(loss_ref))
+    assert np.abs(pt.double().cpu().numpy() - p_ref1).max() <= 1e-3 * lr
+    np.testing.assert_allclose(mt.double().cpu().numpy(), (1 - b1) * g, rtol=1e-6, atol=1e-12)
+    loss2, st2 = solver.train_step(u0_d, tg_d, desc, S, B, pt, mt, vt, 2, lr, b1, b2, eps, kind=1)
+    assert st2.retcode == 0 and np.isfinite(loss2)
+    # the context now holds the updated parameters
+    us2 = torch.empty_like(us)
+    solver.forward_device(u0_d, us2, desc, S, B)
+    dl2 = torch.empty_like(us)
+    loss_after = solver.loss_device(us2, tg_d, 1, dl2)
+    assert loss_after < loss1
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_training_reduces_the_loss(prec):
+    import torch
+    solver, desc, u0_d, tg_d, p_d, S, B, ns = _problem(prec, seed=3)
+    m = torch.zeros_like(p_d)
+    v = torch.zeros_like(p_d)
+    losses = []
+    for step in range(1, 31):
+        loss, st = solver.train_step(u0_d, tg_d, desc, S, B, p_d, m, v, step, lr=3e-3, kind=1)
+        assert st.retcode == 0 and st.retcode_adj == 0
+        losses.append(loss)
+    assert losses[-1] < 0.7 * losses[0], losses[::5]
