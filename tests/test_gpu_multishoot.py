@@ -111,3 +111,48 @@ def test_failed_group_gives_inf_loss():
     sse = lambda u, uh: float(np.sum((u - uh) ** 2))  # noqa: E731
     loss, preds = gbnde.multiple_shoot(p, data, ts, model, sse, 5, abstol=1e-12, reltol=1e-12, maxiters=2)
     assert loss == float("inf")
+
+
+def test_config4_structure_uneven_batch():
+    """cfg4 structure: state 32, MLP 32 -> 128 -> 128 -> 32 tanh (24,864
+    parameters), data from du/dt = -0.1 u + W tanh(u), trajectories of uneven
+    length (points at dt = 0.05) with their own group sizes, all segments in
+    one launch; predictions and loss against the FP64 oracle."""
+    import gbnde
+    from oracle import mlp as omlp
+    from oracle import multishoot as oms
+    from oracle import tsit5 as ots
+    S, H = 32, 128
+    rng = np.random.default_rng(21)
+    W = rng.standard_normal((S, S)) / np.sqrt(S)
+
+    class Osc:
+        def f(self, u, t):
+            return -0.1 * u + W @ np.tanh(u)
+
+    model = gbnde.Chain(gbnde.Dense(S, H, "tanh"), gbnde.Dense(H, H, "tanh"), gbnde.Dense(H, S))
+    p = model.init_params(rng)
+    assert p.size == 24864
+    trajs = []
+    for k in range(6):
+        n = int(rng.integers(40, 121))
+        gs = int(rng.integers(5, 41))
+        ts = 0.05 * np.arange(n)
+        data, _ = ots.solve_forward(Osc(), rng.standard_normal((S, 1)), ts[0], ts[-1], ts, 1e-10, 1e-10)
+        trajs.append((data[:, 0, :].astype(np.float32), ts, gs))
+    tol = 1e-7
+    mse = lambda u, uh: float(np.mean((u - uh) ** 2))  # noqa: E731
+    loss, preds = gbnde.multiple_shoot_batch(p, trajs, model, mse, abstol=tol, reltol=tol)
+    om = omlp.MLP(model.dims, model.acts)
+    k = 0
+    Lref = 0.0
+    for data, ts, gs in trajs:
+        opreds, ok = oms.solve_groups(omlp.MLPRHS(om, p.astype(np.float64)), data.astype(np.float64), ts, gs,
+                                      tol, tol)
+        assert ok
+        for b in opreds:
+            assert _rel(preds[k], b) < 1e-4
+            k += 1
+        Lref += oms.multiple_shoot_loss(opreds, data.astype(np.float64), gs, 100.0, mse)
+    assert k == len(preds)
+    assert abs(loss - Lref) / Lref < 1e-4
