@@ -20,9 +20,10 @@
 // the six stages' images stacked along K (K = 6 x 128 trajectories, MN-major
 // operands, 3 split products),
 //   sum_s b_s dW_l(s) = sum_s b_s delta_{l+1}(s) a_l(s)^T,
-// and the epilogue adds H times that accumulator to the CTA's mu with L2
-// reductions: one drain per accepted step instead of one per stage, and no
-// weight-gradient work at all for rejected steps. Stage 7 of a step is stage
+// and the epilogue adds H times that accumulator to the CTA's mu
+// (Kahan-compensated, each element owned by one thread): one drain per
+// accepted step instead of one per stage, and no weight-gradient work at all
+// for rejected steps. Stage 7 of a step is stage
 // 1 of the next (FSAL): its images go to the second of two stage-1 slots,
 // already weighted by b_1. Bias gradients are column sums of the cotangents
 // (warp butterfly reductions, deterministic order) kept in small per-CTA
@@ -392,8 +393,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
 
     // ---- weight gradients of an accepted step -------------------------------------
     // One stage-stacked op per layer and 128-row half; mu += H * accumulator
-    // (L2 reductions: each mu element has one writing thread per CTA). Then the
-    // bias quadrature mu_b += H (P1 + Pmid).
+    // with Kahan compensation (mu_comp), each mu element owned by one thread of
+    // the CTA. Then the bias quadrature mu_b += H (P1 + Pmid), compensated too.
+    auto kahan = [&](float& acc, float& cmp, float x) {
+      const float y = x - cmp;
+      const float t2 = acc + y;
+      cmp = (t2 - acc) - y;
+      acc = t2;
+    };
     auto commit_step = [&](float Hf) -> bool {
       tc::epi_bar();
       if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_DW | ((uint32_t)fs << 8))) return false;
@@ -404,32 +411,72 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         const int isA = A.a_isA[l];
         const int Nn2 = isA ? out : in;  // N side of the dW op
         float* __restrict__ Pw = mu_acc + m.woff[l];
+        float* __restrict__ Cw = mu_comp + m.woff[l];
         for (int hh = 0; hh < A.nh[l]; ++hh) {
+          const int mrow = 128 * hh + th.r;  // M-side feature of this lane
+          // element i of chunk cc of this lane: isA -> row mrow (in feature),
+          // 32 consecutive out features; else row mrow (out feature), in
+          // features at stride `out`
+          auto addr = [&](int cc, int i, bool* okp) -> size_t {
+            const int n0 = 64 * cc + 32 * th.ch;
+            *okp = isA ? (mrow < in && n0 + i < out) : (mrow < out && n0 + i < in);
+            return isA ? (size_t)mrow * out + n0 + i : (size_t)(n0 + i) * out + mrow;
+          };
+          float av[32], cv[32];
+          // a full row of 32 contiguous, 16-byte aligned elements (isA)
+          auto vec4 = [&](int cc) -> bool {
+            const int n0 = 64 * cc + 32 * th.ch;
+            return isA && mrow < in && n0 + 32 <= out &&
+                   (reinterpret_cast<uintptr_t>(Pw + (size_t)mrow * out + n0) & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(Cw + (size_t)mrow * out + n0) & 15) == 0;
+          };
+          auto fetch = [&](int cc) {
+            if (vec4(cc)) {
+              const size_t o = (size_t)mrow * out + 64 * cc + 32 * th.ch;
+#pragma unroll
+              for (int i = 0; i < 32; i += 4) {
+                const float4 a4 = *reinterpret_cast<const float4*>(Pw + o + i);
+                const float4 c4 = *reinterpret_cast<const float4*>(Cw + o + i);
+                av[i] = a4.x; av[i + 1] = a4.y; av[i + 2] = a4.z; av[i + 3] = a4.w;
+                cv[i] = c4.x; cv[i + 1] = c4.y; cv[i + 2] = c4.z; cv[i + 3] = c4.w;
+              }
+              return;
+            }
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              bool okp;
+              const size_t o = addr(cc, i, &okp);
+              av[i] = okp ? Pw[o] : 0.f;
+              cv[i] = okp ? Cw[o] : 0.f;
+            }
+          };
+          // the first chunk's mu is read while the accumulator is computed
+          fetch(0);
           uint32_t col;
           if (!tc::epi_wait_acc(es, sh, &col)) return false;
-          const int mrow = 128 * hh + th.r;  // M-side feature of this lane
-          for (int cc = 0; cc < (Nn2 + 63) / 64; ++cc) {
-            const int n0 = 64 * cc + 32 * th.ch;
-            tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
-            if (isA) {
-              // row mrow = in feature; 32 consecutive out features
-              float* rowp = Pw + (size_t)mrow * out + n0;
-              const bool full = mrow < in && n0 + 32 <= out && (reinterpret_cast<uintptr_t>(rowp) & 15) == 0;
-              if (full) {
+          const int nch = (Nn2 + 63) / 64;
+          for (int cc = 0; cc < nch; ++cc) {
+            if (cc > 0) fetch(cc);
+            tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + 32 * th.ch), v);
+            if (vec4(cc)) {
+              const size_t o = (size_t)mrow * out + 64 * cc + 32 * th.ch;
 #pragma unroll
-                for (int i = 0; i < 32; i += 4)
-                  tc::red_add_v4(rowp + i, Hf * v[i], Hf * v[i + 1], Hf * v[i + 2], Hf * v[i + 3]);
-              } else if (mrow < in) {
+              for (int i = 0; i < 32; ++i) kahan(av[i], cv[i], Hf * v[i]);
 #pragma unroll
-                for (int i = 0; i < 32; ++i)
-                  if (n0 + i < out) tc::red_add(rowp + i, Hf * v[i]);
+              for (int i = 0; i < 32; i += 4) {
+                *reinterpret_cast<float4*>(Pw + o + i) = make_float4(av[i], av[i + 1], av[i + 2], av[i + 3]);
+                *reinterpret_cast<float4*>(Cw + o + i) = make_float4(cv[i], cv[i + 1], cv[i + 2], cv[i + 3]);
               }
-            } else if (mrow < out) {
-              // row mrow = out feature; in features n0.. at stride `out`
-              float* colp = Pw + (size_t)n0 * out + mrow;
+            } else {
 #pragma unroll
-              for (int i = 0; i < 32; ++i)
-                if (n0 + i < in) tc::red_add(colp + (size_t)i * out, Hf * v[i]);
+              for (int i = 0; i < 32; ++i) {
+                bool okp;
+                const size_t o = addr(cc, i, &okp);
+                if (!okp) continue;
+                kahan(av[i], cv[i], Hf * v[i]);
+                Pw[o] = av[i];
+                Cw[o] = cv[i];
+              }
             }
           }
           tc::epi_release_acc(es, sh);
@@ -441,7 +488,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         int l = 0;
         while (l + 1 < L && f >= A.boffp[l + 1]) ++l;
         const int o = f - A.boffp[l];
-        if (o < m.dims[l + 1]) tc::red_add(mu_acc + m.boff[l] + o, Hf * (__ldcg(P1 + f) + __ldcg(Pmid + f)));
+        if (o < m.dims[l + 1])
+          kahan(mu_acc[m.boff[l] + o], mu_comp[m.boff[l] + o], Hf * (__ldcg(P1 + f) + __ldcg(Pmid + f)));
       }
       tc::epi_bar();
       return true;
