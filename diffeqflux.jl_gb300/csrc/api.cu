@@ -53,6 +53,35 @@ int launch_loss(const float* usave, const float* target, size_t n, int kind, flo
                 double* partial, int nblk, cudaStream_t st);
 int launch_adam(float* p, float* m, float* v, const float* g, size_t n, double lr, double b1, double b2,
                 double eps, long long step, cudaStream_t st);
+int launch_plan_intervals(Interval* iv, int niv, const double* steplog, const long long* fcounters,
+                          const int* fstatus, long long dense_slots, long long maxsteps, int* flags,
+                          cudaStream_t st);
+int launch_loss_finalize(const double* part, int nblk, size_t n, int kind, double* out, cudaStream_t st);
+int launch_adam_graph(float* p, float* m, float* v, const float* g, size_t n, double lr, double b1, double b2,
+                      double eps, const double* coef, const int* flags, const int* bstatus, cudaStream_t st);
+
+// Launches of one eager training step, recorded for the graph-mode step,
+// which replays them inside one captured CUDA graph.
+struct StepRecord {
+  bool fwd = false, bwd = false, loss = false, tc = false, bwd_tc_on = false;
+  FwdTcArgs fwd_tc{};
+  FwdArgs fwd_f32{};
+  int fwd_grid = 0;
+  size_t fwd_smem = 0;
+  BwdTcArgs bwd_tc{};
+  BwdArgs bwd_f32{};
+  int bwd_grid = 0;
+  size_t bwd_smem = 0;
+  int red_stride = 0;  // tensor-core form: per-CTA mu slot stride
+  float* dp = nullptr;
+  const float* l_us = nullptr;
+  const float* l_tg = nullptr;
+  size_t l_n = 0;
+  int l_kind = 0;
+  float* l_dl = nullptr;
+  double* l_part = nullptr;
+  int l_nblk = 0;
+};
 }  // namespace gbnde
 
 using namespace gbnde;
@@ -149,6 +178,14 @@ struct gbnde_ctx {
   bool tc_bwd_ok = false;  // tensor-core adjoint covers this model
   DBuf timg, thscr, tbpart, tmucomp, tlamcomp;
   DBuf tr_us, tr_dl, tr_du0, tr_dp;  // training-step scratch
+  // graph-mode training step
+  bool recording = false;
+  StepRecord rec;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<char> gkey;   // the arguments the graph was captured for
+  DBuf gstat;               // device: loss (double), Adam coefficients (2 doubles), flags (ints)
+  double* gpin = nullptr;   // pinned host mirror of the Adam coefficients
+  bool graph_failed = false;
   // multiple shooting workspace
   DBuf ms_segs, ms_saveat, ms_u0, ms_usave, ms_dense, ms_steplog, ms_nacc, ms_ret, ms_cnt, ms_dldu,
       ms_dldu0, ms_bar, ms_mu, ms_dldp;
@@ -297,6 +334,8 @@ void gbnde_destroy(gbnde_ctx* c) {
   for (DBuf* b : bufs) b->release();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->gpin) cudaFreeHost(c->gpin);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
 }
@@ -543,13 +582,28 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
     ta.dense = a.dense;
     ta.dense_slots = a.dense_slots;
     ta.kring = c->kbuf.as<float>();
+    if (c->recording) {
+      c->rec.fwd = true;
+      c->rec.tc = true;
+      c->rec.fwd_tc = ta;
+      c->rec.fwd_grid = grid;
+    }
     if (launch_fwd_tc(ta, grid, st)) {
       cudaError_t e = cudaGetLastError();
       return fail(GBNDE_ERR_CUDA, "forward (tc) launch failed: %s", cudaGetErrorString(e));
     }
-  } else if (launch_fwd_f32(a, grid, smem, st)) {
-    cudaError_t e = cudaGetLastError();
-    return fail(GBNDE_ERR_CUDA, "forward launch failed: %s", cudaGetErrorString(e));
+  } else {
+    if (c->recording) {
+      c->rec.fwd = true;
+      c->rec.tc = false;
+      c->rec.fwd_f32 = a;
+      c->rec.fwd_grid = grid;
+      c->rec.fwd_smem = smem;
+    }
+    if (launch_fwd_f32(a, grid, smem, st)) {
+      cudaError_t e = cudaGetLastError();
+      return fail(GBNDE_ERR_CUDA, "forward launch failed: %s", cudaGetErrorString(e));
+    }
   }
   CK(cudaEventRecord(c->ev[1], st));
   long long cnt[CT_NSLOTS + 2];
@@ -793,6 +847,14 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   }
   t.dwops.nops = n;
   CK(cudaEventRecord(c->ev[2], st));
+  if (c->recording) {
+    c->rec.bwd = true;
+    c->rec.bwd_tc_on = true;
+    c->rec.bwd_tc = t;
+    c->rec.bwd_grid = grid;
+    c->rec.red_stride = Ppad;
+    c->rec.dp = dp_d;
+  }
   if (launch_bwd_tc(t, grid, st)) {
     cudaError_t e = cudaGetLastError();
     return fail(GBNDE_ERR_CUDA, "backward (tc) launch failed: %s", cudaGetErrorString(e));
@@ -913,6 +975,14 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
     if (int rr = backward_tc(c, a, st, dp_d)) return rr;
   } else {
     CK(cudaEventRecord(c->ev[2], st));
+    if (c->recording) {
+      c->rec.bwd = true;
+      c->rec.bwd_tc_on = false;
+      c->rec.bwd_f32 = a;
+      c->rec.bwd_grid = grid;
+      c->rec.bwd_smem = smem;
+      c->rec.dp = dp_d;
+    }
     if (launch_bwd_f32(a, grid, smem, st)) {
       cudaError_t e = cudaGetLastError();
       return fail(GBNDE_ERR_CUDA, "backward launch failed: %s", cudaGetErrorString(e));
@@ -1190,6 +1260,16 @@ int gbnde_loss_device(gbnde_ctx* c, const float* usave, const float* target, int
   const size_t n = (size_t)c->S * c->B * c->nsave;
   const int nblk = 304;
   if (int r = c->loss_part.ensure(nblk * sizeof(double))) return r;
+  if (c->recording) {
+    c->rec.loss = true;
+    c->rec.l_us = usave;
+    c->rec.l_tg = target;
+    c->rec.l_n = n;
+    c->rec.l_kind = kind;
+    c->rec.l_dl = dLdu;
+    c->rec.l_part = c->loss_part.as<double>();
+    c->rec.l_nblk = nblk;
+  }
   if (launch_loss(usave, target, n, kind, dLdu, c->loss_part.as<double>(), nblk, c->stream))
     return fail(GBNDE_ERR_CUDA, "loss launch failed");
   std::vector<double> part(nblk);
@@ -1243,6 +1323,161 @@ int gbnde_train_step(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, cons
     }
   }
   if (stats) *stats = sf;
+  return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Captures the recorded step (parameter upload, forward, loss, interval plan,
+// adjoint, reduction, Adam) into one CUDA graph on the context's stream.
+int capture_step(gbnde_ctx* c, const gbnde_adam* opt, float* p, float* m, float* v) {
+  StepRecord& R = c->rec;
+  const BwdArgs& b = R.bwd_tc_on ? R.bwd_tc.b : R.bwd_f32;
+  const FwdArgs& f = R.tc ? R.fwd_tc.f : R.fwd_f32;
+  if (!R.fwd || !R.bwd || !R.loss || !f.dense || !b.dense) return -1;  // the adjoint must read dense storage
+  if (c->gstat.ensure(64)) return -1;
+  if (!c->gpin && cudaMallocHost(&c->gpin, 2 * sizeof(double)) != cudaSuccess) {
+    c->gpin = nullptr;
+    cudaGetLastError();
+    return -1;
+  }
+  double* gloss = c->gstat.as<double>();
+  double* gcoef = gloss + 1;
+  int* gflags = reinterpret_cast<int*>(gloss + 3);
+  cudaStream_t st = c->stream;
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  bool ok = cudaMemcpyAsync(c->params.p, p, c->P * sizeof(float), cudaMemcpyDeviceToDevice, st) == cudaSuccess;
+  ok = ok && bind_params(c) == 0;
+  ok = ok && cudaMemsetAsync(c->sync.p, 0, 64, st) == cudaSuccess;
+  ok = ok && cudaMemsetAsync(c->counters.p, 0, CT_NSLOTS * sizeof(long long) + 16, st) == cudaSuccess;
+  ok = ok && (R.tc ? launch_fwd_tc(R.fwd_tc, R.fwd_grid, st) : launch_fwd_f32(R.fwd_f32, R.fwd_grid, R.fwd_smem, st)) == 0;
+  ok = ok && launch_loss(R.l_us, R.l_tg, R.l_n, R.l_kind, R.l_dl, R.l_part, R.l_nblk, st) == 0;
+  ok = ok && launch_loss_finalize(R.l_part, R.l_nblk, R.l_n, R.l_kind, gloss, st) == 0;
+  ok = ok && cudaMemsetAsync(c->bsync.p, 0, 64, st) == cudaSuccess;
+  ok = ok && cudaMemsetAsync(c->bcounters.p, 0, CT_NSLOTS * sizeof(long long), st) == cudaSuccess;
+  ok = ok && launch_plan_intervals(const_cast<Interval*>(b.iv), b.niv, b.fsteps, f.counters, f.status, f.dense_slots, f.maxsteps, gflags,
+                                   st) == 0;
+  ok = ok && (R.bwd_tc_on ? launch_bwd_tc(R.bwd_tc, R.bwd_grid, st)
+                          : launch_bwd_f32(R.bwd_f32, R.bwd_grid, R.bwd_smem, st)) == 0;
+  ok = ok && (R.bwd_tc_on ? launch_reduce_mu_comp(b.mu_acc, R.bwd_tc.mu_comp, R.bwd_grid, R.red_stride, (int)c->P,
+                                                  R.dp, st)
+                          : launch_reduce_mu(b.mu_acc, R.bwd_grid, (int)c->P, R.dp, st)) == 0;
+  ok = ok && launch_adam_graph(p, m, v, R.dp, c->P, opt->lr, opt->beta1, opt->beta2, opt->eps, gcoef, gflags,
+                               b.status, st) == 0;
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(st, &g);
+  if (!ok || e != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return -1;
+  }
+  const cudaError_t ei = cudaGraphInstantiate(&c->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) {
+    c->gexec = nullptr;
+    cudaGetLastError();
+    return -1;
+  }
+  return 0;
+}
+
+template <class T>
+void key_put(std::vector<char>& k, const T& x) {
+  const char* p = reinterpret_cast<const char*>(&x);
+  k.insert(k.end(), p, p + sizeof(T));
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbnde_graph_train_step(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, const float* u0,
+                           const float* target, int kind, const gbnde_adam* opt, long long step, float* p,
+                           float* m, float* v, double* loss, gbnde_stats* stats, int* graphed) {
+  if (graphed) *graphed = 0;
+  if (!c || !d || !u0 || !target || !opt || !p || !m || !v || !loss)
+    return fail(GBNDE_ERR_INVALID, "null argument");
+  if (step < 1) return fail(GBNDE_ERR_INVALID, "step counts from 1");
+  if (!d->saveat || d->nsave < 1) return fail(GBNDE_ERR_INVALID, "saveat must hold >= 1 time");
+  if (int r = set_device(c)) return r;
+  // the graph is tied to these arguments (pointers included)
+  std::vector<char> key;
+  key_put(key, d->t0); key_put(key, d->t1); key_put(key, d->abstol); key_put(key, d->reltol);
+  key_put(key, d->dt0); key_put(key, d->dtmin); key_put(key, d->maxiters); key_put(key, d->nsave);
+  key_put(key, d->sensealg); key_put(key, d->flags);
+  for (int i = 0; i < d->nsave; ++i) key_put(key, d->saveat[i]);
+  key_put(key, S); key_put(key, B); key_put(key, u0); key_put(key, target); key_put(key, kind);
+  key_put(key, opt->lr); key_put(key, opt->beta1); key_put(key, opt->beta2); key_put(key, opt->eps);
+  key_put(key, p); key_put(key, m); key_put(key, v);
+  if (!(c->gexec && key == c->gkey)) {
+    // an eager step that records its launches, then the capture
+    if (c->gexec) {
+      cudaGraphExecDestroy(c->gexec);
+      c->gexec = nullptr;
+    }
+    c->gkey.clear();
+    c->rec = StepRecord{};
+    c->recording = true;
+    gbnde_stats se{};
+    const int r = gbnde_train_step(c, d, S, B, u0, target, kind, opt, step, p, m, v, loss, &se);
+    c->recording = false;
+    if (stats) *stats = se;
+    if (r) return r;
+    if (se.retcode == GBNDE_RET_SUCCESS && se.retcode_adj == GBNDE_RET_SUCCESS && !c->graph_failed) {
+      if (capture_step(c, opt, p, m, v) == 0) c->gkey = key;
+      else c->graph_failed = true;  // this context keeps stepping eagerly
+    }
+    return 0;
+  }
+  // replay: the Adam bias corrections of this step, then the graph
+  c->gpin[0] = 1.0 / (1.0 - std::pow(opt->beta1, (double)step));
+  c->gpin[1] = 1.0 / (1.0 - std::pow(opt->beta2, (double)step));
+  cudaStream_t st = c->stream;
+  double* gloss = c->gstat.as<double>();
+  CK(cudaMemcpyAsync(gloss + 1, c->gpin, 2 * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaGraphLaunch(c->gexec, st));
+  double gl[4];
+  long long fc[CT_NSLOTS], bc[CT_NSLOTS];
+  int fs[4], bs[4];
+  const StepRecord& R = c->rec;
+  const FwdArgs& f = R.tc ? R.fwd_tc.f : R.fwd_f32;
+  const BwdArgs& b = R.bwd_tc_on ? R.bwd_tc.b : R.bwd_f32;
+  CK(cudaMemcpyAsync(gl, gloss, sizeof gl, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(fc, f.counters, sizeof fc, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(fs, f.status, sizeof fs, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(bc, b.counters, sizeof bc, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(bs, b.status, sizeof bs, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  int flags[2];
+  std::memcpy(flags, &gl[3], sizeof flags);
+  // the host-side record of the last forward is not refreshed by a replay
+  c->have_fwd = false;
+  if (flags[0] != 0 || fs[ST_RETCODE] != GBNDE_RET_SUCCESS || bs[ST_RETCODE] != GBNDE_RET_SUCCESS) {
+    // a failed solve or outgrown stage storage: nothing was updated; redo the
+    // step eagerly (which also regrows the storage) and capture again later
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+    c->gkey.clear();
+    return gbnde_train_step(c, d, S, B, u0, target, kind, opt, step, p, m, v, loss, stats);
+  }
+  *loss = gl[0];
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    stats->nf = fc[CT_NF];
+    stats->naccept = fc[CT_NACCEPT];
+    stats->nreject = fc[CT_NREJECT];
+    stats->nf_adj = bc[CT_NF];
+    stats->naccept_adj = bc[CT_NACCEPT];
+    stats->nreject_adj = bc[CT_NREJECT];
+    stats->retcode = fs[ST_RETCODE];
+    stats->retcode_adj = bs[ST_RETCODE];
+  }
+  if (graphed) *graphed = 1;
   return 0;
 }
 

@@ -89,4 +89,82 @@ int launch_adam(float* p, float* m, float* v, const float* g, size_t n, double l
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+// ---- graph-mode training step helpers ---------------------------------------------
+// Inside one captured CUDA graph nothing goes back to the host between the
+// solves, so the host-side pieces of an eager step move to the device:
+
+// Backward interval plan from the forward's step log: for each interval
+// [t_lo, t_hi] (static, uploaded once) the forward steps covering it. A
+// forward that failed, or took more steps than the dense storage holds,
+// leaves every interval on step 0 (so the adjoint stays in bounds) and raises
+// flags[0]; the host then redoes the step outside the graph.
+__global__ void plan_intervals_kernel(Interval* iv, int niv, const double* steplog, const long long* fcounters,
+                                      const int* fstatus, long long dense_slots, long long maxsteps, int* flags) {
+  const long long ns = fcounters[CT_NACCEPT];
+  const bool bad = fstatus[ST_RETCODE] != GBNDE_RET_SUCCESS || ns < 1 || ns >= dense_slots || ns > maxsteps;
+  if (blockIdx.x == 0 && threadIdx.x == 0) flags[0] = bad ? 1 : 0;
+  for (int k = threadIdx.x; k < niv; k += blockDim.x) {
+    int nlo = 0, nhi = 0;
+    if (!bad) {
+      const double lo = iv[k].t_lo, hi = iv[k].t_hi;
+      for (long long n = 0; n < ns; ++n) {
+        const double tn = steplog[2 * n];
+        if (tn <= lo) nlo = (int)n;
+        if (tn < hi) nhi = (int)n;
+      }
+    }
+    iv[k].nlo = nlo;
+    iv[k].nhi = nhi;
+    iv[k].ckpt = 0;
+  }
+}
+
+int launch_plan_intervals(Interval* iv, int niv, const double* steplog, const long long* fcounters,
+                          const int* fstatus, long long dense_slots, long long maxsteps, int* flags,
+                          cudaStream_t st) {
+  plan_intervals_kernel<<<1, 128, 0, st>>>(iv, niv, steplog, fcounters, fstatus, dense_slots, maxsteps, flags);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// The loss from its per-block partials, in block order (the same sum the
+// host forms after an eager step).
+__global__ void loss_finalize_kernel(const double* part, int nblk, size_t n, int kind, double* out) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < nblk; ++i) s += part[i];
+    out[0] = (kind == 1) ? s / (double)n : s;
+  }
+}
+
+int launch_loss_finalize(const double* part, int nblk, size_t n, int kind, double* out, cudaStream_t st) {
+  loss_finalize_kernel<<<1, 32, 0, st>>>(part, nblk, n, kind, out);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// Adam with the bias corrections read from device memory (coef[0] =
+// 1/(1 - b1^t), coef[1] = 1/(1 - b2^t), written before each graph launch);
+// skipped when the forward or the adjoint failed.
+__global__ void adam_graph_kernel(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,
+                                  const float* __restrict__ g, size_t n, float lr, float b1, float b2, float eps,
+                                  const double* coef, const int* flags, const int* bstatus) {
+  if (flags[0] != 0 || bstatus[ST_RETCODE] != GBNDE_RET_SUCCESS) return;
+  const float c1 = (float)coef[0], c2 = (float)coef[1];
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = fmaf(b1, m[i], (1.f - b1) * gi);
+    const float vi = fmaf(b2, v[i], (1.f - b2) * gi * gi);
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  }
+}
+
+int launch_adam_graph(float* p, float* m, float* v, const float* g, size_t n, double lr, double b1, double b2,
+                      double eps, const double* coef, const int* flags, const int* bstatus, cudaStream_t st) {
+  const int blocks = (int)std::min<size_t>((n + 255) / 256, 1216);
+  adam_graph_kernel<<<blocks, 256, 0, st>>>(p, m, v, g, n, (float)lr, (float)b1, (float)b2, (float)eps, coef, flags,
+                                            bstatus);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 }  // namespace gbnde

@@ -100,6 +100,9 @@ _SIGS = {
     "gbnde_train_step": (C.c_int, [_P, C.POINTER(SolveDesc), C.c_int, C.c_int, _P, _P, C.c_int,
                                    C.POINTER(Adam), C.c_longlong, _P, _P, _P, C.POINTER(C.c_double),
                                    C.POINTER(Stats)]),
+    "gbnde_graph_train_step": (C.c_int, [_P, C.POINTER(SolveDesc), C.c_int, C.c_int, _P, _P, C.c_int,
+                                         C.POINTER(Adam), C.c_longlong, _P, _P, _P, C.POINTER(C.c_double),
+                                         C.POINTER(Stats), C.POINTER(C.c_int)]),
     "gbnde_forward_steps": (C.c_longlong, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong]),
     "gbnde_forward_trace": (C.c_longlong, [_P, C.POINTER(C.c_double), C.c_longlong]),
     "gbnde_stream": (C.c_void_p, [_P]),

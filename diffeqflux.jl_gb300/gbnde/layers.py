@@ -264,6 +264,20 @@ class Solver:
                                              C.byref(st)))
         return out.value, st
 
+    def graph_train_step(self, u0_cm, target_cm, desc, S, B, p, m, v, step, lr=1e-3, beta1=0.9,
+                         beta2=0.999, eps=1e-8, kind=1):
+        """gbnde_graph_train_step: the same iteration replayed as one CUDA graph
+        after the first call; returns (loss, stats, ran_as_graph)."""
+        opt = _lib.Adam(float(lr), float(beta1), float(beta2), float(eps))
+        out = C.c_double()
+        st = _lib.Stats()
+        g = C.c_int()
+        _lib.check(self.lib.gbnde_graph_train_step(self.h, C.byref(desc), S, B, u0_cm.data_ptr(),
+                                                   target_cm.data_ptr(), int(kind), C.byref(opt), int(step),
+                                                   p.data_ptr(), m.data_ptr(), v.data_ptr(), C.byref(out),
+                                                   C.byref(st), C.byref(g)))
+        return out.value, st, bool(g.value)
+
 
 # ---------------------------------------------------------------------------
 # solution type

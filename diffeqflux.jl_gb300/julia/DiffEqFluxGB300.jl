@@ -186,19 +186,29 @@ the save points, entirely on the GPU: `u0`, `target`, `p`, `m`, `v` are
 `CuArray{Float32}` (CUDA.jl), `p`, `m`, `v` updated in place.
 """
 function gb300_train_step!(ctx::Ctx, tspan, saveat::Vector{Float64}, abstol, reltol, u0, target, p, m, v,
-                           step::Integer; lr = 1e-3, beta1 = 0.9, beta2 = 0.999, eps = 1e-8, loss = :mse)
+                           step::Integer; lr = 1e-3, beta1 = 0.9, beta2 = 0.999, eps = 1e-8, loss = :mse,
+                           graph = false)
     S, B = size(u0)
     opt = Ref(AdamDesc(lr, beta1, beta2, eps))
     l = Ref{Cdouble}(0)
     st = Stats()
+    g = Ref{Cint}(0)
     GC.@preserve saveat begin
         d = Ref(SolveDesc(tspan[1], tspan[2], abstol, reltol, 0, 0, 100000, pointer(saveat),
                           length(saveat), 0, 0))
-        check(ccall((:gbnde_train_step, libgbnde), Cint,
-                    (Ptr{Cvoid}, Ref{SolveDesc}, Cint, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ref{AdamDesc},
-                     Clonglong, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Cdouble}, Ref{Stats}),
-                    ctx.h, d, S, B, pointer(u0), pointer(target), loss === :mse ? 1 : 0, opt, step,
-                    pointer(p), pointer(m), pointer(v), l, st))
+        if graph  # replayed as one CUDA graph from the second call on
+            check(ccall((:gbnde_graph_train_step, libgbnde), Cint,
+                        (Ptr{Cvoid}, Ref{SolveDesc}, Cint, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ref{AdamDesc},
+                         Clonglong, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Cdouble}, Ref{Stats}, Ref{Cint}),
+                        ctx.h, d, S, B, pointer(u0), pointer(target), loss === :mse ? 1 : 0, opt, step,
+                        pointer(p), pointer(m), pointer(v), l, st, g))
+        else
+            check(ccall((:gbnde_train_step, libgbnde), Cint,
+                        (Ptr{Cvoid}, Ref{SolveDesc}, Cint, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ref{AdamDesc},
+                         Clonglong, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Cdouble}, Ref{Stats}),
+                        ctx.h, d, S, B, pointer(u0), pointer(target), loss === :mse ? 1 : 0, opt, step,
+                        pointer(p), pointer(m), pointer(v), l, st))
+        end
     end
     l[], st
 end

@@ -206,8 +206,9 @@ int gbnde_loss_device(gbnde_ctx* ctx, const float* usave_dev, const float* targe
  * iteration count used for the bias corrections:
  *   m = b1 m + (1 - b1) g;  v = b2 v + (1 - b2) g^2;
  *   p -= lr (m / (1 - b1^step)) / (sqrt(v / (1 - b2^step)) + eps).
- * All launches are on the context's stream. Not capturable as one CUDA graph:
- * the host reads the forward's step log to plan the adjoint intervals. */
+ * All launches are on the context's stream; the host reads the forward's step
+ * log to plan the adjoint intervals (gbnde_graph_train_step moves that plan
+ * to the device and replays the whole iteration as one CUDA graph). */
 typedef struct {
   double lr, beta1, beta2, eps;
 } gbnde_adam;
@@ -215,6 +216,23 @@ typedef struct {
 int gbnde_train_step(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int S, int B, const float* u0_dev,
                      const float* target_dev, int loss_kind, const gbnde_adam* opt, long long step,
                      float* p_dev, float* m_dev, float* v_dev, double* loss, gbnde_stats* stats);
+
+/* The same iteration replayed as one CUDA graph. The first call (and any call
+ * whose arguments or buffers differ from the captured ones) runs
+ * gbnde_train_step eagerly while recording its launches, then captures
+ * parameter upload, forward, loss, an on-device plan of the adjoint
+ * intervals, adjoint, reduction and Adam into a graph; later calls launch
+ * that graph and read back only the loss and the solver counters. A replay
+ * whose solve failed or outgrew the stage storage updates nothing on the
+ * device and is redone eagerly. *graphed (may be NULL) is set to 1 when the
+ * step ran as a graph replay. Needs an adjoint that reads the dense stage
+ * storage (InterpolatingAdjoint, not FFJORD); otherwise every step runs
+ * eagerly. After a replay the context holds no forward solve for
+ * gbnde_backward. Buffers must stay allocated while the graph is in use. */
+int gbnde_graph_train_step(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int S, int B, const float* u0_dev,
+                           const float* target_dev, int loss_kind, const gbnde_adam* opt, long long step,
+                           float* p_dev, float* m_dev, float* v_dev, double* loss, gbnde_stats* stats,
+                           int* graphed);
 
 /* ---- fused loss without any device allocation ----------------------------------
  * No counterpart in the reference. Same loss and cotangent as

@@ -90,3 +90,26 @@ def test_training_reduces_the_loss(prec):
         assert st.retcode == 0 and st.retcode_adj == 0
         losses.append(loss)
     assert losses[-1] < 0.7 * losses[0], losses[::5]
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_graph_train_step_replays_the_eager_step(prec):
+    """gbnde_graph_train_step: the first call runs eagerly and captures the
+    iteration; later calls replay the graph. The parameter trajectory and the
+    losses equal those of eager gbnde_train_step on the same data."""
+    import torch
+    solver, desc, u0_d, tg_d, p0, S, B, ns = _problem(prec, seed=5)
+    solver_e, desc_e, _, _, _, _, _, _ = _problem(prec, seed=5)
+    pg, mg, vg = p0.clone(), torch.zeros_like(p0), torch.zeros_like(p0)
+    pe, me, ve = p0.clone(), torch.zeros_like(p0), torch.zeros_like(p0)
+    graphed = []
+    for step in range(1, 7):
+        lg, sg, g = solver.graph_train_step(u0_d, tg_d, desc, S, B, pg, mg, vg, step, lr=2e-3, kind=1)
+        le, se = solver_e.train_step(u0_d, tg_d, desc_e, S, B, pe, me, ve, step, lr=2e-3, kind=1)
+        assert sg.retcode == 0 and sg.retcode_adj == 0
+        assert abs(lg - le) <= 1e-9 * abs(le), (step, lg, le)
+        assert sg.nf == se.nf and sg.nf_adj == se.nf_adj
+        assert torch.equal(pg, pe), step
+        graphed.append(g)
+    assert graphed[0] is False
+    assert all(graphed[1:]), graphed
