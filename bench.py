@@ -379,6 +379,34 @@ def run_gpu(args):
             "traffic": traffic, "traffic_source": traffic_src,
             "basis": "GEMM FLOPs of the adjoint launch: F*nf_recompute + 3F*nf_adj, F = 2*B*sum(in*out)"}
 
+    # ---- the training iteration as one CUDA graph (gbnde_graph_train_step) -------
+    # forward, loss, adjoint and Adam (lr 1e-3) replayed as one graph from the
+    # second call on; auxiliary figure (the working set, about 1 GB of stage
+    # storage and images, exceeds L2, so no flush between steps)
+    graph = None
+    if not args.no_graph:
+        pg = p_d.clone()
+        mg = torch.zeros_like(pg)
+        vg = torch.zeros_like(pg)
+        flags = []
+        for st_i in (1, 2):
+            solver.graph_train_step(u0_d, tg_d, form.desc, S, B, pg, mg, vg, st_i, lr=1e-3, kind=1)
+        torch.cuda.synchronize()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(lstream)
+        for k in range(args.steps):
+            lg, sg, gd = solver.graph_train_step(u0_d, tg_d, form.desc, S, B, pg, mg, vg, 3 + k, lr=1e-3, kind=1)
+            flags.append(gd)
+        g1.record(lstream)
+        g1.synchronize()
+        gms = g0.elapsed_time(g1) / args.steps
+        graph = {"value": 1000.0 / gms, "unit": "train_steps/s", "ms_per_step": gms, "steps": args.steps,
+                 "all_replayed_as_graph": all(flags), "last_loss": lg,
+                 "note": "forward + fused MSE + adjoint + Adam per step, one CUDA graph launch each"}
+        solver.set_params_device(p_d)
+        torch.cuda.synchronize()
+
     # ---- the plain FP32 form on the same inputs: speed ratio and agreement ------
     fp32 = None
     if args.precision == "bf16" and not args.no_fp32_form:
@@ -417,6 +445,7 @@ def run_gpu(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": args.steps * Form.LAUNCHES_PER_EVAL,
         "fp32_form": fp32,
+        "graph_train_step": graph,
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk,
@@ -445,6 +474,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32-form", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
