@@ -427,7 +427,8 @@ static int validate_desc(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B) 
   }
   if (tdir < 0 && c->precision == GBNDE_PREC_BF16 && !c->ff_on)
     return fail(GBNDE_ERR_UNSUPPORTED, "reverse time spans run in the FP32 form");
-  if (d->sensealg != GBNDE_SENSE_INTERPOLATING && d->sensealg != GBNDE_SENSE_BACKSOLVE)
+  if (d->sensealg != GBNDE_SENSE_INTERPOLATING && d->sensealg != GBNDE_SENSE_BACKSOLVE &&
+      d->sensealg != GBNDE_SENSE_GAUSS)
     return fail(GBNDE_ERR_INVALID, "unknown sensealg %d", d->sensealg);
   if ((long long)B * S > (1LL << 31)) return fail(GBNDE_ERR_UNSUPPORTED, "S*B too large");
   return 0;
@@ -701,7 +702,7 @@ static int build_intervals(gbnde_ctx* c, std::vector<Interval>& ivs, int* max_sl
     iv.nlo = (int)nlo;
     iv.nhi = (int)nhi;
     auto it = std::find(c->ckstep.begin(), c->ckstep.end(), (int)nlo);
-    if (c->sensealg == GBNDE_SENSE_INTERPOLATING && it == c->ckstep.end())
+    if (c->sensealg != GBNDE_SENSE_BACKSOLVE && it == c->ckstep.end())
       return fail(GBNDE_ERR_STATE, "no checkpoint for forward step %lld", nlo);
     iv.ckpt = it == c->ckstep.end() ? 0 : (int)(it - c->ckstep.begin());
     iv.save_lo = -1;
@@ -881,7 +882,9 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   int max_slots = 1, save_last = 0, nsave_last = 0;
   if (int r = build_intervals(c, ivs, &max_slots, &save_last, &nsave_last)) return r;
   const bool backsolve = c->sensealg == GBNDE_SENSE_BACKSOLVE;
-  const bool tcbwd = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && c->dense_valid && !c->ff_on;
+  const bool gauss = c->sensealg == GBNDE_SENSE_GAUSS;
+  const bool tcbwd =
+      c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && !gauss && c->dense_valid && !c->ff_on;
   // the FP32 adjoint reads dense slots only in its own layout; after a
   // tensor-core forward it recomputes each interval from the checkpoints
   const bool dense_f32 = c->dense_valid && !backsolve && !c->dense_tl;

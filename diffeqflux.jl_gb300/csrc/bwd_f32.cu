@@ -74,6 +74,8 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
   __shared__ double red[40];
   const int S = a.S, TM = a.TM, LD = a.LD, G = gridDim.x;
   const bool backsolve = (a.sensealg == GBNDE_SENSE_BACKSOLVE);
+  // quadrature adjoint: lam only in the solve, mu by Gauss-Legendre per step
+  const bool gauss = (a.sensealg == GBNDE_SENSE_GAUSS);
   const double Nnorm = (double)S * (double)a.B * (backsolve ? 2.0 : 1.0);
 
   Smem sm;
@@ -241,7 +243,7 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
         const float u = sm.uraw[s * LD + m];
         g *= 3.f * u * u;
       }
-      kl_out[base + e] = g;
+      if (kl_out) kl_out[base + e] = g;
       if (ku_out) ku_out[base + e] = -fo[s * LD + m];
     }
     __syncthreads();
@@ -338,7 +340,7 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
                    for (int q = 0; q < 7; ++q) acc = fmaf(hb[q], kk[q][g], acc);
                    return un[g] + acc;
                  },
-                 klb(0), backsolve ? kub(0) : nullptr, P1, (float)c_tab.b[0], nullptr, nullptr);
+                 klb(0), backsolve ? kub(0) : nullptr, gauss ? nullptr : P1, (float)c_tab.b[0], nullptr, nullptr);
       }
       ++nf_adj;
     }
@@ -453,8 +455,8 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
         const float* kk[7];
         const float* un = nullptr;
         if (!backsolve) udense(tt, hb, kk, un);
-        float* P = (i < 6) ? Pmid : Pb[iP7];
-        if (i == 6) {
+        float* P = gauss ? nullptr : (i < 6) ? Pmid : Pb[iP7];
+        if (i == 6 && P) {
           for (size_t q = threadIdx.x; q < (size_t)a.P; q += blockDim.x) P[q] = 0.f;
           __syncthreads();
         }
@@ -513,12 +515,50 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       double q11;
       double q = pi_q(eest, qold, &q11);
       if (eest <= 1.0) {
-        // mu += H * (P1 + Pmid)
-        const float Hf = (float)H;
-        const float* P1 = Pb[iP1];
-        for (size_t i = threadIdx.x; i < (size_t)a.P; i += blockDim.x)
-          mu_acc[i] = fmaf(Hf, P1[i] + Pmid[i], mu_acc[i]);
-        __syncthreads();
+        if (gauss) {
+          // mu += int over the step of lam^T df/dp: 4-point Gauss-Legendre on
+          // [t - H, t], lam(theta) = lam_n + H sum_j b_j(theta) k_j from this
+          // step's stages (the free interpolant), u from the forward
+          const double gth[4] = {0.06943184420297371, 0.33000947820757187, 0.6699905217924281,
+                                 0.9305681557970262};
+          const double gw[4] = {0.17392742256872679, 0.3260725774312732, 0.3260725774312732,
+                                0.17392742256872679};
+          const float* kl7[7];
+          for (int q = 0; q < 7; ++q) kl7[q] = klb(q);
+          for (int gq = 0; gq < 4; ++gq) {
+            const double tt = t - gth[gq] * H;
+            float bl[7];
+            interp_weights(gth[gq], bl);
+            for (int q = 0; q < 7; ++q) bl[q] = (float)(H * (double)bl[q]);
+            float hb[7];
+            const float* kk[7];
+            const float* un = nullptr;
+            udense(tt, hb, kk, un);
+            for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+              adj_eval(tile, tt, iv,
+                       [&](size_t g) {
+                         float s = 0.f;
+                         for (int q = 0; q < 7; ++q) s = fmaf(bl[q], kl7[q][g], s);
+                         return lcur[g] + s;
+                       },
+                       [&](size_t g) {
+                         float acc = 0.f;
+                         for (int q = 0; q < 7; ++q) acc = fmaf(hb[q], kk[q][g], acc);
+                         return un[g] + acc;
+                       },
+                       nullptr, nullptr, mu_acc, (float)(H * gw[gq]), nullptr, nullptr);
+            }
+            ++nf_adj;
+          }
+          __syncthreads();
+        } else {
+          // mu += H * (P1 + Pmid)
+          const float Hf = (float)H;
+          const float* P1 = Pb[iP1];
+          for (size_t i = threadIdx.x; i < (size_t)a.P; i += blockDim.x)
+            mu_acc[i] = fmaf(Hf, P1[i] + Pmid[i], mu_acc[i]);
+          __syncthreads();
+        }
         const int tmp = iP1;
         iP1 = iP7;
         iP7 = tmp;

@@ -7,7 +7,8 @@ reference re-exports (src/DiffEqFlux.jl:53-56).
 """
 from ._lib import GbndeError, load  # noqa: F401
 from .layers import (  # noqa: F401
-    Array, BacksolveAdjoint, Chain, Dense, GB300Tsit5, InterpolatingAdjoint, NeuralODE,
+    Array, BacksolveAdjoint, Chain, Dense, GaussAdjoint, GB300Tsit5, InterpolatingAdjoint, NeuralODE,
+    QuadratureAdjoint,
     ODESolution, Solver, Tsit5, WrappedFunction, ZygoteVJP, cube,
 )
 from .ffjord import FFJORD, FFJORDDistribution  # noqa: F401

@@ -13,7 +13,7 @@ MAX_LAYERS = 8
 
 ACT = {"identity": 0, "tanh": 1, "softplus": 2}
 PREC = {"fp32": 0, "bf16": 1}
-SENSE = {"interpolating": 0, "backsolve": 1}
+SENSE = {"interpolating": 0, "backsolve": 1, "gauss": 2}
 
 OK = 0
 ERR_INVALID = -1

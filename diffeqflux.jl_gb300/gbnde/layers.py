@@ -127,6 +127,30 @@ class BacksolveAdjoint:
         self.checkpointing = checkpointing
 
 
+class GaussAdjoint:
+    """Quadrature adjoint: the backward solve carries lam only, and dL/dp is
+    integrated by 4-point Gauss-Legendre over every accepted adjoint step
+    (lam from the step's interpolant, u from the forward's dense output).
+    Runs in the FP32 adjoint kernel in both precision forms."""
+    code = _lib.SENSE["gauss"]
+
+    def __init__(self, autojacvec=None, checkpointing=False):
+        self.autojacvec = autojacvec
+        self.checkpointing = checkpointing
+
+
+class QuadratureAdjoint(GaussAdjoint):
+    """QuadratureAdjoint(abstol, reltol): the reference integrates the
+    parameter quadrature with adaptive Gauss-Kronrod over each save interval
+    on a stored lam interpolant; here the same integral is taken with the
+    per-step Gauss-Legendre rule of GaussAdjoint (exact to the interpolant's
+    order), so abstol/reltol of the quadrature are accepted and unused."""
+
+    def __init__(self, autojacvec=None, abstol=1e-6, reltol=1e-3):
+        super().__init__(autojacvec)
+        self.abstol, self.reltol = abstol, reltol
+
+
 class Tsit5:
     """Tsit5 marker routing the solve to the GB300 kernels.
 
@@ -365,8 +389,9 @@ class NeuralODE:
             raise TypeError("alg must be Tsit5()/GB300Tsit5(); other solvers are not on the GB300 path")
         if sensealg is None:
             sensealg = InterpolatingAdjoint(autojacvec=ZygoteVJP())
-        if not isinstance(sensealg, (InterpolatingAdjoint, BacksolveAdjoint)):
-            raise TypeError("sensealg must be InterpolatingAdjoint() or BacksolveAdjoint()")
+        if not isinstance(sensealg, (InterpolatingAdjoint, BacksolveAdjoint, GaussAdjoint)):
+            raise TypeError("sensealg must be InterpolatingAdjoint(), BacksolveAdjoint(), GaussAdjoint() or "
+                            "QuadratureAdjoint()")
         if saveat is None and save_everystep is not False:
             raise NotImplementedError(
                 "save_everystep=true is not offered by the GB300 solver; pass saveat or "

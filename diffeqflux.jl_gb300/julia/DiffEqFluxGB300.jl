@@ -113,7 +113,8 @@ const CTXS = IdDict{Any, Ctx}()
 ctx_for(model, prec) = get!(() -> Ctx(model, prec), CTXS, (model, prec))
 
 sensecode(s) = s isa BacksolveAdjoint ? 1 : s isa InterpolatingAdjoint ? 0 :
-               error("GB300 supports InterpolatingAdjoint() and BacksolveAdjoint()")
+               (s isa QuadratureAdjoint || s isa GaussAdjoint) ? 2 :
+               error("GB300 supports InterpolatingAdjoint, BacksolveAdjoint, QuadratureAdjoint and GaussAdjoint")
 
 # ---- the differentiable solve -------------------------------------------------------------
 """

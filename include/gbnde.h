@@ -58,11 +58,18 @@ typedef enum {
   GBNDE_PREC_BF16 = 1
 } gbnde_precision;
 
-/* sensealg: InterpolatingAdjoint (default of NeuralODE, src/neural_de.jl:57)
- * or BacksolveAdjoint (test/BasicNeuralDE/neural_de_tests.jl:36). */
+/* sensealg: InterpolatingAdjoint (default of NeuralODE, src/neural_de.jl:57),
+ * BacksolveAdjoint (test/BasicNeuralDE/neural_de_tests.jl:36), or the
+ * quadrature adjoints QuadratureAdjoint / GaussAdjoint (re-exported at
+ * src/DiffEqFlux.jl:53, used at test/AdvancedNeuralDE/second_order_ode_tests.jl:59):
+ * the backward solve carries lam only, and dL/dp = int lam^T df/dp dt is
+ * integrated separately, here with 4-point Gauss-Legendre over every accepted
+ * adjoint step (lam from that step's interpolant, u from the forward's dense
+ * output). The quadrature adjoints run in the FP32 adjoint kernel. */
 typedef enum {
   GBNDE_SENSE_INTERPOLATING = 0,
-  GBNDE_SENSE_BACKSOLVE = 1
+  GBNDE_SENSE_BACKSOLVE = 1,
+  GBNDE_SENSE_GAUSS = 2
 } gbnde_sensealg;
 
 typedef enum {

@@ -325,6 +325,54 @@ def adjoint_interpolating(rhs, fwd, saveat, dL_dusave, t0, abstol, reltol, maxit
     return lam, mu, integ
 
 
+def adjoint_gauss(rhs, fwd, saveat, dL_dusave, t0, abstol, reltol, npts=4, maxiters=100000):
+    """Quadrature adjoint (QuadratureAdjoint / GaussAdjoint, re-exported at
+    src/DiffEqFlux.jl:53): the backward solve carries lam only (same
+    tableau, controller and lam-norm as InterpolatingAdjoint), and
+    dL/dp = int_{t0}^{T} lam^T df/dp dt is integrated by ``npts``-point
+    Gauss-Legendre over every accepted adjoint step, with lam(theta) from that
+    step's free interpolant and u from the forward dense output. Returns
+    (dL/du0, dL/dp, integrator)."""
+    saveat = [float(s) for s in saveat]
+    idx = {}
+    for i, s in enumerate(saveat):
+        idx.setdefault(s, []).append(i)
+    stops = _backward_stops(saveat, t0)
+    t_last = stops[0]
+    lam0 = sum(dL_dusave[..., i] for i in idx[t_last])
+    mu = np.zeros(rhs.nparams())
+    xg, wg = np.polynomial.legendre.leggauss(npts)
+    thetas, weights = (xg + 1.0) / 2.0, wg / 2.0
+
+    def F(y, t):
+        u = fwd.dense(t)[0]
+        gu, _ = rhs.vjp(u, t, y[0])
+        return (-gu,)
+
+    def on_stop(t, y):
+        if t in idx:
+            return (y[0] + sum(dL_dusave[..., i] for i in idx[t]),)
+        return None
+
+    def on_accept(t, h, y, K):
+        for th, w in zip(thetas, weights):
+            bw = T.interp_weights(th)
+            lam = y[0] + h * sum(bw[j] * K[j][0] for j in range(7))
+            tg = t + th * h
+            u = fwd.dense(tg)[0]
+            _, gp = rhs.vjp(u, tg, lam)
+            mu[:] += w * abs(h) * gp
+
+    integ = Tsit5(F, (lam0,), t_last, t0, abstol, reltol, tstops=stops[1:], on_stop=on_stop,
+                  maxiters=maxiters, on_accept=on_accept)
+    if t_last > t0:
+        integ.solve()
+    lam = integ.y[0] if t_last > t0 else lam0
+    if t0 in idx and t_last > t0:
+        lam = lam + sum(dL_dusave[..., i] for i in idx[t0])
+    return lam, mu, integ
+
+
 def adjoint_backsolve(rhs, usave, saveat, dL_dusave, t0, abstol, reltol, maxiters=100000):
     """BacksolveAdjoint (checkpointing on): co-integrate u backwards with (lam, mu),
     reset u to the saved forward value at each save point."""

@@ -222,3 +222,37 @@ def test_torch_autograd_bridge():
     du0, dp, _ = s.backward(2.0 * us)
     assert np.allclose(x.grad.cpu().numpy(), du0, rtol=1e-5, atol=1e-6)
     assert np.allclose(pt.grad.cpu().numpy(), dp, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+@pytest.mark.parametrize("marker", ["GaussAdjoint", "QuadratureAdjoint"])
+def test_quadrature_adjoint_against_oracle(prec, marker):
+    """QuadratureAdjoint / GaussAdjoint: lam-only backward solve plus 4-point
+    Gauss-Legendre quadrature of lam^T df/dp over every accepted adjoint step,
+    against the FP64 oracle's restatement (itself checked against central
+    finite differences) and against the InterpolatingAdjoint gradient."""
+    import gbnde
+    from oracle import tsit5 as ots
+    S, H, B = 8, 32, 96
+    model, p, rng = _setup([S, H, H, S], ["tanh", "tanh", "identity"], False, B, 13)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    ts = np.linspace(0.0, 1.0, 6)
+    tol = 1e-6
+    out = {}
+    for name, sense in (("q", getattr(gbnde, marker)()), ("i", gbnde.InterpolatingAdjoint())):
+        node = gbnde.NeuralODE(model, (0.0, 1.0), gbnde.Tsit5(prec), saveat=ts, abstol=tol, reltol=tol,
+                               sensealg=sense)
+        s = node.solver
+        s.set_params(p)
+        us, st = s.forward(u0, node.desc())
+        assert st.retcode == 0
+        du0, dp, sta = s.backward(2.0 * us / us.size)
+        assert sta.retcode_adj == 0
+        out[name] = (us, du0, dp)
+    rhs = _oracle(model, p)
+    ous, fwd = ots.solve_forward(rhs, u0.astype(np.float64), 0.0, 1.0, ts, tol, tol)
+    gu, gp, _ = ots.adjoint_gauss(rhs, fwd, ts, 2.0 * ous / ous.size, 0.0, tol, tol)
+    tolg = 1e-4 if prec == "fp32" else 1e-3
+    assert _rel(out["q"][1], gu) < tolg
+    assert _rel(out["q"][2], gp) < tolg
+    assert _rel(out["q"][2], out["i"][2].astype(np.float64)) < 1e-3

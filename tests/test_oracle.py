@@ -75,7 +75,7 @@ def test_step_size_controller_behaviour():
     assert counts[0] <= counts[1] <= counts[2]
 
 
-@pytest.mark.parametrize("sense", ["interpolating", "backsolve"])
+@pytest.mark.parametrize("sense", ["interpolating", "backsolve", "gauss"])
 def test_adjoint_matches_finite_differences(sense):
     rng = np.random.default_rng(1)
     m = omlp.MLP([2, 12, 2], ["tanh", "identity"], cube_input=True)
@@ -95,6 +95,8 @@ def test_adjoint_matches_finite_differences(sense):
     dL = 2 * (us - tgt)
     if sense == "interpolating":
         gu, gp, _ = ots.adjoint_interpolating(rhs, fwd, ts, dL, 0.0, tol, tol)
+    elif sense == "gauss":
+        gu, gp, _ = ots.adjoint_gauss(rhs, fwd, ts, dL, 0.0, tol, tol)
     else:
         gu, gp, _ = ots.adjoint_backsolve(rhs, us, ts, dL, 0.0, tol, tol)
     eps = 1e-6
