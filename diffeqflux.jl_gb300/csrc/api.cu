@@ -793,12 +793,12 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   // Every chain operand is also a weight-gradient image: forward op l's A is
   // a_l (image aoff[l]), VJP op l's A is delta_{l+1} (image doff[l]); the MMA
   // warp copies the chunks to the stage's slot. The output layer's forward
-  // product is computed only to pass a_{L-1} through the ring.
+  // op is copy-only: a_{L-1} passes through the ring just to reach its image.
   int n = 0;
   if (2 * L > tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
   for (int l = 0; l < L; ++l) {
     tc::GemmOp& o = t.ops.op[n++];
-    o.kind = 0;
+    o.kind = (l == L - 1) ? 2 : 0;
     o.wimg = c->wimg.as<uint8_t>() + c->wimg_off[l];
     o.npad = c->npad[l];
     o.nchunk = c->nchunk[l];

@@ -315,13 +315,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         }
         tc::epi_release_acc(es, sh);
       }
-      // the output layer's product runs only so that a_{L-1} passes through
-      // the ring (and into its image); its accumulator is not needed
-      {
-        uint32_t col;
-        if (!tc::epi_wait_acc(es, sh, &col)) return false;
-        tc::epi_release_acc(es, sh);
-      }
+      // a_{L-1} went through the ring only to reach its image (a copy-only
+      // op: no product, nothing to wait for)
       // delta_L = c lam (identity output layer). The VJP chain is linear in
       // its input, so every cotangent below carries the stage weight c: the
       // chain chunks double as the weight-gradient images, and kl is divided

@@ -50,6 +50,8 @@ constexpr int kImgSlots = 7;    // weight-gradient image slots per CTA: stages 1
 // kind 1 (weight-gradient GEMM, K = trajectories): A and B both bulk-copied
 //   from per-CTA images (2 pieces, MN-major 64-column blocks), three products
 //   hi.hi + hi.lo + lo.hi.
+// kind 2 (copy only, command mode): epilogue-written A chunks that only go to
+//   their weight-gradient image; no product, no accumulator, no W chunk.
 struct GemmOp {
   const uint8_t* wimg;  // kind 0: weight image; kind 1: B image base of CTA 0
   const uint8_t* aimg;  // kind 1: A image base of CTA 0
@@ -227,6 +229,26 @@ __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh
   volatile int* verr = &sh.err;
   volatile int* vstop = &sh.stop;
   const bool leader = (threadIdx.x & 31) == 0;
+  if (op.kind == 2) {
+    for (int c = 0; c < op.nchunk; ++c) {
+      unsigned long long t0 = 0;
+      while (!mbar_try_wait(&sh.a_full[m.aslot], m.aph)) {
+        if (*vstop || *verr) return false;
+        if (t0 == 0) t0 = globaltimer_ns();
+        else if (globaltimer_ns() - t0 > 4 * kWaitTimeoutNs) { *verr = 2; return false; }
+      }
+      if (leader) {
+        if (img_base != nullptr && op.img_off >= 0) {
+          copy_a_image(op, c, aring + m.aslot * kASlotBytes, img_base);
+          bulk_wait_read_all();
+        }
+        mbar_arrive(&sh.a_empty[m.aslot]);
+      }
+      __syncwarp();
+      if (++m.aslot == kARing) { m.aslot = 0; m.aph ^= 1; }
+    }
+    return true;
+  }
   const int pa[5] = {0, 1, 0, 2, 1};
   const int pb[5] = {0, 0, 1, 0, 1};
   const int reg = (int)(m.g & 1);
@@ -374,6 +396,13 @@ __device__ __forceinline__ bool tma_wait_or_stop(Shared& sh, uint64_t* bar, uint
 __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh, uint8_t* aring,
                                        uint8_t* wring, int f) {
   const bool leader = (threadIdx.x & 31) == 0;
+  if (op.kind == 2) {  // copy only: epilogue-written A chunks, no weights
+    for (int c = 0; c < op.nchunk; ++c) {
+      t.a_pending[t.aslot] = 0;
+      if (++t.aslot == kARing) { t.aslot = 0; t.aph ^= 1; }
+    }
+    return true;
+  }
   const uint32_t bbytes = op.kind == 0 ? 2u * (uint32_t)op.npad * 128u : 2u * (uint32_t)op.nblk_b * 8192u;
   const uint8_t* bbase = op.kind == 0 ? op.wimg : op.wimg + (size_t)blockIdx.x * op.cta_stride;
   const uint8_t* abase = op.kind == 0 ? nullptr : op.aimg + (size_t)blockIdx.x * op.cta_stride;
