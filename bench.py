@@ -413,6 +413,7 @@ def run_gpu(args):
         g_tc = dp_d.double().cpu().numpy()
         loss_tc = loss.value
         f32 = Form(wl, "fp32", local, dev, u0_d, tg_d, p_d)
+        tiles32 = f32.solver.autotune(f32.u0_d, f32.desc, wl["S"], wl["B"])
         f32.grad_eval()
         torch.cuda.synchronize()
         n32 = max(1, min(args.steps, 3))
@@ -422,6 +423,7 @@ def run_gpu(args):
                 "speedup_of_bf16_form": (value / world) * ms32 / 1000.0,
                 "loss_rel_diff": abs(loss_tc - f32.loss.value) / abs(f32.loss.value),
                 "grad_rel_diff": float(np.linalg.norm(g_tc - g32) / np.linalg.norm(g32)),
+                "autotuned_tile_rows": {"forward": tiles32[0], "adjoint": tiles32[1]},
                 "note": "plain FP32 kernels, same inputs; the FP32 form agrees with the FP64 "
                         "oracle to ~1e-6, so the differences bound the BF16 form's error"}
         del f32

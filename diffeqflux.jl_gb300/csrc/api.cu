@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "gbnde.h"
@@ -186,6 +187,9 @@ struct gbnde_ctx {
   DBuf gstat;               // device: loss (double), Adam coefficients (2 doubles), flags (ints)
   double* gpin = nullptr;   // pinned host mirror of the Adam coefficients
   bool graph_failed = false;
+  // autotuner (FP32 kernels): rows per tile chosen by timing, per (S, B)
+  int tm_force_fwd = 0, tm_force_bwd = 0;
+  std::map<std::pair<int, int>, std::pair<int, int>> tuned;
   // multiple shooting workspace
   DBuf ms_segs, ms_saveat, ms_u0, ms_usave, ms_dense, ms_steplog, ms_nacc, ms_ret, ms_cnt, ms_dldu,
       ms_dldu0, ms_bar, ms_mu, ms_dldp;
@@ -458,6 +462,12 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   const int frows = c->ff_on ? 2 * sumdims + c->mlp.maxdim + 1 : 2 * c->mlp.maxdim;
   int TM = 0;
   if (choose_tm(frows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "layer too wide");
+  {
+    int want = c->tm_force_fwd;
+    auto it = c->tuned.find({S, B});
+    if (!want && it != c->tuned.end()) want = it->second.first;
+    if (want > 0 && (size_t)frows * (want + 4) * sizeof(float) <= kSmemBudget) TM = want;
+  }
   const int LD = TM + 4;
   const size_t smem = (size_t)frows * LD * sizeof(float);
   const bool tcform = c->precision == GBNDE_PREC_BF16 && !c->ff_on;
@@ -895,6 +905,12 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   rows = c->ff_on ? 2 * rows + 4 * c->mlp.maxdim + 1 : rows + 2 * c->mlp.maxdim + S;
   int TM = 0;
   if (choose_tm(rows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "network too wide");
+  {
+    int want = c->tm_force_bwd;
+    auto it = c->tuned.find({S, B});
+    if (!want && it != c->tuned.end()) want = it->second.second;
+    if (want > 0 && (size_t)rows * (want + 4) * sizeof(float) <= kSmemBudget) TM = want;
+  }
   const int LD = TM + 4;
   const size_t smem = (size_t)rows * LD * sizeof(float);
   const int ntiles = (B + TM - 1) / TM;
@@ -1481,6 +1497,82 @@ int gbnde_graph_train_step(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B
     stats->retcode_adj = bs[ST_RETCODE];
   }
   if (graphed) *graphed = 1;
+  return 0;
+}
+
+int gbnde_autotune(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, const float* u0, int* tiles) {
+  if (!c || !d || !u0) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (int r = validate_desc(c, d, S, B)) return r;
+  if (int r = set_device(c)) return r;
+  if (!c->have_params) return fail(GBNDE_ERR_STATE, "parameters not set");
+  c->ff_on = 0;
+  const bool tcform = c->precision == GBNDE_PREC_BF16;
+  if (tcform) {
+    // the tensor-core kernels run one 128-trajectory tile per CTA and one CTA
+    // per SM (tensor memory is allocated whole): nothing to choose
+    if (tiles) tiles[0] = tiles[1] = 128;
+    return 0;
+  }
+  const size_t SB = (size_t)S * B, nsv = SB * d->nsave;
+  int r = 0;
+  if ((r = c->tr_us.ensure(nsv * 4)) || (r = c->tr_dl.ensure(nsv * 4)) || (r = c->tr_du0.ensure(SB * 4)) ||
+      (r = c->tr_dp.ensure(c->P * 4)))
+    return r;
+  float* us = c->tr_us.as<float>();
+  float* dl = c->tr_dl.as<float>();
+  const int cand[4] = {8, 16, 32, 64};
+  c->tuned.erase({S, B});
+  // forward: fastest rows per tile over two timed solves each
+  double best = 1e300;
+  int best_f = 0;
+  for (int tm : cand) {
+    c->tm_force_fwd = tm;
+    double tsum = 0.0;
+    bool okc = true;
+    for (int rep = 0; rep < 3 && okc; ++rep) {
+      gbnde_stats st{};
+      if (forward_impl(c, d, S, B, u0, false, us, false, &st) || st.retcode != GBNDE_RET_SUCCESS) okc = false;
+      else if (rep > 0) tsum += c->fwd_ms;
+    }
+    cudaGetLastError();
+    if (okc && tsum < best) { best = tsum; best_f = tm; }
+  }
+  c->tm_force_fwd = best_f;
+  // backward: the cotangent of the mean square of the saved states
+  int best_b = 0;
+  best = 1e300;
+  for (int tm : cand) {
+    c->tm_force_bwd = tm;
+    double tsum = 0.0;
+    bool okc = true;
+    for (int rep = 0; rep < 3 && okc; ++rep) {
+      gbnde_stats st{}, sb{};
+      double L = 0.0;
+      if (forward_impl(c, d, S, B, u0, false, us, false, &st) || st.retcode != GBNDE_RET_SUCCESS ||
+          cudaMemsetAsync(dl, 0, nsv * 4, c->stream) != cudaSuccess ||
+          gbnde_loss_device(c, us, dl, 1, dl, &L) ||
+          backward_impl(c, dl, false, c->tr_du0.as<float>(), c->tr_dp.as<float>(), false, &sb) ||
+          sb.retcode_adj != GBNDE_RET_SUCCESS)
+        okc = false;
+      else if (rep > 0) tsum += c->bwd_ms;
+    }
+    cudaGetLastError();
+    if (okc && tsum < best) { best = tsum; best_b = tm; }
+  }
+  c->tm_force_fwd = c->tm_force_bwd = 0;
+  if (!best_f || !best_b) return fail(GBNDE_ERR_UNSUPPORTED, "no tile size ran for this shape");
+  c->tuned[{S, B}] = {best_f, best_b};
+  // a captured training step holds the old tile sizes: capture again
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  c->gkey.clear();
+  if (tiles) {
+    tiles[0] = best_f;
+    tiles[1] = best_b;
+  }
+  g_last_error.clear();
   return 0;
 }
 

@@ -302,6 +302,13 @@ class Solver:
                                                    C.byref(st), C.byref(g)))
         return out.value, st, bool(g.value)
 
+    def autotune(self, u0_cm, desc, S, B):
+        """gbnde_autotune: times the FP32 kernels at each rows-per-tile choice on
+        this shape and keeps the fastest; returns (forward, adjoint) tile rows."""
+        t = (C.c_int * 2)()
+        _lib.check(self.lib.gbnde_autotune(self.h, C.byref(desc), S, B, u0_cm.data_ptr(), t))
+        return int(t[0]), int(t[1])
+
 
 # ---------------------------------------------------------------------------
 # solution type

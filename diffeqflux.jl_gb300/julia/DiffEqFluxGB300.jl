@@ -24,7 +24,7 @@ module DiffEqFluxGB300
 
 using ChainRulesCore, ComponentArrays, DiffEqFlux, Lux, SciMLBase, SciMLSensitivity
 
-export GB300Tsit5, gb300, gb300_train_step!
+export GB300Tsit5, gb300, gb300_train_step!, gb300_autotune!
 
 const libgbnde = joinpath(@__DIR__, "..", "gbnde", "libgbnde.so")
 
@@ -212,6 +212,25 @@ function gb300_train_step!(ctx::Ctx, tspan, saveat::Vector{Float64}, abstol, rel
         end
     end
     l[], st
+end
+
+"""
+    gb300_autotune!(ctx, tspan, saveat, abstol, reltol, u0) -> (forward_rows, adjoint_rows)
+
+Times the FP32 kernels at each rows-per-tile choice on `u0`'s shape
+(`CuArray{Float32}`, S x B) and keeps the fastest in `ctx` for later solves.
+"""
+function gb300_autotune!(ctx::Ctx, tspan, saveat::Vector{Float64}, abstol, reltol, u0)
+    S, B = size(u0)
+    tiles = zeros(Cint, 2)
+    GC.@preserve saveat begin
+        d = Ref(SolveDesc(tspan[1], tspan[2], abstol, reltol, 0, 0, 100000, pointer(saveat),
+                          length(saveat), 0, 0))
+        check(ccall((:gbnde_autotune, libgbnde), Cint,
+                    (Ptr{Cvoid}, Ref{SolveDesc}, Cint, Cint, Ptr{Cvoid}, Ptr{Cint}),
+                    ctx.h, d, S, B, pointer(u0), tiles))
+    end
+    Int(tiles[1]), Int(tiles[2])
 end
 
 # A layer routed to the GB300 kernels keeps the reference's `(layer)(x, p, st)`

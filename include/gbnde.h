@@ -283,6 +283,19 @@ int gbnde_set_stream(gbnde_ctx* ctx, void* stream);
  * backward solver kernels. No reference counterpart (instrumentation). */
 int gbnde_last_kernel_ms(gbnde_ctx* ctx, double* fwd_ms, double* bwd_ms);
 
+/* Autotuner. Times the FP32 form's forward and adjoint kernels on (S, B, u0)
+ * at every rows-per-tile choice that fits shared memory (8, 16, 32, 64
+ * trajectories per tile) and keeps the fastest of each for this (S, B) in
+ * the context; later solves of that shape use them. The cotangent of the
+ * timed adjoint is that of the mean square of the saved states. tiles[0] and
+ * tiles[1] receive the forward and adjoint choices. The BF16 form has one
+ * shape (128 trajectories per CTA, one CTA per SM) and returns 128, 128.
+ * Clobbers the last forward solve (run forward again before a backward).
+ * No reference counterpart (the reference's tile sizes are chosen by its
+ * array library). */
+int gbnde_autotune(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int S, int B,
+                   const float* u0_dev, int* tiles);
+
 /* Self-test of the tensor-core building blocks on the current device:
  * D[128 x N] = A[128 x K] * W[N x K]^T (host arrays, row-major) through bulk
  * copied SW128 weight images, tcgen05.mma into tensor memory and tcgen05.ld.

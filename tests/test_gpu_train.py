@@ -113,3 +113,38 @@ def test_graph_train_step_replays_the_eager_step(prec):
         graphed.append(g)
     assert graphed[0] is False
     assert all(graphed[1:]), graphed
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_autotune_keeps_results(prec):
+    """gbnde_autotune times the kernels at each tile size and keeps the
+    fastest; solves after it give the same states and gradients as before
+    (within FP32 reduction-order noise)."""
+    import torch
+    solver, desc, u0_d, tg_d, p_d, S, B, ns = _problem(prec, B=1000, seed=3)
+    dev = p_d.device
+    solver.set_params_device(p_d)
+
+    def run():
+        us = torch.empty((ns, B, S), dtype=torch.float32, device=dev)
+        dl = torch.empty_like(us)
+        du0 = torch.empty((B, S), dtype=torch.float32, device=dev)
+        dp = torch.empty_like(p_d)
+        st = solver.forward_device(u0_d, us, desc, S, B)
+        assert st.retcode == 0
+        loss = solver.loss_device(us, tg_d, 1, dl)
+        sb = solver.backward_device(dl, du0, dp)
+        assert sb.retcode_adj == 0
+        return us.double(), loss, du0.double(), dp.double()
+
+    before = run()
+    tiles = solver.autotune(u0_d, desc, S, B)
+    if prec == "fp32":
+        assert tiles[0] in (8, 16, 32, 64) and tiles[1] in (8, 16, 32, 64), tiles
+    else:
+        assert tiles == (128, 128)
+    after = run()
+    assert abs(after[1] - before[1]) <= 1e-5 * abs(before[1])
+    for a, b in zip((after[0], after[2], after[3]), (before[0], before[2], before[3])):
+        err = (a - b).norm().item() / b.norm().item()
+        assert err <= 1e-4, err
