@@ -763,10 +763,10 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   int hv = 0;
   for (int l = 1; l < L; ++l) {
     t.hoff[l] = hv;
-    hv += 32 * ((m.dims[l] + 63) / 64);
+    hv += tc::kCW * ((m.dims[l] + 63) / 64);  // per epilogue thread
   }
   t.hx = hv;
-  hv += 32;
+  hv += tc::kCW;
   t.hvals = hv;
   int nb = 0;
   for (int l = 0; l < L; ++l) {

@@ -40,45 +40,46 @@ struct Thr {
   int r, ch, nmine, q, lane;
 };
 
-__device__ __forceinline__ void ld32(const float* p, int n, bool vec, float* x) {
+__device__ __forceinline__ void ldv(const float* p, int n, bool vec, float* x) {
   if (vec) {
 #pragma unroll
-    for (int i = 0; i < 32; i += 4) {
+    for (int i = 0; i < tc::kCW; i += 4) {
       const float4 v = *reinterpret_cast<const float4*>(p + i);
       x[i] = v.x; x[i + 1] = v.y; x[i + 2] = v.z; x[i + 3] = v.w;
     }
   } else {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) x[i] = (i < n) ? p[i] : 0.f;
+    for (int i = 0; i < tc::kCW; ++i) x[i] = (i < n) ? p[i] : 0.f;
   }
 }
 
-__device__ __forceinline__ void st32(float* p, int n, bool vec, const float* x) {
+__device__ __forceinline__ void stv(float* p, int n, bool vec, const float* x) {
   if (vec) {
 #pragma unroll
-    for (int i = 0; i < 32; i += 4)
+    for (int i = 0; i < tc::kCW; i += 4)
       *reinterpret_cast<float4*>(p + i) = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
   } else {
 #pragma unroll
-    for (int i = 0; i < 32; ++i)
+    for (int i = 0; i < tc::kCW; ++i)
       if (i < n) p[i] = x[i];
   }
 }
 
 // Thread-private FP32 scratch in slot-major layout: float4 slot k of thread t
-// at hs4[k * 256 + t], so the 32 lanes of a warp touch 512 contiguous bytes.
-__device__ __forceinline__ void hs_ld32(const float4* hs4, int k0, float* x) {
+// at hs4[k * kEpiThreads + t], so the 32 lanes of a warp touch 512 contiguous
+// bytes. kCW values (kCW / 4 slots) per call.
+__device__ __forceinline__ void hs_ldv(const float4* hs4, int k0, float* x) {
   const uint64_t pol = tc::policy_evict_first();  // last use
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
+  for (int j = 0; j < tc::kCW / 4; ++j) {
     const float4 q = tc::ld_v4f_hint(hs4 + (size_t)(k0 + j) * tc::kEpiThreads + threadIdx.x, pol);
     x[4 * j] = q.x; x[4 * j + 1] = q.y; x[4 * j + 2] = q.z; x[4 * j + 3] = q.w;
   }
 }
-__device__ __forceinline__ void hs_st32(float4* hs4, int k0, const float* x) {
+__device__ __forceinline__ void hs_stv(float4* hs4, int k0, const float* x) {
   const uint64_t pol = tc::policy_evict_last();  // read back within the evaluation
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
+  for (int j = 0; j < tc::kCW / 4; ++j) {
     uint4 u;
     u.x = __float_as_uint(x[4 * j]);
     u.y = __float_as_uint(x[4 * j + 1]);
@@ -119,28 +120,29 @@ __device__ __forceinline__ double epi_partials_sum(const double* p, int n, tc::S
     for (int i = threadIdx.x; i < n; i += 32) v += __ldcg(p + i);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (threadIdx.x == 0) sh.red[15] = v;
+    if (threadIdx.x == 0) sh.red[16] = v;
   }
   tc::epi_bar();
-  const double v = sh.red[15];
+  const double v = sh.red[16];
   tc::epi_bar();
   return v;
 }
 
-// 32 values of this thread's row into the next chain A chunk (3 split
+// kCW values of this thread's row into the next chain A chunk (3 split
 // pieces). The MMA warp also copies the chunk's first two pieces to the
 // stage's weight-gradient image when the op asks for it.
 __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* aring, const Thr& th,
                                      const float* x) {
-  uint4 hi[4], mid[4], lo[4];
+  constexpr int nu = tc::kCW / 8;  // 16-byte units per piece
+  uint4 hi[nu], mid[nu], lo[nu];
 #pragma unroll
-  for (int j = 0; j < 4; ++j) tc::split3_bf16(x + 8 * j, hi[j], mid[j], lo[j]);
+  for (int j = 0; j < nu; ++j) tc::split3_bf16(x + 8 * j, hi[j], mid[j], lo[j]);
   {
     if (!tc::mbar_wait(&sh.a_empty[e.aslot], e.aph ^ 1, &sh.err)) return false;
     uint8_t* base = aring + e.aslot * tc::kASlotBytes;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const uint32_t off = tc::sw128_offset(th.r, 4 * th.ch + j);
+    for (int j = 0; j < nu; ++j) {
+      const uint32_t off = tc::sw128_offset(th.r, nu * th.ch + j);
       *reinterpret_cast<uint4*>(base + off) = hi[j];
       *reinterpret_cast<uint4*>(base + 16384 + off) = mid[j];
       *reinterpret_cast<uint4*>(base + 32768 + off) = lo[j];
@@ -152,11 +154,11 @@ __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* a
   return true;
 }
 
-// Column sums over the warp's 32 trajectory rows: after the butterfly, lane j
-// holds the sum of value j over the 32 lanes.
+// Column sums over the warp's 32 trajectory rows of kCW values per lane:
+// after the butterfly, lane j holds the sum of value j % kCW over the 32 lanes.
 __device__ __forceinline__ float warp_colsum(float* v, int lane) {
 #pragma unroll
-  for (int s = 16; s >= 1; s >>= 1) {
+  for (int s = tc::kCW / 2; s >= 1; s >>= 1) {
 #pragma unroll
     for (int i = 0; i < s; ++i) {
       const bool up = (lane & s) != 0;
@@ -165,6 +167,8 @@ __device__ __forceinline__ float warp_colsum(float* v, int lane) {
       v[i] = keep + __shfl_xor_sync(0xffffffffu, send, s);
     }
   }
+#pragma unroll
+  for (int s = tc::kCW; s < 32; s <<= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], s);
   return v[0];
 }
 
@@ -210,8 +214,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     th.q = warp & 3;
     th.r = 32 * th.q + th.lane;
     th.ch = warp >> 2;
-    th.nmine = min(32, max(0, S - 32 * th.ch));
-    const bool vec = (S % 4 == 0) && th.nmine == 32;
+    th.nmine = min(tc::kCW, max(0, S - tc::kCW * th.ch));
+    const bool vec = (S % 4 == 0) && th.nmine == tc::kCW;
     const uint32_t lane_base = ((uint32_t)(th.q * 32)) << 16;
     tc::EpiState es;
     tc::epi_state_init(es);
@@ -244,8 +248,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // lam, its compensation, the stages and the dense forward slots use the
     // tile layout; the cotangents dL/du(t_i) and dL/du0 the API layout
     const size_t SBt = (size_t)a.ntiles * tc::kTileVec;
-    auto gofs = [&](int tile) -> size_t { return ((size_t)tile * 128 + th.r) * S + 32 * th.ch; };
-    auto tofs = [&](int tile) -> size_t { return tc::tl_offset(tile, th.ch, th.r); };
+    auto gofs = [&](int tile) -> size_t { return ((size_t)tile * 128 + th.r) * S + tc::kCW * th.ch; };
+    auto tofs = [&](int tile) -> size_t { return tc::tl_offset_cw(tile, th.ch, th.r); };
     auto valid = [&](int tile) -> bool { return tile * 128 + th.r < a.B && th.nmine > 0; };
     // P is a multiple of 4 floats per CTA slot (the host pads it)
     auto zero_cta = [&](float* p) {
@@ -265,15 +269,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     asm volatile("fence.proxy.async.global;" ::: "memory");
     for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
       if (!valid(tile)) continue;
-      float v[32], z[32];
-      for (int i = 0; i < 32; ++i) { v[i] = 0.f; z[i] = 0.f; }
+      float v[tc::kCW], z[tc::kCW];
+      for (int i = 0; i < tc::kCW; ++i) { v[i] = 0.f; z[i] = 0.f; }
       for (int qq = 0; qq < a.nsave_last; ++qq) {
-        float d[32];
-        ld32(a.dLdu + (size_t)(a.save_last + qq) * SB + gofs(tile), th.nmine, vec, d);
-        for (int i = 0; i < 32; ++i) v[i] += d[i];
+        float d[tc::kCW];
+        ldv(a.dLdu + (size_t)(a.save_last + qq) * SB + gofs(tile), th.nmine, vec, d);
+        for (int i = 0; i < tc::kCW; ++i) v[i] += d[i];
       }
-      tc::tl_st32(a.lam[0] + tofs(tile), v);
-      tc::tl_st32(A.lam_comp[0] + tofs(tile), z);
+      tc::tl_stv(a.lam[0] + tofs(tile), v);
+      tc::tl_stv(A.lam_comp[0] + tofs(tile), z);
     }
     tc::epi_bar();
 
@@ -284,14 +288,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // no quadrature). The cotangent images carry the weight c.
     auto adj_eval = [&](const float* lam_in, const float* x, int slot, float* P, float c, float* kl) -> bool {
       if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_EVAL | ((uint32_t)(slot + 1) << 8))) return false;
-      float v[32];
+      float v[tc::kCW];
       // a_0 = x (or x^3)
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
+      for (int i = 0; i < tc::kCW; ++i) {
         const float y = (i < th.nmine) ? x[i] : 0.f;
         v[i] = m.cube ? y * y * y : y;
       }
-      if (m.cube) hs_st32(hs4, A.hx / 4, x);  // for the chain rule through x^3 at the end
+      if (m.cube) hs_stv(hs4, A.hx / 4, x);  // for the chain rule through x^3 at the end
       if (!emit(es, sh, aring, th, v)) return false;
       // forward recompute of the hidden layers
       for (int l = 0; l < L - 1; ++l) {
@@ -300,17 +304,17 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         uint32_t col;
         if (!tc::epi_wait_acc(es, sh, &col)) return false;
         const int nch = (N + 63) / 64;
-        float bnext[32];
-        tc::load_bias32(b, 32 * th.ch, N, bnext);
+        float bnext[tc::kCW];
+        tc::load_bias_cw(b, tc::kCW * th.ch, N, bnext);
         for (int cc = 0; cc < nch; ++cc) {
-          const int n0 = 64 * cc + 32 * th.ch;
-          float bc[32];
+          const int n0 = 64 * cc + tc::kCW * th.ch;
+          float bc[tc::kCW];
 #pragma unroll
-          for (int i = 0; i < 32; ++i) bc[i] = bnext[i];
-          if (cc + 1 < nch) tc::load_bias32(b, n0 + 64, N, bnext);
-          tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
-          tc::bias_act32(v, bc, m.act[l], n0, N);
-          hs_st32(hs4, (A.hoff[l + 1] + 32 * cc) / 4, v);
+          for (int i = 0; i < tc::kCW; ++i) bc[i] = bnext[i];
+          if (cc + 1 < nch) tc::load_bias_cw(b, n0 + 64, N, bnext);
+          tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+          tc::bias_act_cw(v, bc, m.act[l], n0, N);
+          hs_stv(hs4, (A.hoff[l + 1] + tc::kCW * cc) / 4, v);
           if (!emit(es, sh, aring, th, v)) return false;
         }
         tc::epi_release_acc(es, sh);
@@ -323,14 +327,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       // by c at the end.
       const float cs = P ? c : 1.f;
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = (i < th.nmine) ? cs * lam_in[i] : 0.f;
+      for (int i = 0; i < tc::kCW; ++i) v[i] = (i < th.nmine) ? cs * lam_in[i] : 0.f;
       if (!emit(es, sh, aring, th, v)) return false;
       if (P) {
-        float w[32];
+        float w[tc::kCW];
 #pragma unroll
-        for (int i = 0; i < 32; ++i) w[i] = v[i];
+        for (int i = 0; i < tc::kCW; ++i) w[i] = v[i];
         const float s = warp_colsum(w, th.lane);
-        bpart[th.q * A.nbias + A.boffp[L - 1] + 32 * th.ch + th.lane] = s;
+        if (th.lane < tc::kCW) bpart[th.q * A.nbias + A.boffp[L - 1] + tc::kCW * th.ch + th.lane] = s;
       }
       // VJP chain
       for (int l = L - 1; l >= 1; --l) {
@@ -338,22 +342,22 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         const int nch = (N + 63) / 64;
         // the stored activations of this layer are known before the
         // accumulator: fetch chunk 0 now and chunk cc+1 while working on cc
-        float hnext[32];
-        hs_ld32(hs4, A.hoff[l] / 4, hnext);
+        float hnext[tc::kCW];
+        hs_ldv(hs4, A.hoff[l] / 4, hnext);
         uint32_t col;
         if (!tc::epi_wait_acc(es, sh, &col)) return false;
         for (int cc = 0; cc < nch; ++cc) {
-          const int n0 = 64 * cc + 32 * th.ch;
-          float h[32];
+          const int n0 = 64 * cc + tc::kCW * th.ch;
+          float h[tc::kCW];
 #pragma unroll
-          for (int i = 0; i < 32; ++i) h[i] = hnext[i];
-          if (cc + 1 < nch) hs_ld32(hs4, (A.hoff[l] + 32 * (cc + 1)) / 4, hnext);
-          tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
-          tc::deriv_mul32(v, h, m.act[l - 1], n0, N);
+          for (int i = 0; i < tc::kCW; ++i) h[i] = hnext[i];
+          if (cc + 1 < nch) hs_ldv(hs4, (A.hoff[l] + tc::kCW * (cc + 1)) / 4, hnext);
+          tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+          tc::deriv_mul_cw(v, h, m.act[l - 1], n0, N);
           if (!emit(es, sh, aring, th, v)) return false;
           if (P) {
             const float s = warp_colsum(v, th.lane);
-            bpart[th.q * A.nbias + A.boffp[l - 1] + n0 + th.lane] = s;
+            if (th.lane < tc::kCW) bpart[th.q * A.nbias + A.boffp[l - 1] + n0 + th.lane] = s;
           }
         }
         tc::epi_release_acc(es, sh);
@@ -362,15 +366,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       {
         uint32_t col;
         if (!tc::epi_wait_acc(es, sh, &col)) return false;
-        tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)(32 * th.ch), v);
+        tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(tc::kCW * th.ch), v);
         const float inv = 1.f / cs;
 #pragma unroll
-        for (int i = 0; i < 32; ++i) kl[i] = (i < th.nmine) ? v[i] * inv : 0.f;
+        for (int i = 0; i < tc::kCW; ++i) kl[i] = (i < th.nmine) ? v[i] * inv : 0.f;
         if (m.cube) {
-          float xc[32];
-          hs_ld32(hs4, A.hx / 4, xc);
+          float xc[tc::kCW];
+          hs_ldv(hs4, A.hx / 4, xc);
 #pragma unroll
-          for (int i = 0; i < 32; ++i) kl[i] *= 3.f * xc[i] * xc[i];
+          for (int i = 0; i < tc::kCW; ++i) kl[i] *= 3.f * xc[i] * xc[i];
         }
         tc::epi_release_acc(es, sh);
       }
@@ -400,7 +404,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       tc::epi_bar();
       if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_DW | ((uint32_t)fs << 8))) return false;
       tc::epi_skip_a(es, A.dw_chunks);
-      float v[32];
+      float v[tc::kCW];
       for (int l = 0; l < L; ++l) {
         const int out = m.dims[l + 1], in = m.dims[l];
         const int isA = A.a_isA[l];
@@ -410,26 +414,26 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         for (int hh = 0; hh < A.nh[l]; ++hh) {
           const int mrow = 128 * hh + th.r;  // M-side feature of this lane
           // element i of chunk cc of this lane: isA -> row mrow (in feature),
-          // 32 consecutive out features; else row mrow (out feature), in
+          // kCW consecutive out features; else row mrow (out feature), in
           // features at stride `out`
           auto addr = [&](int cc, int i, bool* okp) -> size_t {
-            const int n0 = 64 * cc + 32 * th.ch;
+            const int n0 = 64 * cc + tc::kCW * th.ch;
             *okp = isA ? (mrow < in && n0 + i < out) : (mrow < out && n0 + i < in);
             return isA ? (size_t)mrow * out + n0 + i : (size_t)(n0 + i) * out + mrow;
           };
-          float av[32], cv[32];
-          // a full row of 32 contiguous, 16-byte aligned elements (isA)
+          float av[tc::kCW], cv[tc::kCW];
+          // a full row of kCW contiguous, 16-byte aligned elements (isA)
           auto vec4 = [&](int cc) -> bool {
-            const int n0 = 64 * cc + 32 * th.ch;
-            return isA && mrow < in && n0 + 32 <= out &&
+            const int n0 = 64 * cc + tc::kCW * th.ch;
+            return isA && mrow < in && n0 + tc::kCW <= out &&
                    (reinterpret_cast<uintptr_t>(Pw + (size_t)mrow * out + n0) & 15) == 0 &&
                    (reinterpret_cast<uintptr_t>(Cw + (size_t)mrow * out + n0) & 15) == 0;
           };
           auto fetch = [&](int cc) {
             if (vec4(cc)) {
-              const size_t o = (size_t)mrow * out + 64 * cc + 32 * th.ch;
+              const size_t o = (size_t)mrow * out + 64 * cc + tc::kCW * th.ch;
 #pragma unroll
-              for (int i = 0; i < 32; i += 4) {
+              for (int i = 0; i < tc::kCW; i += 4) {
                 const float4 a4 = *reinterpret_cast<const float4*>(Pw + o + i);
                 const float4 c4 = *reinterpret_cast<const float4*>(Cw + o + i);
                 av[i] = a4.x; av[i + 1] = a4.y; av[i + 2] = a4.z; av[i + 3] = a4.w;
@@ -438,7 +442,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
               return;
             }
 #pragma unroll
-            for (int i = 0; i < 32; ++i) {
+            for (int i = 0; i < tc::kCW; ++i) {
               bool okp;
               const size_t o = addr(cc, i, &okp);
               av[i] = okp ? Pw[o] : 0.f;
@@ -452,19 +456,19 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           const int nch = (Nn2 + 63) / 64;
           for (int cc = 0; cc < nch; ++cc) {
             if (cc > 0) fetch(cc);
-            tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + 32 * th.ch), v);
+            tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
             if (vec4(cc)) {
-              const size_t o = (size_t)mrow * out + 64 * cc + 32 * th.ch;
+              const size_t o = (size_t)mrow * out + 64 * cc + tc::kCW * th.ch;
 #pragma unroll
-              for (int i = 0; i < 32; ++i) kahan(av[i], cv[i], Hf * v[i]);
+              for (int i = 0; i < tc::kCW; ++i) kahan(av[i], cv[i], Hf * v[i]);
 #pragma unroll
-              for (int i = 0; i < 32; i += 4) {
+              for (int i = 0; i < tc::kCW; i += 4) {
                 *reinterpret_cast<float4*>(Pw + o + i) = make_float4(av[i], av[i + 1], av[i + 2], av[i + 3]);
                 *reinterpret_cast<float4*>(Cw + o + i) = make_float4(cv[i], cv[i + 1], cv[i + 2], cv[i + 3]);
               }
             } else {
 #pragma unroll
-              for (int i = 0; i < 32; ++i) {
+              for (int i = 0; i < tc::kCW; ++i) {
                 bool okp;
                 const size_t o = addr(cc, i, &okp);
                 if (!okp) continue;
@@ -503,30 +507,30 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     auto dense_u = [&](int tile, int n, const float* hb, float* x) {
       const float* slot = a.dense + (size_t)n * 8 * SBt;
       const size_t g = tofs(tile);
-      // u_n + sum_j hb_j k_j, in halves of 16 components and batches of
+      // u_n + sum_j hb_j k_j, in two parts of kPart components and batches of
       // four vectors (u_n, k1..k3 then k4..k7), each batch in flight together
 #pragma unroll
       for (int hf = 0; hf < 2; ++hf) {
         const float* sp = slot + g;
-        float v4[4][16], acc[16];
+        float v4[4][tc::kPart], acc[tc::kPart];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) tc::tl_ld16(sp + (size_t)j * SBt, hf, v4[j]);
+        for (int j = 0; j < 4; ++j) tc::tl_ldp(sp + (size_t)j * SBt, hf, v4[j]);
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
+        for (int q = 0; q < tc::kPart; ++q) {
           float e = 0.f;
 #pragma unroll
           for (int j = 0; j < 3; ++j) e = fmaf(hb[j], v4[j + 1][q], e);
           acc[q] = e;
-          x[16 * hf + q] = v4[0][q];
+          x[tc::kPart * hf + q] = v4[0][q];
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) tc::tl_ld16(sp + (size_t)(j + 4) * SBt, hf, v4[j]);
+        for (int j = 0; j < 4; ++j) tc::tl_ldp(sp + (size_t)(j + 4) * SBt, hf, v4[j]);
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
+        for (int q = 0; q < tc::kPart; ++q) {
           float e = acc[q];
 #pragma unroll
           for (int j = 0; j < 4; ++j) e = fmaf(hb[j + 3], v4[j][q], e);
-          x[16 * hf + q] += e;
+          x[tc::kPart * hf + q] += e;
         }
       }
     };
@@ -543,16 +547,16 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         float hb[7];
         dense_setup(iv, t, &n, hb);
         for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
-          float lam[32], x[32], kl[32];
+          float lam[tc::kCW], x[tc::kCW], kl[tc::kCW];
           const bool v = valid(tile);
           if (v) {
-            tc::tl_ld32(a.lam[cur] + tofs(tile), lam);
+            tc::tl_ldv(a.lam[cur] + tofs(tile), lam);
             dense_u(tile, n, hb, x);
           } else {
-            for (int i = 0; i < 32; ++i) lam[i] = x[i] = 0.f;
+            for (int i = 0; i < tc::kCW; ++i) lam[i] = x[i] = 0.f;
           }
           ok = adj_eval(lam, x, fs, Pb[iP1], (float)c_tab.b[0], kl);
-          if (v) tc::tl_st32(klb(0) + tofs(tile), kl);
+          if (v) tc::tl_stv(klb(0) + tofs(tile), kl);
         }
         ++nf_adj;
         if (!ok) break;
@@ -562,11 +566,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         double p0 = 0.0, p1 = 0.0;
         for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
           if (!valid(tile)) continue;
-          float l[32], f[32];
-          tc::tl_ld32(a.lam[cur] + tofs(tile), l);
-          tc::tl_ld32(klb(0) + tofs(tile), f);
+          float l[tc::kCW], f[tc::kCW];
+          tc::tl_ldv(a.lam[cur] + tofs(tile), l);
+          tc::tl_ldv(klb(0) + tofs(tile), f);
           #pragma unroll
-          for (int i = 0; i < 32; ++i) {
+          for (int i = 0; i < tc::kCW; ++i) {
             if (i >= th.nmine) continue;
             const float sk = (float)a.abstol + fabsf(l[i]) * (float)a.reltol;
             const double xx = (double)(l[i] / sk), yy = (double)(f[i] / sk);
@@ -595,20 +599,20 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         double p2 = 0.0;
         for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
           const bool v = valid(tile);
-          float l[32], f0[32], x[32], f1[32];
+          float l[tc::kCW], f0[tc::kCW], x[tc::kCW], f1[tc::kCW];
           if (v) {
-            tc::tl_ld32(a.lam[cur] + tofs(tile), l);
-            tc::tl_ld32(klb(0) + tofs(tile), f0);
+            tc::tl_ldv(a.lam[cur] + tofs(tile), l);
+            tc::tl_ldv(klb(0) + tofs(tile), f0);
             dense_u(tile, n, hb, x);
           } else {
-            for (int i = 0; i < 32; ++i) l[i] = f0[i] = x[i] = 0.f;
+            for (int i = 0; i < tc::kCW; ++i) l[i] = f0[i] = x[i] = 0.f;
           }
-          float li[32];
-          for (int i = 0; i < 32; ++i) li[i] = l[i] + hf * f0[i];
+          float li[tc::kCW];
+          for (int i = 0; i < tc::kCW; ++i) li[i] = l[i] + hf * f0[i];
           ok = adj_eval(li, x, -1, nullptr, 0.f, f1);
           if (v) {
             #pragma unroll
-            for (int i = 0; i < 32; ++i) {
+            for (int i = 0; i < tc::kCW; ++i) {
               if (i >= th.nmine) continue;
               const float sk = (float)a.abstol + fabsf(l[i]) * (float)a.reltol;
               const double z = (double)((f1[i] - f0[i]) / sk);
@@ -667,48 +671,48 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
             const bool v = valid(tile);
             const size_t g = tofs(tile);  // tile layout
-            float Y[32], x[32], kl[32];
+            float Y[tc::kCW], x[tc::kCW], kl[tc::kCW];
             if (v) {
-              // Y = lam + (comp + sum_j h a_ij k_j), in two halves of 16
+              // Y = lam + (comp + sum_j h a_ij k_j), in two parts of kPart
               // components whose loads are all in flight together
 #pragma unroll
               for (int hf = 0; hf < 2; ++hf) {
-                float lv[16], sv[16], kv[6][16];
-                tc::tl_ld16(lcur + g, hf, lv);
-                tc::tl_ld16(ccur + g, hf, sv);
+                float lv[tc::kPart], sv[tc::kPart], kv[6][tc::kPart];
+                tc::tl_ldp(lcur + g, hf, lv);
+                tc::tl_ldp(ccur + g, hf, sv);
 #pragma unroll
                 for (int j = 0; j < 6; ++j)
-                  if (j < i) tc::tl_ld16(klb(j) + g, hf, kv[j]);
+                  if (j < i) tc::tl_ldp(klb(j) + g, hf, kv[j]);
 #pragma unroll
-                for (int q = 0; q < 16; ++q) {
+                for (int q = 0; q < tc::kPart; ++q) {
                   float sq = sv[q];
 #pragma unroll
                   for (int j = 0; j < 6; ++j)
                     if (j < i) sq = fmaf(ha[j], kv[j][q], sq);
                   sv[q] = sq;
-                  Y[16 * hf + q] = lv[q] + sq;
+                  Y[tc::kPart * hf + q] = lv[q] + sq;
                 }
                 if (i == 6) {
                   // stage 7 reads k1..k6 anyway: the embedded error
                   // estimate's sum over them is formed here and parked in
                   // the k7 slot; the new lam and its compensation are stored
-                  float lt[16], cn[16];
+                  float lt[tc::kPart], cn[tc::kPart];
 #pragma unroll
-                  for (int q = 0; q < 16; ++q) {
+                  for (int q = 0; q < tc::kPart; ++q) {
                     float e = 0.f;
 #pragma unroll
                     for (int j = 0; j < 6; ++j) e = fmaf(s_hbt[j], kv[j][q], e);
                     lt[q] = e;
-                    cn[q] = sv[q] - (Y[16 * hf + q] - lv[q]);
+                    cn[q] = sv[q] - (Y[tc::kPart * hf + q] - lv[q]);
                   }
-                  tc::tl_st16(klb(6) + g, hf, lt);
-                  tc::tl_st16(lnew + g, hf, Y + 16 * hf);
-                  tc::tl_st16(cnew + g, hf, cn);
+                  tc::tl_stp(klb(6) + g, hf, lt);
+                  tc::tl_stp(lnew + g, hf, Y + tc::kPart * hf);
+                  tc::tl_stp(cnew + g, hf, cn);
                 }
               }
               dense_u(tile, n, hb, x);
             } else {
-              for (int q = 0; q < 32; ++q) Y[q] = x[q] = 0.f;
+              for (int q = 0; q < tc::kCW; ++q) Y[q] = x[q] = 0.f;
             }
             ok = adj_eval(Y, x, slot, P, cw, kl);
             if (v) {
@@ -719,22 +723,22 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
                 const float hbt6 = s_hbt[6];
 #pragma unroll
                 for (int hf = 0; hf < 2; ++hf) {
-                  float lt[16], lv[16], yv[16];
-                  tc::tl_ld16(klb(6) + g, hf, lt);
-                  tc::tl_ld16(lcur + g, hf, lv);
-                  tc::tl_ld16(lnew + g, hf, yv);
+                  float lt[tc::kPart], lv[tc::kPart], yv[tc::kPart];
+                  tc::tl_ldp(klb(6) + g, hf, lt);
+                  tc::tl_ldp(lcur + g, hf, lv);
+                  tc::tl_ldp(lnew + g, hf, yv);
 #pragma unroll
-                  for (int q = 0; q < 16; ++q) {
-                    if (16 * hf + q >= th.nmine) continue;
-                    const float e = fmaf(hbt6, kl[16 * hf + q], lt[q]);
+                  for (int q = 0; q < tc::kPart; ++q) {
+                    if (tc::kPart * hf + q >= th.nmine) continue;
+                    const float e = fmaf(hbt6, kl[tc::kPart * hf + q], lt[q]);
                     const float sc = (float)a.abstol + fmaxf(fabsf(lv[q]), fabsf(yv[q])) * (float)a.reltol;
                     const double rr = (double)(e / sc);
                     perr += isfinite(yv[q]) ? rr * rr : (double)INFINITY;
                   }
                 }
-                tc::tl_st32(klb(i) + g, kl);
+                tc::tl_stv(klb(i) + g, kl);
               } else {
-                tc::tl_st32(klb(i) + g, kl);
+                tc::tl_stv(klb(i) + g, kl);
               }
             }
           }
@@ -773,14 +777,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       if (iv.nsave_lo > 0) {
         for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
           if (!valid(tile)) continue;
-          float v[32];
-          tc::tl_ld32(a.lam[cur] + tofs(tile), v);
+          float v[tc::kCW];
+          tc::tl_ldv(a.lam[cur] + tofs(tile), v);
           for (int qq = 0; qq < iv.nsave_lo; ++qq) {
-            float d[32];
-            ld32(a.dLdu + (size_t)(iv.save_lo + qq) * SB + gofs(tile), th.nmine, vec, d);
-            for (int i = 0; i < 32; ++i) v[i] += d[i];
+            float d[tc::kCW];
+            ldv(a.dLdu + (size_t)(iv.save_lo + qq) * SB + gofs(tile), th.nmine, vec, d);
+            for (int i = 0; i < tc::kCW; ++i) v[i] += d[i];
           }
-          tc::tl_st32(a.lam[cur] + tofs(tile), v);
+          tc::tl_stv(a.lam[cur] + tofs(tile), v);
         }
       }
     }
@@ -788,9 +792,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     if (ret == GBNDE_RET_SUCCESS) {
       for (int tile = blockIdx.x; tile < a.ntiles; tile += G)
         if (valid(tile)) {
-          float v[32];
-          tc::tl_ld32(a.lam[cur] + tofs(tile), v);
-          st32(a.dLdu0 + gofs(tile), th.nmine, vec, v);
+          float v[tc::kCW];
+          tc::tl_ldv(a.lam[cur] + tofs(tile), v);
+          stv(a.dLdu0 + gofs(tile), th.nmine, vec, v);
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {

@@ -7,7 +7,7 @@
 // FP32 accumulation in tensor memory, weights streamed by bulk copies.
 //
 // Epilogue thread (warp w, lane l) owns trajectory row r = 32*(w%4) + l of the
-// 128-trajectory tile and state components [32*(w/4), 32*(w/4)+32); every
+// 128-trajectory tile and state components [kCW*(w/4), kCW*(w/4)+kCW); every
 // state/stage value a thread touches in global memory is its own, so the
 // stage arithmetic needs no synchronisation. State updates use a compensated
 // (TwoSum) sum whose low-order part is carried across steps. t, h, the error
@@ -27,27 +27,27 @@ struct Thr {
   int r, ch, nmine;
 };
 
-__device__ __forceinline__ void ld32(const float* p, int n, bool vec, float* x) {
+__device__ __forceinline__ void ldv(const float* p, int n, bool vec, float* x) {
   if (vec) {
 #pragma unroll
-    for (int i = 0; i < 32; i += 4) {
+    for (int i = 0; i < tc::kCW; i += 4) {
       const float4 v = *reinterpret_cast<const float4*>(p + i);
       x[i] = v.x; x[i + 1] = v.y; x[i + 2] = v.z; x[i + 3] = v.w;
     }
   } else {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) x[i] = (i < n) ? p[i] : 0.f;
+    for (int i = 0; i < tc::kCW; ++i) x[i] = (i < n) ? p[i] : 0.f;
   }
 }
 
-__device__ __forceinline__ void st32(float* p, int n, bool vec, const float* x) {
+__device__ __forceinline__ void stv(float* p, int n, bool vec, const float* x) {
   if (vec) {
 #pragma unroll
-    for (int i = 0; i < 32; i += 4)
+    for (int i = 0; i < tc::kCW; i += 4)
       *reinterpret_cast<float4*>(p + i) = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
   } else {
 #pragma unroll
-    for (int i = 0; i < 32; ++i)
+    for (int i = 0; i < tc::kCW; ++i)
       if (i < n) p[i] = x[i];
   }
 }
@@ -86,10 +86,10 @@ __device__ __forceinline__ double epi_partials_sum(const double* p, int n, tc::S
     for (int i = threadIdx.x; i < n; i += 32) v += __ldcg(p + i);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (threadIdx.x == 0) sh.red[15] = v;
+    if (threadIdx.x == 0) sh.red[16] = v;
   }
   tc::epi_bar();
-  const double v = sh.red[15];
+  const double v = sh.red[16];
   tc::epi_bar();
   return v;
 }
@@ -99,9 +99,9 @@ __device__ __forceinline__ double epi_partials_sum(const double* p, int n, tc::S
 __device__ __forceinline__ bool epi_rhs(const FwdTcArgs& A, tc::EpiState& e, tc::Shared& sh,
                                         uint8_t* aring, const Thr& th, const float* Y, float* kout) {
   const MlpDev& m = A.f.mlp;
-  float x[32];
+  float x[tc::kCW];
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
+  for (int i = 0; i < tc::kCW; ++i) {
     const float y = (i < th.nmine) ? Y[i] : 0.f;
     x[i] = m.cube ? y * y * y : y;
   }
@@ -114,16 +114,16 @@ __device__ __forceinline__ bool epi_rhs(const FwdTcArgs& A, tc::EpiState& e, tc:
     uint32_t col;
     if (!tc::epi_wait_acc(e, sh, &col)) return false;
     const int nch = (N + 63) / 64;
-    float bnext[32];
-    tc::load_bias32(b, 32 * th.ch, N, bnext);
+    float bnext[tc::kCW];
+    tc::load_bias_cw(b, tc::kCW * th.ch, N, bnext);
     for (int c = 0; c < nch; ++c) {
-      float v[32], bc[32];
-      const int n0 = 64 * c + 32 * th.ch;
+      float v[tc::kCW], bc[tc::kCW];
+      const int n0 = 64 * c + tc::kCW * th.ch;
 #pragma unroll
-      for (int i = 0; i < 32; ++i) bc[i] = bnext[i];
-      if (c + 1 < nch) tc::load_bias32(b, n0 + 64, N, bnext);
-      tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
-      tc::bias_act32(v, bc, act, n0, N);
+      for (int i = 0; i < tc::kCW; ++i) bc[i] = bnext[i];
+      if (c + 1 < nch) tc::load_bias_cw(b, n0 + 64, N, bnext);
+      tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+      tc::bias_act_cw(v, bc, act, n0, N);
       if (!tc::epi_write_a(e, sh, aring, th.r, th.ch, v)) return false;
     }
     tc::epi_release_acc(e, sh);
@@ -132,13 +132,13 @@ __device__ __forceinline__ bool epi_rhs(const FwdTcArgs& A, tc::EpiState& e, tc:
     const float* b = A.bias[m.nlayers - 1];
     uint32_t col;
     if (!tc::epi_wait_acc(e, sh, &col)) return false;
-    float v[32], bc[32];
-    tc::load_bias32(b, 32 * th.ch, m.dims[m.nlayers], bc);
-    tc::tmem_ld32(sh.tmem_base + lane_base + col + (uint32_t)(32 * th.ch), v);
+    float v[tc::kCW], bc[tc::kCW];
+    tc::load_bias_cw(b, tc::kCW * th.ch, m.dims[m.nlayers], bc);
+    tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(tc::kCW * th.ch), v);
     // output layer: bias and its activation (identity for most models)
-    tc::bias_act32(v, bc, m.act[m.nlayers - 1], 32 * th.ch, m.dims[m.nlayers]);
+    tc::bias_act_cw(v, bc, m.act[m.nlayers - 1], tc::kCW * th.ch, m.dims[m.nlayers]);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) kout[i] = (i < th.nmine) ? v[i] : 0.f;
+    for (int i = 0; i < tc::kCW; ++i) kout[i] = (i < th.nmine) ? v[i] : 0.f;
     tc::epi_release_acc(e, sh);
   }
   return true;
@@ -176,8 +176,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
     Thr th;
     th.r = 32 * (warp & 3) + (threadIdx.x & 31);
     th.ch = warp >> 2;
-    th.nmine = min(32, max(0, S - 32 * th.ch));
-    const bool vec = (S % 4 == 0) && th.nmine == 32;
+    th.nmine = min(tc::kCW, max(0, S - tc::kCW * th.ch));
+    const bool vec = (S % 4 == 0) && th.nmine == tc::kCW;
     tc::EpiState es;
     tc::epi_state_init(es);
     unsigned int gen = 0;
@@ -193,28 +193,28 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
       if (dense) return A.dense + ((size_t)min(naccept, A.dense_slots - 1) * 8 + 1 + j) * SBt;
       return A.kring + (size_t)j * SBt;
     };
-    auto gofs = [&](int tile) -> size_t { return ((size_t)tile * 128 + th.r) * S + 32 * th.ch; };
-    auto tofs = [&](int tile) -> size_t { return tc::tl_offset(tile, th.ch, th.r); };
+    auto gofs = [&](int tile) -> size_t { return ((size_t)tile * 128 + th.r) * S + tc::kCW * th.ch; };
+    auto tofs = [&](int tile) -> size_t { return tc::tl_offset_cw(tile, th.ch, th.r); };
     auto valid = [&](int tile) -> bool { return tile * 128 + th.r < a.B && th.nmine > 0; };
     bool ok = true;
 
     // ---- k1 = f(u0); state, compensation and slot 0 ---------------------------
     for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
-      float Y[32], k[32];
+      float Y[tc::kCW], k[tc::kCW];
       const bool v = valid(tile);
       const size_t g = gofs(tile);
-      if (v) ld32(a.u0 + g, th.nmine, vec, Y);
+      if (v) ldv(a.u0 + g, th.nmine, vec, Y);
       else
-        for (int i = 0; i < 32; ++i) Y[i] = 0.f;
+        for (int i = 0; i < tc::kCW; ++i) Y[i] = 0.f;
       ok = epi_rhs(A, es, sh, aring, th, Y, k);
       if (v) {
-        float z[32];
-        for (int i = 0; i < 32; ++i) z[i] = 0.f;
+        float z[tc::kCW];
+        for (int i = 0; i < tc::kCW; ++i) z[i] = 0.f;
         const size_t tg = tofs(tile);
-        tc::tl_st32(a.ubuf[0] + tg, Y);
-        tc::tl_st32(A.comp[0] + tg, z);
-        if (dense) tc::tl_st32(A.dense + tg, Y);
-        tc::tl_st32(kptr(0) + tg, k);
+        tc::tl_stv(a.ubuf[0] + tg, Y);
+        tc::tl_stv(A.comp[0] + tg, z);
+        if (dense) tc::tl_stv(A.dense + tg, Y);
+        tc::tl_stv(kptr(0) + tg, k);
       }
     }
     nf = 1;
@@ -222,9 +222,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
     while (isave < a.nsave && a.saveat[isave] == a.t0) {
       for (int tile = blockIdx.x; tile < a.ntiles; tile += G)
         if (valid(tile)) {
-          float Y[32];
-          ld32(a.u0 + gofs(tile), th.nmine, vec, Y);
-          st32(a.usave + (size_t)isave * SB + gofs(tile), th.nmine, vec, Y);
+          float Y[tc::kCW];
+          ldv(a.u0 + gofs(tile), th.nmine, vec, Y);
+          stv(a.usave + (size_t)isave * SB + gofs(tile), th.nmine, vec, Y);
         }
       ++isave;
     }
@@ -238,11 +238,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
       double p0 = 0.0, p1 = 0.0;
       for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
         if (!valid(tile)) continue;
-        float u[32], f[32];
-        ld32(a.u0 + gofs(tile), th.nmine, vec, u);
-        tc::tl_ld32(kptr(0) + tofs(tile), f);
+        float u[tc::kCW], f[tc::kCW];
+        ldv(a.u0 + gofs(tile), th.nmine, vec, u);
+        tc::tl_ldv(kptr(0) + tofs(tile), f);
         #pragma unroll
-        for (int i = 0; i < 32; ++i) {
+        for (int i = 0; i < tc::kCW; ++i) {
           if (i >= th.nmine) continue;
           const float sk = (float)a.abstol + fabsf(u[i]) * (float)a.reltol;
           const double x = (double)(u[i] / sk), y = (double)(f[i] / sk);
@@ -267,18 +267,18 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
       double p2 = 0.0;
       for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
         const bool v = valid(tile);
-        float u[32], f0[32], Y[32], f1[32];
+        float u[tc::kCW], f0[tc::kCW], Y[tc::kCW], f1[tc::kCW];
         if (v) {
-          ld32(a.u0 + gofs(tile), th.nmine, vec, u);
-          tc::tl_ld32(kptr(0) + tofs(tile), f0);
+          ldv(a.u0 + gofs(tile), th.nmine, vec, u);
+          tc::tl_ldv(kptr(0) + tofs(tile), f0);
         } else {
-          for (int i = 0; i < 32; ++i) u[i] = f0[i] = 0.f;
+          for (int i = 0; i < tc::kCW; ++i) u[i] = f0[i] = 0.f;
         }
-        for (int i = 0; i < 32; ++i) Y[i] = u[i] + hf * f0[i];
+        for (int i = 0; i < tc::kCW; ++i) Y[i] = u[i] + hf * f0[i];
         ok = epi_rhs(A, es, sh, aring, th, Y, f1);
         if (v) {
           #pragma unroll
-          for (int i = 0; i < 32; ++i) {
+          for (int i = 0; i < tc::kCW; ++i) {
             if (i >= th.nmine) continue;
             const float sk = (float)a.abstol + fabsf(u[i]) * (float)a.reltol;
             const double z = (double)((f1[i] - f0[i]) / sk);
@@ -325,49 +325,49 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
           for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
             const bool v = valid(tile);
             const size_t g = tofs(tile);  // tile layout
-            float u[32], s[32], Y[32], k[32];
+            float u[tc::kCW], s[tc::kCW], Y[tc::kCW], k[tc::kCW];
             if (v) {
-              tc::tl_ld32(ucur + g, u);
-              tc::tl_ld32(ccur + g, s);
+              tc::tl_ldv(ucur + g, u);
+              tc::tl_ldv(ccur + g, s);
               if (i < 6) {
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
                   if (j >= i) break;
-                  float kj[32];
-                  tc::tl_ld32(kptr(j) + g, kj);
+                  float kj[tc::kCW];
+                  tc::tl_ldv(kptr(j) + g, kj);
 #pragma unroll
-                  for (int q = 0; q < 32; ++q) s[q] = fmaf(ha[j], kj[q], s[q]);
+                  for (int q = 0; q < tc::kCW; ++q) s[q] = fmaf(ha[j], kj[q], s[q]);
                 }
               } else {
                 // stage 7 reads k1..k6 anyway: the embedded error estimate's
                 // sum over them is formed here and parked in the k7 slot
-                float ut[32];
+                float ut[tc::kCW];
 #pragma unroll
-                for (int q = 0; q < 32; ++q) ut[q] = 0.f;
+                for (int q = 0; q < tc::kCW; ++q) ut[q] = 0.f;
 #pragma unroll
                 for (int j = 0; j < 6; ++j) {
-                  float kj[32];
-                  tc::tl_ld32(kptr(j) + g, kj);
+                  float kj[tc::kCW];
+                  tc::tl_ldv(kptr(j) + g, kj);
 #pragma unroll
-                  for (int q = 0; q < 32; ++q) {
+                  for (int q = 0; q < tc::kCW; ++q) {
                     s[q] = fmaf(ha[j], kj[q], s[q]);
                     ut[q] = fmaf(hbt[j], kj[q], ut[q]);
                   }
                 }
-                tc::tl_st32(kptr(6) + g, ut);
+                tc::tl_stv(kptr(6) + g, ut);
               }
 #pragma unroll
-              for (int q = 0; q < 32; ++q) Y[q] = u[q] + s[q];
+              for (int q = 0; q < tc::kCW; ++q) Y[q] = u[q] + s[q];
               if (i == 6) {
-                float cn[32];
+                float cn[tc::kCW];
 #pragma unroll
-                for (int q = 0; q < 32; ++q) cn[q] = s[q] - (Y[q] - u[q]);
-                tc::tl_st32(unew + g, Y);
-                tc::tl_st32(cnew + g, cn);
+                for (int q = 0; q < tc::kCW; ++q) cn[q] = s[q] - (Y[q] - u[q]);
+                tc::tl_stv(unew + g, Y);
+                tc::tl_stv(cnew + g, cn);
               }
             } else {
 #pragma unroll
-              for (int q = 0; q < 32; ++q) Y[q] = 0.f;
+              for (int q = 0; q < tc::kCW; ++q) Y[q] = 0.f;
             }
             ok = epi_rhs(A, es, sh, aring, th, Y, k);
             if (v) {
@@ -375,22 +375,22 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
                 // u, the stage value and the error sum over k1..k6 again
                 // (stored above): nothing of the stage arithmetic stays in
                 // registers across epi_rhs
-                float ut[32];
-                tc::tl_ld32(kptr(6) + g, ut);
-                tc::tl_ld32(ucur + g, u);
-                tc::tl_ld32(unew + g, Y);
+                float ut[tc::kCW];
+                tc::tl_ldv(kptr(6) + g, ut);
+                tc::tl_ldv(ucur + g, u);
+                tc::tl_ldv(unew + g, Y);
 #pragma unroll
-                for (int q = 0; q < 32; ++q) ut[q] = fmaf(hbt[6], k[q], ut[q]);
-                tc::tl_st32(kptr(i) + g, k);
+                for (int q = 0; q < tc::kCW; ++q) ut[q] = fmaf(hbt[6], k[q], ut[q]);
+                tc::tl_stv(kptr(i) + g, k);
                 #pragma unroll
-                for (int q = 0; q < 32; ++q) {
+                for (int q = 0; q < tc::kCW; ++q) {
                   if (q >= th.nmine) continue;
                   const float sc = (float)a.abstol + fmaxf(fabsf(u[q]), fabsf(Y[q])) * (float)a.reltol;
                   const double rr = (double)(ut[q] / sc);
                   perr += isfinite(Y[q]) ? rr * rr : (double)INFINITY;
                 }
               } else {
-                tc::tl_st32(kptr(i) + g, k);
+                tc::tl_stv(kptr(i) + g, k);
               }
             }
           }
@@ -427,24 +427,24 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
             for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
               if (!valid(tile)) continue;
               const size_t g = gofs(tile), tg = tofs(tile);
-              float o[32];
+              float o[tc::kCW];
               if (sv == tnew) {
-                tc::tl_ld32(unew + tg, o);
+                tc::tl_ldv(unew + tg, o);
               } else {
-                float u[32];
-                tc::tl_ld32(ucur + tg, u);
-                tc::tl_ld32(ccur + tg, o);
+                float u[tc::kCW];
+                tc::tl_ldv(ucur + tg, u);
+                tc::tl_ldv(ccur + tg, o);
 #pragma unroll
                 for (int j = 0; j < 7; ++j) {
-                  float kj[32];
-                  tc::tl_ld32(kptr(j) + tg, kj);
+                  float kj[tc::kCW];
+                  tc::tl_ldv(kptr(j) + tg, kj);
 #pragma unroll
-                  for (int q = 0; q < 32; ++q) o[q] = fmaf(hb[j], kj[q], o[q]);
+                  for (int q = 0; q < tc::kCW; ++q) o[q] = fmaf(hb[j], kj[q], o[q]);
                 }
 #pragma unroll
-                for (int q = 0; q < 32; ++q) o[q] = u[q] + o[q];
+                for (int q = 0; q < tc::kCW; ++q) o[q] = u[q] + o[q];
               }
-              st32(dst + g, th.nmine, vec, o);
+              stv(dst + g, th.nmine, vec, o);
             }
             ++isave;
           }
@@ -454,9 +454,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
             float* dst = a.ckpt + (size_t)nck * SB;
             for (int tile = blockIdx.x; tile < a.ntiles; tile += G)
               if (valid(tile)) {
-                float u[32];
-                tc::tl_ld32(ucur + tofs(tile), u);
-                st32(dst + gofs(tile), th.nmine, vec, u);
+                float u[tc::kCW];
+                tc::tl_ldv(ucur + tofs(tile), u);
+                stv(dst + gofs(tile), th.nmine, vec, u);
               }
             if (blockIdx.x == 0 && threadIdx.x == 0) a.ckpt_step[nck] = (int)naccept;
             ++nck;
@@ -471,13 +471,13 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
           for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
             if (!valid(tile)) continue;
             const size_t g = tofs(tile);  // tile layout
-            float kk[32];
-            tc::tl_ld32(k7 + g, kk);
-            tc::tl_st32(kptr(0) + g, kk);
+            float kk[tc::kCW];
+            tc::tl_ldv(k7 + g, kk);
+            tc::tl_stv(kptr(0) + g, kk);
             if (dense && naccept < A.dense_slots) {
-              float un[32];
-              tc::tl_ld32(unew + g, un);
-              tc::tl_st32(A.dense + (size_t)naccept * 8 * SBt + g, un);
+              float un[tc::kCW];
+              tc::tl_ldv(unew + g, un);
+              tc::tl_stv(A.dense + (size_t)naccept * 8 * SBt + g, un);
             }
           }
           cur ^= 1;

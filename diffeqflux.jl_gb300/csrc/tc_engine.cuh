@@ -10,15 +10,18 @@
 // warp with bulk copies. Ops alternate between two 256-column accumulator
 // regions so that the epilogue can drain one while the next op accumulates.
 //
-// Warp roles (384 threads, three warpgroups): warps 0-7 epilogue (EPI),
-// warp 8 MMA issuer, warp 9 weight producer, warps 10-11 idle. The MMA and
-// producer warps run the op list cyclically until the epilogue raises the
-// stop flag. The kernel is launched with kLaunchRegs registers per thread;
-// the control warpgroup then gives registers back (setmaxnreg.dec to
-// kCtlRegs) and the two epilogue warpgroups take them (setmaxnreg.inc to
-// kEpiRegs): 256 * kEpiRegs + 128 * kCtlRegs == 384 * kLaunchRegs, checked at
-// compile time here and against the compiled kernel's register count before
-// every launch (a split above the launch's registers would never complete).
+// Warp roles: kNWG epilogue warpgroups (warps 0 .. 4 kNWG - 1), then one
+// control warpgroup: the MMA issuer, the weight producer and two idle warps.
+// Epilogue warp w serves the 32 accumulator rows (tensor-memory lanes) of
+// w % 4 and column group w / 4 (kCW columns of every 64-column chunk). The
+// MMA and producer warps run the op list cyclically until the epilogue
+// raises the stop flag. The kernel is launched with kLaunchRegs registers
+// per thread; the control warpgroup then gives registers back
+// (setmaxnreg.dec to kCtlRegs) and the epilogue warpgroups take them
+// (setmaxnreg.inc to kEpiRegs): kEpiThreads * kEpiRegs + 128 * kCtlRegs ==
+// kThreads * kLaunchRegs, checked at compile time here and against the
+// compiled kernel's register count before every launch (a split above the
+// launch's registers would never complete).
 #pragma once
 #include "kernels.h"
 #include "tc_ptx.cuh"
@@ -26,13 +29,32 @@
 namespace gbnde {
 namespace tc {
 
-constexpr int kEpiThreads = 256;
-constexpr int kThreads = 384;
-constexpr int kMmaWarp = 8;
-constexpr int kTmaWarp = 9;
-constexpr int kLaunchRegs = 168;   // 65536 / 384, rounded down to a multiple of 8
-constexpr int kEpiRegs = 224;
-constexpr int kCtlRegs = 56;
+// Four epilogue warpgroups (16 columns per thread) hide more of the
+// epilogue's memory and tensor-memory latency than two (32 columns per
+// thread, more registers each): the adjoint kernel runs 6.7 % faster at
+// B = 16384, 64-256-256-64, and the forward within 1 %.
+#ifndef GBNDE_TC_NWG
+#define GBNDE_TC_NWG 4
+#endif
+constexpr int kNWG = GBNDE_TC_NWG;   // epilogue warpgroups: 2 or 4
+static_assert(kNWG == 2 || kNWG == 4, "two or four epilogue warpgroups");
+constexpr int kCW = 64 / kNWG;       // columns of each 64-column chunk per epilogue thread
+constexpr int kEpiThreads = 128 * kNWG;
+constexpr int kThreads = kEpiThreads + 128;
+constexpr int kMmaWarp = 4 * kNWG;
+constexpr int kTmaWarp = kMmaWarp + 1;
+// Launch registers: 65536 / kThreads, rounded down to a multiple of 8 and
+// within one scheduler's 16384 registers for its share of the warps
+// (kThreads / 128 warps each); then the split.
+constexpr int kLaunchRegs = kNWG == 2 ? 168 : 96;
+#ifndef GBNDE_TC_EPI_REGS
+#define GBNDE_TC_EPI_REGS (GBNDE_TC_NWG == 2 ? 224 : 104)
+#endif
+#ifndef GBNDE_TC_CTL_REGS
+#define GBNDE_TC_CTL_REGS (GBNDE_TC_NWG == 2 ? 56 : 64)
+#endif
+constexpr int kEpiRegs = GBNDE_TC_EPI_REGS;
+constexpr int kCtlRegs = GBNDE_TC_CTL_REGS;
 static_assert(kEpiThreads * kEpiRegs + (kThreads - kEpiThreads) * kCtlRegs == kThreads * kLaunchRegs,
               "register split must equal the launch's registers");
 static_assert(kThreads * kLaunchRegs <= 65536, "launch registers exceed the register file");
@@ -91,10 +113,10 @@ struct Shared {
   uint32_t tmem_base;
   int stop;
   int err;
-  double red[16];
+  double red[24];  // [0, 16): per-warp sums; 16..: broadcasts
 };
 
-__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory"); }
 
 // Register split between the warpgroups (all four warps of a warpgroup
 // execute the same instruction).
@@ -105,7 +127,7 @@ __device__ __forceinline__ void regs_give_ctl() {
   asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kCtlRegs));
 }
 
-// Deterministic sum of a double over the 256 epilogue threads.
+// Deterministic sum of a double over the epilogue threads.
 __device__ __forceinline__ double epi_sum(double v, Shared& sh) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -114,7 +136,7 @@ __device__ __forceinline__ double epi_sum(double v, Shared& sh) {
   if ((threadIdx.x & 31) == 0) sh.red[w] = v;
   epi_bar();
   double s = 0.0;
-  for (int i = 0; i < 8; ++i) s += sh.red[i];
+  for (int i = 0; i < kEpiThreads / 32; ++i) s += sh.red[i];
   epi_bar();
   return s;
 }
@@ -146,9 +168,10 @@ __device__ __forceinline__ void init_shared(Shared& sh) {
 }
 
 // ---- tile layout of the solvers' internal state vectors ---------------------------
-// The epilogue thread of row r and column half ch owns 32 components of that
-// row; in the tile layout they are 8 float4 groups with the rows innermost:
-// tile T, half ch, group j, row r at float ((T * 2 + ch) * 8 + j) * 512 + 4 r.
+// The 64 components of a row are two halves of 8 float4 groups each, with
+// the rows innermost: tile T, half h, group j, row r at float
+// ((T * 2 + h) * 8 + j) * 512 + 4 r. The epilogue thread of row r and column
+// group g owns the kCW components from kCW g: kCW / 4 consecutive groups.
 // A warp (32 consecutive rows) reading group j touches 512 contiguous bytes,
 // where the column-major API layout would touch 32 separate lines. One vector
 // holds ntiles * kTileVec floats (components padded to 64, pads kept zero).
@@ -156,19 +179,40 @@ constexpr int kTileVec = 128 * 64;
 __device__ __forceinline__ size_t tl_offset(int tile, int ch, int r) {
   return (size_t)(tile * 2 + ch) * 4096 + (size_t)r * 4;
 }
-__device__ __forceinline__ void tl_ld32(const float* p, float* x) {
+// Offset of the first of the kCW components of column group g, row r.
+__device__ __forceinline__ size_t tl_offset_cw(int tile, int g, int r) {
+  const int c0 = kCW * g;
+  return (size_t)(tile * 2 + (c0 >> 5)) * 4096 + (size_t)((c0 & 31) >> 2) * 512 + (size_t)r * 4;
+}
+// the kCW components of a thread (kCW / 4 groups)
+__device__ __forceinline__ void tl_ldv(const float* p, float* x) {
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
+  for (int j = 0; j < kCW / 4; ++j) {
     const float4 q = *reinterpret_cast<const float4*>(p + j * 512);
     x[4 * j] = q.x; x[4 * j + 1] = q.y; x[4 * j + 2] = q.z; x[4 * j + 3] = q.w;
   }
 }
-__device__ __forceinline__ void tl_st32(float* p, const float* x) {
+__device__ __forceinline__ void tl_stv(float* p, const float* x) {
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
+  for (int j = 0; j < kCW / 4; ++j)
     *reinterpret_cast<float4*>(p + j * 512) = make_float4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
 }
-// half hf (components 16 hf .. 16 hf + 15) of the same
+// Part `part` (0 or 1) of the same: components kPart part .. kPart part + kPart - 1.
+constexpr int kPart = kCW / 2;
+__device__ __forceinline__ void tl_ldp(const float* p, int part, float* x) {
+#pragma unroll
+  for (int j = 0; j < kPart / 4; ++j) {
+    const float4 q = *reinterpret_cast<const float4*>(p + (part * (kPart / 4) + j) * 512);
+    x[4 * j] = q.x; x[4 * j + 1] = q.y; x[4 * j + 2] = q.z; x[4 * j + 3] = q.w;
+  }
+}
+__device__ __forceinline__ void tl_stp(float* p, int part, const float* x) {
+#pragma unroll
+  for (int j = 0; j < kPart / 4; ++j)
+    *reinterpret_cast<float4*>(p + (part * (kPart / 4) + j) * 512) =
+        make_float4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
+}
+// components 16 hf .. 16 hf + 15 of the same (hf < kCW / 16)
 __device__ __forceinline__ void tl_ld16(const float* p, int hf, float* x) {
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
@@ -516,8 +560,9 @@ __device__ __forceinline__ void epi_state_init(EpiState& e) {
   e.g = 0;
 }
 
-// Write this thread's 32 columns (its row r, column half ch) of an A chunk:
-// values x[0..31] for columns [32*ch, 32*ch+32) of the chunk, split in 3 pieces.
+// Write this thread's kCW columns (its row r, column group ch) of an A chunk:
+// values x[0 .. kCW) for columns [kCW*ch, kCW*ch + kCW) of the chunk, split in
+// 3 pieces.
 __device__ __forceinline__ bool epi_write_a(EpiState& e, Shared& sh, uint8_t* aring, int r, int ch,
                                             const float* x) {
   volatile int* verr = &sh.err;
@@ -525,10 +570,10 @@ __device__ __forceinline__ bool epi_write_a(EpiState& e, Shared& sh, uint8_t* ar
   if (!mbar_wait(&sh.a_empty[e.aslot], e.aph ^ 1, verr)) return false;
   uint8_t* base = aring + e.aslot * kASlotBytes;
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < kCW / 8; ++j) {
     uint4 hi, mid, lo;
     split3_bf16(x + 8 * j, hi, mid, lo);
-    const uint32_t off = sw128_offset(r, 4 * ch + j);
+    const uint32_t off = sw128_offset(r, (kCW / 8) * ch + j);
     *reinterpret_cast<uint4*>(base + off) = hi;
     *reinterpret_cast<uint4*>(base + 16384 + off) = mid;
     *reinterpret_cast<uint4*>(base + 32768 + off) = lo;
@@ -539,61 +584,67 @@ __device__ __forceinline__ bool epi_write_a(EpiState& e, Shared& sh, uint8_t* ar
   return true;
 }
 
-// Bias values of columns [n0, n0 + 32) of a layer with N outputs (zero past
+// Bias values of columns [n0, n0 + kCW) of a layer with N outputs (zero past
 // N), loaded together (vector loads where aligned) so that a single memory
 // round trip covers them; callers issue the next chunk's load before working
 // on the current one.
-__device__ __forceinline__ void load_bias32(const float* __restrict__ b, int n0, int N, float* out) {
+__device__ __forceinline__ void load_bias_cw(const float* __restrict__ b, int n0, int N, float* out) {
   const float* p = b + n0;
-  if (n0 + 32 <= N && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+  if (n0 + kCW <= N && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < kCW / 4; ++i) {
       const float4 q = __ldg(reinterpret_cast<const float4*>(p) + i);
       out[4 * i] = q.x; out[4 * i + 1] = q.y; out[4 * i + 2] = q.z; out[4 * i + 3] = q.w;
     }
   } else {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) out[i] = (n0 + i < N) ? __ldg(p + i) : 0.f;
+    for (int i = 0; i < kCW; ++i) out[i] = (n0 + i < N) ? __ldg(p + i) : 0.f;
   }
 }
 
-// v <- act(v + bias) on 32 columns starting at n0 (columns at or past N -> 0,
+// v <- act(v + bias) on kCW columns starting at n0 (columns at or past N -> 0,
 // the zero padding of the next GEMM's K dimension). The activation branch is
 // taken once per chunk, not per element.
-__device__ __forceinline__ void bias_act32(float* v, const float* bias, int act, int n0, int N) {
+__device__ __forceinline__ void bias_act_cw(float* v, const float* bias, int act, int n0, int N) {
   if (act == GBNDE_ACT_TANH) {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = tanh_tc(v[i] + bias[i]);
+    for (int i = 0; i < kCW; ++i) v[i] = tanh_tc(v[i] + bias[i]);
   } else if (act == GBNDE_ACT_SOFTPLUS) {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = act_apply_tc(v[i] + bias[i], GBNDE_ACT_SOFTPLUS);
+    for (int i = 0; i < kCW; ++i) v[i] = act_apply_tc(v[i] + bias[i], GBNDE_ACT_SOFTPLUS);
   } else {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] += bias[i];
+    for (int i = 0; i < kCW; ++i) v[i] += bias[i];
   }
-  if (n0 + 32 > N) {
+  if (n0 + kCW > N) {
 #pragma unroll
-    for (int i = 0; i < 32; ++i)
+    for (int i = 0; i < kCW; ++i)
       if (n0 + i >= N) v[i] = 0.f;
   }
 }
 
-// v <- v * act'(z) on 32 columns starting at n0, with act' taken from the
+// v <- v * act'(z) on kCW columns starting at n0, with act' taken from the
 // stored activation outputs y (tanh: 1 - y^2; softplus: 1 - exp(-y));
 // columns at or past N -> 0. The activation branch is taken once per chunk.
-__device__ __forceinline__ void deriv_mul32(float* v, const float* y, int act, int n0, int N) {
+__device__ __forceinline__ void deriv_mul_cw(float* v, const float* y, int act, int n0, int N) {
   if (act == GBNDE_ACT_TANH) {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] *= fmaf(-y[i], y[i], 1.f);
+    for (int i = 0; i < kCW; ++i) v[i] *= fmaf(-y[i], y[i], 1.f);
   } else if (act == GBNDE_ACT_SOFTPLUS) {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] *= -expm1f(-y[i]);
+    for (int i = 0; i < kCW; ++i) v[i] *= -expm1f(-y[i]);
   }
-  if (n0 + 32 > N) {
+  if (n0 + kCW > N) {
 #pragma unroll
-    for (int i = 0; i < 32; ++i)
+    for (int i = 0; i < kCW; ++i)
       if (n0 + i >= N) v[i] = 0.f;
   }
+}
+
+// TMEM -> registers: this warp's 32 lanes, kCW columns from taddr.
+__device__ __forceinline__ void tmem_ld_cw(uint32_t taddr, float* v) {
+  if constexpr (kCW == 32) tmem_ld32(taddr, v);
+  else tmem_ld16(taddr, v);
 }
 
 // Skip A-ring slots that the producer warp fills (weight-gradient ops).
