@@ -247,6 +247,149 @@ class Form:
         return tot
 
 
+# ---------------------------------------------------------------------------
+# The other workloads, each through the host API a user calls (host arrays in
+# and out, copies included), a few evaluations each: latency of the batch-1
+# spiral fit, FFJORD at d = 16 / B = 65536, and uneven multiple shooting.
+# The BF16 form covers widths <= 256 and no time input, so these run the FP32
+# form.
+# ---------------------------------------------------------------------------
+def _timed(fn, n):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(n):
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    return sorted(ts)[len(ts) // 2]
+
+
+def _kernel_ms(solver):
+    import ctypes as C
+    fm, bm = C.c_double(), C.c_double()
+    solver.lib.gbnde_last_kernel_ms(solver.h, C.byref(fm), C.byref(bm))
+    return fm.value, bm.value
+
+
+def aux_spiral(device):
+    """cube -> Dense(2, 50, tanh) -> Dense(50, 2), u0 = [2, 0], tspan (0, 1.5),
+    30 save points, Tsit5 1e-7 / 1e-5, SSE loss, InterpolatingAdjoint; batch 1."""
+    import gbnde
+    rng = np.random.default_rng(0)
+    model = gbnde.Chain(gbnde.cube(), gbnde.Dense(2, 50, "tanh"), gbnde.Dense(50, 2))
+    p = model.init_params(rng)
+    ts = np.linspace(0.0, 1.5, 30)
+    node = gbnde.NeuralODE(model, (0.0, 1.5), gbnde.Tsit5("fp32"), saveat=ts, abstol=1e-7,
+                           reltol=1e-5, sensealg=gbnde.InterpolatingAdjoint())
+    s = node.solver
+    s.set_params(p)
+    from scipy.integrate import solve_ivp
+    u0 = np.array([[2.0], [0.0]], np.float32)
+    A = np.array([[-0.1, 2.0], [-2.0, -0.1]])
+    # target: du/dt = A^T u.^3 (docs/src/examples/neural_ode.md:24-30) at 1e-10
+    sol = solve_ivp(lambda t, u: A.T @ u ** 3, (0.0, 1.5), [2.0, 0.0], method="DOP853", t_eval=ts,
+                    rtol=1e-10, atol=1e-10)
+    tgt = sol.y[:, None, :].astype(np.float32)
+    out = {}
+
+    def step():
+        us, st = s.forward(u0, node.desc())
+        du0, dp, sb = s.backward((2.0 * (us - tgt)).astype(np.float32))
+        out["st"], out["sb"] = st, sb
+    sec = _timed(step, 20)
+    kf, kb = _kernel_ms(s)
+    return {"workload": "spiral_b1_s2_cube_h50_nsave30", "latency_ms": 1000.0 * sec,
+            "fwd_kernel_ms": kf, "bwd_kernel_ms": kb,
+            "unit": "ms per gradient evaluation (forward + adjoint, host API)", "precision": "fp32",
+            "nf_fwd": out["st"].nf, "nf_adj": out["sb"].nf_adj,
+            "note": "batch 1: latency-bound (launch and controller round trips), no roofline"}
+
+
+def aux_ffjord(device, B=65536, d=16, H=512):
+    """FFJORD, (d+1) -> H -> H -> d softplus with time input, B samples of a
+    seeded 8-component Gaussian mixture, Hutchinson trace, Tsit5 1e-5 / 1e-5;
+    negative log-likelihood and its adjoint gradient."""
+    import gbnde
+    rng = np.random.default_rng(3)
+    means = 2.0 * rng.standard_normal((8, d))
+    var = rng.uniform(0.2, 1.0, (8, d))
+    comp = rng.integers(0, 8, B)
+    x = (means[comp] + np.sqrt(var[comp]) * rng.standard_normal((B, d))).T.astype(np.float32)
+    model = gbnde.Chain(gbnde.Dense(d + 1, H, "softplus"), gbnde.Dense(H, H, "softplus"), gbnde.Dense(H, d))
+    p = model.init_params(rng)
+    fj = gbnde.FFJORD(model, (0.0, 1.0), (d,), gbnde.Tsit5("fp32"), abstol=1e-5, reltol=1e-5,
+                      time_input=True)
+    noise = fj.draw_noise(rng, B)
+    out = {}
+    g = (-np.ones(B) / B).astype(np.float32)
+
+    def step():
+        logpx, zT, st = fj.forward_np(x, p, noise)
+        dx, dp, sb = fj.backward_np(g)
+        out["st"], out["sb"], out["nll"] = st, sb, -float(np.mean(logpx))
+    sec = _timed(step, 2)
+    kf, kb = _kernel_ms(fj.solver)
+    st, sb = out["st"], out["sb"]
+    F = gemm_flops_per_rhs([d + 1, H, H, d], B)
+    # forward RHS = MLP + one VJP (2F with the VJP's two products ~ 3F); the
+    # adjoint RHS counted as 4F (recompute, VJP, double backward)
+    flops = 3 * F * st.nf + 4 * F * sb.nf_adj
+    return {"workload": f"ffjord_b{B}_d{d}_h{H}x2_softplus", "value": 1.0 / sec, "unit": "grad_evals/s",
+            "ms_per_eval": 1000.0 * sec, "precision": "fp32", "nf_fwd": st.nf, "nf_adj": sb.nf_adj,
+            "nll": out["nll"], "gemm_tflops_per_s": flops / sec / 1e12,
+            "fwd_kernel_ms": kf, "bwd_kernel_ms": kb,
+            "note": "host API (x, noise, logpx, gradients through host memory); FP32 SIMT kernels"}
+
+
+def aux_multishoot(device, ntraj=256, S=32, H=128):
+    """Multiple shooting: ntraj trajectories of the oscillator network
+    du/dt = -0.1 u + W tanh(u), W ~ N(0, 1/S), n_i ~ U{40..400} points at
+    dt = 0.05, group sizes U{5..40}, continuity weight 100, MSE; every group of
+    every trajectory in one launch; the loss gradient through the library's
+    discrete adjoint."""
+    import torch
+    from scipy.integrate import solve_ivp
+
+    import gbnde
+    rng = np.random.default_rng(4)
+    W = rng.standard_normal((S, S)) / np.sqrt(S)
+    n = rng.integers(40, 401, ntraj)
+    gs = rng.integers(5, 41, ntraj)
+    T = 0.05 * (int(n.max()) - 1)
+    y0 = rng.standard_normal((S, ntraj))
+
+    def f(t, y):
+        u = y.reshape(S, ntraj)
+        return (-0.1 * u + W @ np.tanh(u)).ravel()
+    tall = 0.05 * np.arange(int(n.max()))
+    sol = solve_ivp(f, (0.0, T), y0.ravel(), method="DOP853", t_eval=tall, rtol=1e-8, atol=1e-10)
+    Y = sol.y.reshape(S, ntraj, -1)
+    trajs = [(Y[:, k, :n[k]].astype(np.float32), tall[:n[k]], int(gs[k])) for k in range(ntraj)]
+    model = gbnde.Chain(gbnde.Dense(S, H, "tanh"), gbnde.Dense(H, H, "tanh"), gbnde.Dense(H, S))
+    p0 = torch.from_numpy(model.init_params(rng))
+    solver = gbnde.Solver(model, "fp32", device)
+    mse = lambda u, uh: ((u - uh) ** 2).mean()  # noqa: E731
+    out = {}
+
+    def step():
+        p = p0.clone().requires_grad_(True)
+        loss, _ = gbnde.multiple_shoot_batch(p, trajs, solver, mse, abstol=1e-6, reltol=1e-3)
+        loss.backward()
+        out["loss"] = float(loss)
+    sec = _timed(step, 3)
+    kf, kb = _kernel_ms(solver)
+    nseg = sum(len(gbnde.group_ranges(int(n[k]), int(gs[k]))) for k in range(ntraj))
+    return {"workload": f"multishoot_{ntraj}traj_s{S}_h{H}x2_uneven", "value": 1.0 / sec,
+            "unit": "grad_evals/s", "ms_per_eval": 1000.0 * sec, "precision": "fp32",
+            "segments": nseg, "points": int(n.sum()), "loss": out["loss"],
+            "fwd_kernel_ms": kf, "bwd_kernel_ms": kb,
+            "note": "host API: packing, loss and continuity terms in torch on the host, the packed "
+                    "segments in one forward and one adjoint launch"}
+
+
 def profiled_traffic(kernel, workload_name):
     """DRAM bytes per launch of `kernel` on `workload_name` from the committed
     ncu summaries: a line `traffic_bytes_per_launch <kernel> <workload> = N`."""
@@ -428,6 +571,15 @@ def run_gpu(args):
                         "oracle to ~1e-6, so the differences bound the BF16 form's error"}
         del f32
 
+    aux = None
+    if rank == 0 and not args.no_aux:
+        aux = {}
+        for name, fn in (("spiral", aux_spiral), ("ffjord", aux_ffjord), ("multiple_shooting", aux_multishoot)):
+            try:
+                aux[name] = fn(local)
+            except Exception as e:  # reported, never silently dropped
+                aux[name] = {"error": f"{type(e).__name__}: {e}"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, el, n, cores = cpu_reference(wl, args.cpu_sample, max_seconds=args.cpu_seconds)
@@ -448,6 +600,7 @@ def run_gpu(args):
         "gpu_launches": args.steps * Form.LAUNCHES_PER_EVAL,
         "fp32_form": fp32,
         "graph_train_step": graph,
+        "other_workloads": aux,
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk,
@@ -477,6 +630,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32-form", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-aux", action="store_true", help="skip the spiral, FFJORD and multiple-shooting figures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
