@@ -304,14 +304,12 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         uint32_t col;
         if (!tc::epi_wait_acc(es, sh, &col)) return false;
         const int nch = (N + 63) / 64;
-        float bnext[tc::kCW];
-        tc::load_bias_cw(b, tc::kCW * th.ch, N, bnext);
+        // (the bias is loaded just before use: prefetching it a chunk ahead
+        // costs registers the epilogue does not have, measured slower)
         for (int cc = 0; cc < nch; ++cc) {
           const int n0 = 64 * cc + tc::kCW * th.ch;
           float bc[tc::kCW];
-#pragma unroll
-          for (int i = 0; i < tc::kCW; ++i) bc[i] = bnext[i];
-          if (cc + 1 < nch) tc::load_bias_cw(b, n0 + 64, N, bnext);
+          tc::load_bias_cw(b, n0, N, bc);
           tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
           tc::bias_act_cw(v, bc, m.act[l], n0, N);
           hs_stv(hs4, (A.hoff[l + 1] + tc::kCW * cc) / 4, v);
@@ -340,18 +338,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       for (int l = L - 1; l >= 1; --l) {
         const int N = m.dims[l];
         const int nch = (N + 63) / 64;
-        // the stored activations of this layer are known before the
-        // accumulator: fetch chunk 0 now and chunk cc+1 while working on cc
-        float hnext[tc::kCW];
-        hs_ldv(hs4, A.hoff[l] / 4, hnext);
+        // the stored activations are loaded per chunk just before use (a
+        // chunk-ahead prefetch costs registers and measured slower)
         uint32_t col;
         if (!tc::epi_wait_acc(es, sh, &col)) return false;
         for (int cc = 0; cc < nch; ++cc) {
           const int n0 = 64 * cc + tc::kCW * th.ch;
           float h[tc::kCW];
-#pragma unroll
-          for (int i = 0; i < tc::kCW; ++i) h[i] = hnext[i];
-          if (cc + 1 < nch) hs_ldv(hs4, (A.hoff[l] + tc::kCW * (cc + 1)) / 4, hnext);
+          hs_ldv(hs4, (A.hoff[l] + tc::kCW * cc) / 4, h);
           tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
           tc::deriv_mul_cw(v, h, m.act[l - 1], n0, N);
           if (!emit(es, sh, aring, th, v)) return false;

@@ -114,14 +114,10 @@ __device__ __forceinline__ bool epi_rhs(const FwdTcArgs& A, tc::EpiState& e, tc:
     uint32_t col;
     if (!tc::epi_wait_acc(e, sh, &col)) return false;
     const int nch = (N + 63) / 64;
-    float bnext[tc::kCW];
-    tc::load_bias_cw(b, tc::kCW * th.ch, N, bnext);
     for (int c = 0; c < nch; ++c) {
       float v[tc::kCW], bc[tc::kCW];
       const int n0 = 64 * c + tc::kCW * th.ch;
-#pragma unroll
-      for (int i = 0; i < tc::kCW; ++i) bc[i] = bnext[i];
-      if (c + 1 < nch) tc::load_bias_cw(b, n0 + 64, N, bnext);
+      tc::load_bias_cw(b, n0, N, bc);
       tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
       tc::bias_act_cw(v, bc, act, n0, N);
       if (!tc::epi_write_a(e, sh, aring, th.r, th.ch, v)) return false;
