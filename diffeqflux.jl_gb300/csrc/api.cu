@@ -177,7 +177,7 @@ struct gbnde_ctx {
   int npadT[GBNDE_MAX_LAYERS] = {}, nchunkT[GBNDE_MAX_LAYERS] = {};
   bool tc_shape_ok = false;
   bool tc_bwd_ok = false;  // tensor-core adjoint covers this model
-  DBuf timg, thscr, tbpart, tmucomp, tlamcomp;
+  DBuf timg, thscr, tmucomp, tlamcomp;
   DBuf tr_us, tr_dl, tr_du0, tr_dp;  // training-step scratch
   // graph-mode training step
   bool recording = false;
@@ -331,7 +331,7 @@ void gbnde_destroy(gbnde_ctx* c) {
                   &c->bnd_d, &c->dldu, &c->dldu0, &c->dldp, &c->lam, &c->ub, &c->kl, &c->ku,
                   &c->ibuf, &c->mu_acc, &c->mu_stage, &c->iv_d, &c->bsync, &c->bcounters,
                   &c->loss_part, &c->wimg, &c->comp, &c->dense, &c->timg, &c->thscr,
-                  &c->tbpart, &c->tmucomp, &c->tlamcomp, &c->ms_segs, &c->ms_saveat, &c->ms_u0,
+                  &c->tmucomp, &c->tlamcomp, &c->ms_segs, &c->ms_saveat, &c->ms_u0,
                   &c->ms_usave, &c->ms_dense, &c->ms_steplog, &c->ms_nacc, &c->ms_ret, &c->ms_cnt,
                   &c->ms_dldu, &c->ms_dldu0, &c->ms_bar, &c->ms_mu, &c->ms_dldp, &c->ffnoise,
                   &c->ffu0, &c->ffus, &c->tr_us, &c->tr_dl, &c->tr_du0, &c->tr_dp};
@@ -777,14 +777,13 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   int r = 0;
   if ((r = c->timg.ensure((size_t)grid * tc::kImgSlots * t.img_cta)) ||
       (r = c->thscr.ensure((size_t)grid * tc::kEpiThreads * t.hvals * 4)) ||
-      (r = c->tbpart.ensure((size_t)grid * 4 * t.nbias * 4)) ||
       (r = c->tmucomp.ensure((size_t)grid * P * 4)) || (r = c->tlamcomp.ensure(2 * SBt * 4)) ||
       (r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4)))
     return r;
   // per-CTA quadrature slots padded to a multiple of 4 floats (float4 sweeps)
   const int Ppad = (P + 3) / 4 * 4;
   t.b.P = Ppad;
-  if ((r = c->mu_acc.ensure((size_t)grid * Ppad * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * t.nbias * 4)) ||
+  if ((r = c->mu_acc.ensure((size_t)grid * Ppad * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * 4 * t.nbias * 4)) ||
       (r = c->tmucomp.ensure((size_t)grid * Ppad * 4)))
     return r;
   t.b.mu_acc = c->mu_acc.as<float>();
@@ -792,7 +791,6 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   t.pbias = c->mu_stage.as<float>();
   t.img = c->timg.as<uint8_t>();
   t.hscr = c->thscr.as<float>();
-  t.bpart = c->tbpart.as<float>();
   t.mu_comp = c->tmucomp.as<float>();
   t.lam_comp[0] = c->tlamcomp.as<float>();
   t.lam_comp[1] = c->tlamcomp.as<float>() + SBt;

@@ -230,12 +230,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     uint8_t* img = A.img + (size_t)blockIdx.x * tc::kImgSlots * A.img_cta;
     int fs = 0;
     float4* hs4 = reinterpret_cast<float4*>(A.hscr + (size_t)blockIdx.x * tc::kEpiThreads * A.hvals);
-    float* bpart = A.bpart + (size_t)blockIdx.x * 4 * A.nbias;
     float* mu_acc = a.mu_acc + (size_t)blockIdx.x * a.P;
     float* mu_comp = A.mu_comp + (size_t)blockIdx.x * a.P;
-    // pending bias quadrature (nbias floats each): stage 1, stages 2..6, stage 7
-    float* Pb[3] = {A.pbias + (size_t)blockIdx.x * 3 * A.nbias, A.pbias + ((size_t)blockIdx.x * 3 + 1) * A.nbias,
-                    A.pbias + ((size_t)blockIdx.x * 3 + 2) * A.nbias};
+    // pending bias quadrature: stage 1, stages 2..6, stage 7; each holds one
+    // nbias row per 32-row group of the tile (rows q = warp % 4), into which
+    // that group's warps add their column sums (one adder per element, so the
+    // sums are deterministic); the step commit adds the four rows
+    float* Pb[3] = {A.pbias + (size_t)blockIdx.x * 12 * A.nbias, A.pbias + ((size_t)blockIdx.x * 12 + 4) * A.nbias,
+                    A.pbias + ((size_t)blockIdx.x * 12 + 8) * A.nbias};
     int iP1 = 0, iP7 = 2;
     float* Pmid = Pb[1];
     tc::CmdPoster cmdp;
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       for (size_t i = threadIdx.x; i < (size_t)a.P / 4; i += tc::kEpiThreads) p4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     };
     auto zero_bias = [&](float* p) {
-      for (int i = threadIdx.x; i < A.nbias; i += tc::kEpiThreads) p[i] = 0.f;
+      for (int i = threadIdx.x; i < 4 * A.nbias; i += tc::kEpiThreads) p[i] = 0.f;
     };
 
     // scratch images start at zero (padding rows/blocks are never written)
@@ -332,7 +334,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
 #pragma unroll
         for (int i = 0; i < tc::kCW; ++i) w[i] = v[i];
         const float s = warp_colsum(w, th.lane);
-        if (th.lane < tc::kCW) bpart[th.q * A.nbias + A.boffp[L - 1] + tc::kCW * th.ch + th.lane] = s;
+        if (th.lane < tc::kCW) tc::red_add(P + th.q * A.nbias + A.boffp[L - 1] + tc::kCW * th.ch + th.lane, s);
       }
       // VJP chain
       for (int l = L - 1; l >= 1; --l) {
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           if (!emit(es, sh, aring, th, v)) return false;
           if (P) {
             const float s = warp_colsum(v, th.lane);
-            if (th.lane < tc::kCW) bpart[th.q * A.nbias + A.boffp[l - 1] + n0 + th.lane] = s;
+            if (th.lane < tc::kCW) tc::red_add(P + th.q * A.nbias + A.boffp[l - 1] + n0 + th.lane, s);
           }
         }
         tc::epi_release_acc(es, sh);
@@ -371,15 +373,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           for (int i = 0; i < tc::kCW; ++i) kl[i] *= 3.f * xc[i] * xc[i];
         }
         tc::epi_release_acc(es, sh);
-      }
-      if (P) {
-        tc::epi_bar();
-        for (int f = threadIdx.x; f < A.nbias; f += tc::kEpiThreads) {
-          // the column sums already carry the stage weight
-          const float s = ((bpart[f] + bpart[A.nbias + f]) + bpart[2 * A.nbias + f]) + bpart[3 * A.nbias + f];
-          tc::red_add(P + f, s);
-        }
-        tc::epi_bar();
       }
       return true;
     };
@@ -482,7 +475,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         while (l + 1 < L && f >= A.boffp[l + 1]) ++l;
         const int o = f - A.boffp[l];
         if (o < m.dims[l + 1])
-          kahan(mu_acc[m.boff[l] + o], mu_comp[m.boff[l] + o], Hf * (__ldcg(P1 + f) + __ldcg(Pmid + f)));
+          kahan(mu_acc[m.boff[l] + o], mu_comp[m.boff[l] + o],
+                Hf * ((((__ldcg(P1 + f) + __ldcg(P1 + A.nbias + f)) + __ldcg(P1 + 2 * A.nbias + f)) +
+                       __ldcg(P1 + 3 * A.nbias + f)) +
+                      (((__ldcg(Pmid + f) + __ldcg(Pmid + A.nbias + f)) + __ldcg(Pmid + 2 * A.nbias + f)) +
+                       __ldcg(Pmid + 3 * A.nbias + f))));
       }
       tc::epi_bar();
       return true;
@@ -506,25 +503,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
 #pragma unroll
       for (int hf = 0; hf < 2; ++hf) {
         const float* sp = slot + g;
-        float v4[4][tc::kPart], acc[tc::kPart];
+        float v8[8][tc::kPart];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) tc::tl_ldp(sp + (size_t)j * SBt, hf, v4[j]);
+        for (int j = 0; j < 8; ++j) tc::tl_ldp(sp + (size_t)j * SBt, hf, v8[j]);
 #pragma unroll
         for (int q = 0; q < tc::kPart; ++q) {
           float e = 0.f;
 #pragma unroll
-          for (int j = 0; j < 3; ++j) e = fmaf(hb[j], v4[j + 1][q], e);
-          acc[q] = e;
-          x[tc::kPart * hf + q] = v4[0][q];
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) tc::tl_ldp(sp + (size_t)(j + 4) * SBt, hf, v4[j]);
-#pragma unroll
-        for (int q = 0; q < tc::kPart; ++q) {
-          float e = acc[q];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) e = fmaf(hb[j + 3], v4[j][q], e);
-          x[tc::kPart * hf + q] += e;
+          for (int j = 0; j < 7; ++j) e = fmaf(hb[j], v8[j + 1][q], e);
+          x[tc::kPart * hf + q] = v8[0][q] + e;
         }
       }
     };

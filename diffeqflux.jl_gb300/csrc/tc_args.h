@@ -21,7 +21,7 @@ struct BwdTcArgs {
   tc::OpList ops;               // one adjoint evaluation: forward recompute + VJP chain
   tc::OpList dwops;             // one accepted step: stage-stacked weight-gradient ops
   int dw_chunks;                // K chunks of all dwops (A-ring slots the producer fills)
-  float* pbias;                 // [grid][3][nbias] pending bias quadrature: stage 1, 2..6, 7
+  float* pbias;                 // [grid][3][4][nbias] pending bias quadrature: stage 1, 2..6, 7 (x 4 row groups)
   const float* bias[GBNDE_MAX_LAYERS];
   float* lam_comp[2];           // compensation of lam
   float* mu_comp;               // [grid][P] Kahan compensation of mu_acc
@@ -36,9 +36,8 @@ struct BwdTcArgs {
   long long doff[GBNDE_MAX_LAYERS];  // image offset of delta_{l+1} (l = 0..L-1)
   int a_isA[GBNDE_MAX_LAYERS];       // 1: a_l is the A operand (rows = in) of layer l's dW
   int nh[GBNDE_MAX_LAYERS];          // M halves (128 rows) of layer l's dW
-  float* bpart;                 // [grid][4][nbias] bias partial sums
   int nbias;
-  int boffp[GBNDE_MAX_LAYERS];  // offset of layer l's bias inside bpart rows
+  int boffp[GBNDE_MAX_LAYERS];  // offset of layer l's bias inside a pending-bias row
 };
 
 
