@@ -47,16 +47,22 @@ def workload_name(B):
     return f"neuralode_b{B}_s64_h256x2_tanh_nsave20"
 
 
+def glorot_params(dims, rng):
+    """Flat parameters of Dense layers dims[0] -> ... -> dims[-1]: Glorot-uniform
+    weights (column-major out x in, the ComponentArray order) and zero biases."""
+    parts = []
+    for i in range(len(dims) - 1):
+        lim = np.sqrt(6.0 / (dims[i] + dims[i + 1]))
+        W = rng.uniform(-lim, lim, size=(dims[i + 1], dims[i]))
+        parts += [W.T.reshape(-1), np.zeros(dims[i + 1])]
+    return np.concatenate(parts).astype(np.float32)
+
+
 def workload(S=64, H=256, B=16384, nsave=20, seed=1):
     from scipy.linalg import expm
     rng = np.random.default_rng(seed)
     dims = [S, H, H, S]
-    parts = []
-    for i in range(3):
-        lim = np.sqrt(6.0 / (dims[i] + dims[i + 1]))
-        W = rng.uniform(-lim, lim, size=(dims[i + 1], dims[i]))
-        parts += [W.T.reshape(-1), np.zeros(dims[i + 1])]
-    p = np.concatenate(parts).astype(np.float32)
+    p = glorot_params(dims, rng)
     u0 = rng.standard_normal((S, B)).astype(np.float32)
     Q, _ = np.linalg.qr(rng.standard_normal((S, S)))
     M = Q @ np.diag(-rng.uniform(0.1, 2.0, S)) @ Q.T
@@ -390,6 +396,125 @@ def aux_multishoot(device, ntraj=256, S=32, H=128):
                     "segments in one forward and one adjoint launch"}
 
 
+# ---------------------------------------------------------------------------
+# Sweep over (state, hidden width, batch): the training iteration (forward,
+# fused MSE, adjoint, Adam) replayed as one CUDA graph per step, FP32 form
+# with autotuned tiles and BF16 form where the engine covers the shape, and
+# the FP64 oracle on a small sample of the same point. Bounded: a few steps
+# per point (the configuration's 200 Adam steps are the same iteration).
+# ---------------------------------------------------------------------------
+SWEEP_S = (16, 64, 256)
+SWEEP_H = (128, 512, 1024)
+SWEEP_B = (1024, 16384, 262144)
+
+
+def sweep_data(S, H, B, dev, seed=5, nsave=20):
+    """u0 ~ N(0, 1), Glorot weights, targets of du/dt = M u with
+    M = Q diag(-U(0.1, 2)) Q^T (exp(M t) from scipy, the products on the GPU)."""
+    import torch
+    from scipy.linalg import expm
+    rng = np.random.default_rng(seed)
+    dims = [S, H, H, S]
+    p = glorot_params(dims, rng)
+    Q, _ = np.linalg.qr(rng.standard_normal((S, S)))
+    M = Q @ np.diag(-rng.uniform(0.1, 2.0, S)) @ Q.T
+    ts = np.linspace(0.0, 1.0, nsave)
+    g = torch.Generator(device=dev).manual_seed(seed)
+    u0 = torch.randn((B, S), generator=g, device=dev, dtype=torch.float32)  # column-major S x B
+    E = torch.from_numpy(np.stack([expm(M * t) for t in ts]).astype(np.float32)).to(dev)
+    tg = torch.matmul(u0.unsqueeze(0), E.transpose(1, 2)).contiguous()      # nsave x B x S
+    return dims, p, ts, u0, tg, E
+
+
+def sweep_point(S, H, B, prec, dev, warmup, steps, tune):
+    import torch
+
+    import gbnde
+    dims, p, ts, u0, tg, E = sweep_data(S, H, B, dev)
+    model = gbnde.Chain(gbnde.Dense(S, H, "tanh"), gbnde.Dense(H, H, "tanh"), gbnde.Dense(H, S))
+    solver = gbnde.Solver(model, prec, dev.index or 0)
+    desc = gbnde.Solver.solve_desc(0.0, 1.0, ts, 1e-7, 1e-5, 0)
+    out = {"precision": prec}
+    pd = torch.from_numpy(p).to(dev)
+    solver.set_params_device(pd)
+    if tune:
+        out["tile_rows"] = list(solver.autotune(u0, desc, S, B))
+    m, v = torch.zeros_like(pd), torch.zeros_like(pd)
+    graphed = []
+    for k in range(warmup):
+        solver.graph_train_step(u0, tg, desc, S, B, pd, m, v, 1 + k, lr=1e-3, kind=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        loss, st, gd = solver.graph_train_step(u0, tg, desc, S, B, pd, m, v, 1 + warmup + k, lr=1e-3, kind=1)
+        graphed.append(gd)
+    torch.cuda.synchronize()
+    sec = (time.perf_counter() - t0) / steps
+    F = gemm_flops_per_rhs(dims, B)
+    flops = F * (st.nf + st.nf_recompute + 3 * st.nf_adj)
+    out.update({"value": 1.0 / sec, "unit": "train_steps/s", "ms_per_step": 1000.0 * sec,
+                "steps": steps, "replayed_as_graph": all(graphed), "loss": loss,
+                "nf_fwd": st.nf, "nf_adj": st.nf_adj, "gemm_tflops_per_s": flops / sec / 1e12})
+    if prec == "bf16":
+        # a step of seconds-long loops: against the sustained measured peak
+        peak = measured_peaks().get("bf16_tflops_sustained")
+        if peak:
+            out["frac_of_bf16_peak_sustained"] = flops / sec / 1e12 / peak
+    solver.close()
+    return out, (dims, p, ts, u0, tg)
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def run_sweep(args):
+    """One JSON line per (state, hidden, batch) point."""
+    import torch
+    dev = torch.device("cuda", 0)
+    pts = [(S, H, B) for B in SWEEP_B for S in SWEEP_S for H in SWEEP_H]
+    if args.sweep_max_batch:
+        pts = [x for x in pts if x[2] <= args.sweep_max_batch]
+    for S, H, B in pts:
+        line = {"sweep_point": {"state": S, "hidden": H, "batch": B}, "data": "synthetic (seeded)",
+                "config": "NeuralODE S -> H -> H -> S tanh, tspan (0, 1), 20 saves, Tsit5 1e-7 / 1e-5, "
+                          "MSE to a random stable linear ODE, InterpolatingAdjoint, Adam lr 1e-3"}
+        big = B > 16384
+        # the first graph step runs eagerly and captures, later ones replay;
+        # at B = 262144 a step takes seconds, so one replayed step is timed
+        warm, steps = (1, 1) if big else (2, 5)
+        data = None
+        for prec in ("fp32", "bf16"):
+            if prec == "bf16" and not (S <= 64 and H <= 256):
+                line["bf16"] = {"unsupported": "the tensor-core engine covers state <= 64 and widths <= 256"}
+                continue
+            try:
+                r, data = sweep_point(S, H, B, prec, dev, warm, steps, tune=(prec == "fp32" and not big))
+                line[prec] = r
+            except Exception as e:  # reported per point
+                line[prec] = {"error": f"{type(e).__name__}: {e}"}
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+        if "value" in line.get("fp32", {}) and "value" in line.get("bf16", {}):
+            line["bf16_over_fp32"] = line["bf16"]["value"] / line["fp32"]["value"]
+        if data is not None and not args.no_cpu:
+            dims, p, ts, u0, tg = data
+            n = min(32, B)
+            wl = {"dims": dims, "p": p, "ts": ts, "abstol": 1e-7, "reltol": 1e-5, "B": B,
+                  "u0": u0[:n].T.cpu().numpy(), "target": tg[:, :n, :].permute(2, 1, 0).cpu().numpy()}
+            v, el, ne, cores = cpu_reference(wl, n, max_seconds=3.0)
+            line["cpu_oracle"] = {"value": v, "unit": "grad_evals/s", "cores": cores, "kind": "port",
+                                  "sample": f"{n} of {B} trajectories, {ne} evaluation(s) in {el:.1f} s, "
+                                            f"scaled linearly to the batch"}
+        del data
+        torch.cuda.empty_cache()
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def profiled_traffic(kernel, workload_name):
     """DRAM bytes per launch of `kernel` on `workload_name` from the committed
     ncu summaries: a line `traffic_bytes_per_launch <kernel> <workload> = N`."""
@@ -505,11 +630,7 @@ def run_gpu(args):
         e_ms = float(t.item())
     e2e = world * args.steps / (e_ms / 1000.0)
 
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
+    peaks = measured_peaks()
     peak_tf = peaks.get("bf16_tflops", 1900.0)
     peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
     bwd_ms_avg = k_bwd / args.steps
@@ -631,9 +752,13 @@ def main():
     ap.add_argument("--no-fp32-form", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-aux", action="store_true", help="skip the spiral, FFJORD and multiple-shooting figures")
+    ap.add_argument("--sweep", action="store_true", help="state x hidden x batch sweep, one JSON line per point")
+    ap.add_argument("--sweep-max-batch", type=int, default=0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.sweep:
+        return run_sweep(args)
     return run_gpu(args)
 
 

@@ -225,7 +225,11 @@ int choose_tm(int maxdim_rows_total, size_t budget, int* TM) {
   return -1;
 }
 
-constexpr size_t kSmemBudget = 200 * 1024;
+// dynamic shared memory of the FP32 kernels: the 227 KB a CTA may hold, less
+// 1 KB for their static reduction arrays
+constexpr size_t kSmemBudget = 227 * 1024 - 1024;
+// the packed multiple-shooting kernels hold more static shared memory
+constexpr size_t kSmemBudgetMs = 200 * 1024;
 
 }  // namespace
 
@@ -462,11 +466,13 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   const int frows = c->ff_on ? 2 * sumdims + c->mlp.maxdim + 1 : 2 * c->mlp.maxdim;
   int TM = 0;
   if (choose_tm(frows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "layer too wide");
+  while (TM > 8 && TM / 2 >= B) TM /= 2;  // small batches: no tile rows past the batch
   {
     int want = c->tm_force_fwd;
     auto it = c->tuned.find({S, B});
     if (!want && it != c->tuned.end()) want = it->second.first;
     if (want > 0 && (size_t)frows * (want + 4) * sizeof(float) <= kSmemBudget) TM = want;
+    else if (c->tm_force_fwd) return fail(GBNDE_ERR_UNSUPPORTED, "%d tile rows do not fit", want);
   }
   const int LD = TM + 4;
   const size_t smem = (size_t)frows * LD * sizeof(float);
@@ -903,11 +909,13 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   rows = c->ff_on ? 2 * rows + 4 * c->mlp.maxdim + 1 : rows + 2 * c->mlp.maxdim + S;
   int TM = 0;
   if (choose_tm(rows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "network too wide");
+  while (TM > 8 && TM / 2 >= B) TM /= 2;
   {
     int want = c->tm_force_bwd;
     auto it = c->tuned.find({S, B});
     if (!want && it != c->tuned.end()) want = it->second.second;
     if (want > 0 && (size_t)rows * (want + 4) * sizeof(float) <= kSmemBudget) TM = want;
+    else if (c->tm_force_bwd) return fail(GBNDE_ERR_UNSUPPORTED, "%d tile rows do not fit", want);
   }
   const int LD = TM + 4;
   const size_t smem = (size_t)rows * LD * sizeof(float);
@@ -1087,7 +1095,7 @@ int gbnde_multishoot_forward(gbnde_ctx* c, int S, int nseg, const gbnde_segment*
   c->ms_MS = 256;
   const size_t SN = (size_t)S * nseg;
   int TM = 0;
-  if (choose_tm(2 * c->mlp.maxdim, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "layer too wide");
+  if (choose_tm(2 * c->mlp.maxdim, kSmemBudgetMs, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "layer too wide");
   TM = std::min(TM, 64);
   const size_t smem = (size_t)2 * c->mlp.maxdim * (TM + 4) * sizeof(float);
   int r = 0;
@@ -1150,7 +1158,7 @@ int gbnde_multishoot_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, flo
   for (int l = 0; l <= c->mlp.nlayers; ++l) rows += c->mlp.dims[l];
   rows = c->ff_on ? 2 * rows + 4 * c->mlp.maxdim + 1 : rows + 2 * c->mlp.maxdim + S;
   int TM = 0;
-  if (choose_tm(rows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "network too wide");
+  if (choose_tm(rows, kSmemBudgetMs, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "network too wide");
   TM = std::min(TM, 64);
   const size_t smem = (size_t)rows * (TM + 4) * sizeof(float);
   MsArgs m = ms_args(c, TM);
