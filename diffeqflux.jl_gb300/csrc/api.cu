@@ -187,6 +187,7 @@ struct gbnde_ctx {
   DBuf gstat;               // device: loss (double), Adam coefficients (2 doubles), flags (ints)
   double* gpin = nullptr;   // pinned host mirror of the Adam coefficients
   bool graph_failed = false;
+  int f32time = 0;  // Float32 time of the last forward solve (its adjoint follows)
   // autotuner (FP32 kernels): rows per tile chosen by timing, per (S, B)
   int tm_force_fwd = 0, tm_force_bwd = 0;
   std::map<std::pair<int, int>, std::pair<int, int>> tuned;
@@ -439,6 +440,9 @@ static int validate_desc(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B) 
       d->sensealg != GBNDE_SENSE_GAUSS)
     return fail(GBNDE_ERR_INVALID, "unknown sensealg %d", d->sensealg);
   if ((long long)B * S > (1LL << 31)) return fail(GBNDE_ERR_UNSUPPORTED, "S*B too large");
+  if (d->flags & ~GBNDE_FLAG_FP32_TIME) return fail(GBNDE_ERR_INVALID, "unknown flags 0x%x", d->flags);
+  if ((d->flags & GBNDE_FLAG_FP32_TIME) && c->precision != GBNDE_PREC_FP32)
+    return fail(GBNDE_ERR_UNSUPPORTED, "Float32 time is a mode of the FP32 form");
   return 0;
 }
 
@@ -551,6 +555,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   a.abstol = d->abstol;
   a.reltol = d->reltol;
   a.dt0 = d->dt0;
+  a.f32time = (d->flags & GBNDE_FLAG_FP32_TIME) ? 1 : 0;
   a.dtmin = d->dtmin > 0 ? d->dtmin : 0.0;
   a.dtmax = std::fabs(d->t1 - d->t0);
   a.maxiters = maxiters;
@@ -660,6 +665,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   c->B = B;
   c->nsave = nsave;
   c->t0 = d->t0;
+  c->f32time = (d->flags & GBNDE_FLAG_FP32_TIME) ? 1 : 0;
   c->t1 = d->t1;
   c->abstol = d->abstol;
   c->reltol = d->reltol;
@@ -961,6 +967,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   a.abstol = c->abstol;
   a.reltol = c->reltol;
   a.dtmax = c->saveat.back() - c->t0;
+  a.f32time = c->f32time;
   a.maxiters = c->maxiters;
   a.iv = c->iv_d.as<Interval>();
   a.niv = (int)ivs.size();

@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       const double d1 = sqrt(grid_partials_sum(pp + G, G, red) / Nnorm);
       par ^= 1;
       double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
-      dt0 = fmin(dt0, a.dtmax);
+      dt0 = rt32(fmin(dt0, a.dtmax), a.f32time);
       const float hf = (float)dt0;
       const double tp = t - dt0;
       float hb[7];
@@ -424,14 +424,14 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       par ^= 1;
       const double mm = fmax(d1, d2);
       const double dt1 = (mm <= 1e-15) ? fmax(1e-6, dt0 * 1e-3) : pow(10.0, -(2.0 + log10(mm)) / 5.0);
-      dt = fmin(100.0 * dt0, fmin(dt1, a.dtmax));
+      dt = rt32(fmin(100.0 * dt0, fmin(dt1, a.dtmax)), a.f32time);
     }
 
     // ---- adaptive steps down to t_lo ----------------------------------------
     while (t > t_lo) {
       if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
       ++iter;
-      const double rem = t - t_lo;
+      const double rem = rt32(t - t_lo, a.f32time);
       const bool clipped = dt >= rem;
       const double H = clipped ? rem : dt;
       float* lcur = a.lam[cur];
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       double* pp = a.partials + (size_t)par * 2 * G;
       if (threadIdx.x == 0) pp[blockIdx.x] = perr;
       if (!grid_barrier(a.bar, gen, a.status)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
-      const double eest = sqrt(grid_partials_sum(pp, G, red) / Nnorm);
+      const double eest = rt32(sqrt(grid_partials_sum(pp, G, red) / Nnorm), a.f32time);
       par ^= 1;
       if (!isfinite(eest)) { ret = GBNDE_RET_UNSTABLE; break; }
       double q11;
@@ -565,13 +565,13 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
         ++nacc;
         cur ^= 1;
         swp = !swp;
-        t = clipped ? t_lo : t - H;
+        t = clipped ? t_lo : rt32(t - H, a.f32time);
         if (q >= 1.0 && q <= 1.0) q = 1.0;
-        qold = fmax(eest, kQoldInit);
-        dt = fmin(H / q, a.dtmax);
+        qold = rt32(fmax(eest, kQoldInit), a.f32time);
+        dt = rt32(fmin(H / q, a.dtmax), a.f32time);
       } else {
         ++nrej;
-        dt = H / fmin(1.0 / kQmin, q11 / kGamma);
+        dt = rt32(H / fmin(1.0 / kQmin, q11 / kGamma), a.f32time);
       }
     }
     if (ret != GBNDE_RET_SUCCESS) break;

@@ -146,6 +146,10 @@ __device__ __forceinline__ double grid_partials_sum(const double* partials, int 
   return v;
 }
 
+// The value x as the nearest Float32 when `on` (the Float32-time mode: t, dt,
+// the error estimate and qold are kept as Float32 values), else unchanged.
+__device__ __forceinline__ double rt32(double x, int on) { return on ? (double)(float)x : x; }
+
 // PI controller (FP64). Returns q, writes q11.
 __device__ __forceinline__ double pi_q(double eest, double qold, double* q11) {
   if (eest == 0.0) {

@@ -183,8 +183,9 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
 
   // ---- initial step (Hairer's algorithm as the integrator implements it) --
   double dt;
+  const int f32t = a.f32time;
   if (a.dt0 > 0.0) {
-    dt = a.dt0;
+    dt = rt32(a.dt0, f32t);
   } else {
     double p0 = 0.0, p1 = 0.0;
     const float* k1 = kb(a, 0, swp);
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
       par ^= 1;
       const double smalldt = fmax(a.dtmin, 1e-6);
       double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? smalldt : 0.01 * (d0 / d1);
-      dt0 = fmin(dt0, a.dtmax);
+      dt0 = rt32(fmin(dt0, a.dtmax), f32t);
       const float hf = (float)(tdir * dt0);
       // f1 = f(u0 + dt0*f0) into the stage-2 buffer (scratch here)
       float* f1b = kb(a, 1, swp);
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
       par ^= 1;
       const double m = fmax(d1, d2);
       const double dt1 = (m <= 1e-15) ? fmax(1e-6, dt0 * 1e-3) : pow(10.0, -(2.0 + log10(m)) / 5.0);
-      dt = fmax(a.dtmin, fmin(100.0 * dt0, fmin(dt1, a.dtmax)));
+      dt = rt32(fmax(a.dtmin, fmin(100.0 * dt0, fmin(dt1, a.dtmax))), f32t);
     }
   }
 
@@ -247,7 +248,7 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
     while (tdir * (a.t1 - t) > 0.0) {
       if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
       ++iter;
-      const double rem = fabs(a.t1 - t);
+      const double rem = rt32(fabs(a.t1 - t), f32t);
       const bool clipped = dt >= rem;
       const double habs = clipped ? rem : dt;
       const double h = tdir * habs;
@@ -294,7 +295,7 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
       double* pp = a.partials + (size_t)par * 2 * G;
       if (threadIdx.x == 0) pp[blockIdx.x] = perr;
       if (!grid_barrier(a.bar, gen, a.status)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
-      const double eest = sqrt(grid_partials_sum(pp, G, red) / N);
+      const double eest = rt32(sqrt(grid_partials_sum(pp, G, red) / N), f32t);
       par ^= 1;
       if (!isfinite(eest)) { ret = GBNDE_RET_UNSTABLE; break; }
       double q11;
@@ -307,7 +308,7 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
         tr[3] = eest <= 1.0 ? 1.0 : 0.0;
       }
       if (eest <= 1.0) {
-        const double tnew = clipped ? a.t1 : t + h;
+        const double tnew = clipped ? a.t1 : rt32(t + h, f32t);
         // saveat points in (t, tnew]
         while (isave < a.nsave && tdir * (a.saveat[isave] - tnew) <= 0.0) {
           const double s = a.saveat[isave];
@@ -374,11 +375,11 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
         cur ^= 1;
         t = tnew;
         if (q >= 1.0 && q <= 1.0) q = 1.0;
-        qold = fmax(eest, kQoldInit);
-        dt = fmax(fmin(habs / q, a.dtmax), a.dtmin);
+        qold = rt32(fmax(eest, kQoldInit), f32t);
+        dt = rt32(fmax(fmin(habs / q, a.dtmax), a.dtmin), f32t);
       } else {
         ++nreject;
-        dt = habs / fmin(1.0 / kQmin, q11 / kGamma);
+        dt = rt32(habs / fmin(1.0 / kQmin, q11 / kGamma), f32t);
         if (a.dtmin > 0.0 && dt <= a.dtmin) { ret = GBNDE_RET_DTLESSTHANMIN; break; }
       }
     }

@@ -23,6 +23,7 @@ struct FwdArgs {
   MlpDev mlp;
   int S, B, TM, LD, ntiles;
   double t0, t1, abstol, reltol, dt0, dtmin, dtmax;
+  int f32time;           // t, dt, EEst, qold kept as Float32 values (GBNDE_FLAG_FP32_TIME)
   long long maxiters;
   const double* saveat;  // device, nsave
   int nsave;
@@ -67,6 +68,7 @@ struct BwdArgs {
   int P;                  // number of parameters
   int sensealg;
   double t0, abstol, reltol, dtmax;
+  int f32time;            // as FwdArgs::f32time
   long long maxiters;
   const Interval* iv;     // device, niv (ordered from the last interval to the first)
   int niv;

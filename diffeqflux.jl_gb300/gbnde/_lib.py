@@ -14,6 +14,7 @@ MAX_LAYERS = 8
 ACT = {"identity": 0, "tanh": 1, "softplus": 2}
 PREC = {"fp32": 0, "bf16": 1}
 SENSE = {"interpolating": 0, "backsolve": 1, "gauss": 2}
+FLAG_FP32_TIME = 1  # gbnde_solve_desc.flags
 
 OK = 0
 ERR_INVALID = -1

@@ -202,7 +202,7 @@ class Solver:
         _lib.check(self.lib.gbnde_set_params(self.h, p.ctypes.data, p.size))
 
     @staticmethod
-    def solve_desc(t0, t1, saveat, abstol, reltol, sensealg=0, dt0=0.0, dtmin=0.0, maxiters=100000):
+    def solve_desc(t0, t1, saveat, abstol, reltol, sensealg=0, dt0=0.0, dtmin=0.0, maxiters=100000, flags=0):
         sv = np.ascontiguousarray(saveat, dtype=np.float64)
         d = _lib.SolveDesc()
         d.t0, d.t1 = float(t0), float(t1)
@@ -212,6 +212,7 @@ class Solver:
         d.saveat = sv.ctypes.data_as(C.POINTER(C.c_double))
         d.nsave = sv.size
         d.sensealg = int(sensealg)
+        d.flags = int(flags)
         d._keep = sv
         return d
 
@@ -387,7 +388,7 @@ class NeuralODE:
 
     def __init__(self, model, tspan, alg=None, *, saveat=None, abstol=1e-6, reltol=1e-3,
                  sensealg=None, dt=0.0, dtmin=0.0, maxiters=100000, save_everystep=None,
-                 save_start=None, save_end=True, device=0):
+                 save_start=None, save_end=True, device=0, float32_time=None):
         if not isinstance(model, Chain):
             raise TypeError("model must be a Chain of Dense layers (optionally starting with cube())")
         if alg is None:
@@ -404,6 +405,14 @@ class NeuralODE:
                 "save_everystep=true is not offered by the GB300 solver; pass saveat or "
                 "save_everystep=False")
         self.model = model
+        # A Float32 tspan makes the reference's integrator keep t and dt in
+        # Float32; the FP32 form follows (GBNDE_FLAG_FP32_TIME), the BF16 form
+        # keeps FP64 time by design.
+        if float32_time is None:
+            float32_time = (alg.precision == "fp32" and all(isinstance(x, np.float32) for x in tspan))
+        if float32_time and alg.precision != "fp32":
+            raise ValueError("float32_time is a mode of the FP32 form")
+        self.float32_time = bool(float32_time)
         self.tspan = (float(tspan[0]), float(tspan[1]))
         self.alg = alg
         self.sensealg = sensealg
@@ -412,6 +421,8 @@ class NeuralODE:
         if save_start is None:
             save_start = saveat is not None
         self.saveat = _saveat_points(self.tspan, saveat, save_start, save_end)
+        if self.float32_time:
+            self.saveat = [float(np.float32(s)) for s in self.saveat]
         self.device = device
         self._solver = None
 
@@ -427,7 +438,8 @@ class NeuralODE:
 
     def desc(self):
         return Solver.solve_desc(self.tspan[0], self.tspan[1], self.saveat, self.abstol, self.reltol,
-                                 self.sensealg.code, self.dt, self.dtmin, self.maxiters)
+                                 self.sensealg.code, self.dt, self.dtmin, self.maxiters,
+                                 flags=_lib.FLAG_FP32_TIME if self.float32_time else 0)
 
     def __call__(self, x, p, st=None):
         try:

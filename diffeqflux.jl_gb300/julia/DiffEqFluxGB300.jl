@@ -118,10 +118,13 @@ sensecode(s) = s isa BacksolveAdjoint ? 1 : s isa InterpolatingAdjoint ? 0 :
 
 # ---- the differentiable solve -------------------------------------------------------------
 """
-    gb300_solve(u0, p, ctx, tspan, saveat, abstol, reltol, sensealg) -> Array (S, B, nsave)
+    gb300_solve(u0, p, ctx, tspan, saveat, abstol, reltol, sensealg, flags) -> Array (S, B, nsave)
+
+`flags = GBNDE_FLAG_FP32_TIME` keeps t and dt in Float32 (the FP32 form with a Float32 tspan).
 """
+const GBNDE_FLAG_FP32_TIME = Cint(1)
 function gb300_solve(u0::AbstractMatrix{Float32}, p::AbstractVector{Float32}, ctx::Ctx, tspan,
-                     saveat::Vector{Float64}, abstol, reltol, sensealg)
+                     saveat::Vector{Float64}, abstol, reltol, sensealg, flags = Cint(0))
     S, B = size(u0)
     check(ccall((:gbnde_set_params, libgbnde), Cint, (Ptr{Cvoid}, Ptr{Float32}, Csize_t),
                 ctx.h, p, length(p)))
@@ -129,7 +132,7 @@ function gb300_solve(u0::AbstractMatrix{Float32}, p::AbstractVector{Float32}, ct
     st = Stats()
     GC.@preserve saveat begin
         d = Ref(SolveDesc(tspan[1], tspan[2], abstol, reltol, 0, 0, 100000, pointer(saveat),
-                          length(saveat), sensecode(sensealg), 0))
+                          length(saveat), sensecode(sensealg), flags))
         check(ccall((:gbnde_forward, libgbnde), Cint,
                     (Ptr{Cvoid}, Ref{SolveDesc}, Cint, Cint, Ptr{Float32}, Ptr{Float32}, Ref{Stats}),
                     ctx.h, d, S, B, Matrix(u0), out, st))
@@ -138,8 +141,8 @@ function gb300_solve(u0::AbstractMatrix{Float32}, p::AbstractVector{Float32}, ct
 end
 
 function ChainRulesCore.rrule(::typeof(gb300_solve), u0, p, ctx, tspan, saveat, abstol, reltol,
-                              sensealg)
-    out, st = gb300_solve(u0, p, ctx, tspan, saveat, abstol, reltol, sensealg)
+                              sensealg, flags = Cint(0))
+    out, st = gb300_solve(u0, p, ctx, tspan, saveat, abstol, reltol, sensealg, flags)
     function pullback(Δ)
         Δo = unthunk(Δ[1])
         du0 = similar(u0)
@@ -149,7 +152,7 @@ function ChainRulesCore.rrule(::typeof(gb300_solve), u0, p, ctx, tspan, saveat, 
                     (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Ptr{Float32}, Ref{Stats}),
                     ctx.h, Array{Float32}(Δo), du0, dp, bst))
         (NoTangent(), du0, dp, NoTangent(), NoTangent(), NoTangent(), NoTangent(), NoTangent(),
-         NoTangent())
+         NoTangent(), NoTangent())
     end
     (out, st), pullback
 end
@@ -161,8 +164,10 @@ function (n::NeuralODE)(x, p, st, alg::GB300Tsit5)
     ctx = ctx_for(n.model, alg.precision)
     sense = get(kw, :sensealg, InterpolatingAdjoint(; autojacvec = ZygoteVJP()))
     u0 = x isa AbstractVector ? reshape(x, :, 1) : x
+    # a Float32 tspan keeps t and dt in Float32, as the reference's integrator does
+    flags = (eltype(n.tspan) === Float32 && alg.precision === :fp32) ? GBNDE_FLAG_FP32_TIME : Cint(0)
     out, stats = gb300_solve(Float32.(u0), Float32.(collect(p)), ctx, Float64.(n.tspan), saveat,
-                             get(kw, :abstol, 1e-6), get(kw, :reltol, 1e-3), sense)
+                             get(kw, :abstol, 1e-6), get(kw, :reltol, 1e-3), sense, flags)
     prob = ODEProblem{false}((u, p, t) -> u, x, n.tspan, p)
     us = [x isa AbstractVector ? out[:, 1, i] : out[:, :, i] for i in axes(out, 3)]
     sol = SciMLBase.build_solution(prob, alg, saveat, us; retcode = RETCODES[stats.retcode + 1])

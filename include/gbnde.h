@@ -110,8 +110,16 @@ typedef struct {
   const double* saveat;   /* host array of nsave times inside [t0, t1], increasing from t0 */
   int nsave;              /* >= 1 */
   int sensealg;           /* gbnde_sensealg, used by gbnde_backward */
-  int flags;              /* reserved, 0 */
+  int flags;              /* 0, or GBNDE_FLAG_FP32_TIME */
 } gbnde_solve_desc;
+
+/* gbnde_solve_desc.flags: FP32 form only. t, the step size, the error
+ * estimate and qold are kept as Float32 values (rounded after every update),
+ * as the reference's integrator does for a Float32 tspan
+ * (src/neural_de.jl:52 builds the ODEProblem from the user's tspan); the
+ * forward solve and its adjoint both follow it. Without the flag they are
+ * FP64 (the BF16 form always). */
+#define GBNDE_FLAG_FP32_TIME 1
 
 typedef struct {
   long long nf;           /* RHS evaluations of the forward solve */

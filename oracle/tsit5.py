@@ -67,12 +67,17 @@ class Tsit5:
     ``on_stop(t, y) -> y or None`` is applied at each of them (a discrete
     callback); returning a new ``y`` re-evaluates the FSAL stage.
     ``steps`` replays a fixed list of ``(t_n, h_n)`` instead of adapting.
+    ``time_f32`` keeps t, the step size, the error estimate and qold as
+    Float32 values (rounded after each update), as the reference's integrator
+    does when the time span is Float32 (src/neural_de.jl:52 builds the problem
+    from the user's tspan); the state arithmetic stays FP64.
     """
 
     def __init__(self, F, y0, t0, t1, abstol, reltol, norm_mask=None, dt0=0.0,
                  dtmax=None, dtmin=0.0, maxiters=100000, tstops=(), on_stop=None,
-                 steps=None, record=False, on_accept=None):
+                 steps=None, record=False, on_accept=None, time_f32=False):
         self.F = F
+        self._r = (lambda x: float(np.float32(x))) if time_f32 else (lambda x: x)
         self.y = tuple(np.array(c, dtype=np.float64) for c in y0)
         self.t = float(t0)
         self.t0 = float(t0)
@@ -118,7 +123,7 @@ class Tsit5:
             dt0 = smalldt
         else:
             dt0 = 0.01 * (d0 / d1)
-        dt0 = min(dt0, self.dtmax)
+        dt0 = self._r(min(dt0, self.dtmax))
         y1 = tuple(c + self.tdir * dt0 * k for c, k in zip(y0, k1))
         f1 = self._eval(y1, self.t + self.tdir * dt0)
         s2, _ = _rms_sum([(a - b) / s for a, b, s in zip(f1, k1, sk)], self.mask)
@@ -128,7 +133,7 @@ class Tsit5:
             dt1 = max(1e-6, dt0 * 1e-3)
         else:
             dt1 = 10.0 ** (-(2.0 + math.log10(m)) / T.ORDER)
-        return max(self.dtmin, min(100.0 * dt0, dt1, self.dtmax))
+        return self._r(max(self.dtmin, min(100.0 * dt0, dt1, self.dtmax)))
 
     def _stages(self, k1, h):
         y, t = self.y, self.t
@@ -190,8 +195,9 @@ class Tsit5:
                 clipped = tnext == self.stops[istop]
             else:
                 stop = self.stops[istop]
-                h = self.tdir * min(abs(dt), abs(stop - self.t))
-                clipped = abs(dt) >= abs(stop - self.t)
+                rem = self._r(abs(stop - self.t))
+                h = self.tdir * min(abs(dt), rem)
+                clipped = abs(dt) >= rem
             if it >= self.maxiters:
                 self.retcode = RET_MAXITERS
                 break
@@ -200,7 +206,7 @@ class Tsit5:
             if self.replay is not None:
                 EEst, accept = 0.0, True
             else:
-                EEst = self._eest(K, ynew, h)
+                EEst = self._r(self._eest(K, ynew, h))
                 if not math.isfinite(EEst):
                     self.retcode = RET_UNSTABLE
                     break
@@ -213,7 +219,7 @@ class Tsit5:
                     q = q11 / self.qold ** T.BETA2
                     q = max(1.0 / T.QMAX, min(1.0 / T.QMIN, q / T.GAMMA))
             if accept:
-                tnew = self.stops[istop] if clipped else self.t + h
+                tnew = self.stops[istop] if clipped else self._r(self.t + h)
                 if self.record:
                     self.stepdata.append((self.t, h, self.y, K))
                 self.steps.append((self.t, h))
@@ -237,11 +243,11 @@ class Tsit5:
                 if self.replay is None:
                     if T.QSTEADY_MIN <= q <= T.QSTEADY_MAX:
                         q = 1.0
-                    self.qold = max(EEst, T.QOLDINIT)
+                    self.qold = self._r(max(EEst, T.QOLDINIT))
                     dtnew = abs(h) / q
                     dtnew = min(self.dtmax, dtnew)
                     dtnew = max(dtnew, self.dtmin)
-                    dt = dtnew
+                    dt = self._r(dtnew)
                 if clipped and istop < len(self.stops) - 1:
                     istop += 1
                     if self.on_stop is not None:
@@ -254,7 +260,7 @@ class Tsit5:
                     break
             else:
                 self.nreject += 1
-                dt = abs(h) / min(1.0 / T.QMIN, q11 / T.GAMMA)
+                dt = self._r(abs(h) / min(1.0 / T.QMIN, q11 / T.GAMMA))
                 if dt <= self.dtmin:
                     self.retcode = RET_DTMIN
                     break
@@ -265,7 +271,7 @@ class Tsit5:
 # NeuralODE forward solve
 # ---------------------------------------------------------------------------
 def solve_forward(rhs, u0, t0, t1, saveat, abstol, reltol, dt0=0.0, maxiters=100000,
-                  steps=None, record=True, dtmin=0.0):
+                  steps=None, record=True, dtmin=0.0, time_f32=False):
     """Forward solve; returns (usave [S,B,nsave], integrator)."""
     u0 = np.asarray(u0, dtype=np.float64)
     saveat = [float(s) for s in saveat]
@@ -275,7 +281,7 @@ def solve_forward(rhs, u0, t0, t1, saveat, abstol, reltol, dt0=0.0, maxiters=100
         out[..., i] = y[0]
 
     integ = Tsit5(lambda y, t: (rhs.f(y[0], t),), (u0,), t0, t1, abstol, reltol, dt0=dt0,
-                  maxiters=maxiters, steps=steps, record=record, dtmin=dtmin)
+                  maxiters=maxiters, steps=steps, record=record, dtmin=dtmin, time_f32=time_f32)
     integ.solve(on_save=on_save, saveat=saveat)
     return out, integ
 
@@ -288,7 +294,8 @@ def _backward_stops(saveat, t0):
     return s
 
 
-def adjoint_interpolating(rhs, fwd, saveat, dL_dusave, t0, abstol, reltol, maxiters=100000):
+def adjoint_interpolating(rhs, fwd, saveat, dL_dusave, t0, abstol, reltol, maxiters=100000,
+                          time_f32=False):
     """InterpolatingAdjoint: backward solve of (lam, mu) with u(t) from the
     forward dense output. Returns (dL/du0, dL/dp, integrator)."""
     saveat = [float(s) for s in saveat]
@@ -311,7 +318,7 @@ def adjoint_interpolating(rhs, fwd, saveat, dL_dusave, t0, abstol, reltol, maxit
         return None
 
     integ = Tsit5(F, (lam0, np.zeros(P)), t_last, t0, abstol, reltol, norm_mask=(True, False),
-                  tstops=stops[1:], on_stop=on_stop, maxiters=maxiters)
+                  tstops=stops[1:], on_stop=on_stop, maxiters=maxiters, time_f32=time_f32)
     if t_last > t0:
         integ.solve()
     lam, mu = integ.y

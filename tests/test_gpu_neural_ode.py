@@ -256,3 +256,45 @@ def test_quadrature_adjoint_against_oracle(prec, marker):
     assert _rel(out["q"][1], gu) < tolg
     assert _rel(out["q"][2], gp) < tolg
     assert _rel(out["q"][2], out["i"][2].astype(np.float64)) < 1e-3
+
+
+@pytest.mark.parametrize("B", [1, 64])
+def test_float32_time_mode(B):
+    """GBNDE_FLAG_FP32_TIME (a Float32 tspan, as the reference's integrator keeps
+    t and dt in Float32): every accepted step starts at a Float32 time with a
+    Float32 step; states and gradients match the oracle run in the same mode
+    (replayed steps 2e-5, adaptive adjoint 2e-4)."""
+    import gbnde
+    from oracle import tsit5 as ots
+    model, p, rng = _setup([2, 50, 2], ["tanh", "identity"], True, B, 3)
+    u0 = np.vstack([np.full((1, B), 2.0), 0.1 * rng.standard_normal((1, B))]).astype(np.float32)
+    tspan = (np.float32(0.0), np.float32(1.5))
+    ts = np.linspace(np.float32(0.0), np.float32(1.5), 30, dtype=np.float32)
+    node = gbnde.NeuralODE(model, tspan, gbnde.Tsit5("fp32"), saveat=ts, abstol=1e-7, reltol=1e-5)
+    assert node.float32_time
+    s = node.solver
+    s.set_params(p)
+    us, st = s.forward(u0, node.desc())
+    assert st.retcode == 0
+    steps = s.forward_steps()
+    assert len(steps) == st.naccept
+    for tn, h in steps:
+        assert float(np.float32(tn)) == tn and float(np.float32(h)) == abs(h), (tn, h)
+    rhs = _oracle(model, p)
+    ous, fwd = ots.solve_forward(rhs, u0.astype(np.float64), 0.0, 1.5, ts.astype(np.float64), 1e-7, 1e-5,
+                                 steps=steps, time_f32=True)
+    assert _rel(us, ous) < 2e-5
+    g = (2.0 * (us.astype(np.float64) - 0.5 * ous)).astype(np.float32)
+    du0, dp, sb = s.backward(g)
+    assert sb.retcode_adj == 0
+    gu, gp, integ = ots.adjoint_interpolating(rhs, fwd, ts.astype(np.float64), g.astype(np.float64), 0.0,
+                                              1e-7, 1e-5, time_f32=True)
+    for tn, h in integ.steps:
+        assert float(np.float32(tn)) == tn
+    assert _rel(du0, gu) < 2e-4
+    assert _rel(dp, gp) < 2e-4
+    # without the flag the same problem runs FP64 time
+    node64 = gbnde.NeuralODE(model, (0.0, 1.5), gbnde.Tsit5("fp32"), saveat=ts, abstol=1e-7, reltol=1e-5)
+    assert not node64.float32_time
+    with pytest.raises(ValueError):
+        gbnde.NeuralODE(model, tspan, gbnde.Tsit5("bf16"), saveat=ts, float32_time=True)

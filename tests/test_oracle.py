@@ -162,3 +162,21 @@ def test_oracle_reproduces_golden_fixtures(name):
 def test_linear_fixture_is_the_exact_solution():
     g = _load("linear.npz")
     assert np.abs(g["usave"] - g["exact"]).max() < 1e-8
+
+
+def test_float32_time_mode_keeps_float32_times():
+    """The oracle's Float32-time mode: accepted step times and sizes are Float32
+    values, and the solution agrees with the FP64-time solve to the tolerance."""
+    from oracle import mlp as omlp
+    from oracle import tsit5 as ots
+    rng = np.random.default_rng(2)
+    om = omlp.MLP([2, 16, 2], ["tanh", "identity"], cube_input=True)
+    P = om.nparams()
+    rhs = omlp.MLPRHS(om, 0.3 * rng.standard_normal(P))
+    u0 = np.array([[2.0], [0.0]])
+    ts = np.linspace(0.0, 1.5, 10, dtype=np.float32).astype(np.float64)
+    a, ia = ots.solve_forward(rhs, u0, 0.0, 1.5, ts, 1e-7, 1e-5, time_f32=True)
+    b, ib = ots.solve_forward(rhs, u0, 0.0, 1.5, ts, 1e-7, 1e-5)
+    for tn, h in ia.steps:
+        assert float(np.float32(tn)) == tn and float(np.float32(h)) == abs(h)
+    assert np.abs(a - b).max() < 1e-5 * np.abs(b).max()
