@@ -478,6 +478,10 @@ def run_sweep(args):
     pts = [(S, H, B) for B in SWEEP_B for S in SWEEP_S for H in SWEEP_H]
     if args.sweep_max_batch:
         pts = [x for x in pts if x[2] <= args.sweep_max_batch]
+    if args.sweep_state:
+        pts = [x for x in pts if x[0] == args.sweep_state]
+    if args.sweep_hidden:
+        pts = [x for x in pts if x[1] == args.sweep_hidden]
     for S, H, B in pts:
         line = {"sweep_point": {"state": S, "hidden": H, "batch": B}, "data": "synthetic (seeded)",
                 "config": "NeuralODE S -> H -> H -> S tanh, tspan (0, 1), 20 saves, Tsit5 1e-7 / 1e-5, "
@@ -754,6 +758,8 @@ def main():
     ap.add_argument("--no-aux", action="store_true", help="skip the spiral, FFJORD and multiple-shooting figures")
     ap.add_argument("--sweep", action="store_true", help="state x hidden x batch sweep, one JSON line per point")
     ap.add_argument("--sweep-max-batch", type=int, default=0)
+    ap.add_argument("--sweep-state", type=int, default=0, help="only this state dim")
+    ap.add_argument("--sweep-hidden", type=int, default=0, help="only this hidden width")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -912,7 +912,9 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
 
   int rows = 0;
   for (int l = 0; l <= c->mlp.nlayers; ++l) rows += c->mlp.dims[l];
-  rows = c->ff_on ? 2 * rows + 4 * c->mlp.maxdim + 1 : rows + 2 * c->mlp.maxdim + S;
+  // activations of every layer, two work buffers and, with the cube prefix,
+  // the state before it
+  rows = c->ff_on ? 2 * rows + 4 * c->mlp.maxdim + 1 : rows + 2 * c->mlp.maxdim + (c->mlp.cube ? S : 0);
   int TM = 0;
   if (choose_tm(rows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "network too wide");
   while (TM > 8 && TM / 2 >= B) TM /= 2;

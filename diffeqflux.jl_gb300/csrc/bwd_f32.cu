@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
         if (u_store) u_store[base + e] = u;
       }
       in[s * LD + m] = a.mlp.cube ? u * u * u : u;
-      sm.uraw[s * LD + m] = u;
+      if (a.mlp.cube) sm.uraw[s * LD + m] = u;  // rows reserved only with the cube prefix
       // lam cotangent of the chain output goes to gA
       float l = 0.f;
       if (m < nv) {
