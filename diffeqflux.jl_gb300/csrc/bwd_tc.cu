@@ -13,9 +13,10 @@
 //   VJP chain          g_l = W_l^T delta_{l+1},    l = L..1     (5 split products)
 //                      delta_l = g_l * act'(z_l), delta_L = lam, kl = g_1
 // The VJP chain runs on b_s lam (b_s: the stage's quadrature weight; it is
-// linear, so kl is divided by b_s at the end), and the epilogue writes the
-// activations a_l and the weighted cotangents b_s delta_{l+1} as split-BF16
-// trajectory-major images into the image slot of the stage. Once a step is
+// linear, so kl is divided by b_s at the end). The A chunks of the activations
+// a_l and of the weighted cotangents b_s delta_{l+1} (their first two split
+// pieces) are bulk-copied by the MMA warp from shared memory into the image
+// slot of the stage. Once a step is
 // accepted, one weight-gradient op per layer (and 128-row half) runs over
 // the six stages' images stacked along K (K = 6 x 128 trajectories, MN-major
 // operands, 3 split products),
@@ -26,9 +27,9 @@
 // for rejected steps. Stage 7 of a step is stage
 // 1 of the next (FSAL): its images go to the second of two stage-1 slots,
 // already weighted by b_1. Bias gradients are column sums of the cotangents
-// (warp butterfly reductions, deterministic order) kept in small per-CTA
-// pending buffers. lam uses compensated (TwoSum) sums; t, H and the
-// controller are FP64.
+// (warp butterfly reductions) added into small per-CTA pending buffers, one
+// row per 32-row group of the tile (one adder per element: deterministic).
+// lam uses compensated (TwoSum) sums; t, H and the controller are FP64.
 #include "tc_args.h"
 
 namespace gbnde {
