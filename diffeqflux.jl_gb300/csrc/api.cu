@@ -750,6 +750,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   int gmax = 0;
   if (max_grid_fwd_tc(&gmax)) return fail(GBNDE_ERR_CUDA, "occupancy query failed (tc)");
   const int ntiles = (B + 127) / 128;
+  if (ntiles > gmax) return fail(GBNDE_ERR_UNSUPPORTED, "tensor-core adjoint: more tiles than SMs");
   const int grid = std::min(gmax, ntiles);
   const size_t SBt = (size_t)ntiles * tc::kTileVec;  // tile-layout vectors
   BwdTcArgs t{};
@@ -903,8 +904,14 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   if (int r = build_intervals(c, ivs, &max_slots, &save_last, &nsave_last)) return r;
   const bool backsolve = c->sensealg == GBNDE_SENSE_BACKSOLVE;
   const bool gauss = c->sensealg == GBNDE_SENSE_GAUSS;
-  const bool tcbwd =
-      c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && !gauss && c->dense_valid && !c->ff_on;
+  // The tensor-core adjoint keeps one set of weight-gradient images per CTA
+  // and step, so it covers batches of at most one 128-trajectory tile per SM;
+  // larger batches take the FP32 adjoint (recomputing from the checkpoints).
+  int tc_gmax = 0;
+  const bool tc_one_tile = c->precision == GBNDE_PREC_BF16 && max_grid_fwd_tc(&tc_gmax) == 0 &&
+                           (B + 127) / 128 <= tc_gmax;
+  const bool tcbwd = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && !gauss &&
+                     c->dense_valid && !c->ff_on && tc_one_tile;
   // the FP32 adjoint reads dense slots only in its own layout; after a
   // tensor-core forward it recomputes each interval from the checkpoints
   const bool dense_f32 = c->dense_valid && !backsolve && !c->dense_tl;

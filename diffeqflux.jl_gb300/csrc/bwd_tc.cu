@@ -289,9 +289,16 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // slot: image slot of the stage's weight-gradient operands (-1: none);
     // P/c: pending bias quadrature buffer and the stage weight (P == nullptr:
     // no quadrature). The cotangent images carry the weight c.
-    auto adj_eval = [&](const float* lam_in, const float* x, int slot, float* P, float c, float* kl) -> bool {
-      if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_EVAL | ((uint32_t)(slot + 1) << 8))) return false;
+    // vjp_only: the activations of u(t) are those of the previous evaluation
+    // (same t and u, in the activation scratch, and their images already in
+    // `slot`): only the VJP ops run (x is not read).
+    auto adj_eval = [&](const float* lam_in, const float* x, int slot, float* P, float c, float* kl,
+                        bool vjp_only) -> bool {
+      if (threadIdx.x == 0 &&
+          !tc::epi_post(cmdp, sh, tc::CMD_EVAL | ((uint32_t)(slot + 1) << 8) | ((vjp_only ? (uint32_t)L : 0u) << 16)))
+        return false;
       float v[tc::kCW];
+      if (!vjp_only) {
       // a_0 = x (or x^3)
 #pragma unroll
       for (int i = 0; i < tc::kCW; ++i) {
@@ -319,6 +326,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           if (!emit(es, sh, aring, th, v)) return false;
         }
         tc::epi_release_acc(es, sh);
+      }
       }
       // a_{L-1} went through the ring only to reach its image (a copy-only
       // op: no product, nothing to wait for)
@@ -531,13 +539,17 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
           float lam[tc::kCW], x[tc::kCW], kl[tc::kCW];
           const bool v = valid(tile);
+          // after the first interval, the last evaluation was the previous
+          // step's stage 7 at this same t (the interval boundary), on this
+          // CTA's only tile: its activations are reused, the jump changed lam only
+          const bool reuse = ivi > 0 && G >= a.ntiles;
           if (v) {
             tc::tl_ldv(a.lam[cur] + tofs(tile), lam);
-            dense_u(tile, n, hb, x);
+            if (!reuse) dense_u(tile, n, hb, x);
           } else {
             for (int i = 0; i < tc::kCW; ++i) lam[i] = x[i] = 0.f;
           }
-          ok = adj_eval(lam, x, fs, Pb[iP1], (float)c_tab.b[0], kl);
+          ok = adj_eval(lam, x, fs, Pb[iP1], (float)c_tab.b[0], kl, reuse);
           if (v) tc::tl_stv(klb(0) + tofs(tile), kl);
         }
         ++nf_adj;
@@ -591,7 +603,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           }
           float li[tc::kCW];
           for (int i = 0; i < tc::kCW; ++i) li[i] = l[i] + hf * f0[i];
-          ok = adj_eval(li, x, -1, nullptr, 0.f, f1);
+          ok = adj_eval(li, x, -1, nullptr, 0.f, f1, false);
           if (v) {
             #pragma unroll
             for (int i = 0; i < tc::kCW; ++i) {
@@ -696,7 +708,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             } else {
               for (int q = 0; q < tc::kCW; ++q) Y[q] = x[q] = 0.f;
             }
-            ok = adj_eval(Y, x, slot, P, cw, kl);
+            ok = adj_eval(Y, x, slot, P, cw, kl, false);
             if (v) {
               if (i == 6) {
                 // lam, the stage value and the error sum over k1..k6 again

@@ -228,8 +228,10 @@ __device__ __forceinline__ void tl_st16(float* p, int hf, const float* x) {
 
 // ---- command ring (command mode) -------------------------------------------------
 // In command mode the epilogue decides, round by round, which op list the MMA
-// and producer warps run next: CMD_EVAL (the evaluation list, once) or CMD_DW
-// (the weight-gradient list, once; bits 8.. carry the image slot of stage 1).
+// and producer warps run next: CMD_EVAL (the evaluation list, once; bits 8-15
+// carry the image slot + 1, bits 16-23 the first op to run, so that an
+// evaluation can skip a prefix of the list) or CMD_DW (the weight-gradient
+// list, once; bits 8-15 carry the image slot of stage 1).
 // Thread 0 of the epilogue posts; the MMA and producer leaders both release
 // the slot.
 enum : uint32_t { CMD_EVAL = 1, CMD_DW = 2 };
@@ -383,7 +385,8 @@ __device__ __forceinline__ bool cmd_take(Shared& sh, int& cs, uint32_t& cph, uin
 }
 
 // Command mode: one op list per command. CMD_EVAL carries slot + 1 in bits
-// 8.. (0: no images); `imgs` is this CTA's image region, `img_cta` the bytes
+// 8-15 (0: no images) and the first op in bits 16-23; `imgs` is this CTA's
+// image region, `img_cta` the bytes
 // of one slot. Before a CMD_DW round the image copies must have landed: the
 // elected lane waits for its bulk groups and signals the producer.
 __device__ __forceinline__ void mma_loop_cmd(const OpList& ev, const OpList& dw, Shared& sh, uint8_t* aring,
@@ -402,11 +405,12 @@ __device__ __forceinline__ void mma_loop_cmd(const OpList& ev, const OpList& dw,
         mbar_arrive(&sh.img_done);
       }
       __syncwarp();
-    } else if ((cmd >> 8) != 0) {
-      img_base = imgs + (size_t)((cmd >> 8) - 1) * img_cta;
+    } else if (((cmd >> 8) & 0xffu) != 0) {
+      img_base = imgs + (size_t)(((cmd >> 8) & 0xffu) - 1) * img_cta;
     }
     const OpList& L = isdw ? dw : ev;
-    for (int i = 0; i < L.nops && ok; ++i) ok = mma_op(L.op[i], m, sh, aring, wring, img_base);
+    const int first = isdw ? 0 : (int)((cmd >> 16) & 0xffu);
+    for (int i = first; i < L.nops && ok; ++i) ok = mma_op(L.op[i], m, sh, aring, wring, img_base);
   }
   if (leader) bulk_wait_all();
 }
@@ -540,7 +544,9 @@ __device__ __forceinline__ void tma_loop_cmd(const OpList& ev, const OpList& dw,
       dph ^= 1;
       asm volatile("fence.proxy.async.global;" ::: "memory");
     }
-    for (int i = 0; i < L.nops && run; ++i) run = tma_op(L.op[i], t, sh, aring, wring, (int)(cmd >> 8));
+    const int first = isdw ? 0 : (int)((cmd >> 16) & 0xffu);
+    for (int i = first; i < L.nops && run; ++i)
+      run = tma_op(L.op[i], t, sh, aring, wring, (int)((cmd >> 8) & 0xffu));
   }
   tma_drain(t, sh);
 }

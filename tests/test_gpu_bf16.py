@@ -148,3 +148,29 @@ def test_bf16_forward_with_fp32_adjoint(case):
         gu, gp, _ = ots.adjoint_interpolating(rhs, fwd, ts, dl, 0.0, 1e-6, 1e-4)
     assert _rel(du0, gu) < 2e-3
     assert _rel(dp, gp) < 2e-3
+
+
+def test_bf16_batch_above_one_tile_per_sm():
+    """More 128-trajectory tiles than SMs: the tensor-core forward runs several
+    tiles per CTA, and the gradient (which then takes the FP32 adjoint) must
+    match the FP32 form as at smaller batches."""
+    import torch
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    S, H, B = 16, 64, 128 * (nsm + 8)
+    model, p, rng = _setup([S, H, H, S], ["tanh", "tanh", "identity"], False, B, 4, bias=0.0)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    ts = np.linspace(0.0, 1.0, 8)
+    out = {}
+    for prec in ("fp32", "bf16"):
+        node = _node(model, ts, prec, 1e-7, 1e-5)
+        s = node.solver
+        s.set_params(p)
+        us, st = s.forward(u0, node.desc())
+        assert st.retcode == 0
+        g = np.ones_like(us) / us.size
+        du0, dp, sta = s.backward(g)
+        assert sta.retcode_adj == 0
+        out[prec] = (us, du0, dp)
+    assert _rel(out["bf16"][0], out["fp32"][0].astype(np.float64)) < 1e-4
+    assert _rel(out["bf16"][1], out["fp32"][1].astype(np.float64)) < 1e-3
+    assert _rel(out["bf16"][2], out["fp32"][2].astype(np.float64)) < 1e-3
