@@ -750,8 +750,11 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   int gmax = 0;
   if (max_grid_fwd_tc(&gmax)) return fail(GBNDE_ERR_CUDA, "occupancy query failed (tc)");
   const int ntiles = (B + 127) / 128;
-  if (ntiles > gmax) return fail(GBNDE_ERR_UNSUPPORTED, "tensor-core adjoint: more tiles than SMs");
   const int grid = std::min(gmax, ntiles);
+  // tiles per CTA: each keeps its own stage images (the tile index travels in
+  // 8 bits of the evaluation command)
+  const int tpc = (ntiles + grid - 1) / grid;
+  if (tpc > 255) return fail(GBNDE_ERR_UNSUPPORTED, "tensor-core adjoint: more than 255 tiles per SM");
   const size_t SBt = (size_t)ntiles * tc::kTileVec;  // tile-layout vectors
   BwdTcArgs t{};
   t.b = base;
@@ -788,7 +791,8 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   }
   t.nbias = nb;
   int r = 0;
-  if ((r = c->timg.ensure((size_t)grid * tc::kImgSlots * t.img_cta)) ||
+  t.tpc = tpc;
+  if ((r = c->timg.ensure((size_t)grid * tpc * tc::kImgSlots * t.img_cta)) ||
       (r = c->thscr.ensure((size_t)grid * tc::kEpiThreads * t.hvals * 4)) ||
       (r = c->tmucomp.ensure((size_t)grid * P * 4)) || (r = c->tlamcomp.ensure(2 * SBt * 4)) ||
       (r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4)))
@@ -854,14 +858,14 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
       o.kind = 1;
       o.aimg = t.img + aimg + (size_t)hh * 32768;
       o.wimg = t.img + bimg;
-      o.cta_stride = tc::kImgSlots * t.img_cta;
+      o.cta_stride = (size_t)tpc * tc::kImgSlots * t.img_cta;
       o.slot_stride = t.img_cta;
       o.a_bytes = 32768;
       o.a_step = (uint32_t)(t.nh[l] * 32768);
       o.b_step = (uint32_t)(2 * nblk * 8192);
       o.nblk_b = nblk;
       o.npad = (nside + 15) / 16 * 16;
-      o.nchunk = 2 * 6;
+      o.nchunk = 2 * 6 * tpc;  // K = (tile, stage, 64-trajectory block)
       o.first_dw = 0;
       o.img_off = -1;
       t.dw_chunks += o.nchunk;
@@ -904,14 +908,8 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   if (int r = build_intervals(c, ivs, &max_slots, &save_last, &nsave_last)) return r;
   const bool backsolve = c->sensealg == GBNDE_SENSE_BACKSOLVE;
   const bool gauss = c->sensealg == GBNDE_SENSE_GAUSS;
-  // The tensor-core adjoint keeps one set of weight-gradient images per CTA
-  // and step, so it covers batches of at most one 128-trajectory tile per SM;
-  // larger batches take the FP32 adjoint (recomputing from the checkpoints).
-  int tc_gmax = 0;
-  const bool tc_one_tile = c->precision == GBNDE_PREC_BF16 && max_grid_fwd_tc(&tc_gmax) == 0 &&
-                           (B + 127) / 128 <= tc_gmax;
   const bool tcbwd = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && !gauss &&
-                     c->dense_valid && !c->ff_on && tc_one_tile;
+                     c->dense_valid && !c->ff_on;
   // the FP32 adjoint reads dense slots only in its own layout; after a
   // tensor-core forward it recomputes each interval from the checkpoints
   const bool dense_f32 = c->dense_valid && !backsolve && !c->dense_tl;

@@ -199,8 +199,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
   if (warp >= tc::kMmaWarp) {
     tc::regs_give_ctl();
     if (warp == tc::kMmaWarp)
-      tc::mma_loop_cmd(A.ops, A.dwops, sh, aring, wring, A.img + (size_t)blockIdx.x * tc::kImgSlots * A.img_cta,
-                       A.img_cta);
+      tc::mma_loop_cmd(A.ops, A.dwops, sh, aring, wring,
+                       A.img + (size_t)blockIdx.x * A.tpc * tc::kImgSlots * A.img_cta, A.img_cta);
     else if (warp == tc::kTmaWarp) tc::tma_loop_cmd(A.ops, A.dwops, sh, aring, wring);
   } else {
     tc::regs_take_epi();
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     bool swp = false, ok = true;
     // image slots of this CTA: stage 1 in slot fs (0 or 6), stages 2..6 in
     // slots 1..5, stage 7 in slot 6 - fs (stage 1 of the next step)
-    uint8_t* img = A.img + (size_t)blockIdx.x * tc::kImgSlots * A.img_cta;
+    uint8_t* img = A.img + (size_t)blockIdx.x * A.tpc * tc::kImgSlots * A.img_cta;
     int fs = 0;
     float4* hs4 = reinterpret_cast<float4*>(A.hscr + (size_t)blockIdx.x * tc::kEpiThreads * A.hvals);
     float* mu_acc = a.mu_acc + (size_t)blockIdx.x * a.P;
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     };
 
     // scratch images start at zero (padding rows/blocks are never written)
-    for (size_t i = threadIdx.x; i < tc::kImgSlots * A.img_cta / 16; i += tc::kEpiThreads)
+    for (size_t i = threadIdx.x; i < (size_t)A.tpc * tc::kImgSlots * A.img_cta / 16; i += tc::kEpiThreads)
       reinterpret_cast<uint4*>(img)[i] = make_uint4(0, 0, 0, 0);
     zero_cta(mu_acc);
     zero_cta(mu_comp);
@@ -292,10 +292,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // vjp_only: the activations of u(t) are those of the previous evaluation
     // (same t and u, in the activation scratch, and their images already in
     // `slot`): only the VJP ops run (x is not read).
+    // tile: the tile being evaluated (its index within the CTA selects the
+    // CTA's image set for that tile).
     auto adj_eval = [&](const float* lam_in, const float* x, int slot, float* P, float c, float* kl,
-                        bool vjp_only) -> bool {
+                        bool vjp_only, int tile) -> bool {
+      const uint32_t tj = (uint32_t)((tile - (int)blockIdx.x) / G);
       if (threadIdx.x == 0 &&
-          !tc::epi_post(cmdp, sh, tc::CMD_EVAL | ((uint32_t)(slot + 1) << 8) | ((vjp_only ? (uint32_t)L : 0u) << 16)))
+          !tc::epi_post(cmdp, sh, tc::CMD_EVAL | ((uint32_t)(slot + 1) << 8) |
+                                      ((vjp_only ? (uint32_t)L : 0u) << 16) | (tj << 24)))
         return false;
       float v[tc::kCW];
       if (!vjp_only) {
@@ -549,7 +553,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           } else {
             for (int i = 0; i < tc::kCW; ++i) lam[i] = x[i] = 0.f;
           }
-          ok = adj_eval(lam, x, fs, Pb[iP1], (float)c_tab.b[0], kl, reuse);
+          ok = adj_eval(lam, x, fs, Pb[iP1], (float)c_tab.b[0], kl, reuse, tile);
           if (v) tc::tl_stv(klb(0) + tofs(tile), kl);
         }
         ++nf_adj;
@@ -603,7 +607,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           }
           float li[tc::kCW];
           for (int i = 0; i < tc::kCW; ++i) li[i] = l[i] + hf * f0[i];
-          ok = adj_eval(li, x, -1, nullptr, 0.f, f1, false);
+          ok = adj_eval(li, x, -1, nullptr, 0.f, f1, false, tile);
           if (v) {
             #pragma unroll
             for (int i = 0; i < tc::kCW; ++i) {
@@ -708,7 +712,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             } else {
               for (int q = 0; q < tc::kCW; ++q) Y[q] = x[q] = 0.f;
             }
-            ok = adj_eval(Y, x, slot, P, cw, kl, false);
+            ok = adj_eval(Y, x, slot, P, cw, kl, false, tile);
             if (v) {
               if (i == 6) {
                 // lam, the stage value and the error sum over k1..k6 again

@@ -30,8 +30,9 @@ struct BwdTcArgs {
   int hvals;                    // values per thread in hscr
   int hoff[GBNDE_MAX_LAYERS];   // offset of hidden layer l (1..L-1) inside a thread's hscr
   int hx;                       // offset of the 32 state values kept for the cube prefix
-  uint8_t* img;                 // [grid][kImgSlots][img_cta] weight-gradient operand images
+  uint8_t* img;                 // [grid][tpc][kImgSlots][img_cta] weight-gradient operand images
   size_t img_cta;               // bytes of one stage's images
+  int tpc;                      // 128-trajectory tiles per CTA (image sets per CTA)
   long long aoff[GBNDE_MAX_LAYERS];  // image offset of a_l (l = 0..L-1)
   long long doff[GBNDE_MAX_LAYERS];  // image offset of delta_{l+1} (l = 0..L-1)
   int a_isA[GBNDE_MAX_LAYERS];       // 1: a_l is the A operand (rows = in) of layer l's dW

@@ -230,8 +230,9 @@ __device__ __forceinline__ void tl_st16(float* p, int hf, const float* x) {
 // In command mode the epilogue decides, round by round, which op list the MMA
 // and producer warps run next: CMD_EVAL (the evaluation list, once; bits 8-15
 // carry the image slot + 1, bits 16-23 the first op to run, so that an
-// evaluation can skip a prefix of the list) or CMD_DW (the weight-gradient
-// list, once; bits 8-15 carry the image slot of stage 1).
+// evaluation can skip a prefix of the list, bits 24-31 the CTA's tile index,
+// whose image set the copies go to) or CMD_DW (the weight-gradient list,
+// once; bits 8-15 carry the image slot of stage 1).
 // Thread 0 of the epilogue posts; the MMA and producer leaders both release
 // the slot.
 enum : uint32_t { CMD_EVAL = 1, CMD_DW = 2 };
@@ -406,7 +407,8 @@ __device__ __forceinline__ void mma_loop_cmd(const OpList& ev, const OpList& dw,
       }
       __syncwarp();
     } else if (((cmd >> 8) & 0xffu) != 0) {
-      img_base = imgs + (size_t)(((cmd >> 8) & 0xffu) - 1) * img_cta;
+      const size_t j = (cmd >> 24) & 0xffu;  // tile of the CTA: its own image set
+      img_base = imgs + (j * kImgSlots + (((cmd >> 8) & 0xffu) - 1)) * img_cta;
     }
     const OpList& L = isdw ? dw : ev;
     const int first = isdw ? 0 : (int)((cmd >> 16) & 0xffu);
@@ -440,7 +442,8 @@ __device__ __forceinline__ bool tma_wait_or_stop(Shared& sh, uint64_t* bar, uint
 }
 
 // One op's copies; `f` is the image slot of stage 1 for stage-stacked
-// weight-gradient ops (K chunk c: stage c / 2, trajectory block c % 2).
+// weight-gradient ops (K chunk c: tile c / 12 of the CTA, stage (c % 12) / 2,
+// trajectory block c % 2).
 __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh, uint8_t* aring,
                                        uint8_t* wring, int f) {
   const bool leader = (threadIdx.x & 31) == 0;
@@ -462,8 +465,10 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
   for (int c = 0; c < op.nchunk; ++c) {
     size_t aoff = 0, boff = 0;
     if (op.kind == 1) {
-      const int s = c >> 1, kb = c & 1;
-      const size_t slot = (size_t)stage_slot(s, f) * op.slot_stride;
+      // K chunk c: tile j of the CTA, stage s, 64-trajectory block kb
+      const int j = c / 12, cw = c - 12 * j;
+      const int s = cw >> 1, kb = cw & 1;
+      const size_t slot = ((size_t)j * kImgSlots + stage_slot(s, f)) * op.slot_stride;
       aoff = slot + (size_t)kb * op.a_step;
       boff = slot + (size_t)kb * op.b_step;
       if (!tma_wait_or_stop(sh, &sh.a_empty[t.aslot], t.aph ^ 1)) return false;
