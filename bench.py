@@ -451,7 +451,7 @@ def sweep_point(S, H, B, prec, dev, warmup, steps, tune):
     torch.cuda.synchronize()
     sec = (time.perf_counter() - t0) / steps
     F = gemm_flops_per_rhs(dims, B)
-    flops = F * (st.nf + st.nf_recompute + 3 * st.nf_adj)
+    flops = F * (st.nf + st.nf_recompute + 3 * (st.nf_adj - st.nf_adj_vjp) + 2 * st.nf_adj_vjp)
     out.update({"value": 1.0 / sec, "unit": "train_steps/s", "ms_per_step": 1000.0 * sec,
                 "steps": steps, "replayed_as_graph": all(graphed), "loss": loss,
                 "nf_fwd": st.nf, "nf_adj": st.nf_adj, "gemm_tflops_per_s": flops / sec / 1e12})
@@ -589,7 +589,9 @@ def run_gpu(args):
         k_fwd += fm.value
         k_bwd += bm.value
         F = gemm_flops_per_rhs(wl["dims"], B)
-        flops_b = F * st_b.nf_recompute + 3.0 * F * st_b.nf_adj
+        # a full adjoint evaluation is 3F (recompute + two transpose products),
+        # one that reuses the previous activations 2F
+        flops_b = F * st_b.nf_recompute + 3.0 * F * (st_b.nf_adj - st_b.nf_adj_vjp) + 2.0 * F * st_b.nf_adj_vjp
         flops += flops_b
     torch.cuda.synchronize()
     if dist:
@@ -645,7 +647,8 @@ def run_gpu(args):
             "bound": "tensor", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
             "frac": achieved_tf / peak_tf, "peak_source": peak_src,
             "traffic": traffic, "traffic_source": traffic_src,
-            "basis": "GEMM FLOPs of the adjoint launch: F*nf_recompute + 3F*nf_adj, F = 2*B*sum(in*out)"}
+            "basis": "GEMM FLOPs of the adjoint launch: F*nf_recompute + 3F*(nf_adj - nf_adj_vjp) + "
+                     "2F*nf_adj_vjp (VJP-only evaluations reuse the activations), F = 2*B*sum(in*out)"}
 
     # ---- the training iteration as one CUDA graph (gbnde_graph_train_step) -------
     # forward, loss, adjoint and Adam (lr 1e-3) replayed as one graph from the
@@ -730,7 +733,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "clocks": clk,
         "solver": {"nf_fwd": st_f.nf, "naccept": st_f.naccept, "nreject": st_f.nreject,
-                   "nf_recompute": st_b.nf_recompute, "nf_adj": st_b.nf_adj,
+                   "nf_recompute": st_b.nf_recompute, "nf_adj": st_b.nf_adj, "nf_adj_vjp": st_b.nf_adj_vjp,
                    "naccept_adj": st_b.naccept_adj, "nreject_adj": st_b.nreject_adj,
                    "fwd_kernel_ms": k_fwd / args.steps, "bwd_kernel_ms": bwd_ms_avg,
                    "loss": loss.value},

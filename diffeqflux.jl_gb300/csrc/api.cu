@@ -1048,6 +1048,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
     stats->naccept_adj = cnt[CT_NACCEPT];
     stats->nreject_adj = cnt[CT_NREJECT];
     stats->nf_recompute = cnt[CT_NRECOMP];
+    stats->nf_adj_vjp = cnt[CT_NVJP];
     stats->retcode_adj = status[ST_RETCODE];
   }
   if (status[ST_BARRIER]) return fail(GBNDE_ERR_TIMEOUT, "backward grid barrier timed out");
@@ -1347,6 +1348,7 @@ int gbnde_train_step(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, cons
       return r;
     sf.nf_recompute = sb.nf_recompute;
     sf.nf_adj = sb.nf_adj;
+    sf.nf_adj_vjp = sb.nf_adj_vjp;
     sf.naccept_adj = sb.naccept_adj;
     sf.nreject_adj = sb.nreject_adj;
     sf.retcode_adj = sb.retcode_adj;
@@ -1511,6 +1513,8 @@ int gbnde_graph_train_step(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B
     stats->naccept = fc[CT_NACCEPT];
     stats->nreject = fc[CT_NREJECT];
     stats->nf_adj = bc[CT_NF];
+    stats->nf_adj_vjp = bc[CT_NVJP];
+    stats->nf_recompute = bc[CT_NRECOMP];
     stats->naccept_adj = bc[CT_NACCEPT];
     stats->nreject_adj = bc[CT_NREJECT];
     stats->retcode = fs[ST_RETCODE];

@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     unsigned int gen = 0;
     int par = 0, cur = 0;
     int ret = GBNDE_RET_SUCCESS;
-    long long nf_adj = 0, nacc = 0, nrej = 0, iter = 0;
+    long long nf_adj = 0, nacc = 0, nrej = 0, iter = 0, nf_vjp = 0;
     double dt = 0.0, qold = kQoldInit;
     bool swp = false, ok = true;
     // image slots of this CTA: stage 1 in slot fs (0 or 6), stages 2..6 in
@@ -554,6 +554,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             for (int i = 0; i < tc::kCW; ++i) lam[i] = x[i] = 0.f;
           }
           ok = adj_eval(lam, x, fs, Pb[iP1], (float)c_tab.b[0], kl, reuse, tile);
+          if (reuse && tile == (int)blockIdx.x) ++nf_vjp;
           if (v) tc::tl_stv(klb(0) + tofs(tile), kl);
         }
         ++nf_adj;
@@ -797,6 +798,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       a.counters[CT_NF] = nf_adj;
+      a.counters[CT_NVJP] = nf_vjp;
       a.counters[CT_NACCEPT] = nacc;
       a.counters[CT_NREJECT] = nrej;
       a.counters[CT_NRECOMP] = 0;

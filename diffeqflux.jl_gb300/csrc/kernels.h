@@ -15,6 +15,7 @@ enum CounterSlot {
   CT_NCKPT = 3,
   CT_NRECOMP = 4,
   CT_NATTEMPT = 6,
+  CT_NVJP = 7,  // adjoint evaluations that ran the VJP only
   CT_NSLOTS = 8
 };
 

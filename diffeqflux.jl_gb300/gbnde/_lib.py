@@ -70,6 +70,7 @@ class Stats(C.Structure):
         ("nf_adj", C.c_longlong), ("naccept_adj", C.c_longlong), ("nreject_adj", C.c_longlong),
         ("retcode", C.c_int), ("retcode_adj", C.c_int),
         ("t_final", C.c_double),
+        ("nf_adj_vjp", C.c_longlong),
     ]
 
     def as_dict(self):

@@ -64,7 +64,8 @@ mutable struct Stats
     retcode::Cint
     retcode_adj::Cint
     t_final::Cdouble
-    Stats() = new(0, 0, 0, 0, 0, 0, 0, 0, 0, 0.0)
+    nf_adj_vjp::Clonglong
+    Stats() = new(0, 0, 0, 0, 0, 0, 0, 0, 0, 0.0, 0)
 end
 
 const RETCODES = (SciMLBase.ReturnCode.Success, SciMLBase.ReturnCode.MaxIters,

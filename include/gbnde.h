@@ -132,6 +132,8 @@ typedef struct {
   int retcode;            /* gbnde_retcode of the forward solve */
   int retcode_adj;        /* gbnde_retcode of the adjoint solve */
   double t_final;
+  long long nf_adj_vjp;   /* adjoint evaluations that ran the VJP only, reusing the activations of
+                             the previous evaluation at the same t and u (interval starts) */
 } gbnde_stats;
 
 /* ---- context ------------------------------------------------------------ */
