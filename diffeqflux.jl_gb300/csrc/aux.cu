@@ -48,9 +48,34 @@ __global__ void loss_kernel(const float* __restrict__ u, const float* __restrict
                             int kind, float* __restrict__ dL, double* __restrict__ part) {
   __shared__ double red[40];
   const float scale = (kind == 1) ? (float)(2.0 / (double)n) : 2.f;
+  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, nth = (size_t)gridDim.x * blockDim.x;
   double s = 0.0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
+  size_t done = 0;
+  if (((reinterpret_cast<uintptr_t>(u) | reinterpret_cast<uintptr_t>(tg) | reinterpret_cast<uintptr_t>(dL)) & 15) == 0) {
+    // 128-bit accesses; the squares go into two compensated (Kahan) FP32 sums
+    // per thread (a few hundred terms each), added in FP64 at the end
+    const size_t n4 = n / 4;
+    const float4* u4 = reinterpret_cast<const float4*>(u);
+    const float4* t4 = reinterpret_cast<const float4*>(tg);
+    float4* d4 = reinterpret_cast<float4*>(dL);
+    float a0 = 0.f, c0 = 0.f, a1 = 0.f, c1 = 0.f;
+    auto kadd = [](float& acc, float& cmp, float x) {
+      const float y = x - cmp;
+      const float t2 = acc + y;
+      cmp = (t2 - acc) - y;
+      acc = t2;
+    };
+    for (size_t i = tid; i < n4; i += nth) {
+      const float4 x = __ldcs(u4 + i), y = __ldcs(t4 + i);
+      const float e0 = x.x - y.x, e1 = x.y - y.y, e2 = x.z - y.z, e3 = x.w - y.w;
+      __stcs(d4 + i, make_float4(scale * e0, scale * e1, scale * e2, scale * e3));
+      kadd(a0, c0, fmaf(e0, e0, e1 * e1));
+      kadd(a1, c1, fmaf(e2, e2, e3 * e3));
+    }
+    s = ((double)a0 - (double)c0) + ((double)a1 - (double)c1);
+    done = n4 * 4;
+  }
+  for (size_t i = done + tid; i < n; i += nth) {
     const float d = u[i] - tg[i];
     s += (double)d * (double)d;
     dL[i] = scale * d;
