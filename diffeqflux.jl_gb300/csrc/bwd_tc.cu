@@ -814,28 +814,16 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
   if (warp == tc::kMmaWarp) tc::tmem_dealloc(sh.tmem_base, 512);
 }
 
-// dLdp[i] = sum over CTAs of (mu_acc - mu_comp) in FP64: eight partial sums
-// (CTA b into sum b % 8, in CTA order) so that sixteen loads are in flight,
-// combined in a fixed tree. Per-CTA slots are `stride` floats apart; `P`
-// parameters are written.
+// dLdp[i] = sum over CTAs of (mu_acc - mu_comp), FP64 accumulation in CTA order.
+// Per-CTA slots are `stride` floats apart; `P` parameters are written.
 __global__ void reduce_mu_comp_kernel(const float* __restrict__ acc, const float* __restrict__ comp,
                                       int nblk, int stride, int P, float* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P) return;
-  double s[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  int b = 0;
-  for (; b + 8 <= nblk; b += 8) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const size_t o = (size_t)(b + k) * stride + i;
-      s[k] += (double)__ldcs(acc + o) - (double)__ldcs(comp + o);
-    }
-  }
-  for (; b < nblk; ++b) {
-    const size_t o = (size_t)b * stride + i;
-    s[b & 7] += (double)__ldcs(acc + o) - (double)__ldcs(comp + o);
-  }
-  out[i] = (float)(((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7])));
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b)
+    s += (double)acc[(size_t)b * stride + i] - (double)comp[(size_t)b * stride + i];
+  out[i] = (float)s;
 }
 
 int launch_bwd_tc(const BwdTcArgs& a, int grid, cudaStream_t st) {

@@ -48,7 +48,9 @@ def test_loss_noalloc_matches_loss_device_twice():
                                         C.byref(out), stream)
             assert rc == 0, (call, kind, rc)
             torch.cuda.synchronize()
-            assert abs(out.value - ref) <= 1e-12 * abs(ref), (call, kind, out.value, ref)
+            # the allocation-free kernel sums every square in FP64, loss_device in
+            # compensated FP32 partial sums: about 1e-9 relative apart
+            assert abs(out.value - ref) <= 1e-8 * abs(ref), (call, kind, out.value, ref)
             assert torch.equal(dl_new, dl_ref)
     # sizes beyond the fixed scratch are refused, not truncated
     big = C.c_size_t(4096 * 65536 + 1)
