@@ -814,16 +814,29 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
   if (warp == tc::kMmaWarp) tc::tmem_dealloc(sh.tmem_base, 512);
 }
 
-// dLdp[i] = sum over CTAs of (mu_acc - mu_comp), FP64 accumulation in CTA order.
-// Per-CTA slots are `stride` floats apart; `P` parameters are written.
+// dLdp[i] = sum over CTAs of (mu_acc - mu_comp), in CTA order, as a
+// compensated (Kahan) FP32 sum: FP64 arithmetic is slow on this GPU and
+// made this pass compute-bound; the compensation keeps the sum of the ~100
+// per-CTA terms to FP32 rounding. Per-CTA slots are `stride` floats apart;
+// `P` parameters are written.
 __global__ void reduce_mu_comp_kernel(const float* __restrict__ acc, const float* __restrict__ comp,
                                       int nblk, int stride, int P, float* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P) return;
-  double s = 0.0;
-  for (int b = 0; b < nblk; ++b)
-    s += (double)acc[(size_t)b * stride + i] - (double)comp[(size_t)b * stride + i];
-  out[i] = (float)s;
+  float s = 0.f, c = 0.f;
+  auto add = [&](float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  };
+  for (int b = 0; b < nblk; ++b) {
+    const size_t o = (size_t)b * stride + i;
+    // both parts of the CTA's compensated sum enter as terms
+    add(__ldcs(acc + o));
+    add(-__ldcs(comp + o));
+  }
+  out[i] = s - c;
 }
 
 int launch_bwd_tc(const BwdTcArgs& a, int grid, cudaStream_t st) {
