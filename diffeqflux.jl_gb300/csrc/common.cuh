@@ -227,12 +227,6 @@ __device__ __forceinline__ void with_act(int act, F&& fn) {
   else fn(ActIdentity{});
 }
 
-// act'(z) from the activation output y (tanh: 1 - y^2; softplus: 1 - exp(-y)).
-__device__ __forceinline__ float act_deriv_from_out(float y, int act) {
-  if (act == GBNDE_ACT_TANH) return 1.f - y * y;
-  if (act == GBNDE_ACT_SOFTPLUS) return -expm1f(-y);
-  return 1.f;
-}
 
 // Free interpolant weights b_i(theta) (FP64 in, FP32 out).
 __device__ __forceinline__ void interp_weights(double th, float* bw) {

@@ -176,9 +176,6 @@ __device__ __forceinline__ void init_shared(Shared& sh) {
 // where the column-major API layout would touch 32 separate lines. One vector
 // holds ntiles * kTileVec floats (components padded to 64, pads kept zero).
 constexpr int kTileVec = 128 * 64;
-__device__ __forceinline__ size_t tl_offset(int tile, int ch, int r) {
-  return (size_t)(tile * 2 + ch) * 4096 + (size_t)r * 4;
-}
 // Offset of the first of the kCW components of column group g, row r.
 __device__ __forceinline__ size_t tl_offset_cw(int tile, int g, int r) {
   const int c0 = kCW * g;
@@ -212,20 +209,6 @@ __device__ __forceinline__ void tl_stp(float* p, int part, const float* x) {
     *reinterpret_cast<float4*>(p + (part * (kPart / 4) + j) * 512) =
         make_float4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
 }
-// components 16 hf .. 16 hf + 15 of the same (hf < kCW / 16)
-__device__ __forceinline__ void tl_ld16(const float* p, int hf, float* x) {
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const float4 q = *reinterpret_cast<const float4*>(p + (4 * hf + j) * 512);
-    x[4 * j] = q.x; x[4 * j + 1] = q.y; x[4 * j + 2] = q.z; x[4 * j + 3] = q.w;
-  }
-}
-__device__ __forceinline__ void tl_st16(float* p, int hf, const float* x) {
-#pragma unroll
-  for (int j = 0; j < 4; ++j)
-    *reinterpret_cast<float4*>(p + (4 * hf + j) * 512) = make_float4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
-}
-
 // ---- command ring (command mode) -------------------------------------------------
 // In command mode the epilogue decides, round by round, which op list the MMA
 // and producer warps run next: CMD_EVAL (the evaluation list, once; bits 8-15

@@ -276,14 +276,10 @@ __device__ __forceinline__ float4 ld_v4f_hint(const void* ptr, uint64_t pol) {
   return v;
 }
 
-// Fire-and-forget global adds (performed at L2; no value returned, so the
+// Fire-and-forget global add (performed at L2; no value returned, so the
 // issuing thread does not wait for the memory round trip). Each address of a
-// pending quadrature buffer has one writing thread, so the adds to an address
+// pending quadrature buffer has one adding thread, so the adds to an address
 // happen in that thread's program order: the sums stay deterministic.
-__device__ __forceinline__ void red_add_v4(float* p, float a, float b, float c, float d) {
-  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
-               : "memory");
-}
 __device__ __forceinline__ void red_add(float* p, float a) {
   asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p), "f"(a) : "memory");
 }
