@@ -193,3 +193,54 @@ int launch_adam_graph(float* p, float* m, float* v, const float* g, size_t n, do
 }
 
 }  // namespace gbnde
+
+// ---- bounded-wait self-test ------------------------------------------------------
+// Two CTAs meet at the solvers' grid barrier; with `absent` = 0 or 1 that CTA
+// returns first and never arrives, so the other's wait runs out after
+// limit_ns and records the barrier timeout, as a solve would report it. No
+// fault, no trap: the waiting CTA leaves its loop and the kernel ends.
+namespace gbnde {
+namespace {
+__global__ void barrier_selftest_kernel(unsigned int* counter, int* status, int absent,
+                                        unsigned long long limit_ns, unsigned long long* waited) {
+  if ((int)blockIdx.x == absent) return;
+  unsigned int gen = 0;
+  const unsigned long long t0 = globaltimer_ns();
+  grid_barrier_ns(counter, gen, status, limit_ns);
+  if (threadIdx.x == 0) atomicMax(waited, globaltimer_ns() - t0);
+}
+}  // namespace
+}  // namespace gbnde
+
+extern "C" int gbnde_barrier_selftest(int absent, double limit_ms, int* timed_out, double* waited_ms) {
+  if (!timed_out || !waited_ms || absent < -1 || absent > 1 || !(limit_ms > 0.0) || limit_ms > 1000.0)
+    return GBNDE_ERR_INVALID;
+  struct Blk {
+    unsigned int counter;
+    int status[gbnde::ST_NSLOTS];
+    unsigned long long waited;
+  };
+  Blk* d = nullptr;
+  if (cudaMalloc(&d, sizeof(Blk)) != cudaSuccess) return GBNDE_ERR_NOMEM;
+  int rc = GBNDE_OK;
+  if (cudaMemset(d, 0, sizeof(Blk)) != cudaSuccess) rc = GBNDE_ERR_CUDA;
+  if (rc == GBNDE_OK) {
+    unsigned int* counter = &d->counter;
+    int* status = d->status;
+    unsigned long long* waited = &d->waited;
+    unsigned long long limit_ns = (unsigned long long)(limit_ms * 1e6);
+    void* args[] = {(void*)&counter, (void*)&status, (void*)&absent, (void*)&limit_ns, (void*)&waited};
+    // cooperative: both CTAs are resident, so only the absent one can keep the other waiting
+    if (cudaLaunchCooperativeKernel((const void*)gbnde::barrier_selftest_kernel, dim3(2), dim3(64), args, 0,
+                                    nullptr) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess)
+      rc = GBNDE_ERR_CUDA;
+  }
+  Blk h{};
+  if (rc == GBNDE_OK && cudaMemcpy(&h, d, sizeof(Blk), cudaMemcpyDeviceToHost) != cudaSuccess) rc = GBNDE_ERR_CUDA;
+  cudaFree(d);
+  if (rc != GBNDE_OK) return rc;
+  *timed_out = h.status[gbnde::ST_BARRIER];
+  *waited_ms = (double)h.waited / 1e6;
+  return GBNDE_OK;
+}

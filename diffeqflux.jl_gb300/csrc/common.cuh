@@ -81,8 +81,8 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
 // at 0 for the launch; generation g waits for g*gridDim.x arrivals. Waits at
 // most kBarrierTimeoutNs, then records ST_BARRIER and returns false; every
 // caller then leaves its loop, so the kernel ends instead of hanging.
-__device__ __forceinline__ bool grid_barrier(unsigned int* counter, unsigned int& gen,
-                                             int* status) {
+__device__ __forceinline__ bool grid_barrier_ns(unsigned int* counter, unsigned int& gen, int* status,
+                                                unsigned long long limit_ns) {
   __syncthreads();
   gen += 1;
   __shared__ int s_ok;
@@ -94,7 +94,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* counter, unsigned int
     int ok = 1;
     while (ld_acquire_u32(counter) < target) {
       if (*((volatile int*)&status[ST_BARRIER]) != 0) { ok = 0; break; }
-      if (globaltimer_ns() - t_start > kBarrierTimeoutNs) {
+      if (globaltimer_ns() - t_start > limit_ns) {
         atomicExch(&status[ST_BARRIER], 1);
         ok = 0;
         break;
@@ -106,6 +106,10 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* counter, unsigned int
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+__device__ __forceinline__ bool grid_barrier(unsigned int* counter, unsigned int& gen, int* status) {
+  return grid_barrier_ns(counter, gen, status, kBarrierTimeoutNs);
 }
 
 // Deterministic block sum of a double: warp butterflies (commutative pairs give

@@ -113,6 +113,7 @@ _SIGS = {
     "gbnde_autotune": (C.c_int, [_P, C.POINTER(SolveDesc), C.c_int, C.c_int, _P, C.POINTER(C.c_int)]),
     "gbnde_tc_selftest": (C.c_int, [_FP, _FP, C.c_int, C.c_int, C.c_int, _FP]),
     "gbnde_act_selftest": (C.c_int, [_FP, C.c_int, C.c_int, _FP, _FP]),
+    "gbnde_barrier_selftest": (C.c_int, [C.c_int, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "gbnde_strerror": (C.c_char_p, [C.c_int]),
     "gbnde_last_error": (C.c_char_p, []),
 }

@@ -306,6 +306,14 @@ int gbnde_last_kernel_ms(gbnde_ctx* ctx, double* fwd_ms, double* bwd_ms);
 int gbnde_autotune(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int S, int B,
                    const float* u0_dev, int* tiles);
 
+/* Self-test of the bounded waits (failure detection without a fault): two
+ * CTAs meet at the solvers' grid barrier; with absent = 0 or 1 that CTA never
+ * arrives and the other gives up after limit_ms (<= 1000), as a solve does
+ * after its barrier limit (then retcode BarrierTimeout). absent = -1: both
+ * arrive. timed_out: 1 when the wait ran out; waited_ms: how long it waited.
+ * No reference counterpart (test support). */
+int gbnde_barrier_selftest(int absent, double limit_ms, int* timed_out, double* waited_ms);
+
 /* Self-test of the tensor-core building blocks on the current device:
  * D[128 x N] = A[128 x K] * W[N x K]^T (host arrays, row-major) through bulk
  * copied SW128 weight images, tcgen05.mma into tensor memory and tcgen05.ld.

@@ -298,3 +298,25 @@ def test_float32_time_mode(B):
     assert not node64.float32_time
     with pytest.raises(ValueError):
         gbnde.NeuralODE(model, tspan, gbnde.Tsit5("bf16"), saveat=ts, float32_time=True)
+
+
+def test_barrier_wait_runs_out_and_reports():
+    """Failure detection without a GPU fault: a grid barrier whose other CTA
+    never arrives gives up after its limit and records the timeout; with both
+    CTAs present it passes at once; the device stays usable afterwards."""
+    import ctypes as C
+
+    import gbnde
+    from gbnde import _lib
+    lib = gbnde.load(build_if_missing=True)
+    t, w = C.c_int(-1), C.c_double(-1.0)
+    _lib.check(lib.gbnde_barrier_selftest(-1, 50.0, C.byref(t), C.byref(w)))
+    assert t.value == 0 and w.value < 50.0, (t.value, w.value)
+    _lib.check(lib.gbnde_barrier_selftest(1, 50.0, C.byref(t), C.byref(w)))
+    assert t.value == 1 and 45.0 <= w.value < 1000.0, (t.value, w.value)
+    # a solve on the same device afterwards
+    model, p, rng = _setup([2, 16, 2], ["tanh", "identity"], False, 4, 0)
+    node = gbnde.NeuralODE(model, (0.0, 1.0), gbnde.Tsit5("fp32"), saveat=[0.0, 1.0])
+    node.solver.set_params(p)
+    _, st = node.solver.forward(rng.standard_normal((2, 4)).astype(np.float32), node.desc())
+    assert st.retcode == 0
