@@ -844,6 +844,11 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
     o.img_nh = (uint16_t)t.nh[l];
   }
   t.ops.nops = n;
+  // re-emission list: the same ops with the forward ones copy-only (their
+  // chunks, stored activations re-emitted by the epilogue, only reach the
+  // images); for an evaluation at the same t and u(t) as the previous one
+  t.ops7 = t.ops;
+  for (int l = 0; l < L; ++l) t.ops7.op[l].kind = 2;
   n = 0;
   t.dw_chunks = 0;
   for (int l = 0; l < L; ++l) {

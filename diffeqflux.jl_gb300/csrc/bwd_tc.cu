@@ -199,9 +199,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
   if (warp >= tc::kMmaWarp) {
     tc::regs_give_ctl();
     if (warp == tc::kMmaWarp)
-      tc::mma_loop_cmd(A.ops, A.dwops, sh, aring, wring,
+      tc::mma_loop_cmd(A.ops, A.dwops, A.ops7, sh, aring, wring,
                        A.img + (size_t)blockIdx.x * A.tpc * tc::kImgSlots * A.img_cta, A.img_cta);
-    else if (warp == tc::kTmaWarp) tc::tma_loop_cmd(A.ops, A.dwops, sh, aring, wring);
+    else if (warp == tc::kTmaWarp) tc::tma_loop_cmd(A.ops, A.dwops, A.ops7, sh, aring, wring);
   } else {
     tc::regs_take_epi();
     // ======================= epilogue warps =======================
@@ -251,6 +251,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // lam, its compensation, the stages and the dense forward slots use the
     // tile layout; the cotangents dL/du(t_i) and dL/du0 the API layout
     const size_t SBt = (size_t)a.ntiles * tc::kTileVec;
+    const bool c67_same = c_tab.c[5] == c_tab.c[6];  // stages 6 and 7 at one time (Tsit5: c = 1)
     auto gofs = [&](int tile) -> size_t { return ((size_t)tile * 128 + th.r) * S + tc::kCW * th.ch; };
     auto tofs = [&](int tile) -> size_t { return tc::tl_offset_cw(tile, th.ch, th.r); };
     auto valid = [&](int tile) -> bool { return tile * 128 + th.r < a.B && th.nmine > 0; };
@@ -292,17 +293,34 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // vjp_only: the activations of u(t) are those of the previous evaluation
     // (same t and u, in the activation scratch, and their images already in
     // `slot`): only the VJP ops run (x is not read).
+    // reemit: the previous evaluation was at the same t and u(t) (Tsit5's
+    // stages 6 and 7 share c = 1): x and the stored activations are emitted
+    // again, only to reach this stage's images, instead of being recomputed.
     // tile: the tile being evaluated (its index within the CTA selects the
     // CTA's image set for that tile).
     auto adj_eval = [&](const float* lam_in, const float* x, int slot, float* P, float c, float* kl,
-                        bool vjp_only, int tile) -> bool {
+                        bool vjp_only, int tile, bool reemit) -> bool {
       const uint32_t tj = (uint32_t)((tile - (int)blockIdx.x) / G);
       if (threadIdx.x == 0 &&
-          !tc::epi_post(cmdp, sh, tc::CMD_EVAL | ((uint32_t)(slot + 1) << 8) |
+          !tc::epi_post(cmdp, sh, (reemit ? tc::CMD_EVAL_RE : tc::CMD_EVAL) | ((uint32_t)(slot + 1) << 8) |
                                       ((vjp_only ? (uint32_t)L : 0u) << 16) | (tj << 24)))
         return false;
       float v[tc::kCW];
-      if (!vjp_only) {
+      if (reemit && !vjp_only) {
+#pragma unroll
+        for (int i = 0; i < tc::kCW; ++i) {
+          const float y = (i < th.nmine) ? x[i] : 0.f;
+          v[i] = m.cube ? y * y * y : y;
+        }
+        if (!emit(es, sh, aring, th, v)) return false;
+        for (int l = 0; l < L - 1; ++l) {
+          const int nch = (m.dims[l + 1] + 63) / 64;
+          for (int cc = 0; cc < nch; ++cc) {
+            hs_ldv(hs4, (A.hoff[l + 1] + tc::kCW * cc) / 4, v);
+            if (!emit(es, sh, aring, th, v)) return false;
+          }
+        }
+      } else if (!vjp_only) {
       // a_0 = x (or x^3)
 #pragma unroll
       for (int i = 0; i < tc::kCW; ++i) {
@@ -553,7 +571,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           } else {
             for (int i = 0; i < tc::kCW; ++i) lam[i] = x[i] = 0.f;
           }
-          ok = adj_eval(lam, x, fs, Pb[iP1], (float)c_tab.b[0], kl, reuse, tile);
+          ok = adj_eval(lam, x, fs, Pb[iP1], (float)c_tab.b[0], kl, reuse, tile, false);
           if (reuse && tile == (int)blockIdx.x) ++nf_vjp;
           if (v) tc::tl_stv(klb(0) + tofs(tile), kl);
         }
@@ -608,7 +626,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           }
           float li[tc::kCW];
           for (int i = 0; i < tc::kCW; ++i) li[i] = l[i] + hf * f0[i];
-          ok = adj_eval(li, x, -1, nullptr, 0.f, f1, false, tile);
+          ok = adj_eval(li, x, -1, nullptr, 0.f, f1, false, tile, false);
           if (v) {
             #pragma unroll
             for (int i = 0; i < tc::kCW; ++i) {
@@ -713,7 +731,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             } else {
               for (int q = 0; q < tc::kCW; ++q) Y[q] = x[q] = 0.f;
             }
-            ok = adj_eval(Y, x, slot, P, cw, kl, false, tile);
+            // stage 7 (i == 6) is at the same time as stage 6 (c6 = c7 = 1): on
+            // a CTA's only tile its activations are re-emitted, not recomputed
+            ok = adj_eval(Y, x, slot, P, cw, kl, false, tile, i == 6 && G >= a.ntiles && c67_same);
             if (v) {
               if (i == 6) {
                 // lam, the stage value and the error sum over k1..k6 again

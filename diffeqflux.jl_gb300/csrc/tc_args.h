@@ -20,6 +20,7 @@ struct BwdTcArgs {
   BwdArgs b;
   tc::OpList ops;               // one adjoint evaluation: forward recompute + VJP chain
   tc::OpList dwops;             // one accepted step: stage-stacked weight-gradient ops
+  tc::OpList ops7;              // an evaluation whose activations are re-emitted (copy-only forward ops)
   int dw_chunks;                // K chunks of all dwops (A-ring slots the producer fills)
   float* pbias;                 // [grid][3][4][nbias] pending bias quadrature: stage 1, 2..6, 7 (x 4 row groups)
   const float* bias[GBNDE_MAX_LAYERS];
