@@ -733,7 +733,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             }
             // stage 7 (i == 6) is at the same time as stage 6 (c6 = c7 = 1): on
             // a CTA's only tile its activations are re-emitted, not recomputed
-            ok = adj_eval(Y, x, slot, P, cw, kl, false, tile, i == 6 && G >= a.ntiles && c67_same);
+            const bool re = i == 6 && G >= a.ntiles && c67_same;
+            ok = adj_eval(Y, x, slot, P, cw, kl, false, tile, re);
+            if (re) ++nf_vjp;
             if (v) {
               if (i == 6) {
                 // lam, the stage value and the error sum over k1..k6 again

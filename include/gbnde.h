@@ -132,8 +132,9 @@ typedef struct {
   int retcode;            /* gbnde_retcode of the forward solve */
   int retcode_adj;        /* gbnde_retcode of the adjoint solve */
   double t_final;
-  long long nf_adj_vjp;   /* adjoint evaluations that ran the VJP only, reusing the activations of
-                             the previous evaluation at the same t and u (interval starts) */
+  long long nf_adj_vjp;   /* adjoint evaluations that ran the VJP products only, reusing the
+                             activations of the previous evaluation at the same t and u(t)
+                             (interval starts, and stage 7 of every step) */
 } gbnde_stats;
 
 /* ---- context ------------------------------------------------------------ */
