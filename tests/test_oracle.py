@@ -182,8 +182,9 @@ def test_float32_time_mode_keeps_float32_times():
     assert np.abs(a - b).max() < 1e-5 * np.abs(b).max()
 
 
-def test_adjoint_linear_known_answer():
-    """The InterpolatingAdjoint against closed forms on du/dt = M u with
+@pytest.mark.parametrize("sense", ["interpolating", "backsolve", "gauss"])
+def test_adjoint_linear_known_answer(sense):
+    """The adjoints against closed forms on du/dt = M u with
     L = sum_k g_k . u(t_k): dL/du0 = sum_k exp(M t_k)^T g_k exactly, and dL/dM
     against central differences of the matrix-exponential solution (no
     integrator in the reference values)."""
@@ -210,7 +211,12 @@ def test_adjoint_linear_known_answer():
     ts = np.linspace(0.0, 1.0, 6)
     g = rng.standard_normal((S, B, len(ts)))
     us, fwd = ots.solve_forward(Lin(M), u0, 0.0, 1.0, ts, 1e-12, 1e-12)
-    gu, gp, _ = ots.adjoint_interpolating(Lin(M), fwd, ts, g, 0.0, 1e-12, 1e-12)
+    if sense == "interpolating":
+        gu, gp, _ = ots.adjoint_interpolating(Lin(M), fwd, ts, g, 0.0, 1e-12, 1e-12)
+    elif sense == "backsolve":
+        gu, gp, _ = ots.adjoint_backsolve(Lin(M), us, ts, g, 0.0, 1e-12, 1e-12)
+    else:
+        gu, gp, _ = ots.adjoint_gauss(Lin(M), fwd, ts, g, 0.0, 1e-12, 1e-12)
     exact_u0 = sum(expm(M * t).T @ g[..., k] for k, t in enumerate(ts))
     assert np.abs(gu - exact_u0).max() < 1e-8 * np.abs(exact_u0).max()
 
