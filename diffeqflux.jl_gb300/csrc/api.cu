@@ -649,6 +649,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
     stats->nreject = cnt[CT_NREJECT];
     stats->retcode = status[ST_RETCODE];
     stats->t_final = tfinal;
+    stats->fwd_path = tcform ? GBNDE_PATH_TC : GBNDE_PATH_FP32;
   }
   c->fwd_retcode = status[ST_RETCODE];
   if (status[ST_BARRIER]) return fail(GBNDE_ERR_TIMEOUT, "forward grid barrier timed out");
@@ -1055,6 +1056,8 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
     stats->nf_recompute = cnt[CT_NRECOMP];
     stats->nf_adj_vjp = cnt[CT_NVJP];
     stats->retcode_adj = status[ST_RETCODE];
+    stats->adj_path = tcbwd ? GBNDE_PATH_TC
+                      : (a.dense != nullptr || backsolve) ? GBNDE_PATH_FP32 : GBNDE_PATH_FP32_RECOMPUTE;
   }
   if (status[ST_BARRIER]) return fail(GBNDE_ERR_TIMEOUT, "backward grid barrier timed out");
   return 0;
@@ -1161,6 +1164,7 @@ int gbnde_multishoot_forward(gbnde_ctx* c, int S, int nseg, const gbnde_segment*
     stats->naccept = cnt[1];
     stats->nreject = cnt[2];
     stats->retcode = worst;
+    stats->fwd_path = GBNDE_PATH_FP32;
   }
   c->ms_have = (worst == GBNDE_RET_SUCCESS);
   return 0;
@@ -1205,7 +1209,10 @@ int gbnde_multishoot_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, flo
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]));
   c->bwd_ms = ms;
-  if (stats) stats->retcode_adj = GBNDE_RET_SUCCESS;
+  if (stats) {
+    stats->retcode_adj = GBNDE_RET_SUCCESS;
+    stats->adj_path = GBNDE_PATH_FP32;
+  }
   return 0;
 }
 
@@ -1524,6 +1531,8 @@ int gbnde_graph_train_step(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B
     stats->nreject_adj = bc[CT_NREJECT];
     stats->retcode = fs[ST_RETCODE];
     stats->retcode_adj = bs[ST_RETCODE];
+    stats->fwd_path = c->rec.tc ? GBNDE_PATH_TC : GBNDE_PATH_FP32;
+    stats->adj_path = c->rec.bwd_tc_on ? GBNDE_PATH_TC : GBNDE_PATH_FP32;
   }
   if (graphed) *graphed = 1;
   return 0;

@@ -1,15 +1,19 @@
 // noalloc.cu -- the save-point loss (sum or mean of squared errors and its
 // cotangent) for callers that are not allowed to allocate device memory.
 //
-// Who needs this: a host function enqueued with cudaLaunchHostFunc may not
-// call CUDA API functions at all that could allocate; real-time loops cannot
-// afford the implicit device synchronisation of cudaMalloc/cudaFree; and hosts
-// that own every device byte through their own pool (a Julia or Python
+// Who needs this: real-time loops cannot afford the implicit device-wide
+// synchronisation of cudaMalloc/cudaFree in the middle of an iteration, and
+// hosts that own every device byte through their own pool (a Julia or Python
 // framework's caching allocator with a fixed budget) forbid allocations
 // outside it. gbnde_loss_device needs a context, and a context allocates. This
 // entry point takes only caller-owned buffers and keeps its scratch (one FP64
 // partial sum per chunk of the input) in a fixed array compiled into the
 // library.
+//
+// The call launches a kernel, copies the partial sums to the host and
+// synchronises the stream before it returns, so it is an ordinary host-side
+// call: it must not be made from a stream callback (a host function enqueued
+// with cudaLaunchHostFunc may make no CUDA calls).
 //
 // The scratch array lives in every device that loads the library, for the
 // life of the process (kMaxChunks doubles = 32 KB). All calls on a device
@@ -81,7 +85,9 @@ extern "C" int gbnde_loss_noalloc(const float* u, const float* target, size_t n,
   using namespace gbnde;
   if (!u || !target || !dL || !loss || n == 0) return GBNDE_ERR_INVALID;
   if (kind != 0 && kind != 1) return GBNDE_ERR_INVALID;
-  if ((long long)n > kChunk * (long long)kMaxChunks) return GBNDE_ERR_UNSUPPORTED;
+  // unsigned comparison: every size_t above the limit is refused (a signed
+  // cast would let sizes above LLONG_MAX wrap negative and pass)
+  if (n > (size_t)kChunk * (size_t)kMaxChunks) return GBNDE_ERR_UNSUPPORTED;
   double* scratch = nullptr;
   if (int r = scratch_ptr(&scratch)) return r;
   const int nchunks = (int)(((long long)n + kChunk - 1) / kChunk);

@@ -31,6 +31,10 @@ RET_UNSTABLE = 3
 RET_BARRIER_TIMEOUT = 4
 RETCODE_NAMES = {0: "Success", 1: "MaxIters", 2: "DtLessThanMin", 3: "Unstable", 4: "BarrierTimeout"}
 
+# gbnde_stats.fwd_path / adj_path (gbnde_path)
+PATH_NONE, PATH_FP32, PATH_FP32_RECOMPUTE, PATH_TC, PATH_TC_RECOMPUTE = 0, 1, 2, 3, 4
+PATH_NAMES = {0: "none", 1: "fp32", 2: "fp32_recompute", 3: "tc", 4: "tc_recompute"}
+
 
 class MlpDesc(C.Structure):
     _fields_ = [
@@ -71,6 +75,7 @@ class Stats(C.Structure):
         ("retcode", C.c_int), ("retcode_adj", C.c_int),
         ("t_final", C.c_double),
         ("nf_adj_vjp", C.c_longlong),
+        ("fwd_path", C.c_int), ("adj_path", C.c_int),
     ]
 
     def as_dict(self):

@@ -30,12 +30,18 @@ class _SolveSaveat(torch.autograd.Function):
             _sync(u0_cm)
             solver.set_params_device(pc)
             stats = solver.forward_device(u0_cm, out, desc, S, B)
-            ctx._keep = (u0_cm, out, pc)
+            ctx._keep = (u0_cm, out, pc, desc)
             arr = out.permute(2, 1, 0)
         else:
-            solver.set_params(p.detach().cpu().numpy())
-            a, stats = solver.forward(u0.detach().cpu().numpy(), desc)
+            pn = p.detach().cpu().numpy()
+            un = u0.detach().cpu().numpy()
+            solver.set_params(pn)
+            a, stats = solver.forward(un, desc)
+            ctx._keep = (un, pn, desc)
             arr = torch.from_numpy(a.copy())
+        # the library differentiates the context's last forward: remember
+        # which one this is
+        ctx.generation = solver.generation
         ctx.node = node
         ctx.stats = stats
         node.last_stats = stats
@@ -48,6 +54,23 @@ class _SolveSaveat(torch.autograd.Function):
         solver = node.solver
         if ctx.stats.retcode != _lib.RET_SUCCESS:
             raise RuntimeError("cannot differentiate a failed solve (retcode %d)" % ctx.stats.retcode)
+        if solver.generation != ctx.generation:
+            # Another solve ran on this context after this node's forward (the
+            # layer was called twice before backward, or a training step ran):
+            # solve this node's forward again, from the same u0 and p, so that
+            # the adjoint reads its own checkpoints. The solve is deterministic,
+            # so the checkpoints are the ones the saved states came from.
+            if ctx.is_cuda:
+                u0_cm, out, pc, desc = ctx._keep
+                S, B = u0_cm.shape
+                redo = torch.empty_like(out)
+                solver.set_params_device(pc)
+                solver.forward_device(u0_cm, redo, desc, S, B)
+            else:
+                un, pn, desc = ctx._keep
+                solver.set_params(pn)
+                solver.forward(un, desc)
+            ctx.generation = solver.generation
         if ctx.is_cuda:
             g_cm = g.to(torch.float32).permute(2, 1, 0).contiguous()
             S, B, _ = g.shape

@@ -72,6 +72,7 @@ class FFJORD:
         zT = np.empty((B, self.d), np.float32)
         st = _lib.Stats()
         nz = None if noise is None else np.ascontiguousarray(noise, np.float32)
+        s.bump()
         _lib.check(s.lib.gbnde_ffjord_forward(s.h, C.byref(self.desc()), self.d, B, x.ctypes.data,
                                               None if nz is None else nz.ctypes.data, logpx.ctypes.data,
                                               zT.ctypes.data, C.byref(st)))
@@ -112,11 +113,17 @@ class FFJORD:
         class _Fn(torch.autograd.Function):
             @staticmethod
             def forward(ctx, xt, pt):
-                lp, _, _ = layer.forward_np(xt.detach().cpu().numpy(), pt.detach().cpu().numpy(), noise)
+                ctx.inputs = (xt.detach().cpu().numpy(), pt.detach().cpu().numpy())
+                lp, _, _ = layer.forward_np(ctx.inputs[0], ctx.inputs[1], noise)
+                ctx.generation = layer.solver.generation
                 return torch.from_numpy(lp).to(pt.device)
 
             @staticmethod
             def backward(ctx, g):
+                if layer.solver.generation != ctx.generation:
+                    # another solve ran on the context since this forward: the
+                    # adjoint needs this call's own solve, so it is run again
+                    layer.forward_np(ctx.inputs[0], ctx.inputs[1], noise)
                 dx, dp, _ = layer.backward_np(g.detach().cpu().numpy())
                 return torch.from_numpy(np.ascontiguousarray(dx)).to(g.device), torch.from_numpy(dp).to(g.device)
 

@@ -184,6 +184,16 @@ class Solver:
         self.h = h
         self.nparams = int(self.lib.gbnde_nparams(h))
         self.state_dim = model.dims[-1]
+        # Count of solves run on this context. The library's backward
+        # differentiates the context's LAST forward solve; an autograd node
+        # records the count of its own forward and re-solves when another
+        # forward (or a training step) has run since.
+        self.generation = 0
+
+    def bump(self):
+        """Marks that a call replaced the context's last forward solve."""
+        self.generation += 1
+        return self.generation
 
     def close(self):
         if getattr(self, "h", None):
@@ -218,6 +228,7 @@ class Solver:
 
     def forward(self, u0, desc):
         """u0: (S, B) array. Returns (usave (S, B, nsave), stats)."""
+        self.bump()
         u0 = np.asarray(u0, dtype=np.float32)
         S, B = u0.shape
         buf = np.ascontiguousarray(u0.T)            # column-major S x B
@@ -259,6 +270,7 @@ class Solver:
         _lib.check(self.lib.gbnde_set_params_device(self.h, p.data_ptr(), p.numel()))
 
     def forward_device(self, u0_cm, usave_cm, desc, S, B):
+        self.bump()
         st = _lib.Stats()
         _lib.check(self.lib.gbnde_forward_device(self.h, C.byref(desc), S, B, u0_cm.data_ptr(),
                                                  usave_cm.data_ptr(), C.byref(st)))
@@ -280,6 +292,7 @@ class Solver:
                    eps=1e-8, kind=1):
         """One Adam iteration on device tensors (gbnde_train_step): p, m, v are
         updated in place; returns (loss, stats)."""
+        self.bump()
         opt = _lib.Adam(float(lr), float(beta1), float(beta2), float(eps))
         out = C.c_double()
         st = _lib.Stats()
@@ -293,6 +306,7 @@ class Solver:
                          beta2=0.999, eps=1e-8, kind=1):
         """gbnde_graph_train_step: the same iteration replayed as one CUDA graph
         after the first call; returns (loss, stats, ran_as_graph)."""
+        self.bump()
         opt = _lib.Adam(float(lr), float(beta1), float(beta2), float(eps))
         out = C.c_double()
         st = _lib.Stats()
@@ -306,6 +320,7 @@ class Solver:
     def autotune(self, u0_cm, desc, S, B):
         """gbnde_autotune: times the FP32 kernels at each rows-per-tile choice on
         this shape and keeps the fastest; returns (forward, adjoint) tile rows."""
+        self.bump()
         t = (C.c_int * 2)()
         _lib.check(self.lib.gbnde_autotune(self.h, C.byref(desc), S, B, u0_cm.data_ptr(), t))
         return int(t[0]), int(t[1])

@@ -67,6 +67,7 @@ class MultipleShooter:
         out = np.empty((len(packed.saveat), S), dtype=np.float32)
         ret = np.zeros(packed.nseg, dtype=np.int32)
         st = _lib.Stats()
+        s.bump()
         _lib.check(s.lib.gbnde_multishoot_forward(
             s.h, S, packed.nseg, packed.segs, packed.saveat.ctypes.data_as(C.POINTER(C.c_double)),
             len(packed.saveat), packed.u0.ctypes.data, self.abstol, self.reltol, self.maxiters,

@@ -65,7 +65,9 @@ mutable struct Stats
     retcode_adj::Cint
     t_final::Cdouble
     nf_adj_vjp::Clonglong
-    Stats() = new(0, 0, 0, 0, 0, 0, 0, 0, 0, 0.0, 0)
+    fwd_path::Cint
+    adj_path::Cint
+    Stats() = new(0, 0, 0, 0, 0, 0, 0, 0, 0, 0.0, 0, 0, 0)
 end
 
 const RETCODES = (SciMLBase.ReturnCode.Success, SciMLBase.ReturnCode.MaxIters,

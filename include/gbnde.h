@@ -135,7 +135,26 @@ typedef struct {
   long long nf_adj_vjp;   /* adjoint evaluations that ran the VJP products only, reusing the
                              activations of the previous evaluation at the same t and u(t)
                              (interval starts, and stage 7 of every step) */
+  int fwd_path;           /* gbnde_path of the forward solve that ran */
+  int adj_path;           /* gbnde_path of the adjoint solve that ran */
 } gbnde_stats;
+
+/* Which kernels a solve ran on (gbnde_stats.fwd_path / adj_path). A BF16
+ * context runs the tensor-core kernels where they cover the model and the
+ * solve; the rest (FFJORD, multiple shooting, the Backsolve and quadrature
+ * adjoints, and gradients past the tensor-core adjoint's storage) runs on the
+ * plain FP32 kernels, and these fields say so. */
+typedef enum {
+  GBNDE_PATH_NONE = 0,            /* no solve of this kind ran in the call */
+  GBNDE_PATH_FP32 = 1,            /* plain FP32 kernels (adjoint: dense stage storage,
+                                     or Backsolve's co-integrated u) */
+  GBNDE_PATH_FP32_RECOMPUTE = 2,  /* plain FP32 adjoint, each save interval recomputed
+                                     from its checkpoint: O(checkpoints) memory */
+  GBNDE_PATH_TC = 3,              /* tensor-core (BF16-form) kernels; adjoint on the
+                                     forward's dense stage storage */
+  GBNDE_PATH_TC_RECOMPUTE = 4     /* tensor-core adjoint, each save interval recomputed on
+                                     the tensor-core forward from its checkpoint */
+} gbnde_path;
 
 /* ---- context ------------------------------------------------------------ */
 /* Replaces the model/parameter setup that StatefulLuxLayer does per call
@@ -256,7 +275,6 @@ int gbnde_graph_train_step(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int S, 
  * No counterpart in the reference. Same loss and cotangent as
  * gbnde_loss_device (kind 0: sum of squared errors, kind 1: their mean) on n
  * floats of caller-owned device memory, for callers that must not allocate:
- * host functions run by cudaLaunchHostFunc (no CUDA calls that may allocate),
  * real-time loops that cannot take the device-wide synchronisation of
  * cudaMalloc/cudaFree, and hosts whose own pool owns every device byte. It
  * needs no context: its scratch is a 32 KB array compiled into the library
@@ -266,7 +284,10 @@ int gbnde_graph_train_step(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int S, 
  * before any stream capture. All calls on a device share the scratch: calls
  * whose kernels overlap on the GPU (other streams or host threads) race and
  * may return wrong losses. stream: a cudaStream_t, or NULL for the default
- * stream; the call returns after the loss is on the host. */
+ * stream. The call synchronises that stream and returns after the loss is on
+ * the host, so it is made from ordinary host code, never from a stream
+ * callback (a host function enqueued with cudaLaunchHostFunc may make no CUDA
+ * calls). */
 #define GBNDE_LOSS_NOALLOC_MAX_N (4096LL * 65536LL)
 int gbnde_loss_noalloc(const float* usave_dev, const float* target_dev, size_t n, int kind,
                        float* dL_dusave_dev, double* loss, void* stream);

@@ -32,14 +32,16 @@ def test_ctypes_layout_matches_c(tmp_path):
     src = tmp_path / "sz.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "gbnde.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(gbnde_mlp_desc),"
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(gbnde_mlp_desc),"
         " sizeof(gbnde_solve_desc), sizeof(gbnde_stats), offsetof(gbnde_solve_desc, saveat),"
-        " offsetof(gbnde_stats, retcode), offsetof(gbnde_stats, t_final));return 0;}\n")
+        " offsetof(gbnde_stats, retcode), offsetof(gbnde_stats, t_final),"
+        " offsetof(gbnde_stats, fwd_path), offsetof(gbnde_stats, adj_path));return 0;}\n")
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
     assert vals == [C.sizeof(L.MlpDesc), C.sizeof(L.SolveDesc), C.sizeof(L.Stats),
-                    L.SolveDesc.saveat.offset, L.Stats.retcode.offset, L.Stats.t_final.offset]
+                    L.SolveDesc.saveat.offset, L.Stats.retcode.offset, L.Stats.t_final.offset,
+                    L.Stats.fwd_path.offset, L.Stats.adj_path.offset]
 
 
 def test_strerror_and_errors_without_device(lib):

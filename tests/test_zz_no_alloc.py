@@ -52,8 +52,9 @@ def test_loss_noalloc_matches_loss_device_twice():
             # compensated FP32 partial sums: about 1e-9 relative apart
             assert abs(out.value - ref) <= 1e-8 * abs(ref), (call, kind, out.value, ref)
             assert torch.equal(dl_new, dl_ref)
-    # sizes beyond the fixed scratch are refused, not truncated
-    big = C.c_size_t(4096 * 65536 + 1)
+    # sizes beyond the fixed scratch are refused, not truncated -- also those
+    # that a signed comparison would see as negative
     out = C.c_double()
-    assert lib.gbnde_loss_noalloc(us.data_ptr(), us.data_ptr(), big, 0, us.data_ptr(), C.byref(out),
-                                  stream) == _lib.ERR_UNSUPPORTED
+    for big in (4096 * 65536 + 1, 2**63 + 5, 2**64 - 1):
+        assert lib.gbnde_loss_noalloc(us.data_ptr(), us.data_ptr(), C.c_size_t(big), 0, us.data_ptr(),
+                                      C.byref(out), stream) == _lib.ERR_UNSUPPORTED, big
