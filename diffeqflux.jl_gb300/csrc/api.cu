@@ -57,6 +57,9 @@ int launch_adam(float* p, float* m, float* v, const float* g, size_t n, double l
 int launch_plan_intervals(Interval* iv, int niv, const double* steplog, const long long* fcounters,
                           const int* fstatus, long long dense_slots, long long maxsteps, int* flags,
                           cudaStream_t st);
+int launch_ms_loss(const float* u, const float* d, const int* colseg, const int* segoff, const int* segn,
+                   const int* nxt, int S, int ncol, int kind, double cont, float* dL, double* part, int nblk,
+                   cudaStream_t st);
 int launch_loss_finalize(const double* part, int nblk, size_t n, int kind, double* out, cudaStream_t st);
 int launch_adam_graph(float* p, float* m, float* v, const float* g, size_t n, double lr, double b1, double b2,
                       double eps, const double* coef, const int* flags, const int* bstatus, cudaStream_t st);
@@ -195,6 +198,11 @@ struct gbnde_ctx {
   DBuf ms_segs, ms_saveat, ms_u0, ms_usave, ms_dense, ms_steplog, ms_nacc, ms_ret, ms_cnt, ms_dldu,
       ms_dldu0, ms_bar, ms_mu, ms_dldp;
   bool ms_have = false;
+  // multiple-shooting loss on the device: the data, the column/segment maps
+  // and the per-block partials; ms_dl_ok: ms_dldu holds the last loss's cotangent
+  DBuf ms_data, ms_map, ms_part;
+  std::vector<gbnde_segment> ms_hsegs;
+  bool ms_dl_ok = false;
   // FFJORD
   DBuf ffnoise, ffu0, ffus;
   int fS = 0;          // state dim of the last forward (d + 1 for FFJORD)
@@ -1112,6 +1120,8 @@ int gbnde_multishoot_forward(gbnde_ctx* c, int S, int nseg, const gbnde_segment*
   }
   if (int r = set_device(c)) return r;
   c->ms_have = false;
+  c->ms_dl_ok = false;
+  c->ms_hsegs.assign(segs, segs + nseg);
   c->ms_S = S;
   c->ms_nseg = nseg;
   c->ms_nsave = nsave_total;
@@ -1170,10 +1180,67 @@ int gbnde_multishoot_forward(gbnde_ctx* c, int S, int nseg, const gbnde_segment*
   return 0;
 }
 
+int gbnde_multishoot_loss(gbnde_ctx* c, const float* data, const int* seg_next, int loss_kind,
+                          double continuity_term, double* loss) {
+  if (!c || !data || !seg_next || !loss) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (loss_kind != 0 && loss_kind != 1) return fail(GBNDE_ERR_INVALID, "loss_kind must be 0 or 1");
+  if (!c->ms_have) return fail(GBNDE_ERR_STATE, "the loss needs a successful multishoot forward first");
+  if (int r = set_device(c)) return r;
+  const int S = c->ms_S, nseg = c->ms_nseg, ncol = c->ms_nsave;
+  // column -> segment, segment offsets/lengths and successors (every save
+  // column belongs to exactly one segment; a segment is continued by at most
+  // one other)
+  std::vector<int> map((size_t)ncol + 3 * (size_t)nseg, -1);
+  int* colseg = map.data();
+  int* segoff = colseg + ncol;
+  int* segn = segoff + nseg;
+  int* nxt = segn + nseg;
+  std::vector<char> taken(nseg, 0);
+  for (int g = 0; g < nseg; ++g) {
+    const gbnde_segment& q = c->ms_hsegs[g];
+    segoff[g] = q.save_off;
+    segn[g] = q.nsave;
+    for (int k = 0; k < q.nsave; ++k) {
+      if (colseg[q.save_off + k] != -1) return fail(GBNDE_ERR_INVALID, "save column %d is in two segments", q.save_off + k);
+      colseg[q.save_off + k] = g;
+    }
+    const int nx = seg_next[g];
+    if (nx < -1 || nx >= nseg || nx == g || (nx >= 0 && taken[nx]))
+      return fail(GBNDE_ERR_INVALID, "seg_next[%d] = %d is not a segment that continues it", g, nx);
+    if (nx >= 0) taken[nx] = 1;
+    nxt[g] = nx;
+  }
+  for (int j = 0; j < ncol; ++j)
+    if (colseg[j] < 0) return fail(GBNDE_ERR_INVALID, "save column %d is in no segment", j);
+  const int nblk = std::max(1, std::min(1024, (int)(((size_t)S * ncol + 255) / 256)));
+  int r = 0;
+  if ((r = c->ms_data.ensure((size_t)S * ncol * 4)) || (r = c->ms_map.ensure(map.size() * sizeof(int))) ||
+      (r = c->ms_part.ensure(nblk * sizeof(double))) || (r = c->ms_dldu.ensure((size_t)S * ncol * 4)))
+    return r;
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(c->ms_data.p, data, (size_t)S * ncol * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->ms_map.p, map.data(), map.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  const int* dm = c->ms_map.as<int>();
+  if (launch_ms_loss(c->ms_usave.as<float>(), c->ms_data.as<float>(), dm, dm + ncol, dm + ncol + nseg,
+                     dm + ncol + 2 * nseg, S, ncol, loss_kind, continuity_term, c->ms_dldu.as<float>(),
+                     c->ms_part.as<double>(), nblk, st))
+    return fail(GBNDE_ERR_CUDA, "multishoot loss launch failed");
+  std::vector<double> part(nblk);
+  CK(cudaMemcpyAsync(part.data(), c->ms_part.p, nblk * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  double s = 0.0;
+  for (double x : part) s += x;
+  *loss = s;
+  c->ms_dl_ok = true;
+  return 0;
+}
+
 int gbnde_multishoot_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, float* dLdp,
                               gbnde_stats* stats) {
-  if (!c || !dLdu || !dLdu0 || !dLdp) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (!c || !dLdp) return fail(GBNDE_ERR_INVALID, "null argument");
   if (!c->ms_have) return fail(GBNDE_ERR_STATE, "backward needs a successful multishoot forward first");
+  if (!dLdu && !c->ms_dl_ok)
+    return fail(GBNDE_ERR_STATE, "dL_dusave = NULL needs a gbnde_multishoot_loss after the forward");
   if (int r = set_device(c)) return r;
   const int S = c->ms_S, nseg = c->ms_nseg;
   const size_t SN = (size_t)S * nseg;
@@ -1193,7 +1260,10 @@ int gbnde_multishoot_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, flo
       (r = c->ms_dldp.ensure((size_t)P * 4)))
     return r;
   cudaStream_t st = c->stream;
-  CK(cudaMemcpyAsync(c->ms_dldu.p, dLdu, (size_t)S * c->ms_nsave * 4, cudaMemcpyHostToDevice, st));
+  if (dLdu) {
+    CK(cudaMemcpyAsync(c->ms_dldu.p, dLdu, (size_t)S * c->ms_nsave * 4, cudaMemcpyHostToDevice, st));
+    c->ms_dl_ok = false;  // the device cotangent is now the caller's
+  }
   m.dLdu = c->ms_dldu.as<float>();
   m.dLdu0 = c->ms_dldu0.as<float>();
   m.bar = c->ms_bar.as<float>();
@@ -1203,7 +1273,7 @@ int gbnde_multishoot_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, flo
   if (launch_ms_bwd(m, grid, smem, st)) return fail(GBNDE_ERR_CUDA, "multishoot backward launch failed");
   if (launch_reduce_mu(m.mu_acc, grid, P, c->ms_dldp.as<float>(), st)) return fail(GBNDE_ERR_CUDA, "reduce failed");
   CK(cudaEventRecord(c->ev[3], st));
-  CK(cudaMemcpyAsync(dLdu0, c->ms_dldu0.p, SN * 4, cudaMemcpyDeviceToHost, st));
+  if (dLdu0) CK(cudaMemcpyAsync(dLdu0, c->ms_dldu0.p, SN * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(dLdp, c->ms_dldp.p, (size_t)P * 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   float ms = 0.f;

@@ -90,6 +90,58 @@ int launch_loss(const float* usave, const float* target, size_t n, int kind, flo
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+// Multiple-shooting loss over the packed saves (S x nsave columns, one per
+// save of every segment, in segment order; src/multiple_shooting.jl:69-81):
+// column j of segment g adds w_g * sum_s (u - d)^2 (w_g = 1 or 1 / (S n_g)),
+// and the last column of a segment g whose trajectory continues in segment
+// nxt[g] adds cont * sum_s |u[j] - d[first column of nxt[g]]| (the default
+// continuity loss, :243). dL is written once per element (the fit term and,
+// on a segment's last column, the continuity term of that same column), so
+// nothing is accumulated concurrently. One FP64 partial per block.
+struct MsLossArgs {
+  const float* u;       // S x ncol predictions
+  const float* d;       // S x ncol data, same packing
+  const int* colseg;    // segment of each column
+  const int* segoff;    // first column of each segment
+  const int* segn;      // columns of each segment
+  const int* nxt;       // next segment of the same trajectory, or -1
+  int S, ncol, kind;
+  double cont;
+  float* dL;
+  double* part;
+};
+
+__global__ void ms_loss_kernel(MsLossArgs a) {
+  __shared__ double red[40];
+  const size_t n = (size_t)a.S * a.ncol;
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(i / a.S), r = (int)(i - (size_t)j * a.S);
+    const int g = a.colseg[j];
+    const double w = a.kind == 1 ? 1.0 / ((double)a.S * a.segn[g]) : 1.0;
+    const float e = a.u[i] - a.d[i];
+    s += w * (double)e * (double)e;
+    float gr = (float)(2.0 * w) * e;
+    const int nx = a.nxt[g];
+    if (nx >= 0 && j == a.segoff[g] + a.segn[g] - 1) {
+      const float c = a.u[i] - a.d[(size_t)a.segoff[nx] * a.S + r];
+      s += a.cont * fabs((double)c);
+      gr += (float)a.cont * (c > 0.f ? 1.f : (c < 0.f ? -1.f : 0.f));
+    }
+    a.dL[i] = gr;
+  }
+  s = block_sum_double(s, red);
+  if (threadIdx.x == 0) a.part[blockIdx.x] = s;
+}
+
+int launch_ms_loss(const float* u, const float* d, const int* colseg, const int* segoff, const int* segn,
+                   const int* nxt, int S, int ncol, int kind, double cont, float* dL, double* part, int nblk,
+                   cudaStream_t st) {
+  MsLossArgs a{u, d, colseg, segoff, segn, nxt, S, ncol, kind, cont, dL, part};
+  ms_loss_kernel<<<nblk, 256, 0, st>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 // Adam on n parameters: moments in FP32, the update in FP32 with the bias
 // corrections c1 = 1 / (1 - b1^t), c2 = 1 / (1 - b2^t) computed on the host.
 __global__ void adam_kernel(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,

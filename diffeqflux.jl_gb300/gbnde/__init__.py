@@ -13,4 +13,5 @@ from .layers import (  # noqa: F401
 )
 from .ffjord import FFJORD, FFJORDDistribution  # noqa: F401
 from .layers import AugmentedNDELayer, DimMover  # noqa: F401
-from .multiple_shooting import group_ranges, multiple_shoot, multiple_shoot_batch  # noqa: F401
+from .multiple_shooting import (group_ranges, mse_loss, multiple_shoot, multiple_shoot_batch,  # noqa: F401
+                                sse_loss)

@@ -62,7 +62,7 @@ class _SolveSaveat(torch.autograd.Function):
             # so the checkpoints are the ones the saved states came from.
             if ctx.is_cuda:
                 u0_cm, out, pc, desc = ctx._keep
-                S, B = u0_cm.shape
+                B, S = u0_cm.shape   # column-major S x B
                 redo = torch.empty_like(out)
                 solver.set_params_device(pc)
                 solver.forward_device(u0_cm, redo, desc, S, B)

@@ -9,7 +9,11 @@ continuity_term * continuity_loss(pred_prev_end, data_first). All groups -- of
 one trajectory or, with `multiple_shoot_batch`, of many trajectories with
 uneven lengths and group sizes -- run in one kernel launch. With torch tensors
 for `p` the predictions are differentiable; their backward is the kernel's
-discrete adjoint.
+discrete adjoint. With `loss_function` = `mse_loss` / `sse_loss` (or "mse" /
+"sse") and the default continuity loss, the loss and its cotangent are one
+device kernel (gbnde_multishoot_loss) and the gradient runs from that
+cotangent without a host round trip; any other loss function runs on the
+host in torch/numpy, per group, as the reference's loop does.
 """
 import ctypes as C
 import math
@@ -30,27 +34,69 @@ def _default_continuity_loss(u_end, u_0):
     return (u_end - u_0).abs().sum() if hasattr(u_end, "abs") else np.sum(np.abs(u_end - u_0))
 
 
-class _Packed:
-    """Segment table of one or many trajectories."""
+def sse_loss(u, uh):
+    """``sum(abs2, u .- uh)``: recognised by multiple_shoot, which then evaluates
+    the whole loss (and the continuity terms) in one kernel on the device."""
+    return ((u - uh) ** 2).sum()
 
-    def __init__(self, trajectories):
-        # trajectories: list of (data S x n, tsteps n, group_size)
-        segs, saveat, u0, self.groups = [], [], [], []
-        for ti, (data, ts, gs) in enumerate(trajectories):
+
+def mse_loss(u, uh):
+    """``mean(abs2, u .- uh)`` per group; the device-fused form, as sse_loss."""
+    return ((u - uh) ** 2).mean()
+
+
+_FUSED_KIND = {sse_loss: 0, mse_loss: 1, "sse": 0, "mse": 1}
+
+
+class _Layout:
+    """Segment table of a set of trajectories (lengths and group sizes): the
+    packed save times, each trajectory's packed column indices into its data,
+    the first data column of every segment and each segment's successor."""
+
+    def __init__(self, shapes):
+        segs, saveat, self.groups, self.cols, self.starts, nxt = [], [], [], [], [], []
+        for ti, (ts, gs) in enumerate(shapes):
             ts = np.asarray(ts, dtype=np.float64)
-            for rg in group_ranges(len(ts), gs):
+            rgs = group_ranges(len(ts), gs)
+            idx = []
+            for k, rg in enumerate(rgs):
                 seg = _lib.Segment()
                 seg.t0, seg.t1 = float(ts[rg.start]), float(ts[rg.stop - 1])
                 seg.save_off = len(saveat)
                 seg.nsave = len(rg)
+                nxt.append(len(segs) + 1 if k + 1 < len(rgs) else -1)
                 segs.append(seg)
                 saveat.extend(ts[rg.start:rg.stop].tolist())
-                u0.append(np.asarray(data, dtype=np.float32)[:, rg.start])
+                idx.extend(range(rg.start, rg.stop))
                 self.groups.append((ti, rg))
+            self.cols.append(np.asarray(idx, dtype=np.int64))
+            self.starts.append(np.asarray([rg.start for rg in rgs], dtype=np.int64))
         self.segs = (_lib.Segment * len(segs))(*segs)
         self.saveat = np.ascontiguousarray(saveat, dtype=np.float64)
-        self.u0 = np.ascontiguousarray(np.stack(u0, axis=1).T)  # nseg x S (column-major S x nseg)
+        self.seg_next = np.ascontiguousarray(nxt, dtype=np.int32)
         self.nseg = len(segs)
+
+
+class _Packed:
+    """Segment table and packed values (initial states, data at the saves) of
+    one or many trajectories; the table is reused across calls with the same
+    lengths and group sizes."""
+
+    _cache = {}
+
+    def __init__(self, trajectories):
+        # trajectories: list of (data S x n, tsteps n, group_size)
+        key = tuple((len(ts), int(gs), float(ts[0]), float(ts[-1])) for _, ts, gs in trajectories)
+        lay = _Packed._cache.get(key)
+        if lay is None:
+            lay = _Layout([(ts, gs) for _, ts, gs in trajectories])
+            _Packed._cache = {key: lay}  # keep the last layout only
+        self.layout = lay
+        self.segs, self.saveat, self.nseg, self.groups = lay.segs, lay.saveat, lay.nseg, lay.groups
+        ds = [np.asarray(d, dtype=np.float32) for d, _, _ in trajectories]
+        # u0: nseg x S (column-major S x nseg); data at the saves: nsave_total x S
+        self.u0 = np.ascontiguousarray(np.concatenate([d[:, st].T for d, st in zip(ds, lay.starts)], axis=0))
+        self.data = np.ascontiguousarray(np.concatenate([d[:, c].T for d, c in zip(ds, lay.cols)], axis=0))
 
 
 class MultipleShooter:
@@ -62,7 +108,10 @@ class MultipleShooter:
 
     def forward(self, packed, p):
         s = self.solver
-        s.set_params(p)
+        if hasattr(p, "is_cuda") and p.is_cuda:
+            s.set_params_device(p.detach().to(dtype=__import__("torch").float32).contiguous())
+        else:
+            s.set_params(p.detach().cpu().numpy() if hasattr(p, "detach") else p)
         S = s.state_dim
         out = np.empty((len(packed.saveat), S), dtype=np.float32)
         ret = np.zeros(packed.nseg, dtype=np.int32)
@@ -85,6 +134,77 @@ class MultipleShooter:
                                                    C.byref(st)))
         return du0.T, dp
 
+    def loss(self, packed, kind, continuity_term):
+        """gbnde_multishoot_loss on the saves of the last forward; the cotangent stays on the device."""
+        s = self.solver
+        out = C.c_double()
+        _lib.check(s.lib.gbnde_multishoot_loss(s.h, packed.data.ctypes.data, packed.layout.seg_next.ctypes.data,
+                                               int(kind), float(continuity_term), C.byref(out)))
+        return out.value
+
+    def backward_fused(self):
+        """dL/dp of the last gbnde_multishoot_loss (its cotangent never leaves the device)."""
+        s = self.solver
+        dp = np.empty(s.nparams, dtype=np.float32)
+        st = _lib.Stats()
+        _lib.check(s.lib.gbnde_multishoot_backward(s.h, None, None, dp.ctypes.data, C.byref(st)))
+        return dp
+
+
+class _Groups:
+    """The group predictions (S x len(range) each), sliced from the packed saves on access."""
+
+    def __init__(self, us, groups, segs):
+        self._us, self._groups, self._segs = us, groups, segs
+
+    def __len__(self):
+        return len(self._groups)
+
+    def __getitem__(self, k):
+        if isinstance(k, slice):
+            return [self[i] for i in range(*k.indices(len(self)))]
+        seg = self._segs[k]
+        return self._us[:, seg.save_off:seg.save_off + seg.nsave]
+
+    def __iter__(self):
+        return (self[k] for k in range(len(self)))
+
+
+def _fused_loss(shooter, packed, p, kind, continuity_term):
+    """Forward of every group, loss and continuity terms in one kernel, and
+    (with a torch p) the adjoint as the loss's backward. Returns (loss, preds)."""
+    try:
+        import torch
+    except ImportError:  # pragma: no cover
+        torch = None
+    us, ret, _ = shooter.forward(packed, p)
+    shooter._nseg = packed.nseg
+    preds = _Groups(us, packed.groups, packed.segs)
+    if np.any(ret != 0):
+        return math.inf, preds
+    L = shooter.loss(packed, kind, continuity_term)
+    if torch is None or not isinstance(p, torch.Tensor):
+        return L, preds
+    solver = shooter.solver
+    gen = solver.generation
+
+    class _Fn(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, pt):
+            return torch.tensor(L, dtype=torch.float64, device=pt.device)
+
+        @staticmethod
+        def backward(ctx, g):
+            if solver.generation != gen:
+                # another solve ran on the context: this call's forward and
+                # loss are solved again (deterministic: the same cotangent)
+                shooter.forward(packed, p)
+                shooter.loss(packed, kind, continuity_term)
+            dp = torch.from_numpy(shooter.backward_fused()).to(g.device)
+            return (g.to(torch.float32) * dp).to(p.dtype)
+
+    return _Fn.apply(p), preds
+
 
 def _predict(shooter, packed, p):
     """Saved states (S x nsave_total); differentiable in p when p is a torch tensor."""
@@ -96,15 +216,20 @@ def _predict(shooter, packed, p):
         class _Fn(torch.autograd.Function):
             @staticmethod
             def forward(ctx, pt):
-                us, ret, st = shooter.forward(packed, pt.detach().cpu().numpy())
+                ctx.pn = pt.detach().cpu().numpy()
+                us, ret, st = shooter.forward(packed, ctx.pn)
                 shooter._nseg = packed.nseg
                 ctx.ret = ret
+                ctx.generation = shooter.solver.generation
                 return torch.from_numpy(np.ascontiguousarray(us)).to(pt.device), torch.from_numpy(ret)
 
             @staticmethod
             def backward(ctx, g, _gret):
                 if np.any(ctx.ret != 0):
                     raise RuntimeError("cannot differentiate multiple shooting with a failed group")
+                if shooter.solver.generation != ctx.generation:
+                    shooter.forward(packed, ctx.pn)  # another solve ran since: solve this one again
+                    shooter._nseg = packed.nseg
                 _, dp = shooter.backward(g.detach().cpu().numpy())
                 return torch.from_numpy(dp).to(g.device)
 
@@ -154,10 +279,18 @@ def multiple_shoot_batch(p, trajectories, model_or_solver, loss_function, *, con
     The loss sums the per-trajectory multiple-shooting losses."""
     from .layers import Chain, Solver
     solver = model_or_solver if isinstance(model_or_solver, Solver) else Solver(model_or_solver, precision, device)
-    if continuity_loss is None:
-        continuity_loss = _default_continuity_loss
     packed = _Packed(trajectories)
     shooter = MultipleShooter(solver, abstol, reltol, maxiters)
+    try:
+        kind = _FUSED_KIND.get(loss_function)
+    except TypeError:  # an unhashable loss object
+        kind = None
+    if kind is not None and continuity_loss is None:
+        # sum/mean of squares with the default continuity loss: the whole loss
+        # on the device, no per-group host work
+        return _fused_loss(shooter, packed, p, kind, continuity_term)
+    if continuity_loss is None:
+        continuity_loss = _default_continuity_loss
     us, ret = _predict(shooter, packed, p)
     preds_loss, preds = _loss(packed, us, trajectories, loss_function, continuity_loss, continuity_term)
     if np.any(ret != 0):

@@ -220,9 +220,25 @@ int gbnde_multishoot_forward(gbnde_ctx* ctx, int S, int nseg, const gbnde_segmen
                              const double* saveat, int nsave_total, const float* u0,
                              double abstol, double reltol, long long maxiters, float* usave,
                              int* retcodes, gbnde_stats* stats);
+/* The loss of multiple_shoot on the device (src/multiple_shooting.jl:69-81):
+ * over the saves of the last gbnde_multishoot_forward,
+ *   loss = sum_g lf(data_g, pred_g)
+ *        + continuity_term * sum_{g : seg_next[g] >= 0} sum(abs, pred_g[:, end] - data_{seg_next[g]}[:, 1])
+ * with loss_function lf = sum of squares (loss_kind 0) or their mean over the
+ * group's S x nsave entries (loss_kind 1), and the default continuity loss
+ * sum(abs, u_end - u_0) (:243). data: S x nsave_total host array packed like
+ * the saves (column j = the data point of save j). seg_next[g]: the segment
+ * that continues segment g's trajectory (the next group), or -1 for a
+ * trajectory's last group. Keeps dL/dusave on the device for
+ * gbnde_multishoot_backward(ctx, NULL, ...). The forward must have succeeded
+ * (a failed group makes the reference's loss Inf; the caller reports that). */
+int gbnde_multishoot_loss(gbnde_ctx* ctx, const float* data, const int* seg_next, int loss_kind,
+                          double continuity_term, double* loss);
 /* Gradient of a loss of the saved states of the last multiple-shooting forward:
  * the discrete adjoint of its accepted steps (exact gradient of the computed
- * solution). dL_dusave: S x nsave_total; outputs dL/du0 (S x nseg), dL/dp. */
+ * solution). dL_dusave: S x nsave_total host cotangent, or NULL for the one
+ * gbnde_multishoot_loss left on the device. Outputs dL/du0 (S x nseg; may be
+ * NULL) and dL/dp. */
 int gbnde_multishoot_backward(gbnde_ctx* ctx, const float* dL_dusave, float* dL_du0,
                               float* dL_dp, gbnde_stats* stats);
 

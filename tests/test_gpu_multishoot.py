@@ -156,3 +156,85 @@ def test_config4_structure_uneven_batch():
         Lref += oms.multiple_shoot_loss(opreds, data.astype(np.float64), gs, 100.0, mse)
     assert k == len(preds)
     assert abs(loss - Lref) / Lref < 1e-4
+
+
+def _uneven_trajs(S, H, ntraj, seed):
+    rng = np.random.default_rng(seed)
+    model, p, _, _ = _problem(S, H, 10, seed)
+    trajs = []
+    for k in range(ntraj):
+        n = int(rng.integers(10, 41))
+        gs = int(rng.integers(3, 9))
+        _, _, data, ts = _problem(S, H, n, 1000 * seed + k)
+        trajs.append((data, ts, gs))
+    return model, p, trajs
+
+
+@pytest.mark.parametrize("kind", ["mse", "sse"])
+@pytest.mark.parametrize("device", ["cpu", "cuda"])
+def test_fused_device_loss_matches_host_loop_and_oracle(kind, device):
+    """loss_function = mse_loss / sse_loss with the default continuity loss: the
+    loss and its cotangent in one device kernel (gbnde_multishoot_loss), the
+    adjoint from that cotangent. Against the host loop over groups (torch, same
+    kernels): loss 1e-6, gradient 1e-5 relative; against the FP64 oracle's loss
+    (src/multiple_shooting.jl:69-81): 1e-4."""
+    import torch
+
+    import gbnde
+    from oracle import mlp as omlp
+    from oracle import multishoot as oms
+    S, H = 4, 16
+    model, p, trajs = _uneven_trajs(S, H, 8, 3)
+    solver = gbnde.Solver(model, "fp32", 0)
+    tol = 1e-8
+    lf = gbnde.mse_loss if kind == "mse" else gbnde.sse_loss
+    host = (lambda u, uh: ((u - uh) ** 2).mean()) if kind == "mse" else (lambda u, uh: ((u - uh) ** 2).sum())
+    dev = torch.device(device, 0) if device == "cuda" else torch.device("cpu")
+    pf = torch.tensor(p, device=dev, requires_grad=True)
+    Lf, preds = gbnde.multiple_shoot_batch(pf, trajs, solver, lf, abstol=tol, reltol=tol)
+    Lf.backward()
+    ph = torch.tensor(p, requires_grad=True)
+    Lh, preds_h = gbnde.multiple_shoot_batch(ph, trajs, solver, host, abstol=tol, reltol=tol)
+    Lh.backward()
+    assert abs(float(Lf) - float(Lh)) / abs(float(Lh)) < 1e-6
+    assert _rel(pf.grad.cpu().numpy(), ph.grad.numpy()) < 1e-5
+    assert len(preds) == len(preds_h)
+    for a, b in zip(preds, preds_h):
+        assert np.array_equal(np.asarray(a), b.detach().numpy())
+    om = omlp.MLP(model.dims, model.acts)
+    ofn = (lambda u, uh: float(np.mean((u - uh) ** 2))) if kind == "mse" else None
+    Lref = 0.0
+    for data, ts, gs in trajs:
+        opreds, ok = oms.solve_groups(omlp.MLPRHS(om, p.astype(np.float64)), data.astype(np.float64), ts, gs,
+                                      tol, tol)
+        assert ok
+        Lref += oms.multiple_shoot_loss(opreds, data.astype(np.float64), gs, 100.0, ofn)
+    assert abs(float(Lf) - Lref) / Lref < 1e-4
+    solver.close()
+
+
+def test_fused_loss_gradient_against_finite_differences_and_failure():
+    """The fused path's gradient against central differences of the oracle's
+    multiple-shooting loss (1e-3), and a failed group still gives Inf."""
+    import torch
+
+    import gbnde
+    S, H = 3, 8
+    model, p, data, ts = _problem(S, H, 25, 0)
+    tol = 1e-8
+    pt = torch.tensor(p, requires_grad=True)
+    loss, preds = gbnde.multiple_shoot(pt, data, ts, model, gbnde.sse_loss, 5, abstol=tol, reltol=tol)
+    L0, _ = _oracle_loss(model, p, [(data, ts, 5)], tol)
+    assert abs(float(loss.detach()) - L0) / L0 < 1e-5
+    loss.backward()
+    eps = 1e-5
+    fd = np.zeros(p.size)
+    for i in range(p.size):
+        e = np.zeros(p.size)
+        e[i] = eps
+        fd[i] = (_oracle_loss(model, p + e, [(data, ts, 5)], tol)[0] -
+                 _oracle_loss(model, p - e, [(data, ts, 5)], tol)[0]) / (2 * eps)
+    assert _rel(pt.grad.numpy(), fd) < 1e-3
+    loss, preds = gbnde.multiple_shoot(p, data, ts, model, gbnde.sse_loss, 5, abstol=1e-12, reltol=1e-12,
+                                       maxiters=2)
+    assert loss == float("inf")
