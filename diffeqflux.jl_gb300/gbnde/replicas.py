@@ -46,6 +46,21 @@ def average_gradients(grad, group=None):
     return t if isinstance(grad, torch.Tensor) else t.numpy()
 
 
+def sum_over_ranks(x, group=None):
+    """Sum of a vector (or scalar) over the ranks: the multiple-shooting loss
+    and its gradient are sums over trajectories, so sharding trajectories
+    across ranks needs a sum, not a mean. Returns a new numpy array / float."""
+    import torch
+    import torch.distributed as dist
+    scalar = np.ndim(x) == 0
+    a = np.atleast_1d(np.asarray(x, dtype=np.float64)).copy()
+    if not dist.is_available() or not dist.is_initialized():
+        return float(a[0]) if scalar else a
+    t = torch.from_numpy(a)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    return float(t[0]) if scalar else t.numpy()
+
+
 def max_over_ranks(value, group=None):
     """Largest value over the replicas (step time of a synchronised step)."""
     import torch
