@@ -6,7 +6,13 @@ the augmented system [z; delta_logp] with right-hand side
 [f(z [, t]); -trace(df/dz)] is solved from (x, 0), keeping only the end state,
 and logpx = logpz(z(t1)) - delta_logp(t1) with the standard-normal base.
 `st` carries the reference's flags: monte_carlo (Hutchinson trace, the
-default) or the exact trace; regularize=True is not offered. The Hutchinson
+default) or the exact trace; regularize=True is not offered. `basedist` is the
+base density: None for the standard normal, or an object with
+``logpdf(z) -> (B,)`` on z of shape (d, B) (a torch-differentiable function of
+z when the layer is called with torch tensors); logpx = basedist.logpdf(z(t1))
+- delta_logp(t1) (src/ffjord.jl:170-176), differentiated through the
+library's dL/dz(t1). Like the reference without regularisation, the layer
+returns (logpx, delta_logp, delta_logp). The Hutchinson
 noise is drawn once per sample per solve (Rademacher by default, Gaussian on
 request) from `st["rng"]` -- the reference draws fresh Gaussian noise on every
 right-hand-side call, which makes its ODE stochastic. With torch tensors the
@@ -25,8 +31,9 @@ class FFJORD:
                  maxiters=100000, time_input=False, noise="rademacher", device=0):
         if not isinstance(model, Chain):
             raise TypeError("model must be a Chain of Dense layers")
-        if basedist is not None:
-            raise NotImplementedError("only the standard-normal base distribution is offered")
+        if basedist is not None and not callable(getattr(basedist, "logpdf", None)):
+            raise TypeError("basedist must be None (standard normal) or have logpdf(z) -> (B,)")
+        self.basedist = basedist
         if model.cube_input:
             raise ValueError("FFJORD models take no cube prefix")
         d = int(np.prod(input_dims))
@@ -79,6 +86,10 @@ class FFJORD:
         self._keep = nz
         return logpx, zT.T, st
 
+    def logpz_std(self, z):
+        """log density of the standard-normal base at z (d x B): the library's logpx uses it."""
+        return -0.5 * (z ** 2).sum(0) - 0.5 * self.d * np.log(2.0 * np.pi)
+
     def backward_np(self, dlogpx, dzT=None):
         s = self.solver
         g = np.ascontiguousarray(dlogpx, np.float32)
@@ -105,8 +116,12 @@ class FFJORD:
             is_torch = False
         if not is_torch:
             logpx, zT, _ = self.forward_np(x, ps, noise)
+            delta = self.logpz_std(zT.astype(np.float64)) - logpx
+            if self.basedist is not None:
+                logpx = np.asarray(self.basedist.logpdf(zT)) - delta
             out = logpx.reshape(1, -1)
-            return (out, out, out), st
+            dl = delta.reshape(1, -1)
+            return (out, dl, dl), st
         import torch
         layer = self
 
@@ -114,23 +129,30 @@ class FFJORD:
             @staticmethod
             def forward(ctx, xt, pt):
                 ctx.inputs = (xt.detach().cpu().numpy(), pt.detach().cpu().numpy())
-                lp, _, _ = layer.forward_np(ctx.inputs[0], ctx.inputs[1], noise)
+                lp, zT, _ = layer.forward_np(ctx.inputs[0], ctx.inputs[1], noise)
                 ctx.generation = layer.solver.generation
-                return torch.from_numpy(lp).to(pt.device)
+                return torch.from_numpy(lp).to(pt.device), torch.from_numpy(np.ascontiguousarray(zT)).to(pt.device)
 
             @staticmethod
-            def backward(ctx, g):
+            def backward(ctx, g, gz):
                 if layer.solver.generation != ctx.generation:
                     # another solve ran on the context since this forward: the
                     # adjoint needs this call's own solve, so it is run again
                     layer.forward_np(ctx.inputs[0], ctx.inputs[1], noise)
-                dx, dp, _ = layer.backward_np(g.detach().cpu().numpy())
+                dx, dp, _ = layer.backward_np(g.detach().cpu().numpy(),
+                                              None if gz is None else gz.detach().cpu().numpy())
                 return torch.from_numpy(np.ascontiguousarray(dx)).to(g.device), torch.from_numpy(dp).to(g.device)
 
         xt = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x, np.float32))
         pt = ps if isinstance(ps, torch.Tensor) else torch.as_tensor(np.asarray(ps, np.float32))
-        lp = _Fn.apply(xt, pt).reshape(1, -1)
-        return (lp, lp, lp), st
+        lp_std, zT = _Fn.apply(xt, pt)
+        delta = (-0.5 * (zT.double() ** 2).sum(0) - 0.5 * self.d * np.log(2.0 * np.pi)) - lp_std.double()
+        if self.basedist is not None:
+            lp = (self.basedist.logpdf(zT).double() - delta).to(lp_std.dtype)
+        else:
+            lp = lp_std
+        dl = delta.to(lp_std.dtype).reshape(1, -1)
+        return (lp.reshape(1, -1), dl, dl), st
 
 
 class FFJORDDistribution:
