@@ -137,6 +137,13 @@ def host_cores():
 
 def cpu_model():
     try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
         for ln in open("/proc/cpuinfo"):
             if ln.lower().startswith(("model name", "cpu part")):
                 return ln.split(":", 1)[1].strip()
@@ -404,7 +411,7 @@ def aux_multishoot(device, ntraj=256, S=32, H=128):
         p = p0.clone().requires_grad_(True)
         loss, _ = gbnde.multiple_shoot_batch(p, trajs, solver, gbnde.mse_loss, abstol=1e-6, reltol=1e-3)
         loss.backward()
-        out["loss"] = float(loss)
+        out["loss"] = float(loss.detach())
     sec = _timed(step, 5)
     kf, kb = _kernel_ms(solver)
     nseg = sum(len(gbnde.group_ranges(int(n[k]), int(gs[k]))) for k in range(ntraj))

@@ -68,6 +68,8 @@ int launch_adam_graph(float* p, float* m, float* v, const float* g, size_t n, do
 // which replays them inside one captured CUDA graph.
 struct StepRecord {
   bool fwd = false, bwd = false, loss = false, tc = false, bwd_tc_on = false;
+  bool wide = false;  // the tensor-core kernels ran in stash mode (fwd_tcw / bwd_tcw)
+  FwdTcwArgs fwd_tcw{};
   FwdTcArgs fwd_tc{};
   FwdArgs fwd_f32{};
   int fwd_grid = 0;
@@ -180,6 +182,13 @@ struct gbnde_ctx {
   int npadT[GBNDE_MAX_LAYERS] = {}, nchunkT[GBNDE_MAX_LAYERS] = {};
   bool tc_shape_ok = false;
   bool tc_bwd_ok = false;  // tensor-core adjoint covers this model
+  // stash mode (fwd_tcw / bwd_tcw): state up to 256, widths up to 1024, time
+  // row; weight images per 256-row N-block of each layer (W and W^T)
+  bool tc_wide = false, tc_wide_bwd = false;
+  int nsc = 1;  // 64-component chunks of the state in the tensor-core kernels
+  size_t wb_off[GBNDE_MAX_LAYERS][4] = {}, wbT_off[GBNDE_MAX_LAYERS][4] = {};
+  int wb_npad[GBNDE_MAX_LAYERS][4] = {}, wbT_npad[GBNDE_MAX_LAYERS][4] = {};
+  DBuf stash;
   DBuf timg, thscr, tmucomp, tlamcomp;
   DBuf tr_us, tr_dl, tr_du0, tr_dp;  // training-step scratch
   // graph-mode training step
@@ -327,10 +336,20 @@ int gbnde_create(gbnde_ctx** out, const gbnde_mlp_desc* mlp, int precision, int 
   c->tc_bwd_ok = c->tc_shape_ok && mlp->act[mlp->nlayers - 1] == GBNDE_ACT_IDENTITY;
   for (int l = 0; l < mlp->nlayers; ++l)
     c->tc_bwd_ok = c->tc_bwd_ok && std::min(mlp->dims[l], mlp->dims[l + 1]) <= 256;
+  // beyond that, stash mode: state <= 256, every width <= 1024 (16 K-chunks,
+  // 4 N-blocks), no cube prefix; its adjoint needs an identity output layer
   if (precision == GBNDE_PREC_BF16 && !c->tc_shape_ok) {
+    bool w = S <= 256 && !mlp->cube_input;
+    for (int l = 0; l <= mlp->nlayers; ++l) w = w && mlp->dims[l] <= 1024;
+    c->tc_wide = w;
+    c->tc_wide_bwd = w && mlp->act[mlp->nlayers - 1] == GBNDE_ACT_IDENTITY;
+    c->nsc = (S + 63) / 64;
+  }
+  if (precision == GBNDE_PREC_BF16 && !c->tc_shape_ok && !c->tc_wide) {
     gbnde_destroy(c);
     return fail(GBNDE_ERR_UNSUPPORTED,
-                "BF16 form supports state dim <= 64 and hidden widths <= 256 (no time input)");
+                "BF16 form supports state dim <= 256 and widths <= 1024 (no cube prefix beyond state 64 / "
+                "width 256)");
   }
   *out = c;
   return 0;
@@ -371,6 +390,21 @@ static int bind_params(gbnde_ctx* c) {
   }
   if (launch_transpose_params(m, p, c->wtr.as<float>(), c->stream))
     return fail(GBNDE_ERR_CUDA, "transpose kernel launch failed");
+  if (c->precision == GBNDE_PREC_BF16 && c->tc_wide) {
+    // per 256-row N-block: W rows [256 b, ...) of layer l (forward), W^T rows
+    // (input features) [256 b, ...) (VJP)
+    for (int l = 0; l < m.nlayers; ++l) {
+      const int in = m.dims[l], out = m.dims[l + 1];
+      for (int b = 0; b * 256 < out; ++b)
+        if (launch_prep_weight_image(m.W[l] + (size_t)256 * b * in, std::min(256, out - 256 * b), in,
+                                     c->wb_npad[l][b], c->wimg.as<uint8_t>() + c->wb_off[l][b], c->stream))
+          return fail(GBNDE_ERR_CUDA, "weight image kernel launch failed");
+      for (int b = 0; b * 256 < in; ++b)
+        if (launch_prep_weight_image(m.Wt[l] + (size_t)256 * b * out, std::min(256, in - 256 * b), out,
+                                     c->wbT_npad[l][b], c->wimg.as<uint8_t>() + c->wbT_off[l][b], c->stream))
+          return fail(GBNDE_ERR_CUDA, "weight image kernel launch failed");
+    }
+  }
   if (c->precision == GBNDE_PREC_BF16 && c->tc_shape_ok) {
     for (int l = 0; l < m.nlayers; ++l) {
       if (launch_prep_weight_image(m.W[l], m.dims[l + 1], m.dims[l], c->npad[l],
@@ -402,6 +436,23 @@ static int alloc_params(gbnde_ctx* c) {
       c->nchunkT[l] = (c->mlp.dims[l + 1] + 63) / 64;
       c->wtimg_off[l] = off;
       off += (size_t)c->nchunkT[l] * 2 * c->npadT[l] * 128;
+    }
+    if (int r = c->wimg.ensure(off)) return r;
+  }
+  if (c->precision == GBNDE_PREC_BF16 && c->tc_wide) {
+    size_t off = 0;
+    for (int l = 0; l < c->mlp.nlayers; ++l) {
+      const int in = c->mlp.dims[l], out = c->mlp.dims[l + 1];
+      for (int b = 0; b * 256 < out; ++b) {
+        c->wb_npad[l][b] = (std::min(256, out - 256 * b) + 15) / 16 * 16;
+        c->wb_off[l][b] = off;
+        off += (size_t)((in + 63) / 64) * 2 * c->wb_npad[l][b] * 128;
+      }
+      for (int b = 0; b * 256 < in; ++b) {
+        c->wbT_npad[l][b] = (std::min(256, in - 256 * b) + 15) / 16 * 16;
+        c->wbT_off[l][b] = off;
+        off += (size_t)((out + 63) / 64) * 2 * c->wbT_npad[l][b] * 128;
+      }
     }
     if (int r = c->wimg.ensure(off)) return r;
   }
@@ -489,6 +540,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   const int LD = TM + 4;
   const size_t smem = (size_t)frows * LD * sizeof(float);
   const bool tcform = c->precision == GBNDE_PREC_BF16 && !c->ff_on;
+  const bool wide = tcform && c->tc_wide;
   const int ntiles = tcform ? (B + 127) / 128 : (B + TM - 1) / TM;
   int gmax = 0;
   if (tcform) {
@@ -506,7 +558,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   // quarter of the free device memory; grows only when a solve needs more.
   // the BF16 form keeps its internal vectors (state, stages, dense slots) in
   // the tile layout: ntiles * 128 rows x 64 components each
-  const size_t SBv = tcform ? (size_t)ntiles * tc::kTileVec : SB;
+  const size_t SBv = tcform ? (size_t)ntiles * c->nsc * tc::kTileVec : SB;
   const size_t slot = 8 * SBv * sizeof(float);
   auto size_dense = [&](long long want) {
     want = std::min<long long>(std::max<long long>(want, 64), maxiters + 1);
@@ -593,8 +645,52 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   a.ffd = c->ff_d;
   a.exact = c->ff_exact;
   a.noise = c->ff_on ? c->ffnoise.as<float>() : nullptr;
+  if (wide && (r = c->stash.ensure((size_t)grid * tc::kStashCta))) return r;
   CK(cudaEventRecord(c->ev[0], st));
-  if (tcform) {
+  if (wide) {
+    FwdTcwArgs wa{};
+    FwdTcArgs& ta = wa.t;
+    ta.f = a;
+    ta.f.ntiles = ntiles;
+    ta.f.TM = 128;
+    int n = 0;
+    for (int l = 0; l < c->mlp.nlayers; ++l) {
+      const int out = c->mlp.dims[l + 1];
+      for (int b = 0; b * 256 < out; ++b) {
+        if (n >= tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+        tc::GemmOp& o = ta.ops.op[n++];
+        o.kind = 3;
+        o.wimg = c->wimg.as<uint8_t>() + c->wb_off[l][b];
+        o.npad = c->wb_npad[l][b];
+        o.nchunk = (c->mlp.dims[l] + 63) / 64;
+        o.sbuf = l & 1;
+        o.first_nb = b == 0;
+        o.aimg = c->stash.as<uint8_t>() + (size_t)o.sbuf * tc::kStashChunks * tc::kASlotBytes;
+        o.cta_stride = tc::kStashCta;
+        o.img_off = -1;
+      }
+      ta.bias[l] = c->mlp.bias[l];
+    }
+    ta.ops.nops = n;
+    ta.comp[0] = c->comp.as<float>();
+    ta.comp[1] = c->comp.as<float>() + SBv;
+    ta.dense = a.dense;
+    ta.dense_slots = a.dense_slots;
+    ta.kring = c->kbuf.as<float>();
+    wa.stash = c->stash.as<uint8_t>();
+    wa.nsc = c->nsc;
+    if (c->recording) {
+      c->rec.fwd = true;
+      c->rec.tc = true;
+      c->rec.wide = true;
+      c->rec.fwd_tcw = wa;
+      c->rec.fwd_grid = grid;
+    }
+    if (launch_fwd_tcw(wa, grid, st)) {
+      cudaError_t e = cudaGetLastError();
+      return fail(GBNDE_ERR_CUDA, "forward (tc, stash mode) launch failed: %s", cudaGetErrorString(e));
+    }
+  } else if (tcform) {
     FwdTcArgs ta{};
     ta.f = a;
     ta.f.ntiles = ntiles;
@@ -615,6 +711,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
     if (c->recording) {
       c->rec.fwd = true;
       c->rec.tc = true;
+      c->rec.wide = false;
       c->rec.fwd_tc = ta;
       c->rec.fwd_grid = grid;
     }
@@ -1458,7 +1555,8 @@ namespace {
 int capture_step(gbnde_ctx* c, const gbnde_adam* opt, float* p, float* m, float* v) {
   StepRecord& R = c->rec;
   const BwdArgs& b = R.bwd_tc_on ? R.bwd_tc.b : R.bwd_f32;
-  const FwdArgs& f = R.tc ? R.fwd_tc.f : R.fwd_f32;
+  const FwdArgs& f = R.tc ? (R.wide ? R.fwd_tcw.t.f : R.fwd_tc.f) : R.fwd_f32;
+  if (R.wide) return -1;  // stash-mode steps run eagerly
   if (!R.fwd || !R.bwd || !R.loss || !f.dense || !b.dense) return -1;  // the adjoint must read dense storage
   if (c->gstat.ensure(64)) return -1;
   if (!c->gpin && cudaMallocHost(&c->gpin, 2 * sizeof(double)) != cudaSuccess) {
@@ -1568,7 +1666,7 @@ int gbnde_graph_train_step(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B
   long long fc[CT_NSLOTS], bc[CT_NSLOTS];
   int fs[4], bs[4];
   const StepRecord& R = c->rec;
-  const FwdArgs& f = R.tc ? R.fwd_tc.f : R.fwd_f32;
+  const FwdArgs& f = R.tc ? (R.wide ? R.fwd_tcw.t.f : R.fwd_tc.f) : R.fwd_f32;
   const BwdArgs& b = R.bwd_tc_on ? R.bwd_tc.b : R.bwd_f32;
   CK(cudaMemcpyAsync(gl, gloss, sizeof gl, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(fc, f.counters, sizeof fc, cudaMemcpyDeviceToHost, st));

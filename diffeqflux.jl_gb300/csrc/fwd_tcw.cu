@@ -1,0 +1,546 @@
+// fwd_tcw.cu -- persistent Tsit5 forward solve, BF16 tensor-core form, for
+// networks beyond the single-accumulator engine: state dim up to 256, hidden
+// widths up to 1024, optionally t appended as an input row.
+//
+// Same algorithm and controller as fwd_tc.cu (the integrator loop of
+// `solve(prob, Tsit5(); saveat, abstol, reltol)` at src/neural_de.jl:55-58).
+// The right-hand side runs on the tensor-core engine in stash mode
+// (tc_engine.cuh): every layer input is written by the epilogue into the
+// CTA's global stash as split-BF16 64-column chunks, and a layer wider than
+// 256 outputs is computed as several N-block ops (at most 256 TMEM columns
+// each) that all bulk-load the same stash chunks. Layer l's input lives in
+// stash buffer l % 2.
+//
+// State vectors are kept in 64-component chunks: chunk c of tile T is the
+// "virtual tile" T * nsc + c of the tile layout (tc::tl_offset_cw), so the
+// per-thread stage arithmetic is that of the single-chunk kernel, repeated
+// over the chunks. Epilogue thread (warp w, lane l) owns trajectory row
+// r = 32 (w % 4) + l and columns kCW (w / 4) .. + kCW of every chunk.
+#include "tc_args.h"
+
+namespace gbnde {
+
+namespace {
+
+struct ThrW {
+  int r, ch;
+};
+
+__device__ __forceinline__ int nmine_of(int S, int c, int ch) {
+  return min(tc::kCW, max(0, S - 64 * c - tc::kCW * ch));
+}
+
+__device__ __forceinline__ void ldv_api(const float* p, int n, float* x) {
+#pragma unroll
+  for (int i = 0; i < tc::kCW; ++i) x[i] = (i < n) ? p[i] : 0.f;
+}
+__device__ __forceinline__ void stv_api(float* p, int n, const float* x) {
+#pragma unroll
+  for (int i = 0; i < tc::kCW; ++i)
+    if (i < n) p[i] = x[i];
+}
+
+__device__ __forceinline__ bool epi_grid_barrier(const FwdArgs& a, unsigned int& gen, int* okflag) {
+  tc::epi_bar();
+  gen += 1;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(a.bar, 1u);
+    const unsigned int target = gen * gridDim.x;
+    const unsigned long long t0 = globaltimer_ns();
+    int ok = 1;
+    while (ld_acquire_u32(a.bar) < target) {
+      if (*((volatile int*)&a.status[ST_BARRIER]) != 0) { ok = 0; break; }
+      if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+        atomicExch(&a.status[ST_BARRIER], 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    *okflag = ok;
+  }
+  tc::epi_bar();
+  return *okflag != 0;
+}
+
+__device__ __forceinline__ double epi_partials_sum(const double* p, int n, tc::Shared& sh) {
+  if (threadIdx.x < 32) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) v += __ldcg(p + i);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) sh.red[16] = v;
+  }
+  tc::epi_bar();
+  const double v = sh.red[16];
+  tc::epi_bar();
+  return v;
+}
+
+}  // namespace
+
+// One right-hand side of a tile on the stash engine. in(c, x) fills this
+// thread's kCW columns of input chunk c (c < kc0); out(c, v) receives its
+// kCW columns of output chunk c (c < nsc). Returns false if a wait gave up.
+template <class In, class Out>
+__device__ __forceinline__ bool epi_rhs_w(const FwdTcwArgs& A, tc::EpiState& e, tc::Shared& sh, uint8_t* stash,
+                                          const ThrW& th, In&& in, Out&& out) {
+  const MlpDev& m = A.t.f.mlp;
+  const uint32_t lane_base = ((uint32_t)((threadIdx.x >> 5) & 3) * 32) << 16;
+  const int kc0 = (m.dims[0] + 63) / 64;
+  for (int c = 0; c < kc0; ++c) {
+    float x[tc::kCW];
+    in(c, x);
+    tc::stash_write(stash, sh, 0, c, th.r, th.ch, x);
+  }
+  for (int l = 0; l < m.nlayers - 1; ++l) {
+    const int N = m.dims[l + 1];
+    const int nb = (N + 255) / 256;
+    const int ob = (l + 1) & 1;
+    for (int b = 0; b < nb; ++b) {
+      uint32_t col;
+      if (!tc::epi_wait_acc(e, sh, &col)) return false;
+      const int nch = (min(256, N - 256 * b) + 63) / 64;
+      for (int cc = 0; cc < nch; ++cc) {
+        const int n0 = 256 * b + 64 * cc + tc::kCW * th.ch;
+        float v[tc::kCW], bc[tc::kCW];
+        tc::load_bias_cw(A.t.bias[l], n0, N, bc);
+        tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
+        tc::bias_act_cw(v, bc, m.act[l], n0, N);
+        tc::stash_write(stash, sh, ob, 4 * b + cc, th.r, th.ch, v);
+      }
+      tc::epi_release_acc(e, sh);
+    }
+  }
+  {
+    const int L = m.nlayers, N = m.dims[L];
+    uint32_t col;
+    if (!tc::epi_wait_acc(e, sh, &col)) return false;
+    for (int c = 0; c < (N + 63) / 64; ++c) {
+      const int n0 = 64 * c + tc::kCW * th.ch;
+      float v[tc::kCW], bc[tc::kCW];
+      tc::load_bias_cw(A.t.bias[L - 1], n0, N, bc);
+      tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+      tc::bias_act_cw(v, bc, m.act[L - 1], n0, N);
+      out(c, v);
+    }
+    tc::epi_release_acc(e, sh);
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* aring = smem;
+  uint8_t* wring = smem + tc::kARing * tc::kASlotBytes;
+  __shared__ tc::Shared sh;
+  __shared__ int s_ok;
+  const FwdArgs& a = A.t.f;
+  const int warp = threadIdx.x >> 5;
+
+  tc::init_shared(sh);
+  if (warp == tc::kMmaWarp) tc::tmem_alloc(&sh.tmem_base, 512);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+
+  if (warp >= tc::kMmaWarp) {
+    tc::regs_give_ctl();
+    if (warp == tc::kMmaWarp) tc::mma_loop(A.t.ops, sh, aring, wring);
+    else if (warp == tc::kTmaWarp) tc::tma_loop(A.t.ops, sh, aring, wring);
+  } else {
+    tc::regs_take_epi();
+    // ======================= epilogue warps =======================
+    const int S = a.S, G = gridDim.x, nsc = A.nsc;
+    const size_t SB = (size_t)S * a.B;
+    const double N = (double)SB;
+    const double tdir = a.t1 >= a.t0 ? 1.0 : -1.0;
+    const bool timein = a.mlp.timein != 0;
+    ThrW th;
+    th.r = 32 * (warp & 3) + (threadIdx.x & 31);
+    th.ch = warp >> 2;
+    uint8_t* stash = A.stash + (size_t)blockIdx.x * tc::kStashCta;
+    tc::EpiState es;
+    tc::epi_state_init(es);
+    unsigned int gen = 0;
+    int par = 0, cur = 0;
+    int ret = GBNDE_RET_SUCCESS;
+    long long nf = 0, naccept = 0, nreject = 0, iter = 0;
+    const bool dense = A.t.dense != nullptr;
+    const size_t SBt = (size_t)a.ntiles * nsc * tc::kTileVec;
+    auto kptr = [&](int j) -> float* {
+      if (dense) return A.t.dense + ((size_t)min(naccept, A.t.dense_slots - 1) * 8 + 1 + j) * SBt;
+      return A.t.kring + (size_t)j * SBt;
+    };
+    // chunk c of tile T: the API offset of this thread's first component and
+    // the tile-layout offset of virtual tile T * nsc + c
+    auto gofs = [&](int tile, int c) -> size_t {
+      return ((size_t)tile * 128 + th.r) * S + 64 * c + tc::kCW * th.ch;
+    };
+    auto tofs = [&](int tile, int c) -> size_t { return tc::tl_offset_cw(tile * nsc + c, th.ch, th.r); };
+    auto rowok = [&](int tile) -> bool { return tile * 128 + th.r < a.B; };
+    // input chunk c >= nsc (the time row when S is a multiple of 64): t at
+    // column S, zeros elsewhere; inside the state chunks the time column
+    // (S % 64 != 0) is filled by the callers
+    auto tcol = [&](int c, double tt, float* x) {
+#pragma unroll
+      for (int i = 0; i < tc::kCW; ++i) x[i] = (timein && 64 * c + tc::kCW * th.ch + i == S) ? (float)tt : 0.f;
+    };
+    auto with_t = [&](int c, double tt, float* x) {
+      if (!timein) return;
+#pragma unroll
+      for (int i = 0; i < tc::kCW; ++i)
+        if (64 * c + tc::kCW * th.ch + i == S) x[i] = (float)tt;
+    };
+    bool ok = true;
+
+    // ---- k1 = f(u0); state, compensation and slot 0 ---------------------------
+    for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
+      const bool v = rowok(tile);
+      ok = epi_rhs_w(
+          A, es, sh, stash, th,
+          [&](int c, float* x) {
+            if (c >= nsc) { tcol(c, a.t0, x); return; }
+            const int nm = nmine_of(S, c, th.ch);
+            if (v) ldv_api(a.u0 + gofs(tile, c), nm, x);
+            else
+              for (int i = 0; i < tc::kCW; ++i) x[i] = 0.f;
+            float z[tc::kCW];
+            for (int i = 0; i < tc::kCW; ++i) z[i] = 0.f;
+            const size_t tg = tofs(tile, c);
+            tc::tl_stv(a.ubuf[0] + tg, x);
+            tc::tl_stv(A.t.comp[0] + tg, z);
+            if (dense) tc::tl_stv(A.t.dense + tg, x);
+            with_t(c, a.t0, x);
+          },
+          [&](int c, const float* k) {
+            float kk[tc::kCW];
+            const int nm = nmine_of(S, c, th.ch);
+            for (int i = 0; i < tc::kCW; ++i) kk[i] = (v && i < nm) ? k[i] : 0.f;
+            tc::tl_stv(kptr(0) + tofs(tile, c), kk);
+          });
+    }
+    nf = 1;
+    int isave = 0;
+    while (isave < a.nsave && a.saveat[isave] == a.t0) {
+      for (int tile = blockIdx.x; tile < a.ntiles; tile += G)
+        if (rowok(tile))
+          for (int c = 0; c < nsc; ++c) {
+            float Y[tc::kCW];
+            const int nm = nmine_of(S, c, th.ch);
+            ldv_api(a.u0 + gofs(tile, c), nm, Y);
+            stv_api(a.usave + (size_t)isave * SB + gofs(tile, c), nm, Y);
+          }
+      ++isave;
+    }
+    if (!ok) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto epi_done; }
+
+    // ---- initial step ---------------------------------------------------------------
+    double dt;
+    if (a.dt0 > 0.0) {
+      dt = a.dt0;
+    } else {
+      double p0 = 0.0, p1 = 0.0;
+      for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+        if (!rowok(tile)) continue;
+        for (int c = 0; c < nsc; ++c) {
+          const int nm = nmine_of(S, c, th.ch);
+          float u[tc::kCW], f[tc::kCW];
+          tc::tl_ldv(a.ubuf[0] + tofs(tile, c), u);
+          tc::tl_ldv(kptr(0) + tofs(tile, c), f);
+          for (int i = 0; i < tc::kCW; ++i) {
+            if (i >= nm) continue;
+            const float sk = (float)a.abstol + fabsf(u[i]) * (float)a.reltol;
+            const double x = (double)(u[i] / sk), y = (double)(f[i] / sk);
+            p0 += x * x;
+            p1 += y * y;
+          }
+        }
+      }
+      p0 = tc::epi_sum(p0, sh);
+      p1 = tc::epi_sum(p1, sh);
+      double* pp = a.partials + (size_t)par * 2 * G;
+      if (threadIdx.x == 0) {
+        pp[blockIdx.x] = p0;
+        pp[G + blockIdx.x] = p1;
+      }
+      if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto epi_done; }
+      const double d0 = sqrt(epi_partials_sum(pp, G, sh) / N);
+      const double d1 = sqrt(epi_partials_sum(pp + G, G, sh) / N);
+      par ^= 1;
+      double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? fmax(a.dtmin, 1e-6) : 0.01 * (d0 / d1);
+      dt0 = fmin(dt0, a.dtmax);
+      const float hf = (float)(tdir * dt0);
+      double p2 = 0.0;
+      for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
+        const bool v = rowok(tile);
+        ok = epi_rhs_w(
+            A, es, sh, stash, th,
+            [&](int c, float* x) {
+              if (c >= nsc) { tcol(c, a.t0 + tdir * dt0, x); return; }
+              float u[tc::kCW], f0[tc::kCW];
+              tc::tl_ldv(a.ubuf[0] + tofs(tile, c), u);
+              tc::tl_ldv(kptr(0) + tofs(tile, c), f0);
+              for (int i = 0; i < tc::kCW; ++i) x[i] = u[i] + hf * f0[i];
+              with_t(c, a.t0 + tdir * dt0, x);
+            },
+            [&](int c, const float* f1) {
+              if (!v) return;
+              const int nm = nmine_of(S, c, th.ch);
+              float u[tc::kCW], f0[tc::kCW];
+              tc::tl_ldv(a.ubuf[0] + tofs(tile, c), u);
+              tc::tl_ldv(kptr(0) + tofs(tile, c), f0);
+              for (int i = 0; i < tc::kCW; ++i) {
+                if (i >= nm) continue;
+                const float sk = (float)a.abstol + fabsf(u[i]) * (float)a.reltol;
+                const double z = (double)((f1[i] - f0[i]) / sk);
+                p2 += z * z;
+              }
+            });
+      }
+      nf += 1;
+      if (!ok) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto epi_done; }
+      p2 = tc::epi_sum(p2, sh);
+      pp = a.partials + (size_t)par * 2 * G;
+      if (threadIdx.x == 0) pp[blockIdx.x] = p2;
+      if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto epi_done; }
+      const double d2 = sqrt(epi_partials_sum(pp, G, sh) / N) / dt0;
+      par ^= 1;
+      const double mm = fmax(d1, d2);
+      const double dt1 = (mm <= 1e-15) ? fmax(1e-6, dt0 * 1e-3) : pow(10.0, -(2.0 + log10(mm)) / 5.0);
+      dt = fmax(a.dtmin, fmin(100.0 * dt0, fmin(dt1, a.dtmax)));
+    }
+
+    // ---- step loop ---------------------------------------------------------------------
+    {
+      double t = a.t0, qold = kQoldInit;
+      int ib = 0, nck = 0;
+      while (tdir * (a.t1 - t) > 0.0) {
+        if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
+        ++iter;
+        const double rem = fabs(a.t1 - t);
+        const bool clipped = dt >= rem;
+        const double habs = clipped ? rem : dt;
+        const double h = tdir * habs;
+        const float* ucur = a.ubuf[cur];
+        float* unew = a.ubuf[cur ^ 1];
+        const float* ccur = A.t.comp[cur];
+        float* cnew = A.t.comp[cur ^ 1];
+        double perr = 0.0;
+        for (int i = 1; i < 7 && ok; ++i) {
+          float ha[6];
+#pragma unroll
+          for (int j = 0; j < 6; ++j) ha[j] = (float)(h * c_tab.a[i][j]);
+          float hbt[7];
+#pragma unroll
+          for (int j = 0; j < 7; ++j) hbt[j] = (float)(h * c_tab.btilde[j]);
+          const double ti = t + c_tab.c[i] * h;
+          for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
+            const bool v = rowok(tile);
+            ok = epi_rhs_w(
+                A, es, sh, stash, th,
+                [&](int c, float* Y) {
+                  if (c >= nsc) { tcol(c, ti, Y); return; }
+                  const size_t g = tofs(tile, c);
+                  float u[tc::kCW], s[tc::kCW];
+                  tc::tl_ldv(ucur + g, u);
+                  tc::tl_ldv(ccur + g, s);
+                  if (i < 6) {
+                    for (int j = 0; j < 5; ++j) {
+                      if (j >= i) break;
+                      float kj[tc::kCW];
+                      tc::tl_ldv(kptr(j) + g, kj);
+#pragma unroll
+                      for (int q = 0; q < tc::kCW; ++q) s[q] = fmaf(ha[j], kj[q], s[q]);
+                    }
+                  } else {
+                    // the embedded error estimate's sum over k1..k6, parked in the k7 slot
+                    float ut[tc::kCW];
+#pragma unroll
+                    for (int q = 0; q < tc::kCW; ++q) ut[q] = 0.f;
+                    for (int j = 0; j < 6; ++j) {
+                      float kj[tc::kCW];
+                      tc::tl_ldv(kptr(j) + g, kj);
+#pragma unroll
+                      for (int q = 0; q < tc::kCW; ++q) {
+                        s[q] = fmaf(ha[j], kj[q], s[q]);
+                        ut[q] = fmaf(hbt[j], kj[q], ut[q]);
+                      }
+                    }
+                    tc::tl_stv(kptr(6) + g, ut);
+                  }
+#pragma unroll
+                  for (int q = 0; q < tc::kCW; ++q) Y[q] = u[q] + s[q];
+                  if (i == 6) {
+                    float cn[tc::kCW];
+#pragma unroll
+                    for (int q = 0; q < tc::kCW; ++q) cn[q] = s[q] - (Y[q] - u[q]);
+                    tc::tl_stv(unew + g, Y);
+                    tc::tl_stv(cnew + g, cn);
+                  }
+                  if (!v)
+                    for (int q = 0; q < tc::kCW; ++q) Y[q] = 0.f;
+                  with_t(c, ti, Y);
+                },
+                [&](int c, const float* kin) {
+                  if (!v) return;
+                  const int nm = nmine_of(S, c, th.ch);
+                  const size_t g = tofs(tile, c);
+                  float k[tc::kCW];
+                  for (int q = 0; q < tc::kCW; ++q) k[q] = (q < nm) ? kin[q] : 0.f;
+                  if (i == 6) {
+                    float ut[tc::kCW], u[tc::kCW], Y[tc::kCW];
+                    tc::tl_ldv(kptr(6) + g, ut);
+                    tc::tl_ldv(ucur + g, u);
+                    tc::tl_ldv(unew + g, Y);
+                    for (int q = 0; q < tc::kCW; ++q) {
+                      if (q >= nm) continue;
+                      const float e = fmaf(hbt[6], k[q], ut[q]);
+                      const float sc = (float)a.abstol + fmaxf(fabsf(u[q]), fabsf(Y[q])) * (float)a.reltol;
+                      const double rr = (double)(e / sc);
+                      perr += isfinite(Y[q]) ? rr * rr : (double)INFINITY;
+                    }
+                  }
+                  tc::tl_stv(kptr(i) + g, k);
+                });
+          }
+        }
+        if (!ok) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
+        nf += 6;
+        perr = tc::epi_sum(perr, sh);
+        double* pp = a.partials + (size_t)par * 2 * G;
+        if (threadIdx.x == 0) pp[blockIdx.x] = perr;
+        if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
+        const double eest = sqrt(epi_partials_sum(pp, G, sh) / N);
+        par ^= 1;
+        if (!isfinite(eest)) { ret = GBNDE_RET_UNSTABLE; break; }
+        double q11;
+        double q = pi_q(eest, qold, &q11);
+        if (blockIdx.x == 0 && threadIdx.x == 0 && iter - 1 < a.maxsteps) {
+          double* tr = a.trace + 4 * (iter - 1);
+          tr[0] = t;
+          tr[1] = h;
+          tr[2] = eest;
+          tr[3] = eest <= 1.0 ? 1.0 : 0.0;
+        }
+        if (eest <= 1.0) {
+          const double tnew = clipped ? a.t1 : t + h;
+          while (isave < a.nsave && tdir * (a.saveat[isave] - tnew) <= 0.0) {
+            const double sv = a.saveat[isave];
+            float* dst = a.usave + (size_t)isave * SB;
+            float hb[7];
+            if (sv != tnew) {
+              float bw[7];
+              interp_weights((sv - t) / h, bw);
+              for (int j = 0; j < 7; ++j) hb[j] = (float)(h * (double)bw[j]);
+            }
+            for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+              if (!rowok(tile)) continue;
+              for (int c = 0; c < nsc; ++c) {
+                const size_t tg = tofs(tile, c);
+                float o[tc::kCW];
+                if (sv == tnew) {
+                  tc::tl_ldv(unew + tg, o);
+                } else {
+                  float u[tc::kCW];
+                  tc::tl_ldv(ucur + tg, u);
+                  tc::tl_ldv(ccur + tg, o);
+                  for (int j = 0; j < 7; ++j) {
+                    float kj[tc::kCW];
+                    tc::tl_ldv(kptr(j) + tg, kj);
+#pragma unroll
+                    for (int q = 0; q < tc::kCW; ++q) o[q] = fmaf(hb[j], kj[q], o[q]);
+                  }
+#pragma unroll
+                  for (int q = 0; q < tc::kCW; ++q) o[q] = u[q] + o[q];
+                }
+                stv_api(dst + gofs(tile, c), nmine_of(S, c, th.ch), o);
+              }
+            }
+            ++isave;
+          }
+          bool need = false;
+          while (ib < a.nbnd && tdir * (a.bnd[ib] - tnew) < 0.0) { need = true; ++ib; }
+          if (need && nck < a.max_ckpt) {
+            float* dst = a.ckpt + (size_t)nck * SB;
+            for (int tile = blockIdx.x; tile < a.ntiles; tile += G)
+              if (rowok(tile))
+                for (int c = 0; c < nsc; ++c) {
+                  float u[tc::kCW];
+                  tc::tl_ldv(ucur + tofs(tile, c), u);
+                  stv_api(dst + gofs(tile, c), nmine_of(S, c, th.ch), u);
+                }
+            if (blockIdx.x == 0 && threadIdx.x == 0) a.ckpt_step[nck] = (int)naccept;
+            ++nck;
+          }
+          if (blockIdx.x == 0 && threadIdx.x == 0 && naccept < a.maxsteps) {
+            a.steplog[2 * naccept] = t;
+            a.steplog[2 * naccept + 1] = h;
+          }
+          // FSAL: k7 becomes k1 of the next step (next dense slot, or in place)
+          const float* k7 = kptr(6);
+          ++naccept;
+          for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+            if (!rowok(tile)) continue;
+            for (int c = 0; c < nsc; ++c) {
+              const size_t g = tofs(tile, c);
+              float kk[tc::kCW];
+              tc::tl_ldv(k7 + g, kk);
+              tc::tl_stv(kptr(0) + g, kk);
+              if (dense && naccept < A.t.dense_slots) {
+                float un[tc::kCW];
+                tc::tl_ldv(unew + g, un);
+                tc::tl_stv(A.t.dense + (size_t)naccept * 8 * SBt + g, un);
+              }
+            }
+          }
+          cur ^= 1;
+          t = tnew;
+          if (q >= 1.0 && q <= 1.0) q = 1.0;
+          qold = fmax(eest, kQoldInit);
+          dt = fmax(fmin(habs / q, a.dtmax), a.dtmin);
+        } else {
+          ++nreject;
+          dt = habs / fmin(1.0 / kQmin, q11 / kGamma);
+          if (a.dtmin > 0.0 && dt <= a.dtmin) { ret = GBNDE_RET_DTLESSTHANMIN; break; }
+        }
+      }
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.counters[CT_NCKPT] = nck;
+        a.counters[CT_NATTEMPT] = iter;
+        *a.tfinal = t;
+      }
+    }
+  epi_done:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.counters[CT_NF] = nf;
+      a.counters[CT_NACCEPT] = naccept;
+      a.counters[CT_NREJECT] = nreject;
+      a.counters[5] = cur;
+      const int e = ((volatile int*)&sh.err)[0];
+      a.status[ST_RETCODE] = (a.status[ST_BARRIER] != 0 || e != 0) ? GBNDE_RET_BARRIER_TIMEOUT : ret;
+      if (e) a.status[2] = e;
+    }
+    tc::epi_bar();
+    if (threadIdx.x == 0) ((volatile int*)&sh.stop)[0] = 1;
+  }
+  __syncthreads();
+  tc::tc_fence_after();
+  if (warp == tc::kMmaWarp) tc::tmem_dealloc(sh.tmem_base, 512);
+}
+
+int launch_fwd_tcw(const FwdTcwArgs& a, int grid, cudaStream_t st) {
+  if (tc_check_regs((const void*)fwd_tcw_kernel)) return -1;
+  cudaError_t e = cudaFuncSetAttribute(fwd_tcw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       tc::kSmemBytes);
+  if (e != cudaSuccess) return -1;
+  void* args[] = {(void*)&a};
+  e = cudaLaunchCooperativeKernel((const void*)fwd_tcw_kernel, dim3(grid), dim3(tc::kThreads), args,
+                                  tc::kSmemBytes, st);
+  return e == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace gbnde

@@ -45,6 +45,15 @@ struct BwdTcArgs {
 
 int launch_bwd_tc(const BwdTcArgs& a, int grid, cudaStream_t st);
 
+// Stash-mode forward (fwd_tcw.cu): state up to 256 (nsc 64-component chunks),
+// widths up to 1024, optional time row. The ops are N-block ops of kind 3.
+struct FwdTcwArgs {
+  FwdTcArgs t;
+  uint8_t* stash;  // [grid][2][kStashChunks][kASlotBytes]
+  int nsc;         // 64-component chunks of the state
+};
+int launch_fwd_tcw(const FwdTcwArgs& a, int grid, cudaStream_t st);
+
 // 0 if `kernel` was compiled with exactly tc::kLaunchRegs registers per
 // thread, the count the warpgroup register split is sized for; -1 otherwise
 // (the kernel must then not be launched: its register split would wait for

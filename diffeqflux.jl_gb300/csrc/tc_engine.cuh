@@ -63,9 +63,15 @@ constexpr int kWSlotBytes = 2 * 32768;   // 2 pieces x 256 rows x 128 B
 constexpr int kARing = 2;
 constexpr int kWRing = 2;
 constexpr int kSmemBytes = 1024 + kARing * kASlotBytes + kWRing * kWSlotBytes;
-constexpr int kMaxOps = 18;
+constexpr int kMaxOps = 64;
 constexpr int kCmdRing = 4;
 constexpr int kImgSlots = 7;    // weight-gradient image slots per CTA: stages 1..6 + the next stage 1
+// Stash mode (layers wider than one 256-column accumulator): every chain A
+// operand goes through a per-CTA global "stash" of two buffers of up to
+// kStashChunks K-chunks (ring-slot layout: 3 pieces x 128 rows x 128 B each),
+// written by the epilogue with plain stores and bulk-loaded by the producer.
+constexpr int kStashChunks = 16;                                   // K <= 1024
+constexpr size_t kStashCta = (size_t)2 * kStashChunks * kASlotBytes;  // bytes per CTA
 
 // kind 0 (chain GEMM): A chunks written by the epilogue (3 pieces, K-major),
 //   B = weight image chunks (2 pieces, K-major), five split products.
@@ -74,6 +80,11 @@ constexpr int kImgSlots = 7;    // weight-gradient image slots per CTA: stages 1
 //   hi.hi + hi.lo + lo.hi.
 // kind 2 (copy only, command mode): epilogue-written A chunks that only go to
 //   their weight-gradient image; no product, no accumulator, no W chunk.
+// kind 3 (stash chain GEMM): as kind 0, but the A chunks are bulk-loaded by
+//   the producer from stash buffer `sbuf` (once the epilogue has marked each
+//   chunk written), so one layer's input can feed several N-block ops.
+// kind 4 (stash copy only): stash A chunks loaded into the ring only to be
+//   copied to their weight-gradient image; no product.
 struct GemmOp {
   const uint8_t* wimg;  // kind 0: weight image; kind 1: B image base of CTA 0
   const uint8_t* aimg;  // kind 1: A image base of CTA 0
@@ -95,6 +106,16 @@ struct GemmOp {
   int img_off;
   uint8_t img_isA, img_nblk;
   uint16_t img_nh;
+  // kind 3 / 4: stash buffer of the A operand, and whether this op is the
+  // first reader of that buffer's current contents (the producer then moves
+  // to the buffer's next fill); aimg = stash base of CTA 0 for this buffer,
+  // cta_stride = bytes between CTAs' stashes
+  int sbuf;
+  int first_nb;
+  // kind 1 with the B side split in N-blocks: B chunk = 2 pieces of nblk_b
+  // blocks each, starting b_off0 bytes into each piece, pieces b_pstride
+  // bytes apart (b_pstride == 0: one contiguous copy)
+  uint32_t b_off0, b_pstride;
 };
 
 struct OpList {
@@ -109,6 +130,7 @@ struct Shared {
   uint64_t img_ready;
   uint64_t img_done;  // command mode: the MMA warp's image copies of the step have landed
   uint64_t cmd_full[kCmdRing], cmd_empty[kCmdRing];
+  uint64_t stash_full[2][kStashChunks];  // stash mode: chunk written by all epilogue threads
   uint32_t cmd[kCmdRing];
   uint32_t tmem_base;
   int stop;
@@ -161,6 +183,8 @@ __device__ __forceinline__ void init_shared(Shared& sh) {
       mbar_init(&sh.cmd_full[i], 1);
       mbar_init(&sh.cmd_empty[i], 2);
     }
+    for (int b = 0; b < 2; ++b)
+      for (int i = 0; i < kStashChunks; ++i) mbar_init(&sh.stash_full[b][i], kEpiThreads);
     sh.stop = 0;
     sh.err = 0;
     fence_mbar_init();
@@ -262,7 +286,7 @@ __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh
   volatile int* verr = &sh.err;
   volatile int* vstop = &sh.stop;
   const bool leader = (threadIdx.x & 31) == 0;
-  if (op.kind == 2) {
+  if (op.kind == 2 || op.kind == 4) {
     for (int c = 0; c < op.nchunk; ++c) {
       unsigned long long t0 = 0;
       while (!mbar_try_wait(&sh.a_full[m.aslot], m.aph)) {
@@ -292,8 +316,9 @@ __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh
     }
   }
   const uint32_t d = sh.tmem_base + (uint32_t)(reg * 256);
-  const uint32_t idesc = op.kind == 0 ? idesc_bf16(128, op.npad) : idesc_bf16_mn(128, op.npad);
-  const uint32_t wpiece = op.kind == 0 ? (uint32_t)op.npad * 128 : (uint32_t)op.nblk_b * 8192;
+  const bool chain = op.kind == 0 || op.kind == 3;  // K-major chain GEMM (five split products)
+  const uint32_t idesc = chain ? idesc_bf16(128, op.npad) : idesc_bf16_mn(128, op.npad);
+  const uint32_t wpiece = chain ? (uint32_t)op.npad * 128 : (uint32_t)op.nblk_b * 8192;
   for (int c = 0; c < op.nchunk; ++c) {
     // A chunk ready? (bounded by the stop flag: the epilogue may be done)
     {
@@ -309,9 +334,9 @@ __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh
     if (leader) {
       const uint32_t a0 = smem_u32(aring + m.aslot * kASlotBytes);
       const uint32_t b0 = smem_u32(wring + m.wslot * kWSlotBytes);
-      const bool copy = op.kind == 0 && img_base != nullptr && op.img_off >= 0;
+      const bool copy = chain && img_base != nullptr && op.img_off >= 0;
       if (copy) copy_a_image(op, c, aring + m.aslot * kASlotBytes, img_base);
-      if (op.kind == 0) {
+      if (chain) {
 #pragma unroll
         for (int pr = 0; pr < 5; ++pr) {
 #pragma unroll
@@ -417,6 +442,8 @@ struct TmaState {
   uint32_t issued_w[kWRing] = {0, 0};
   int a_pending[kARing] = {0, 0};     // a producer-filled A slot whose copy may be in flight
   uint32_t a_par[kARing] = {0, 0};    // ... and the phase parity of that fill
+  uint32_t fills[2] = {0, 0};         // stash mode: fills of each stash buffer seen so far
+  uint32_t spar[2] = {0, 0};          // ... and the parity of the one being read
 };
 
 __device__ __forceinline__ bool tma_wait_or_stop(Shared& sh, uint64_t* bar, uint32_t par) {
@@ -439,6 +466,46 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
       t.a_pending[t.aslot] = 0;
       if (++t.aslot == kARing) { t.aslot = 0; t.aph ^= 1; }
     }
+    return true;
+  }
+  if (op.kind == 3 || op.kind == 4) {
+    // stash A chunks (and, for kind 3, the weight chunks)
+    if (op.first_nb) {
+      t.spar[op.sbuf] = t.fills[op.sbuf] & 1u;
+      t.fills[op.sbuf] += 1;
+    }
+    const uint8_t* sbase = op.aimg + (size_t)blockIdx.x * op.cta_stride;
+    const uint32_t wbytes = 2u * (uint32_t)op.npad * 128u;
+    for (int c = 0; c < op.nchunk; ++c) {
+      // the epilogue's generic-proxy writes of chunk c are complete (each
+      // writer fenced them for the async proxy before arriving)
+      if (!tma_wait_or_stop(sh, &sh.stash_full[op.sbuf][c], t.spar[op.sbuf])) return false;
+      if (!tma_wait_or_stop(sh, &sh.a_empty[t.aslot], t.aph ^ 1)) return false;
+      if (leader) {
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        mbar_arrive_expect_tx(&sh.a_full[t.aslot], (uint32_t)kASlotBytes);
+        asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                         smem_u32(&sh.a_full[t.aslot])),
+                     "r"(kEpiThreads - 1)
+                     : "memory");
+        bulk_g2s(aring + t.aslot * kASlotBytes, sbase + (size_t)c * kASlotBytes, (uint32_t)kASlotBytes,
+                 &sh.a_full[t.aslot]);
+      }
+      __syncwarp();
+      t.a_pending[t.aslot] = 1;
+      t.a_par[t.aslot] = t.aph;
+      if (++t.aslot == kARing) { t.aslot = 0; t.aph ^= 1; }
+      if (op.kind == 4) continue;
+      if (!tma_wait_or_stop(sh, &sh.w_empty[t.wslot], t.wph ^ 1)) return false;
+      if (leader) {
+        mbar_arrive_expect_tx(&sh.w_full[t.wslot], wbytes);
+        bulk_g2s(wring + t.wslot * kWSlotBytes, op.wimg + (size_t)c * wbytes, wbytes, &sh.w_full[t.wslot]);
+      }
+      __syncwarp();
+      t.issued_w[t.wslot] += 1;
+      if (++t.wslot == kWRing) { t.wslot = 0; t.wph ^= 1; }
+    }
+    ++t.g;
     return true;
   }
   const uint32_t bbytes = op.kind == 0 ? 2u * (uint32_t)op.npad * 128u : 2u * (uint32_t)op.nblk_b * 8192u;
@@ -477,8 +544,16 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
     if (!tma_wait_or_stop(sh, &sh.w_empty[t.wslot], t.wph ^ 1)) return false;
     if (leader) {
       mbar_arrive_expect_tx(&sh.w_full[t.wslot], bbytes);
-      const uint8_t* src = op.kind == 0 ? bbase + (size_t)c * bbytes : bbase + boff;
-      bulk_g2s(wring + t.wslot * kWSlotBytes, src, bbytes, &sh.w_full[t.wslot]);
+      if (op.kind == 1 && op.b_pstride != 0) {
+        // one N-block of the B image: its blocks in each of the two pieces
+        const uint32_t half = bbytes / 2;
+        for (int q = 0; q < 2; ++q)
+          bulk_g2s(wring + t.wslot * kWSlotBytes + q * half, bbase + boff + op.b_off0 + (size_t)q * op.b_pstride,
+                   half, &sh.w_full[t.wslot]);
+      } else {
+        const uint8_t* src = op.kind == 0 ? bbase + (size_t)c * bbytes : bbase + boff;
+        bulk_g2s(wring + t.wslot * kWSlotBytes, src, bbytes, &sh.w_full[t.wslot]);
+      }
     }
     __syncwarp();
     t.issued_w[t.wslot] += 1;
@@ -581,6 +656,27 @@ __device__ __forceinline__ bool epi_write_a(EpiState& e, Shared& sh, uint8_t* ar
   mbar_arrive(&sh.a_full[e.aslot]);
   if (++e.aslot == kARing) { e.aslot = 0; e.aph ^= 1; }
   return true;
+}
+
+// Stash mode: this thread's kCW columns (row r, column group ch) of K-chunk c
+// of stash buffer b, split in 3 pieces, written with plain global stores in
+// the ring-slot layout; then fenced for the async proxy (the producer's bulk
+// loads) and marked on the chunk's barrier. Every epilogue thread writes its
+// part of every chunk of a layer input exactly once per fill.
+__device__ __forceinline__ void stash_write(uint8_t* stash_cta, Shared& sh, int b, int c, int r, int ch,
+                                            const float* x) {
+  uint8_t* base = stash_cta + ((size_t)b * kStashChunks + c) * kASlotBytes;
+#pragma unroll
+  for (int j = 0; j < kCW / 8; ++j) {
+    uint4 hi, mid, lo;
+    split3_bf16(x + 8 * j, hi, mid, lo);
+    const uint32_t off = sw128_offset(r, (kCW / 8) * ch + j);
+    *reinterpret_cast<uint4*>(base + off) = hi;
+    *reinterpret_cast<uint4*>(base + 16384 + off) = mid;
+    *reinterpret_cast<uint4*>(base + 32768 + off) = lo;
+  }
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+  mbar_arrive(&sh.stash_full[b][c]);
 }
 
 // Bias values of columns [n0, n0 + kCW) of a layer with N outputs (zero past
