@@ -482,6 +482,7 @@ def sweep_point(S, H, B, prec, dev, warmup, steps, tune):
     flops = F * (st.nf + st.nf_recompute + 3 * (st.nf_adj - st.nf_adj_vjp) + 2 * st.nf_adj_vjp)
     out.update({"value": 1.0 / sec, "unit": "train_steps/s", "ms_per_step": 1000.0 * sec,
                 "steps": steps, "replayed_as_graph": all(graphed), "loss": loss,
+                "kernels": {"fwd": _lib_path_name(st.fwd_path), "adj": _lib_path_name(st.adj_path)},
                 "nf_fwd": st.nf, "nf_adj": st.nf_adj, "gemm_tflops_per_s": flops / sec / 1e12})
     if prec == "bf16":
         # a step of seconds-long loops: against the sustained measured peak
@@ -490,6 +491,11 @@ def sweep_point(S, H, B, prec, dev, warmup, steps, tune):
             out["frac_of_bf16_peak_sustained"] = flops / sec / 1e12 / peak
     solver.close()
     return out, (dims, p, ts, u0, tg)
+
+
+def _lib_path_name(code):
+    from gbnde import _lib
+    return _lib.PATH_NAMES.get(int(code), str(code))
 
 
 def measured_peaks():
@@ -520,8 +526,8 @@ def run_sweep(args):
         warm, steps = (1, 1) if big else (2, 5)
         data = None
         for prec in ("fp32", "bf16"):
-            if prec == "bf16" and not (S <= 64 and H <= 256):
-                line["bf16"] = {"unsupported": "the tensor-core engine covers state <= 64 and widths <= 256"}
+            if prec == "bf16" and not (S <= 256 and H <= 1024):
+                line["bf16"] = {"unsupported": "the tensor-core engine covers state <= 256 and widths <= 1024"}
                 continue
             try:
                 r, data = sweep_point(S, H, B, prec, dev, warm, steps, tune=(prec == "fp32" and not big))

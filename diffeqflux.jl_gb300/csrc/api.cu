@@ -1002,6 +1002,189 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   return 0;
 }
 
+// Stash-mode tensor-core adjoint (bwd_tcw.cu): N-block op lists, images and
+// launch. `base` carries the intervals, cotangents and state buffers.
+static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float* dp_d) {
+  const MlpDev& m = c->mlp;
+  const int L = m.nlayers;
+  const int B = c->B, S = c->S;
+  const int P = (int)c->P;
+  int gmax = 0;
+  if (max_grid_fwd_tc(&gmax)) return fail(GBNDE_ERR_CUDA, "occupancy query failed (tc)");
+  const int ntiles = (B + 127) / 128;
+  const int grid = std::min(gmax, ntiles);
+  const int tpc = (ntiles + grid - 1) / grid;
+  if (tpc > 255) return fail(GBNDE_ERR_UNSUPPORTED, "tensor-core adjoint: more than 255 tiles per SM");
+  const size_t SBt = (size_t)ntiles * c->nsc * tc::kTileVec;
+  BwdTcwArgs w{};
+  BwdTcArgs& t = w.t;
+  t.b = base;
+  t.b.ntiles = ntiles;
+  t.b.TM = 128;
+  // weight-gradient images: per layer a_l and delta_{l+1}; the larger side is
+  // the M side (128-row halves), the other the N side (64-column blocks)
+  size_t off = 0;
+  int nblkN[GBNDE_MAX_LAYERS] = {};
+  for (int l = 0; l < L; ++l) {
+    const int out = m.dims[l + 1], in = m.dims[l];
+    t.a_isA[l] = in > out ? 1 : 0;
+    const int mside = t.a_isA[l] ? in : out;
+    t.nh[l] = (mside + 127) / 128;
+    nblkN[l] = ((t.a_isA[l] ? out : in) + 63) / 64;
+    auto img_bytes = [&](int dim, int isA) -> size_t {
+      return isA ? (size_t)2 * t.nh[l] * 32768 : (size_t)2 * 2 * ((dim + 63) / 64) * 8192;
+    };
+    t.aoff[l] = (long long)off;
+    off += img_bytes(in, t.a_isA[l]);
+    t.doff[l] = (long long)off;
+    off += img_bytes(out, !t.a_isA[l]);
+  }
+  t.img_cta = off;
+  int hv = 0;
+  for (int l = 1; l < L; ++l) {
+    t.hoff[l] = hv;
+    hv += tc::kCW * ((m.dims[l] + 63) / 64);
+  }
+  t.hx = hv;
+  t.hvals = hv + 4;
+  int nb = 0;
+  for (int l = 0; l < L; ++l) {
+    t.boffp[l] = nb;
+    nb += 64 * ((m.dims[l + 1] + 63) / 64);
+  }
+  t.nbias = nb;
+  t.tpc = tpc;
+  const int Ppad = (P + 3) / 4 * 4;
+  t.b.P = Ppad;
+  int r = 0;
+  if ((r = c->timg.ensure((size_t)grid * tpc * tc::kImgSlots * t.img_cta)) ||
+      (r = c->thscr.ensure((size_t)grid * tc::kEpiThreads * t.hvals * 4)) ||
+      (r = c->tmucomp.ensure((size_t)grid * Ppad * 4)) || (r = c->tlamcomp.ensure(2 * SBt * 4)) ||
+      (r = c->mu_acc.ensure((size_t)grid * Ppad * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * 4 * t.nbias * 4)) ||
+      (r = c->stash.ensure((size_t)grid * tc::kStashCta)))
+    return r;
+  t.b.mu_acc = c->mu_acc.as<float>();
+  t.b.mu_stage = c->mu_stage.as<float>();
+  t.pbias = c->mu_stage.as<float>();
+  t.img = c->timg.as<uint8_t>();
+  t.hscr = c->thscr.as<float>();
+  t.mu_comp = c->tmucomp.as<float>();
+  t.lam_comp[0] = c->tlamcomp.as<float>();
+  t.lam_comp[1] = c->tlamcomp.as<float>() + SBt;
+  t.b.dense = c->dense.as<float>();
+  for (int l = 0; l < L; ++l) t.bias[l] = m.bias[l];
+  uint8_t* stash = c->stash.as<uint8_t>();
+  auto stash_op = [&](tc::GemmOp& o, int sbuf, int first) {
+    o.sbuf = sbuf;
+    o.first_nb = first;
+    o.aimg = stash + (size_t)sbuf * tc::kStashChunks * tc::kASlotBytes;
+    o.cta_stride = tc::kStashCta;
+  };
+  // evaluation list: forward recompute of layers 0..L-2 (a_l in buffer l % 2,
+  // image of a_l from the first N-block op), a copy-only op for a_{L-1}, then
+  // the VJP layers L-1..0 (delta_{l+1} in buffer (l + 1) % 2, image from the
+  // first N-block op; layer 0 only over the state inputs)
+  int n = 0;
+  auto next_op = [&](tc::OpList& lst) -> tc::GemmOp* {
+    if (n >= tc::kMaxOps) return nullptr;
+    tc::GemmOp* o = &lst.op[n++];
+    *o = tc::GemmOp{};
+    return o;
+  };
+  for (int l = 0; l < L - 1; ++l) {
+    const int in = m.dims[l], out = m.dims[l + 1];
+    for (int b = 0; b * 256 < out; ++b) {
+      tc::GemmOp* o = next_op(t.ops);
+      if (!o) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+      o->kind = 3;
+      o->wimg = c->wimg.as<uint8_t>() + c->wb_off[l][b];
+      o->npad = c->wb_npad[l][b];
+      o->nchunk = (in + 63) / 64;
+      stash_op(*o, l & 1, b == 0);
+      o->img_off = b == 0 ? (int)t.aoff[l] : -1;
+      o->img_isA = (uint8_t)t.a_isA[l];
+      o->img_nblk = (uint8_t)((in + 63) / 64);
+      o->img_nh = (uint16_t)t.nh[l];
+    }
+  }
+  {
+    const int l = L - 1;
+    tc::GemmOp* o = next_op(t.ops);
+    if (!o) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+    o->kind = 4;
+    o->nchunk = (m.dims[l] + 63) / 64;
+    stash_op(*o, l & 1, 1);
+    o->img_off = (int)t.aoff[l];
+    o->img_isA = (uint8_t)t.a_isA[l];
+    o->img_nblk = (uint8_t)((m.dims[l] + 63) / 64);
+    o->img_nh = (uint16_t)t.nh[l];
+  }
+  for (int l = L - 1; l >= 0; --l) {
+    const int in = m.dims[l], out = m.dims[l + 1];
+    const int nout = l == 0 ? S : in;  // inputs whose cotangent is needed
+    for (int b = 0; b * 256 < nout; ++b) {
+      tc::GemmOp* o = next_op(t.ops);
+      if (!o) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+      o->kind = 3;
+      o->wimg = c->wimg.as<uint8_t>() + c->wbT_off[l][b];
+      o->npad = c->wbT_npad[l][b];  // the image's row padding (its pieces are npad rows apart)
+      o->nchunk = (out + 63) / 64;
+      stash_op(*o, (l + 1) & 1, b == 0);
+      o->img_off = b == 0 ? (int)t.doff[l] : -1;
+      o->img_isA = (uint8_t)(!t.a_isA[l]);
+      o->img_nblk = (uint8_t)((out + 63) / 64);
+      o->img_nh = (uint16_t)t.nh[l];
+    }
+  }
+  t.ops.nops = n;
+  t.ops7 = t.ops;
+  // weight gradients of an accepted step: per layer, M halves x N-blocks
+  n = 0;
+  t.dw_chunks = 0;
+  for (int l = 0; l < L; ++l) {
+    const int out = m.dims[l + 1], in = m.dims[l];
+    const int nside = t.a_isA[l] ? out : in;
+    const int nblk = nblkN[l];
+    const long long aimg = t.a_isA[l] ? t.aoff[l] : t.doff[l];
+    const long long bimg = t.a_isA[l] ? t.doff[l] : t.aoff[l];
+    for (int hh = 0; hh < t.nh[l]; ++hh) {
+      for (int nbk = 0; nbk * 256 < nside; ++nbk) {
+        tc::GemmOp* o = next_op(t.dwops);
+        if (!o) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+        const int nbb = std::min(4, nblk - 4 * nbk);
+        o->kind = 1;
+        o->aimg = t.img + aimg + (size_t)hh * 32768;
+        o->wimg = t.img + bimg;
+        o->cta_stride = (size_t)tpc * tc::kImgSlots * t.img_cta;
+        o->slot_stride = t.img_cta;
+        o->a_bytes = 32768;
+        o->a_step = (uint32_t)(t.nh[l] * 32768);
+        o->b_step = (uint32_t)(2 * nblk * 8192);
+        o->nblk_b = nbb;
+        o->b_off0 = (uint32_t)(4 * nbk * 8192);
+        o->b_pstride = (uint32_t)(nblk * 8192);
+        o->npad = (std::min(256, nside - 256 * nbk) + 15) / 16 * 16;
+        o->nchunk = 2 * 6 * tpc;
+        o->first_dw = 0;
+        o->img_off = -1;
+        t.dw_chunks += o->nchunk;
+      }
+    }
+  }
+  t.dwops.nops = n;
+  w.stash = stash;
+  w.nsc = c->nsc;
+  CK(cudaEventRecord(c->ev[2], st));
+  if (launch_bwd_tcw(w, grid, st)) {
+    cudaError_t e = cudaGetLastError();
+    return fail(GBNDE_ERR_CUDA, "backward (tc, stash mode) launch failed: %s", cudaGetErrorString(e));
+  }
+  CK(cudaEventRecord(c->ev[3], st));
+  if (launch_reduce_mu_comp(t.b.mu_acc, t.mu_comp, grid, Ppad, P, dp_d, st))
+    return fail(GBNDE_ERR_CUDA, "reduce launch failed");
+  return 0;
+}
+
 static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* dLdu0,
                          float* dLdp, bool out_host, gbnde_stats* stats) {
   if (!c) return fail(GBNDE_ERR_INVALID, "null context");
@@ -1019,12 +1202,12 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   if (int r = build_intervals(c, ivs, &max_slots, &save_last, &nsave_last)) return r;
   const bool backsolve = c->sensealg == GBNDE_SENSE_BACKSOLVE;
   const bool gauss = c->sensealg == GBNDE_SENSE_GAUSS;
-  const bool tcbwd = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && !gauss &&
-                     c->dense_valid && !c->ff_on;
+  const bool tcbwd = c->precision == GBNDE_PREC_BF16 && (c->tc_bwd_ok || c->tc_wide_bwd) && !backsolve &&
+                     !gauss && c->dense_valid && !c->ff_on;
   // the FP32 adjoint reads dense slots only in its own layout; after a
   // tensor-core forward it recomputes each interval from the checkpoints
   const bool dense_f32 = c->dense_valid && !backsolve && !c->dense_tl;
-  const size_t SBv = tcbwd ? (size_t)((B + 127) / 128) * tc::kTileVec : SB;
+  const size_t SBv = tcbwd ? (size_t)((B + 127) / 128) * c->nsc * tc::kTileVec : SB;
 
   int rows = 0;
   for (int l = 0; l <= c->mlp.nlayers; ++l) rows += c->mlp.dims[l];
@@ -1121,7 +1304,10 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   a.ffd = c->ff_d;
   a.exact = c->ff_exact;
   a.noise = c->ff_on ? c->ffnoise.as<float>() : nullptr;
-  if (tcbwd) {
+  if (tcbwd && c->tc_wide) {
+    if (c->recording) c->rec.bwd = false;  // stash-mode steps run eagerly
+    if (int rr = backward_tcw(c, a, st, dp_d)) return rr;
+  } else if (tcbwd) {
     if (int rr = backward_tc(c, a, st, dp_d)) return rr;
   } else {
     CK(cudaEventRecord(c->ev[2], st));

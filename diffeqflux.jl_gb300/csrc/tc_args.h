@@ -54,6 +54,15 @@ struct FwdTcwArgs {
 };
 int launch_fwd_tcw(const FwdTcwArgs& a, int grid, cudaStream_t st);
 
+// Stash-mode adjoint (bwd_tcw.cu): the BwdTcArgs op lists hold N-block ops
+// (kind 3 chain, kind 4 copy-only, kind 1 weight gradients with B blocks).
+struct BwdTcwArgs {
+  BwdTcArgs t;
+  uint8_t* stash;
+  int nsc;
+};
+int launch_bwd_tcw(const BwdTcwArgs& a, int grid, cudaStream_t st);
+
 // 0 if `kernel` was compiled with exactly tc::kLaunchRegs registers per
 // thread, the count the warpgroup register split is sized for; -1 otherwise
 // (the kernel must then not be launched: its register split would wait for

@@ -442,8 +442,11 @@ struct TmaState {
   uint32_t issued_w[kWRing] = {0, 0};
   int a_pending[kARing] = {0, 0};     // a producer-filled A slot whose copy may be in flight
   uint32_t a_par[kARing] = {0, 0};    // ... and the phase parity of that fill
-  uint32_t fills[2] = {0, 0};         // stash mode: fills of each stash buffer seen so far
-  uint32_t spar[2] = {0, 0};          // ... and the parity of the one being read
+  // stash mode: per buffer, bit c = phase parity of chunk c's next fill, and
+  // the parities of the fill being read (chunks are refilled unevenly: a
+  // buffer holds inputs of different widths in turn)
+  uint32_t ph[2] = {0, 0};
+  uint32_t cur[2] = {0, 0};
 };
 
 __device__ __forceinline__ bool tma_wait_or_stop(Shared& sh, uint64_t* bar, uint32_t par) {
@@ -471,15 +474,15 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
   if (op.kind == 3 || op.kind == 4) {
     // stash A chunks (and, for kind 3, the weight chunks)
     if (op.first_nb) {
-      t.spar[op.sbuf] = t.fills[op.sbuf] & 1u;
-      t.fills[op.sbuf] += 1;
+      t.cur[op.sbuf] = t.ph[op.sbuf];
+      t.ph[op.sbuf] ^= (op.nchunk >= 32) ? 0xffffffffu : ((1u << op.nchunk) - 1u);
     }
     const uint8_t* sbase = op.aimg + (size_t)blockIdx.x * op.cta_stride;
     const uint32_t wbytes = 2u * (uint32_t)op.npad * 128u;
     for (int c = 0; c < op.nchunk; ++c) {
       // the epilogue's generic-proxy writes of chunk c are complete (each
       // writer fenced them for the async proxy before arriving)
-      if (!tma_wait_or_stop(sh, &sh.stash_full[op.sbuf][c], t.spar[op.sbuf])) return false;
+      if (!tma_wait_or_stop(sh, &sh.stash_full[op.sbuf][c], (t.cur[op.sbuf] >> c) & 1u)) return false;
       if (!tma_wait_or_stop(sh, &sh.a_empty[t.aslot], t.aph ^ 1)) return false;
       if (leader) {
         asm volatile("fence.proxy.async.global;" ::: "memory");

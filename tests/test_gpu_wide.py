@@ -68,6 +68,7 @@ def test_wide_forward_and_gradient_vs_oracle(case):
     g = (2.0 * (us.astype(np.float64) - tgt) / us.size).astype(np.float32)
     du0, dp, sta = s.backward(g)
     assert sta.retcode_adj == 0
+    assert sta.adj_path == _lib.PATH_TC
     gu, gp, _ = ots.adjoint_interpolating(omlp.MLPRHS(om, p.astype(np.float64)), fwd2, ts,
                                           2.0 * (ous2 - tgt) / ous2.size, 0.0, tol[0], tol[1])
     assert _rel(du0, gu) < 1e-3, _rel(du0, gu)
