@@ -221,6 +221,8 @@ struct gbnde_ctx {
   DBuf comp, dense;
   long long dense_slots = 0;
   bool dense_valid = false;
+  size_t stage_cap = 0;  // gbnde_set_stage_memory: bytes the dense stage storage may take (0: a quarter of free)
+  DBuf ckcomp, trep;     // tensor-core form: compensation at the checkpoints; replay state of the adjoint
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double fwd_ms = 0.0, bwd_ms = 0.0;
 };
@@ -366,7 +368,8 @@ void gbnde_destroy(gbnde_ctx* c) {
                   &c->tmucomp, &c->tlamcomp, &c->ms_segs, &c->ms_saveat, &c->ms_u0,
                   &c->ms_usave, &c->ms_dense, &c->ms_steplog, &c->ms_nacc, &c->ms_ret, &c->ms_cnt,
                   &c->ms_dldu, &c->ms_dldu0, &c->ms_bar, &c->ms_mu, &c->ms_dldp, &c->ffnoise,
-                  &c->ffu0, &c->ffus, &c->tr_us, &c->tr_dl, &c->tr_du0, &c->tr_dp};
+                  &c->ffu0, &c->ffus, &c->tr_us, &c->tr_dl, &c->tr_du0, &c->tr_dp, &c->stash,
+                  &c->ms_data, &c->ms_map, &c->ms_part, &c->ckcomp, &c->trep};
   for (DBuf* b : bufs) b->release();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -456,6 +459,12 @@ static int alloc_params(gbnde_ctx* c) {
     }
     if (int r = c->wimg.ensure(off)) return r;
   }
+  return 0;
+}
+
+int gbnde_set_stage_memory(gbnde_ctx* c, size_t max_bytes) {
+  if (!c) return fail(GBNDE_ERR_INVALID, "null context");
+  c->stage_cap = max_bytes;
   return 0;
 }
 
@@ -560,15 +569,18 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   // the tile layout: ntiles * 128 rows x 64 components each
   const size_t SBv = tcform ? (size_t)ntiles * c->nsc * tc::kTileVec : SB;
   const size_t slot = 8 * SBv * sizeof(float);
+  const long long cap_slots = c->stage_cap ? (long long)(c->stage_cap / slot) : (long long)1 << 62;
   auto size_dense = [&](long long want) {
     want = std::min<long long>(std::max<long long>(want, 64), maxiters + 1);
+    want = std::min(want, cap_slots);
     const long long have_now = (long long)(c->dense.n / slot);
-    if (want > have_now) {
+    if (have_now > cap_slots) c->dense.release();
+    if (want > (long long)(c->dense.n / slot)) {
       size_t freeb = 0, totb = 0;
       cudaMemGetInfo(&freeb, &totb);
-      const long long budget = (long long)((freeb / 4) / slot) + have_now;
+      const long long budget = (long long)((freeb / 4) / slot) + (long long)(c->dense.n / slot);
       long long ns = std::min(want, budget);
-      if (ns > have_now) {
+      if (ns > (long long)(c->dense.n / slot)) {
         c->dense.release();
         if (ns >= 2 && c->dense.ensure((size_t)ns * slot)) {
           cudaGetLastError();
@@ -577,6 +589,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
       }
     }
     c->dense_slots = (long long)(c->dense.n / slot);
+    if (c->dense_slots < 2) c->dense_slots = 0;
   };
   size_dense(2 * c->last_naccept + 8);
   if (tcform && (r = c->comp.ensure(2 * SBv * 4))) return r;
@@ -584,6 +597,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   if ((r = c->ubuf.ensure(2 * SBv * 4)) || (r = c->kbuf.ensure(7 * SBv * 4))) return r;
   if (usave_host && (r = c->usave.ensure(SB * nsave * 4))) return r;
   if ((r = c->ckpt.ensure(SB * nb * 4)) || (r = c->ckpt_step.ensure(nb * sizeof(int)))) return r;
+  if (tcform && !wide && (r = c->ckcomp.ensure(SBv * nb * 4))) return r;
   const long long maxsteps = std::min<long long>(maxiters, 1LL << 22);
   if ((r = c->steplog.ensure(2 * maxsteps * sizeof(double)))) return r;
   if ((r = c->trace.ensure(4 * maxsteps * sizeof(double)))) return r;
@@ -708,6 +722,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
     ta.dense = a.dense;
     ta.dense_slots = a.dense_slots;
     ta.kring = c->kbuf.as<float>();
+    ta.ckcomp = c->ckcomp.as<float>();
     if (c->recording) {
       c->rec.fwd = true;
       c->rec.tc = true;
@@ -783,7 +798,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   c->dense_tl = tcform;
   c->last_naccept = nacc;
   c->fS = S;
-  if (c->have_fwd && !c->dense_valid && !c->rerun_guard) {
+  if (c->have_fwd && !c->dense_valid && !c->rerun_guard && c->dense_slots < cap_slots) {
     // the solve outgrew the dense stage storage: grow it and solve again once
     // (the backward then interpolates the stored stages instead of recomputing)
     c->rerun_guard = true;
@@ -917,7 +932,24 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   t.mu_comp = c->tmucomp.as<float>();
   t.lam_comp[0] = c->tlamcomp.as<float>();
   t.lam_comp[1] = c->tlamcomp.as<float>() + SBt;
-  t.b.dense = c->dense.as<float>();
+  // dense storage, or (O(checkpoints) mode) replay of each interval into b.ibuf
+  const bool replay = base.dense == nullptr;
+  t.b.dense = replay ? nullptr : c->dense.as<float>();
+  if (replay) {
+    if ((r = c->trep.ensure(2 * SBt * 4))) return r;
+    t.rep[0] = c->trep.as<float>();
+    t.rep[1] = c->trep.as<float>() + SBt;
+    t.ckcomp = c->ckcomp.as<float>();
+  }
+  for (int l = 0; l < L; ++l) {
+    tc::GemmOp& o = t.fwops.op[l];
+    o.kind = 0;
+    o.wimg = c->wimg.as<uint8_t>() + c->wimg_off[l];
+    o.npad = c->npad[l];
+    o.nchunk = c->nchunk[l];
+    o.img_off = -1;
+  }
+  t.fwops.nops = L;
   for (int l = 0; l < L; ++l) t.bias[l] = m.bias[l];
   // op lists: forward recompute + VJP chain (per evaluation), and the
   // stage-stacked weight gradients (per accepted step: K = 6 stages x 128)
@@ -985,7 +1017,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   t.dwops.nops = n;
   CK(cudaEventRecord(c->ev[2], st));
   if (c->recording) {
-    c->rec.bwd = true;
+    c->rec.bwd = !replay;  // an O(checkpoints) step runs eagerly
     c->rec.bwd_tc_on = true;
     c->rec.bwd_tc = t;
     c->rec.bwd_grid = grid;
@@ -1202,8 +1234,12 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   if (int r = build_intervals(c, ivs, &max_slots, &save_last, &nsave_last)) return r;
   const bool backsolve = c->sensealg == GBNDE_SENSE_BACKSOLVE;
   const bool gauss = c->sensealg == GBNDE_SENSE_GAUSS;
-  const bool tcbwd = c->precision == GBNDE_PREC_BF16 && (c->tc_bwd_ok || c->tc_wide_bwd) && !backsolve &&
-                     !gauss && c->dense_valid && !c->ff_on;
+  // tensor-core adjoint: on the dense stage storage, or (single-accumulator
+  // engine, after a tensor-core forward) replaying each interval from its checkpoint
+  const bool tc_replay = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && !gauss &&
+                         !c->dense_valid && c->dense_tl && !c->ff_on;
+  const bool tcbwd = (c->precision == GBNDE_PREC_BF16 && (c->tc_bwd_ok || c->tc_wide_bwd) && !backsolve &&
+                      !gauss && c->dense_valid && !c->ff_on) || tc_replay;
   // the FP32 adjoint reads dense slots only in its own layout; after a
   // tensor-core forward it recomputes each interval from the checkpoints
   const bool dense_f32 = c->dense_valid && !backsolve && !c->dense_tl;
@@ -1237,6 +1273,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   if ((r = c->lam.ensure(2 * SBv * 4)) || (r = c->kl.ensure(7 * SBv * 4))) return r;
   if (backsolve && ((r = c->ub.ensure(2 * SB * 4)) || (r = c->ku.ensure(7 * SB * 4)))) return r;
   if (!tcbwd && !backsolve && !dense_f32 && (r = c->ibuf.ensure((size_t)max_slots * 8 * SB * 4))) return r;
+  if (tc_replay && (r = c->ibuf.ensure((size_t)max_slots * 8 * SBv * 4))) return r;
   if ((r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4))) return r;
   if ((r = c->iv_d.ensure(std::max<size_t>(1, ivs.size()) * sizeof(Interval)))) return r;
   if ((r = c->bsync.ensure(64)) || (r = c->bcounters.ensure(CT_NSLOTS * sizeof(long long)))) return r;
@@ -1283,7 +1320,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   a.nsave_last = nsave_last;
   a.ibuf = c->ibuf.as<float>();
   a.ibuf_slots = max_slots;
-  a.dense = tcbwd || dense_f32 ? c->dense.as<float>() : nullptr;
+  a.dense = (tcbwd && !tc_replay) || dense_f32 ? c->dense.as<float>() : nullptr;
   a.lam[0] = c->lam.as<float>();
   a.lam[1] = c->lam.as<float>() + SBv;
   a.ub[0] = backsolve ? c->ub.as<float>() : nullptr;
@@ -1347,7 +1384,8 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
     stats->nf_recompute = cnt[CT_NRECOMP];
     stats->nf_adj_vjp = cnt[CT_NVJP];
     stats->retcode_adj = status[ST_RETCODE];
-    stats->adj_path = tcbwd ? GBNDE_PATH_TC
+    stats->adj_path = tc_replay ? GBNDE_PATH_TC_RECOMPUTE
+                      : tcbwd     ? GBNDE_PATH_TC
                       : (a.dense != nullptr || backsolve) ? GBNDE_PATH_FP32 : GBNDE_PATH_FP32_RECOMPUTE;
   }
   if (status[ST_BARRIER]) return fail(GBNDE_ERR_TIMEOUT, "backward grid barrier timed out");

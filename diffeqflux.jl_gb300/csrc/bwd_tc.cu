@@ -30,6 +30,15 @@
 // (warp butterfly reductions) added into small per-CTA pending buffers, one
 // row per 32-row group of the tile (one adder per element: deterministic).
 // lam uses compensated (TwoSum) sums; t, H and the controller are FP64.
+//
+// O(checkpoints) mode (no dense storage, b.dense == null): at the start of
+// every save interval the CTA replays that interval's accepted forward steps
+// for its own tiles on the tensor cores (forward op list, CMD_FWD), from the
+// checkpoint's state and compensation with the recorded step sizes -- the
+// same arithmetic as the forward kernel, so the replayed stages are
+// bit-identical -- into the interval buffer b.ibuf, which u(t) is then
+// interpolated from. Each CTA reads only its own tiles, so no grid-wide sync
+// is needed between the replay and the adjoint steps.
 #include "tc_args.h"
 
 namespace gbnde {
@@ -199,9 +208,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
   if (warp >= tc::kMmaWarp) {
     tc::regs_give_ctl();
     if (warp == tc::kMmaWarp)
-      tc::mma_loop_cmd(A.ops, A.dwops, A.ops7, sh, aring, wring,
+      tc::mma_loop_cmd(A.ops, A.dwops, A.ops7, A.fwops, sh, aring, wring,
                        A.img + (size_t)blockIdx.x * A.tpc * tc::kImgSlots * A.img_cta, A.img_cta);
-    else if (warp == tc::kTmaWarp) tc::tma_loop_cmd(A.ops, A.dwops, A.ops7, sh, aring, wring);
+    else if (warp == tc::kTmaWarp) tc::tma_loop_cmd(A.ops, A.dwops, A.ops7, A.fwops, sh, aring, wring);
   } else {
     tc::regs_take_epi();
     // ======================= epilogue warps =======================
@@ -526,8 +535,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       for (int j = 0; j < 7; ++j) hb[j] = (float)(h * (double)bw[j]);
       *nstep = n;
     };
+    // dense slot of forward step n: the forward's storage, or the replayed
+    // interval's buffer (slot n - nlo of the current interval)
+    int nlo_cur = 0;
+    auto slot_of = [&](int n) -> const float* {
+      return a.dense ? a.dense + (size_t)n * 8 * SBt : a.ibuf + (size_t)(n - nlo_cur) * 8 * SBt;
+    };
     auto dense_u = [&](int tile, int n, const float* hb, float* x) {
-      const float* slot = a.dense + (size_t)n * 8 * SBt;
+      const float* slot = slot_of(n);
       const size_t g = tofs(tile);
       // u_n + sum_j hb_j k_j, in two parts of kPart components and batches of
       // four vectors (u_n, k1..k3 then k4..k7), each batch in flight together
@@ -547,10 +562,126 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       }
     };
 
+    // The plain right-hand side of one tile (the forward list): Y -> kout,
+    // with the forward kernel's arithmetic.
+    auto fwd_eval = [&](const float* Y, float* kout) -> bool {
+      if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_FWD)) return false;
+      float v[tc::kCW];
+#pragma unroll
+      for (int i = 0; i < tc::kCW; ++i) {
+        const float y = (i < th.nmine) ? Y[i] : 0.f;
+        v[i] = m.cube ? y * y * y : y;
+      }
+      if (!emit(es, sh, aring, th, v)) return false;
+      for (int l = 0; l < L - 1; ++l) {
+        const int N = m.dims[l + 1];
+        uint32_t col;
+        if (!tc::epi_wait_acc(es, sh, &col)) return false;
+        for (int cc = 0; cc < (N + 63) / 64; ++cc) {
+          const int n0 = 64 * cc + tc::kCW * th.ch;
+          float bc[tc::kCW];
+          tc::load_bias_cw(A.bias[l], n0, N, bc);
+          tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+          tc::bias_act_cw(v, bc, m.act[l], n0, N);
+          if (!emit(es, sh, aring, th, v)) return false;
+        }
+        tc::epi_release_acc(es, sh);
+      }
+      uint32_t col;
+      if (!tc::epi_wait_acc(es, sh, &col)) return false;
+      float bc[tc::kCW];
+      tc::load_bias_cw(A.bias[L - 1], tc::kCW * th.ch, m.dims[L], bc);
+      tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(tc::kCW * th.ch), v);
+      tc::bias_act_cw(v, bc, m.act[L - 1], tc::kCW * th.ch, m.dims[L]);
+#pragma unroll
+      for (int i = 0; i < tc::kCW; ++i) kout[i] = (i < th.nmine) ? v[i] : 0.f;
+      tc::epi_release_acc(es, sh);
+      return true;
+    };
+    long long nf_rec = 0;
+    // Replay of the interval's forward steps nlo..nhi from its checkpoint into
+    // b.ibuf (slot j = step nlo + j: u_n, k1..k7), as fwd_tc.cu computes them.
+    auto replay = [&](const Interval& iv) -> bool {
+      long long evals = 0;
+      for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+        const bool v = valid(tile);
+        const size_t g = tofs(tile);
+        float* ru = A.rep[0];
+        float* rc = A.rep[1];
+        {
+          float u[tc::kCW], cp[tc::kCW], k[tc::kCW];
+          if (v) {
+            ldv(a.ckpt + (size_t)iv.ckpt * SB + gofs(tile), th.nmine, vec, u);
+            tc::tl_ldv(A.ckcomp + (size_t)iv.ckpt * SBt + g, cp);
+          } else {
+            for (int i = 0; i < tc::kCW; ++i) u[i] = cp[i] = 0.f;
+          }
+          tc::tl_stv(ru + g, u);
+          tc::tl_stv(rc + g, cp);
+          tc::tl_stv(a.ibuf + g, u);
+          if (!fwd_eval(u, k)) return false;
+          ++evals;
+          tc::tl_stv(a.ibuf + SBt + g, k);
+        }
+        for (int n = iv.nlo; n <= iv.nhi; ++n) {
+          float* slot = a.ibuf + (size_t)(n - iv.nlo) * 8 * SBt;
+          const double h = a.fsteps[2 * n + 1];
+          for (int i = 1; i < 7; ++i) {
+            float ha[6];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) ha[j] = (float)(h * c_tab.a[i][j]);
+            float u[tc::kCW], sv[tc::kCW], Y[tc::kCW], k[tc::kCW];
+            if (v) {
+              tc::tl_ldv(ru + g, u);
+              tc::tl_ldv(rc + g, sv);
+#pragma unroll
+              for (int j = 0; j < 6; ++j) {
+                if (j >= i) break;
+                float kj[tc::kCW];
+                tc::tl_ldv(slot + (size_t)(1 + j) * SBt + g, kj);
+#pragma unroll
+                for (int q = 0; q < tc::kCW; ++q) sv[q] = fmaf(ha[j], kj[q], sv[q]);
+              }
+#pragma unroll
+              for (int q = 0; q < tc::kCW; ++q) Y[q] = u[q] + sv[q];
+              if (i == 6) {
+                float cn[tc::kCW];
+#pragma unroll
+                for (int q = 0; q < tc::kCW; ++q) cn[q] = sv[q] - (Y[q] - u[q]);
+                tc::tl_stv(ru + g, Y);
+                tc::tl_stv(rc + g, cn);
+              }
+            } else {
+#pragma unroll
+              for (int q = 0; q < tc::kCW; ++q) Y[q] = 0.f;
+            }
+            if (!fwd_eval(Y, k)) return false;
+            ++evals;
+            tc::tl_stv(slot + (size_t)(1 + i) * SBt + g, k);
+          }
+          if (n < iv.nhi) {
+            // the next slot: its state, and k7 as its k1 (FSAL)
+            float* nx = slot + 8 * SBt;
+            float un[tc::kCW], k7[tc::kCW];
+            tc::tl_ldv(ru + g, un);
+            tc::tl_ldv(slot + 7 * SBt + g, k7);
+            tc::tl_stv(nx + g, un);
+            tc::tl_stv(nx + SBt + g, k7);
+          }
+        }
+      }
+      if (blockIdx.x == 0) nf_rec += evals / ((a.ntiles + G - 1 - blockIdx.x) / G);
+      return true;
+    };
+
     for (int ivi = 0; ivi < a.niv && ok && ret == GBNDE_RET_SUCCESS; ++ivi) {
       const Interval iv = a.iv[ivi];
       double t = iv.t_hi;
       const double t_lo = iv.t_lo;
+      if (!a.dense) {
+        nlo_cur = iv.nlo;
+        if (!replay(iv)) { ok = false; break; }
+      }
       // ---- FSAL stage at the interval start: kl1 and P1 = b1 * mu ----
       {
         zero_bias(Pb[iP1]);
@@ -823,7 +954,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       a.counters[CT_NVJP] = nf_vjp;
       a.counters[CT_NACCEPT] = nacc;
       a.counters[CT_NREJECT] = nrej;
-      a.counters[CT_NRECOMP] = 0;
+      a.counters[CT_NRECOMP] = nf_rec;
       const int e = ((volatile int*)&sh.err)[0];
       a.status[ST_RETCODE] = (a.status[ST_BARRIER] != 0 || e != 0) ? GBNDE_RET_BARRIER_TIMEOUT : ret;
       if (e) a.status[2] = e;

@@ -150,9 +150,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
   if (warp >= tc::kMmaWarp) {
     tc::regs_give_ctl();
     if (warp == tc::kMmaWarp)
-      tc::mma_loop_cmd(A.ops, A.dwops, A.ops, sh, aring, wring,
+      tc::mma_loop_cmd(A.ops, A.dwops, A.ops, A.ops, sh, aring, wring,
                        A.img + (size_t)blockIdx.x * A.tpc * tc::kImgSlots * A.img_cta, A.img_cta);
-    else if (warp == tc::kTmaWarp) tc::tma_loop_cmd(A.ops, A.dwops, A.ops, sh, aring, wring);
+    else if (warp == tc::kTmaWarp) tc::tma_loop_cmd(A.ops, A.dwops, A.ops, A.ops, sh, aring, wring);
   } else {
     tc::regs_take_epi();
     // ======================= epilogue warps =======================

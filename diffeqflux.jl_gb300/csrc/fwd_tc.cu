@@ -453,6 +453,13 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tc_kernel(FwdTcArgs A) {
                 float u[tc::kCW];
                 tc::tl_ldv(ucur + tofs(tile), u);
                 stv(dst + gofs(tile), th.nmine, vec, u);
+                if (A.ckcomp) {
+                  // and the compensation, so that the adjoint's replay of the
+                  // interval from here is bit-identical to this solve
+                  float cp[tc::kCW];
+                  tc::tl_ldv(ccur + tofs(tile), cp);
+                  tc::tl_stv(A.ckcomp + (size_t)nck * SBt + tofs(tile), cp);
+                }
               }
             if (blockIdx.x == 0 && threadIdx.x == 0) a.ckpt_step[nck] = (int)naccept;
             ++nck;

@@ -13,6 +13,7 @@ struct FwdTcArgs {
   float* dense;         // slots of 8 x S*B floats: u_n, k1..k7 (or null)
   long long dense_slots;
   float* kring;         // 7 x S*B stage buffers when dense == null
+  float* ckcomp;        // the state's compensation at each checkpoint (tile layout), or null
 };
 
 
@@ -40,6 +41,13 @@ struct BwdTcArgs {
   int nh[GBNDE_MAX_LAYERS];          // M halves (128 rows) of layer l's dW
   int nbias;
   int boffp[GBNDE_MAX_LAYERS];  // offset of layer l's bias inside a pending-bias row
+  // O(checkpoints) mode (b.dense == null): each save interval's forward steps
+  // are replayed on the tensor cores (fwops, CMD_FWD) from the checkpoint
+  // (b.ckpt: u, API layout; ckcomp: its compensation, tile layout) into the
+  // interval buffer b.ibuf (slot j = step nlo + j: u_n, k1..k7, tile layout)
+  tc::OpList fwops;
+  const float* ckcomp;
+  float* rep[2];                // replayed state and its compensation (tile layout)
 };
 
 

@@ -245,7 +245,9 @@ __device__ __forceinline__ void tl_stp(float* p, int part, const float* x) {
 // CMD_EVAL_RE runs the re-emission list instead of the evaluation list: the
 // forward ops are copy-only (the epilogue re-emits stored activations, whose
 // chunks only go to their images), the VJP ops are the same.
-enum : uint32_t { CMD_EVAL = 1, CMD_DW = 2, CMD_EVAL_RE = 3 };
+// CMD_FWD runs the forward list (the plain right-hand side, no images): the
+// adjoint's replay of a save interval's forward steps from its checkpoint.
+enum : uint32_t { CMD_EVAL = 1, CMD_DW = 2, CMD_EVAL_RE = 3, CMD_FWD = 4 };
 
 // Image slot of stacked stage s (0-based) when stage 1 lives in slot f.
 __device__ __forceinline__ int stage_slot(int s, int f) { return s == 0 ? f : s; }
@@ -401,8 +403,8 @@ __device__ __forceinline__ bool cmd_take(Shared& sh, int& cs, uint32_t& cph, uin
 // image region, `img_cta` the bytes
 // of one slot. Before a CMD_DW round the image copies must have landed: the
 // elected lane waits for its bulk groups and signals the producer.
-__device__ __forceinline__ void mma_loop_cmd(const OpList& ev, const OpList& dw, const OpList& ev_re, Shared& sh,
-                                             uint8_t* aring,
+__device__ __forceinline__ void mma_loop_cmd(const OpList& ev, const OpList& dw, const OpList& ev_re,
+                                             const OpList& fw, Shared& sh, uint8_t* aring,
                                              uint8_t* wring, uint8_t* imgs, size_t img_cta) {
   MmaState m;
   int cs = 0;
@@ -418,11 +420,12 @@ __device__ __forceinline__ void mma_loop_cmd(const OpList& ev, const OpList& dw,
         mbar_arrive(&sh.img_done);
       }
       __syncwarp();
-    } else if (((cmd >> 8) & 0xffu) != 0) {
+    } else if ((cmd & 0xffu) != CMD_FWD && ((cmd >> 8) & 0xffu) != 0) {
       const size_t j = (cmd >> 24) & 0xffu;  // tile of the CTA: its own image set
       img_base = imgs + (j * kImgSlots + (((cmd >> 8) & 0xffu) - 1)) * img_cta;
     }
-    const OpList& L = isdw ? dw : ((cmd & 0xffu) == CMD_EVAL_RE ? ev_re : ev);
+    const uint32_t kd = cmd & 0xffu;
+    const OpList& L = isdw ? dw : (kd == CMD_EVAL_RE ? ev_re : (kd == CMD_FWD ? fw : ev));
     const int first = isdw ? 0 : (int)((cmd >> 16) & 0xffu);
     for (int i = first; i < L.nops && ok; ++i) ok = mma_op(L.op[i], m, sh, aring, wring, img_base);
   }
@@ -599,8 +602,8 @@ __device__ __forceinline__ void tma_loop(const OpList& ops, Shared& sh, uint8_t*
   tma_drain(t, sh);
 }
 
-__device__ __forceinline__ void tma_loop_cmd(const OpList& ev, const OpList& dw, const OpList& ev_re, Shared& sh,
-                                             uint8_t* aring,
+__device__ __forceinline__ void tma_loop_cmd(const OpList& ev, const OpList& dw, const OpList& ev_re,
+                                             const OpList& fw, Shared& sh, uint8_t* aring,
                                              uint8_t* wring) {
   TmaState t;
   int cs = 0;
@@ -608,7 +611,8 @@ __device__ __forceinline__ void tma_loop_cmd(const OpList& ev, const OpList& dw,
   bool run = true;
   while (run && cmd_take(sh, cs, cph, &cmd)) {
     const bool isdw = (cmd & 0xffu) == CMD_DW;
-    const OpList& L = isdw ? dw : ((cmd & 0xffu) == CMD_EVAL_RE ? ev_re : ev);
+    const uint32_t kd = cmd & 0xffu;
+    const OpList& L = isdw ? dw : (kd == CMD_EVAL_RE ? ev_re : (kd == CMD_FWD ? fw : ev));
     if (isdw) {
       // the stage images (bulk-copied by the MMA warp) must have landed
       if (!tma_wait_or_stop(sh, &sh.img_done, dph)) break;

@@ -166,6 +166,16 @@ size_t gbnde_nparams(const gbnde_ctx* ctx);
 int gbnde_set_params(gbnde_ctx* ctx, const float* p, size_t n);
 int gbnde_set_params_device(gbnde_ctx* ctx, const float* p_dev, size_t n);
 
+/* Bound on the device memory of the forward's dense stage storage (u_n, k1..k7
+ * per accepted step), which the InterpolatingAdjoint reads. 0 (the default):
+ * up to a quarter of the free device memory. When a solve needs more, the
+ * adjoint recomputes each save interval from its checkpoint instead (memory
+ * O(checkpoints)): the FP32 kernel, or the tensor-core adjoint replaying the
+ * interval on the tensor cores (gbnde_stats.adj_path says which). No
+ * reference counterpart (InterpolatingAdjoint(checkpointing = true) is the
+ * reference's memory switch, src/neural_de.jl:57). */
+int gbnde_set_stage_memory(gbnde_ctx* ctx, size_t max_bytes);
+
 /* ---- NeuralODE forward solve ------------------------------------------------
  * Replaces solve(ODEProblem{false}(dudt, x, tspan, p), Tsit5(); saveat, abstol,
  * reltol, ...) at src/neural_de.jl:52-58. u0: S x B. usave: S x B x nsave.

@@ -179,3 +179,41 @@ def test_bf16_batch_above_one_tile_per_sm():
     assert _rel(out["bf16"][0], out["fp32"][0].astype(np.float64)) < 1e-4
     assert _rel(out["bf16"][1], out["fp32"][1].astype(np.float64)) < 1e-3
     assert _rel(out["bf16"][2], out["fp32"][2].astype(np.float64)) < 1e-3
+
+
+@pytest.mark.parametrize("nsave", [4, 20])
+def test_bf16_checkpoint_replay_matches_dense_storage(nsave):
+    """O(checkpoints) memory in the BF16 form: with the dense stage storage
+    capped (gbnde_set_stage_memory), the tensor-core adjoint replays every
+    save interval's forward steps on the tensor cores from its checkpoint
+    (state and compensation) -- bit-identical to the forward -- so its
+    gradient matches the dense-storage gradient to 1e-5 (to the last bit in
+    practice), and gbnde_stats.adj_path reports the recompute path."""
+    import ctypes as C
+
+    from gbnde import _lib
+    S, H, B = 64, 256, 300
+    model, p, rng = _setup([S, H, H, S], ["tanh", "tanh", "identity"], False, B, 4, bias=0.02)
+    u0 = rng.standard_normal((S, B)).astype(np.float32)
+    ts = np.linspace(0.0, 1.0, nsave)
+    node = _node(model, ts, "bf16", 1e-7, 1e-5)
+    s = node.solver
+    s.set_params(p)
+    us, st = s.forward(u0, node.desc())
+    g = (0.1 * rng.standard_normal(us.shape)).astype(np.float32)
+    du0, dp, sta = s.backward(g)
+    assert sta.adj_path == _lib.PATH_TC and sta.nf_recompute == 0
+    _lib.check(s.lib.gbnde_set_stage_memory(s.h, C.c_size_t(1)))
+    us2, st2 = s.forward(u0, node.desc())
+    assert np.array_equal(us2, us) and st2.naccept == st.naccept
+    du0r, dpr, star = s.backward(g)
+    assert star.retcode_adj == 0
+    assert star.adj_path == _lib.PATH_TC_RECOMPUTE
+    # every interval replays its steps: at least 6 evaluations per forward step, plus its first k1
+    assert star.nf_recompute >= 6 * st.naccept + 1
+    assert _rel(du0r, du0) < 1e-5 and _rel(dpr, dp) < 1e-5
+    assert star.naccept_adj == sta.naccept_adj
+    _lib.check(s.lib.gbnde_set_stage_memory(s.h, C.c_size_t(0)))
+    us3, _ = s.forward(u0, node.desc())
+    _, _, sta3 = s.backward(g)
+    assert sta3.adj_path == _lib.PATH_TC
