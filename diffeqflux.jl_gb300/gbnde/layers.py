@@ -415,10 +415,9 @@ class NeuralODE:
         if not isinstance(sensealg, (InterpolatingAdjoint, BacksolveAdjoint, GaussAdjoint)):
             raise TypeError("sensealg must be InterpolatingAdjoint(), BacksolveAdjoint(), GaussAdjoint() or "
                             "QuadratureAdjoint()")
-        if saveat is None and save_everystep is not False:
-            raise NotImplementedError(
-                "save_everystep=true is not offered by the GB300 solver; pass saveat or "
-                "save_everystep=False")
+        # the reference saves every step when no saveat is given
+        # (save_everystep defaults to true then); with saveat it saves only there
+        self.save_everystep = (saveat is None) if save_everystep is None else bool(save_everystep)
         self.model = model
         # A Float32 tspan makes the reference's integrator keep t and dt in
         # Float32; the FP32 form follows (GBNDE_FLAG_FP32_TIME), the BF16 form
@@ -434,7 +433,8 @@ class NeuralODE:
         self.abstol, self.reltol = float(abstol), float(reltol)
         self.dt, self.dtmin, self.maxiters = float(dt), float(dtmin), int(maxiters)
         if save_start is None:
-            save_start = saveat is not None
+            save_start = saveat is not None or self.save_everystep
+        self.save_start, self.save_end = bool(save_start), bool(save_end)
         self.saveat = _saveat_points(self.tspan, saveat, save_start, save_end)
         if self.float32_time:
             self.saveat = [float(np.float32(s)) for s in self.saveat]
@@ -456,12 +456,53 @@ class NeuralODE:
                                  self.sensealg.code, self.dt, self.dtmin, self.maxiters,
                                  flags=_lib.FLAG_FP32_TIME if self.float32_time else 0)
 
+    def _everystep_points(self, x2, p, is_torch):
+        """save_everystep: the accepted step times of this solve. The save points
+        do not influence the step sizes (only the end of the span clips a
+        step), so a first solve gives the steps, and the solve that saves at
+        exactly those times (each a step end: the state itself, no
+        interpolation) takes the same steps."""
+        s = self.solver
+        d = Solver.solve_desc(self.tspan[0], self.tspan[1], [self.tspan[1]], self.abstol, self.reltol,
+                              self.sensealg.code, self.dt, self.dtmin, self.maxiters,
+                              flags=_lib.FLAG_FP32_TIME if self.float32_time else 0)
+        if is_torch:
+            import torch
+            pc = p.detach().to(torch.float32).contiguous()
+            if x2.is_cuda:
+                S, B = x2.shape
+                u0_cm = x2.detach().to(torch.float32).t().contiguous()
+                out = torch.empty((1, B, S), dtype=torch.float32, device=x2.device)
+                torch.cuda.current_stream(x2.device).synchronize()
+                s.set_params_device(pc.to(x2.device))
+                s.forward_device(u0_cm, out, d, S, B)
+            else:
+                s.set_params(pc.cpu().numpy())
+                s.forward(x2.detach().cpu().numpy(), d)
+        else:
+            s.set_params(p)
+            s.forward(x2, d)
+        steps = s.forward_steps()
+        # each step's end is the next step's start time (as the integrator
+        # stored it, Float32 time included); the last ends at t1
+        ends = [steps[i + 1][0] for i in range(len(steps) - 1)] + ([self.tspan[1]] if steps else [])
+        pts = ([self.tspan[0]] if self.save_start else []) + ends
+        if not self.save_end and pts and pts[-1] == self.tspan[1]:
+            pts = pts[:-1]
+        return pts or [self.tspan[1]]
+
     def __call__(self, x, p, st=None):
         try:
             import torch
             is_torch = isinstance(x, torch.Tensor)
         except ImportError:  # pragma: no cover
             is_torch = False
+        if self.save_everystep:
+            x2 = x if (not is_torch or x.dim() == 2) else x.reshape(-1, 1)
+            if not is_torch:
+                x2 = np.asarray(x, dtype=np.float32)
+                x2 = x2[:, None] if x2.ndim == 1 else x2
+            self.saveat = self._everystep_points(x2, p, is_torch)
         if is_torch:
             from ._torch import solve_saveat
             x2 = x if x.dim() == 2 else x.reshape(-1, 1)

@@ -231,18 +231,42 @@ function ChainRulesCore.rrule(::typeof(_build_sol), prob, alg, saveat, out, vec_
 end
 
 # ---- NeuralODE on the GB300 path (src/neural_de.jl:47-61) --------------------------------
+# Accepted steps (t_n, h_n) of the context's last forward solve.
+function forward_steps(ctx::Ctx)
+    n = ccall((:gbnde_forward_steps, libgbnde), Clonglong, (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Clonglong),
+              ctx.h, C_NULL, C_NULL, 0)
+    t = zeros(Cdouble, n)
+    h = zeros(Cdouble, n)
+    ccall((:gbnde_forward_steps, libgbnde), Clonglong, (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Clonglong),
+          ctx.h, t, h, n)
+    t, h
+end
+
 function (n::NeuralODE)(x, p, st, alg::GB300Tsit5)
     kw = Dict(n.kwargs)
-    get(kw, :save_everystep, false) === true &&
-        throw(ArgumentError("save_everystep = true is not offered by the GB300 solver; pass saveat"))
-    saveat = Float64.(collect(get(kw, :saveat, [n.tspan[2]])))
     ctx = ctx_for(n.model, alg.precision)
     sense = get(kw, :sensealg, InterpolatingAdjoint(; autojacvec = ZygoteVJP()))
     u0 = x isa AbstractVector ? reshape(x, :, 1) : x
     # a Float32 tspan keeps t and dt in Float32, as the reference's integrator does
     flags = (eltype(n.tspan) === Float32 && alg.precision === :fp32) ? GBNDE_FLAG_FP32_TIME : Cint(0)
-    out = gb300_solve(Float32.(u0), Float32.(collect(p)), ctx, Float64.(n.tspan), saveat,
-                      get(kw, :abstol, 1e-6), get(kw, :reltol, 1e-3), sense, flags)
+    abstol, reltol = get(kw, :abstol, 1e-6), get(kw, :reltol, 1e-3)
+    everystep = get(kw, :save_everystep, !haskey(kw, :saveat))
+    saveat = if everystep
+        # every accepted step: the save points never change the step sizes
+        # (only the end of the span clips a step), so a first solve gives the
+        # steps and the solve saving at their ends takes the same steps
+        ChainRulesCore.@ignore_derivatives begin
+            gb300_solve(Float32.(u0), Float32.(collect(p)), ctx, Float64.(n.tspan), Float64[n.tspan[2]],
+                        abstol, reltol, sense, flags)
+            ts, _ = forward_steps(ctx)
+            ends = length(ts) > 0 ? [ts[2:end]; Float64(n.tspan[2])] : [Float64(n.tspan[2])]
+            get(kw, :save_start, true) ? [Float64(n.tspan[1]); ends] : ends
+        end
+    else
+        Float64.(collect(get(kw, :saveat, [n.tspan[2]])))
+    end
+    out = gb300_solve(Float32.(u0), Float32.(collect(p)), ctx, Float64.(n.tspan), saveat, abstol, reltol, sense,
+                      flags)
     retcode = ChainRulesCore.@ignore_derivatives RETCODES[ctx.stats.retcode + 1]
     prob = ChainRulesCore.@ignore_derivatives ODEProblem{false}((u, p, t) -> u, x, n.tspan, p)
     _build_sol(prob, alg, saveat, out, x isa AbstractVector, retcode), st

@@ -76,8 +76,9 @@ def test_layer_api_validation():
         gbnde.Chain(gbnde.Dense(2, 3), gbnde.Dense(4, 2))
     with pytest.raises(TypeError):
         gbnde.NeuralODE(m, (0.0, 1.0), object(), saveat=[0, 1])
-    with pytest.raises(NotImplementedError):
-        gbnde.NeuralODE(m, (0.0, 1.0), gbnde.Tsit5())
+    # no saveat: every step is saved (the reference's save_everystep default)
+    assert gbnde.NeuralODE(m, (0.0, 1.0), gbnde.Tsit5()).save_everystep
+    assert not gbnde.NeuralODE(m, (0.0, 1.0), gbnde.Tsit5(), saveat=[0.0, 1.0]).save_everystep
     node = gbnde.NeuralODE(m, (0.0, 1.0), gbnde.Tsit5(), saveat=0.1)
     assert len(node.saveat) == 11 and node.saveat[0] == 0.0 and abs(node.saveat[-1] - 1.0) < 1e-12
     node = gbnde.NeuralODE(m, (0.0, 1.0), gbnde.Tsit5(), save_everystep=False, save_start=False)

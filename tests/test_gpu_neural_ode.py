@@ -320,3 +320,37 @@ def test_barrier_wait_runs_out_and_reports():
     node.solver.set_params(p)
     _, st = node.solver.forward(rng.standard_normal((2, 4)).astype(np.float32), node.desc())
     assert st.retcode == 0
+
+
+@pytest.mark.parametrize("device", ["cpu", "cuda"])
+def test_save_everystep_states_and_gradient(device):
+    """No saveat: the reference saves every accepted step (save_everystep
+    defaults to true, src/neural_de.jl:55-58 with the kwargs of
+    test/BasicNeuralDE/neural_de_tests.jl:27-42). sol.t are t0 and every step
+    end; the states are the oracle's at those times (replaying the steps), and
+    the gradient of a loss of all of them matches the oracle's adjoint with
+    those save points."""
+    import torch
+
+    import gbnde
+    from oracle import tsit5 as ots
+    model, p, rng = _setup([3, 16, 3], ["tanh", "identity"], False, 5, 9)
+    node = gbnde.NeuralODE(model, (0.0, 1.0), gbnde.Tsit5(), abstol=1e-6, reltol=1e-4)
+    assert node.save_everystep
+    dev = torch.device(device, 0) if device == "cuda" else torch.device("cpu")
+    u0 = rng.standard_normal((3, 5)).astype(np.float32)
+    x = torch.tensor(u0, device=dev, requires_grad=True)
+    pt = torch.tensor(p, device=dev, requires_grad=True)
+    sol, _ = node(x, pt, None)
+    steps = node.solver.forward_steps()
+    assert sol.t[0] == 0.0 and sol.t[-1] == 1.0 and len(sol.t) == len(steps) + 1
+    assert all(abs(sol.t[k + 1] - (steps[k][0] + steps[k][1])) < 1e-12 for k in range(len(steps)))
+    arr = sol.array()
+    w = torch.tensor(rng.standard_normal(tuple(arr.shape)).astype(np.float32), device=dev)
+    (arr * w).sum().backward()
+    rhs = _oracle(model, p)
+    ous, fwd = ots.solve_forward(rhs, u0.astype(np.float64), 0.0, 1.0, sol.t, 1e-6, 1e-4, steps=steps)
+    assert _rel(arr.detach().cpu().numpy(), ous) < 2e-5
+    gu, gp, _ = ots.adjoint_interpolating(rhs, fwd, sol.t, w.cpu().numpy().astype(np.float64), 0.0, 1e-6, 1e-4)
+    assert _rel(x.grad.cpu().numpy(), gu) < 2e-4
+    assert _rel(pt.grad.cpu().numpy(), gp) < 2e-4
