@@ -1755,6 +1755,7 @@ int gbnde_train_step(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, cons
     sf.naccept_adj = sb.naccept_adj;
     sf.nreject_adj = sb.nreject_adj;
     sf.retcode_adj = sb.retcode_adj;
+    sf.adj_path = sb.adj_path;
     // a failed solve leaves the parameters unchanged (its loss is Inf)
     if (sb.retcode_adj == GBNDE_RET_SUCCESS) {
       if (launch_adam(p, m, v, c->tr_dp.as<float>(), c->P, opt->lr, opt->beta1, opt->beta2, opt->eps, step,
