@@ -43,8 +43,8 @@ METRIC = "NeuralODE grad evals/sec, BF16-TC vs plain FP32 GPU, at <=1e-3 rel err
 UNIT = "grad_evals/s"
 
 
-def workload_name(B):
-    return f"neuralode_b{B}_s64_h256x2_tanh_nsave20"
+def workload_name(B, S=64, H=256):
+    return f"neuralode_b{B}_s{S}_h{H}x2_tanh_nsave20"
 
 
 def glorot_params(dims, rng):
@@ -181,7 +181,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    wl = workload(B=args.batch)
+    wl = workload(S=args.state, H=args.hidden, B=args.batch)
     arm = CpuArm(wl)
     for _ in range(args.warmup):
         arm.grad_eval()
@@ -199,7 +199,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(secs) / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {"workload": workload_name(wl["B"]), "batch": wl["B"],
+        "config": {"workload": workload_name(wl["B"], wl["S"], wl["H"]), "batch": wl["B"],
                    "state": wl["S"], "hidden": wl["H"], "nsave": 20, "abstol": 1e-7, "reltol": 1e-5,
                    "sensealg": "InterpolatingAdjoint", "loss": "MSE"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": arm.cores, "kind": "port",
@@ -583,7 +583,7 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    wl = workload(B=args.batch)
+    wl = workload(S=args.state, H=args.hidden, B=args.batch)
     S, B = wl["S"], wl["B"]
     dev = torch.device("cuda", local)
     ns = len(wl["ts"])
@@ -676,8 +676,9 @@ def run_gpu(args):
     peak_tf = peaks.get("bf16_tflops", 1900.0)
     peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
     bwd_ms_avg = k_bwd / args.steps
-    kname = "bwd_tc_kernel" if args.precision == "bf16" else "bwd_f32_kernel"
-    traffic, traffic_src = profiled_traffic(kname, workload_name(B))
+    wide = args.precision == "bf16" and (S > 64 or wl["H"] > 256)
+    kname = ("bwd_tcw_kernel" if wide else "bwd_tc_kernel") if args.precision == "bf16" else "bwd_f32_kernel"
+    traffic, traffic_src = profiled_traffic(kname, workload_name(B, S, wl["H"]))
     achieved_tf = (flops / args.steps) / (bwd_ms_avg / 1000.0) / 1e12
     roof = {"kernel": kname,
             "bound": "tensor", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
@@ -739,6 +740,8 @@ def run_gpu(args):
     if rank == 0 and not args.no_aux:
         aux = {}
         for name, fn in (("spiral", aux_spiral), ("ffjord", aux_ffjord), ("multiple_shooting", aux_multishoot)):
+            if args.aux and name != args.aux:
+                continue
             try:
                 aux[name] = fn(local)
             except Exception as e:  # reported, never silently dropped
@@ -760,7 +763,7 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
         "data": "synthetic (seeded)",
-        "config": {"workload": workload_name(B), "batch": B, "state": S,
+        "config": {"workload": workload_name(B, S, wl["H"]), "batch": B, "state": S,
                    "hidden": wl["H"], "nsave": ns, "abstol": 1e-7, "reltol": 1e-5,
                    "sensealg": "InterpolatingAdjoint", "loss": "MSE", "precision": args.precision,
                    "l2": "flushed between steps (256 MB write)", "parallelism": "replicas"},
@@ -793,6 +796,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["fp32", "bf16"])
     ap.add_argument("--batch", type=int, default=16384)
+    ap.add_argument("--state", type=int, default=64, help="state dim of the NeuralODE (headline: 64)")
+    ap.add_argument("--hidden", type=int, default=256, help="width of its two hidden layers (headline: 256)")
+    ap.add_argument("--aux", default="", choices=["", "spiral", "ffjord", "multiple_shooting"],
+                    help="run only this one of the other workloads")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="the GPU line's cpu_baseline: full gradient evaluations until this many seconds (1-3)")
     ap.add_argument("--no-cpu", action="store_true")
