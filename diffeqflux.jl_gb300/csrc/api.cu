@@ -185,6 +185,9 @@ struct gbnde_ctx {
   // stash mode (fwd_tcw / bwd_tcw): state up to 256, widths up to 1024, time
   // row; weight images per 256-row N-block of each layer (W and W^T)
   bool tc_wide = false, tc_wide_bwd = false;
+  bool fwd_wide = false;  // the last forward ran on the stash engine (its adjoint follows)
+  int force_wide = -1;    // autotuner: -1 tuned/default, 0 single-accumulator, 1 stash engine
+  std::map<std::pair<int, int>, int> tuned_tc;  // (S, B) -> 1: stash engine measured faster
   int nsc = 1;  // 64-component chunks of the state in the tensor-core kernels
   size_t wb_off[GBNDE_MAX_LAYERS][4] = {}, wbT_off[GBNDE_MAX_LAYERS][4] = {};
   int wb_npad[GBNDE_MAX_LAYERS][4] = {}, wbT_npad[GBNDE_MAX_LAYERS][4] = {};
@@ -340,7 +343,9 @@ int gbnde_create(gbnde_ctx** out, const gbnde_mlp_desc* mlp, int precision, int 
     c->tc_bwd_ok = c->tc_bwd_ok && std::min(mlp->dims[l], mlp->dims[l + 1]) <= 256;
   // beyond that, stash mode: state <= 256, every width <= 1024 (16 K-chunks,
   // 4 N-blocks), no cube prefix; its adjoint needs an identity output layer
-  if (precision == GBNDE_PREC_BF16 && !c->tc_shape_ok) {
+  // (tc_wide: the stash engine covers the model; shapes the single-accumulator
+  // engine covers too run on it unless the autotuner measured the stash engine faster)
+  if (precision == GBNDE_PREC_BF16) {
     bool w = S <= 256 && !mlp->cube_input;
     for (int l = 0; l <= mlp->nlayers; ++l) w = w && mlp->dims[l] <= 1024;
     c->tc_wide = w;
@@ -425,8 +430,10 @@ static int bind_params(gbnde_ctx* c) {
 static int alloc_params(gbnde_ctx* c) {
   if (int r = c->params.ensure(c->P * sizeof(float))) return r;
   if (int r = c->wtr.ensure(c->P * sizeof(float))) return r;
+  // one image buffer: the single-accumulator engine's images, then the stash
+  // engine's per-N-block images (both where both engines cover the model)
+  size_t off = 0;
   if (c->precision == GBNDE_PREC_BF16 && c->tc_shape_ok) {
-    size_t off = 0;
     for (int l = 0; l < c->mlp.nlayers; ++l) {
       c->npad[l] = (c->mlp.dims[l + 1] + 15) / 16 * 16;
       c->nchunk[l] = (c->mlp.dims[l] + 63) / 64;
@@ -440,10 +447,8 @@ static int alloc_params(gbnde_ctx* c) {
       c->wtimg_off[l] = off;
       off += (size_t)c->nchunkT[l] * 2 * c->npadT[l] * 128;
     }
-    if (int r = c->wimg.ensure(off)) return r;
   }
   if (c->precision == GBNDE_PREC_BF16 && c->tc_wide) {
-    size_t off = 0;
     for (int l = 0; l < c->mlp.nlayers; ++l) {
       const int in = c->mlp.dims[l], out = c->mlp.dims[l + 1];
       for (int b = 0; b * 256 < out; ++b) {
@@ -457,8 +462,9 @@ static int alloc_params(gbnde_ctx* c) {
         off += (size_t)((out + 63) / 64) * 2 * c->wbT_npad[l][b] * 128;
       }
     }
-    if (int r = c->wimg.ensure(off)) return r;
   }
+  if (off)
+    if (int r = c->wimg.ensure(off)) return r;
   return 0;
 }
 
@@ -549,7 +555,14 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   const int LD = TM + 4;
   const size_t smem = (size_t)frows * LD * sizeof(float);
   const bool tcform = c->precision == GBNDE_PREC_BF16 && !c->ff_on;
-  const bool wide = tcform && c->tc_wide;
+  bool wide = tcform && c->tc_wide && !c->tc_shape_ok;
+  if (tcform && c->tc_wide && c->tc_shape_ok) {
+    if (c->force_wide >= 0) wide = c->force_wide == 1;
+    else {
+      auto it = c->tuned_tc.find({S, B});
+      wide = it != c->tuned_tc.end() && it->second == 1;
+    }
+  }
   const int ntiles = tcform ? (B + 127) / 128 : (B + TM - 1) / TM;
   int gmax = 0;
   if (tcform) {
@@ -796,6 +809,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   c->have_fwd = (status[ST_RETCODE] == GBNDE_RET_SUCCESS) && nacc <= maxsteps;
   c->dense_valid = c->dense_slots > 0 && nacc < c->dense_slots;
   c->dense_tl = tcform;
+  c->fwd_wide = wide;
   c->last_naccept = nacc;
   c->fS = S;
   if (c->have_fwd && !c->dense_valid && !c->rerun_guard && c->dense_slots < cap_slots) {
@@ -888,8 +902,11 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
     t.a_isA[l] = in > out ? 1 : 0;
     const int mside = t.a_isA[l] ? in : out;
     t.nh[l] = (mside + 127) / 128;
+    // per 64-trajectory block (2 of them): the M side in 128-row halves of
+    // 16 KB per piece, the N side in 64-feature blocks of 8 KB per piece
     auto img_bytes = [&](int dim, int isA) -> size_t {
-      return isA ? (size_t)2 * t.nh[l] * 32768 : (size_t)2 * 2 * ((dim + 63) / 64) * 8192;
+      return isA ? (size_t)2 * t.nh[l] * tc::kImgPieces * 16384
+                 : (size_t)2 * tc::kImgPieces * ((dim + 63) / 64) * 8192;
     };
     t.aoff[l] = (long long)off;
     off += img_bytes(in, t.a_isA[l]);
@@ -999,13 +1016,13 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
       if (n >= tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
       tc::GemmOp& o = t.dwops.op[n++];
       o.kind = 1;
-      o.aimg = t.img + aimg + (size_t)hh * 32768;
+      o.aimg = t.img + aimg + (size_t)hh * tc::kImgPieces * 16384;
       o.wimg = t.img + bimg;
       o.cta_stride = (size_t)tpc * tc::kImgSlots * t.img_cta;
       o.slot_stride = t.img_cta;
-      o.a_bytes = 32768;
-      o.a_step = (uint32_t)(t.nh[l] * 32768);
-      o.b_step = (uint32_t)(2 * nblk * 8192);
+      o.a_bytes = tc::kImgPieces * 16384;
+      o.a_step = (uint32_t)(t.nh[l] * tc::kImgPieces * 16384);
+      o.b_step = (uint32_t)(tc::kImgPieces * nblk * 8192);
       o.nblk_b = nblk;
       o.npad = (nside + 15) / 16 * 16;
       o.nchunk = 2 * 6 * tpc;  // K = (tile, stage, 64-trajectory block)
@@ -1063,8 +1080,11 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
     const int mside = t.a_isA[l] ? in : out;
     t.nh[l] = (mside + 127) / 128;
     nblkN[l] = ((t.a_isA[l] ? out : in) + 63) / 64;
+    // per 64-trajectory block (2 of them): the M side in 128-row halves of
+    // 16 KB per piece, the N side in 64-feature blocks of 8 KB per piece
     auto img_bytes = [&](int dim, int isA) -> size_t {
-      return isA ? (size_t)2 * t.nh[l] * 32768 : (size_t)2 * 2 * ((dim + 63) / 64) * 8192;
+      return isA ? (size_t)2 * t.nh[l] * tc::kImgPieces * 16384
+                 : (size_t)2 * tc::kImgPieces * ((dim + 63) / 64) * 8192;
     };
     t.aoff[l] = (long long)off;
     off += img_bytes(in, t.a_isA[l]);
@@ -1185,13 +1205,13 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
         if (!o) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
         const int nbb = std::min(4, nblk - 4 * nbk);
         o->kind = 1;
-        o->aimg = t.img + aimg + (size_t)hh * 32768;
+        o->aimg = t.img + aimg + (size_t)hh * tc::kImgPieces * 16384;
         o->wimg = t.img + bimg;
         o->cta_stride = (size_t)tpc * tc::kImgSlots * t.img_cta;
         o->slot_stride = t.img_cta;
-        o->a_bytes = 32768;
-        o->a_step = (uint32_t)(t.nh[l] * 32768);
-        o->b_step = (uint32_t)(2 * nblk * 8192);
+        o->a_bytes = tc::kImgPieces * 16384;
+        o->a_step = (uint32_t)(t.nh[l] * tc::kImgPieces * 16384);
+        o->b_step = (uint32_t)(tc::kImgPieces * nblk * 8192);
         o->nblk_b = nbb;
         o->b_off0 = (uint32_t)(4 * nbk * 8192);
         o->b_pstride = (uint32_t)(nblk * 8192);
@@ -1237,9 +1257,10 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   // tensor-core adjoint: on the dense stage storage, or (single-accumulator
   // engine, after a tensor-core forward) replaying each interval from its checkpoint
   const bool tc_replay = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && !gauss &&
-                         !c->dense_valid && c->dense_tl && !c->ff_on;
-  const bool tcbwd = (c->precision == GBNDE_PREC_BF16 && (c->tc_bwd_ok || c->tc_wide_bwd) && !backsolve &&
-                      !gauss && c->dense_valid && !c->ff_on) || tc_replay;
+                         !c->dense_valid && c->dense_tl && !c->fwd_wide && !c->ff_on;
+  const bool tcbwd = (c->precision == GBNDE_PREC_BF16 && (c->fwd_wide ? c->tc_wide_bwd : c->tc_bwd_ok) &&
+                      !backsolve && !gauss && c->dense_valid && !c->ff_on) ||
+                     tc_replay;
   // the FP32 adjoint reads dense slots only in its own layout; after a
   // tensor-core forward it recomputes each interval from the checkpoints
   const bool dense_f32 = c->dense_valid && !backsolve && !c->dense_tl;
@@ -1341,7 +1362,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   a.ffd = c->ff_d;
   a.exact = c->ff_exact;
   a.noise = c->ff_on ? c->ffnoise.as<float>() : nullptr;
-  if (tcbwd && c->tc_wide) {
+  if (tcbwd && c->fwd_wide) {
     if (c->recording) c->rec.bwd = false;  // stash-mode steps run eagerly
     if (int rr = backward_tcw(c, a, st, dp_d)) return rr;
   } else if (tcbwd) {
@@ -1938,12 +1959,6 @@ int gbnde_autotune(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, const 
   if (!c->have_params) return fail(GBNDE_ERR_STATE, "parameters not set");
   c->ff_on = 0;
   const bool tcform = c->precision == GBNDE_PREC_BF16;
-  if (tcform) {
-    // the tensor-core kernels run one 128-trajectory tile per CTA and one CTA
-    // per SM (tensor memory is allocated whole): nothing to choose
-    if (tiles) tiles[0] = tiles[1] = 128;
-    return 0;
-  }
   const size_t SB = (size_t)S * B, nsv = SB * d->nsave;
   int r = 0;
   if ((r = c->tr_us.ensure(nsv * 4)) || (r = c->tr_dl.ensure(nsv * 4)) || (r = c->tr_du0.ensure(SB * 4)) ||
@@ -1951,6 +1966,49 @@ int gbnde_autotune(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, const 
     return r;
   float* us = c->tr_us.as<float>();
   float* dl = c->tr_dl.as<float>();
+  if (tcform) {
+    // The tensor-core kernels run 128-trajectory tiles, one CTA per SM
+    // (tensor memory is allocated whole). What there is to choose is the
+    // engine, where both cover the model: the single-accumulator engine
+    // (operands through shared memory, activation reuse in the adjoint) or the
+    // stash engine (operands through a global stash, N-blocked layers). Each
+    // runs a forward solve and its adjoint three times; the faster (last two)
+    // is kept for this (S, B).
+    int mode = c->tc_shape_ok ? 0 : 1;
+    if (c->tc_shape_ok && c->tc_wide && c->tc_wide_bwd == c->tc_bwd_ok) {
+      double best = 1e300;
+      for (int w = 0; w < 2; ++w) {
+        c->force_wide = w;
+        double tsum = 0.0;
+        bool okc = true;
+        for (int rep = 0; rep < 3 && okc; ++rep) {
+          gbnde_stats st{}, sb{};
+          double L = 0.0;
+          if (forward_impl(c, d, S, B, u0, false, us, false, &st) || st.retcode != GBNDE_RET_SUCCESS ||
+              cudaMemsetAsync(dl, 0, nsv * 4, c->stream) != cudaSuccess || gbnde_loss_device(c, us, dl, 1, dl, &L) ||
+              backward_impl(c, dl, false, c->tr_du0.as<float>(), c->tr_dp.as<float>(), false, &sb) ||
+              sb.retcode_adj != GBNDE_RET_SUCCESS)
+            okc = false;
+          else if (rep > 0) tsum += c->fwd_ms + c->bwd_ms;
+        }
+        cudaGetLastError();
+        if (okc && tsum < best) { best = tsum; mode = w; }
+      }
+      c->force_wide = -1;
+      c->tuned_tc[{S, B}] = mode;
+      if (c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+      }
+      c->gkey.clear();
+      g_last_error.clear();
+    }
+    if (tiles) {
+      tiles[0] = 128;
+      tiles[1] = mode;
+    }
+    return 0;
+  }
   const int cand[4] = {8, 16, 32, 64};
   c->tuned.erase({S, B});
   // forward: fastest rows per tile over two timed solves each

@@ -66,6 +66,13 @@ constexpr int kSmemBytes = 1024 + kARing * kASlotBytes + kWRing * kWSlotBytes;
 constexpr int kMaxOps = 64;
 constexpr int kCmdRing = 4;
 constexpr int kImgSlots = 7;    // weight-gradient image slots per CTA: stages 1..6 + the next stage 1
+// Split pieces kept in the weight-gradient images, and the products of a
+// weight-gradient op: 1 (hi, one BF16 product) or 2 (hi and mid; hi.hi +
+// hi.lo + lo.hi). Measured at B = 16384, 64-256-256-64: one piece makes the
+// adjoint 10 % faster with the same step counts, at 1.2e-4 relative gradient
+// difference from the FP32 form (2 pieces: 6e-6); the chain GEMMs keep five
+// products (three make the forward take 23 steps instead of 12).
+constexpr int kImgPieces = 1;
 // Stash mode (layers wider than one 256-column accumulator): every chain A
 // operand goes through a per-CTA global "stash" of two buffers of up to
 // kStashChunks K-chunks (ring-slot layout: 3 pieces x 128 rows x 128 B each),
@@ -76,8 +83,8 @@ constexpr size_t kStashCta = (size_t)2 * kStashChunks * kASlotBytes;  // bytes p
 // kind 0 (chain GEMM): A chunks written by the epilogue (3 pieces, K-major),
 //   B = weight image chunks (2 pieces, K-major), five split products.
 // kind 1 (weight-gradient GEMM, K = trajectories): A and B both bulk-copied
-//   from per-CTA images (2 pieces, MN-major 64-column blocks), three products
-//   hi.hi + hi.lo + lo.hi.
+//   from per-CTA images (kImgPieces pieces, MN-major 64-column blocks):
+//   hi.hi, or hi.hi + hi.lo + lo.hi with two pieces.
 // kind 2 (copy only, command mode): epilogue-written A chunks that only go to
 //   their weight-gradient image; no product, no accumulator, no W chunk.
 // kind 3 (stash chain GEMM): as kind 0, but the A chunks are bulk-loaded by
@@ -260,18 +267,21 @@ struct MmaState {
   long long g = 0;
 };
 
-// Bulk copies of A chunk c (pieces hi and mid, rows 0-63 and 64-127) of a
-// kind-0 op to its weight-gradient image (same SW128 arrangement as the
-// image's 8 KB blocks). Issued by the elected lane.
+// Bulk copies of A chunk c (its first kImgPieces split pieces, rows 0-63 and
+// 64-127) of a chain op to its weight-gradient image (same SW128 arrangement
+// as the image's 8 KB blocks). Issued by the elected lane. Image layout, per
+// 64-trajectory block kc: M side (img_isA) [kc][128-row half][piece][16 KB],
+// N side [kc][piece][64-feature block][8 KB].
 __device__ __forceinline__ void copy_a_image(const GemmOp& op, int c, const uint8_t* achunk, uint8_t* img_base) {
   const uint64_t pol = policy_evict_first();  // read once, at the step's commit
   uint8_t* dst0 = img_base + op.img_off;
 #pragma unroll
-  for (int p = 0; p < 2; ++p) {
+  for (int p = 0; p < kImgPieces; ++p) {
 #pragma unroll
     for (int kc = 0; kc < 2; ++kc) {
-      const size_t o = op.img_isA ? ((size_t)((kc * op.img_nh + (c >> 1)) * 2 + p)) * 16384 + (size_t)(c & 1) * 8192
-                                  : ((size_t)((kc * 2 + p) * op.img_nblk + c)) * 8192;
+      const size_t o = op.img_isA
+                           ? ((size_t)((kc * op.img_nh + (c >> 1)) * kImgPieces + p)) * 16384 + (size_t)(c & 1) * 8192
+                           : ((size_t)((kc * kImgPieces + p) * op.img_nblk + c)) * 8192;
       bulk_s2g(dst0 + o, achunk + p * 16384 + kc * 8192, 8192, pol);
     }
   }
@@ -349,10 +359,11 @@ __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh
           }
         }
       } else {
-        // A chunk: 2 pieces x 2 blocks x 8 KB; B chunk: 2 pieces x nblk x 8 KB.
-        // Products hi.hi, hi.lo, lo.hi; K step of 16 trajectories = 2048 bytes.
+        // A chunk: kImgPieces x 2 blocks x 8 KB; B chunk: kImgPieces x nblk x
+        // 8 KB. Products hi.hi (and hi.lo, lo.hi with two pieces); K step of
+        // 16 trajectories = 2048 bytes.
 #pragma unroll
-        for (int pr = 0; pr < 3; ++pr) {
+        for (int pr = 0; pr < (kImgPieces == 2 ? 3 : 1); ++pr) {
           const int qa = (pr == 2) ? 1 : 0, qb = (pr == 1) ? 1 : 0;
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
@@ -514,7 +525,8 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
     ++t.g;
     return true;
   }
-  const uint32_t bbytes = op.kind == 0 ? 2u * (uint32_t)op.npad * 128u : 2u * (uint32_t)op.nblk_b * 8192u;
+  const uint32_t bbytes =
+      op.kind == 0 ? 2u * (uint32_t)op.npad * 128u : (uint32_t)kImgPieces * (uint32_t)op.nblk_b * 8192u;
   const uint8_t* bbase = op.kind == 0 ? op.wimg : op.wimg + (size_t)blockIdx.x * op.cta_stride;
   const uint8_t* abase = op.kind == 0 ? nullptr : op.aimg + (size_t)blockIdx.x * op.cta_stride;
   if (op.kind == 1 && op.first_dw) {
@@ -551,11 +563,11 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
     if (leader) {
       mbar_arrive_expect_tx(&sh.w_full[t.wslot], bbytes);
       if (op.kind == 1 && op.b_pstride != 0) {
-        // one N-block of the B image: its blocks in each of the two pieces
-        const uint32_t half = bbytes / 2;
-        for (int q = 0; q < 2; ++q)
-          bulk_g2s(wring + t.wslot * kWSlotBytes + q * half, bbase + boff + op.b_off0 + (size_t)q * op.b_pstride,
-                   half, &sh.w_full[t.wslot]);
+        // one N-block of the B image: its blocks in each piece
+        const uint32_t part = bbytes / kImgPieces;
+        for (int q = 0; q < kImgPieces; ++q)
+          bulk_g2s(wring + t.wslot * kWSlotBytes + q * part, bbase + boff + op.b_off0 + (size_t)q * op.b_pstride,
+                   part, &sh.w_full[t.wslot]);
       } else {
         const uint8_t* src = op.kind == 0 ? bbase + (size_t)c * bbytes : bbase + boff;
         bulk_g2s(wring + t.wslot * kWSlotBytes, src, bbytes, &sh.w_full[t.wslot]);

@@ -346,8 +346,12 @@ int gbnde_last_kernel_ms(gbnde_ctx* ctx, double* fwd_ms, double* bwd_ms);
  * trajectories per tile) and keeps the fastest of each for this (S, B) in
  * the context; later solves of that shape use them. The cotangent of the
  * timed adjoint is that of the mean square of the saved states. tiles[0] and
- * tiles[1] receive the forward and adjoint choices. The BF16 form has one
- * shape (128 trajectories per CTA, one CTA per SM) and returns 128, 128.
+ * tiles[1] receive the forward and adjoint choices. The BF16 form runs
+ * 128-trajectory tiles, one CTA per SM; there it times the two tensor-core
+ * engines where both cover the model (single-accumulator: state <= 64,
+ * widths <= 256; stash: state <= 256, widths <= 1024) on a forward solve and
+ * its adjoint, keeps the faster for this (S, B), and returns tiles[0] = 128,
+ * tiles[1] = the engine (0 single-accumulator, 1 stash).
  * Clobbers the last forward solve (run forward again before a backward).
  * No reference counterpart (the reference's tile sizes are chosen by its
  * array library). */
