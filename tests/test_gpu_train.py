@@ -148,3 +148,41 @@ def test_autotune_keeps_results(prec):
     for a, b in zip((after[0], after[2], after[3]), (before[0], before[2], before[3])):
         err = (a - b).norm().item() / b.norm().item()
         assert err <= 1e-4, err
+
+
+def test_autotune_bf16_chooses_an_engine():
+    """The BF16 form's autotuner times the single-accumulator and the stash
+    tensor-core engines on a shape both cover and keeps the faster; the two
+    engines give the same gradient to 1e-4 (the stash engine evaluates every
+    adjoint stage in full, the other reuses stage 6's activations for stage 7)."""
+    import torch
+
+    import gbnde
+    from gbnde import _lib
+    S, H, B = 64, 256, 2048
+    rng = np.random.default_rng(12)
+    model = gbnde.Chain(gbnde.Dense(S, H, "tanh"), gbnde.Dense(H, H, "tanh"), gbnde.Dense(H, S))
+    p = model.init_params(rng)
+    solver = gbnde.Solver(model, "bf16", 0)
+    desc = gbnde.Solver.solve_desc(0.0, 1.0, np.linspace(0, 1, 6), 1e-7, 1e-5, 0)
+    dev = torch.device("cuda", 0)
+    u0 = torch.from_numpy(np.ascontiguousarray(rng.standard_normal((B, S)).astype(np.float32))).to(dev)
+    us = torch.empty((6, B, S), dtype=torch.float32, device=dev)
+    g = torch.from_numpy(rng.standard_normal((6, B, S)).astype(np.float32)).to(dev)
+    du0 = torch.empty((B, S), dtype=torch.float32, device=dev)
+    dp = torch.empty(solver.nparams, dtype=torch.float32, device=dev)
+    solver.set_params(p)
+
+    def grad():
+        st = solver.forward_device(u0, us, desc, S, B)
+        sb = solver.backward_device(g, du0, dp)
+        torch.cuda.synchronize()
+        assert st.fwd_path == _lib.PATH_TC and sb.adj_path == _lib.PATH_TC
+        return dp.double().cpu().numpy(), du0.double().cpu().numpy()
+
+    g0, u0g = grad()
+    rows, engine = solver.autotune(u0, desc, S, B)
+    assert rows == 128 and engine in (0, 1)
+    g1, u1g = grad()
+    assert np.linalg.norm(g1 - g0) <= 1e-4 * np.linalg.norm(g0)
+    assert np.linalg.norm(u1g - u0g) <= 1e-4 * np.linalg.norm(u0g)
