@@ -186,6 +186,8 @@ struct gbnde_ctx {
   // row; weight images per 256-row N-block of each layer (W and W^T)
   bool tc_wide = false, tc_wide_bwd = false;
   bool fwd_wide = false;  // the last forward ran on the stash engine (its adjoint follows)
+  bool ffj_tc_ok = false; // FFJORD (Hutchinson trace) on the stash engine: d + 1 <= 64, identity output
+  DBuf ttrs;              // FFJORD on the stash engine: per-CTA row scratch
   int force_wide = -1;    // autotuner: -1 tuned/default, 0 single-accumulator, 1 stash engine
   std::map<std::pair<int, int>, int> tuned_tc;  // (S, B) -> 1: stash engine measured faster
   int nsc = 1;  // 64-component chunks of the state in the tensor-core kernels
@@ -351,6 +353,7 @@ int gbnde_create(gbnde_ctx** out, const gbnde_mlp_desc* mlp, int precision, int 
     c->tc_wide = w;
     c->tc_wide_bwd = w && mlp->act[mlp->nlayers - 1] == GBNDE_ACT_IDENTITY;
     c->nsc = (S + 63) / 64;
+    c->ffj_tc_ok = c->tc_wide_bwd && S + 1 <= 64;
   }
   if (precision == GBNDE_PREC_BF16 && !c->tc_shape_ok && !c->tc_wide) {
     gbnde_destroy(c);
@@ -554,9 +557,11 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   }
   const int LD = TM + 4;
   const size_t smem = (size_t)frows * LD * sizeof(float);
-  const bool tcform = c->precision == GBNDE_PREC_BF16 && !c->ff_on;
-  bool wide = tcform && c->tc_wide && !c->tc_shape_ok;
-  if (tcform && c->tc_wide && c->tc_shape_ok) {
+  // FFJORD with the Hutchinson trace runs on the stash engine where it covers the model
+  const bool ffj_tc = c->precision == GBNDE_PREC_BF16 && c->ff_on && c->ffj_tc_ok && !c->ff_exact;
+  const bool tcform = c->precision == GBNDE_PREC_BF16 && (!c->ff_on || ffj_tc);
+  bool wide = tcform && c->tc_wide && (!c->tc_shape_ok || ffj_tc);
+  if (tcform && c->tc_wide && c->tc_shape_ok && !ffj_tc) {
     if (c->force_wide >= 0) wide = c->force_wide == 1;
     else {
       auto it = c->tuned_tc.find({S, B});
@@ -680,25 +685,38 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
     ta.f = a;
     ta.f.ntiles = ntiles;
     ta.f.TM = 128;
+    // per layer its N-block ops; FFJORD: the primal blocks (stash buffer
+    // l % 2), then the tangent blocks on the same weights (buffer 2 + l % 2)
     int n = 0;
     for (int l = 0; l < c->mlp.nlayers; ++l) {
       const int out = c->mlp.dims[l + 1];
-      for (int b = 0; b * 256 < out; ++b) {
-        if (n >= tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
-        tc::GemmOp& o = ta.ops.op[n++];
-        o.kind = 3;
-        o.wimg = c->wimg.as<uint8_t>() + c->wb_off[l][b];
-        o.npad = c->wb_npad[l][b];
-        o.nchunk = (c->mlp.dims[l] + 63) / 64;
-        o.sbuf = l & 1;
-        o.first_nb = b == 0;
-        o.aimg = c->stash.as<uint8_t>() + (size_t)o.sbuf * tc::kStashChunks * tc::kASlotBytes;
-        o.cta_stride = tc::kStashCta;
-        o.img_off = -1;
-      }
+      for (int chain = 0; chain < (ffj_tc ? 2 : 1); ++chain)
+        for (int b = 0; b * 256 < out; ++b) {
+          if (n >= tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+          tc::GemmOp& o = ta.ops.op[n++];
+          o.kind = 3;
+          o.wimg = c->wimg.as<uint8_t>() + c->wb_off[l][b];
+          o.npad = c->wb_npad[l][b];
+          o.nchunk = (c->mlp.dims[l] + 63) / 64;
+          o.sbuf = 2 * chain + (l & 1);
+          o.first_nb = b == 0;
+          o.aimg = c->stash.as<uint8_t>() + (size_t)o.sbuf * tc::kStashChunks * tc::kASlotBytes;
+          o.cta_stride = tc::kStashCta;
+          o.img_off = -1;
+        }
       ta.bias[l] = c->mlp.bias[l];
     }
     ta.ops.nops = n;
+    if (ffj_tc) {
+      int hv = 0;
+      for (int l = 1; l < c->mlp.nlayers; ++l) hv += tc::kCW * ((c->mlp.dims[l] + 63) / 64);
+      wa.hvals = hv + 4;
+      if ((r = c->thscr.ensure((size_t)grid * tc::kEpiThreads * wa.hvals * 4)) ||
+          (r = c->ttrs.ensure((size_t)grid * 512 * 4)))
+        return r;
+      wa.hscr = c->thscr.as<float>();
+      wa.trs = c->ttrs.as<float>();
+    }
     ta.comp[0] = c->comp.as<float>();
     ta.comp[1] = c->comp.as<float>() + SBv;
     ta.dense = a.dense;
@@ -1091,13 +1109,22 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
     t.doff[l] = (long long)off;
     off += img_bytes(out, !t.a_isA[l]);
   }
-  t.img_cta = off;
+  // FFJORD: a second operand pair per layer (adot_l, pdotbar_l), laid out
+  // after the first pair's images, one pair's bytes further
+  const bool ffj = c->ff_on != 0;
+  const size_t img0 = off;
+  t.img_cta = ffj ? 2 * off : off;
   int hv = 0;
   for (int l = 1; l < L; ++l) {
     t.hoff[l] = hv;
     hv += tc::kCW * ((m.dims[l] + 63) / 64);
   }
   t.hx = hv;
+  if (ffj)
+    for (int l = 0; l + 1 < L; ++l) {  // the tangent pre-activations pdot_l
+      t.hoff2[l] = hv;
+      hv += tc::kCW * ((m.dims[l + 1] + 63) / 64);
+    }
   t.hvals = hv + 4;
   int nb = 0;
   for (int l = 0; l < L; ++l) {
@@ -1143,50 +1170,56 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
     *o = tc::GemmOp{};
     return o;
   };
-  for (int l = 0; l < L - 1; ++l) {
+  // chain ops: chain 0 the primal operands (a_l, pbar_l: images aoff / doff,
+  // stash buffers 0/1), chain 1 FFJORD's tangent operands (adot_l, pdotbar_l:
+  // images one pair further, stash buffers 2/3)
+  auto chain_op = [&](int kind, int l, int b, int chain, bool vjp) -> tc::GemmOp* {
+    tc::GemmOp* o = next_op(t.ops);
+    if (!o) return nullptr;
     const int in = m.dims[l], out = m.dims[l + 1];
-    for (int b = 0; b * 256 < out; ++b) {
-      tc::GemmOp* o = next_op(t.ops);
-      if (!o) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
-      o->kind = 3;
-      o->wimg = c->wimg.as<uint8_t>() + c->wb_off[l][b];
-      o->npad = c->wb_npad[l][b];
-      o->nchunk = (in + 63) / 64;
-      stash_op(*o, l & 1, b == 0);
-      o->img_off = b == 0 ? (int)t.aoff[l] : -1;
-      o->img_isA = (uint8_t)t.a_isA[l];
-      o->img_nblk = (uint8_t)((in + 63) / 64);
-      o->img_nh = (uint16_t)t.nh[l];
+    const int k = vjp ? out : in;  // K of the op: the operand's width
+    o->kind = kind;
+    if (kind == 3) {
+      o->wimg = c->wimg.as<uint8_t>() + (vjp ? c->wbT_off[l][b] : c->wb_off[l][b]);
+      o->npad = vjp ? c->wbT_npad[l][b] : c->wb_npad[l][b];  // the image's row padding
     }
+    o->nchunk = (k + 63) / 64;
+    stash_op(*o, 2 * chain + ((vjp ? l + 1 : l) & 1), b == 0);
+    o->img_off = b == 0 ? (int)((vjp ? t.doff[l] : t.aoff[l]) + (chain ? img0 : 0)) : -1;
+    o->img_isA = (uint8_t)(vjp ? !t.a_isA[l] : t.a_isA[l]);
+    o->img_nblk = (uint8_t)((k + 63) / 64);
+    o->img_nh = (uint16_t)t.nh[l];
+    return o;
+  };
+  const int nchains = ffj ? 2 : 1;
+  // evaluation list: forward recompute of layers 0..L-2 (per chain; operand
+  // images from the first N-block op), copy-only ops for a_{L-1} (and
+  // adot_{L-1}), then the VJP layers L-1..0 over their inputs (layer 0 only
+  // over the state inputs; FFJORD: the abar / achk ops of an N-block in a
+  // row, then a copy-only op for pdotbar_0's image)
+  for (int l = 0; l < L - 1; ++l)
+    for (int ch = 0; ch < nchains; ++ch)
+      for (int b = 0; b * 256 < m.dims[l + 1]; ++b)
+        if (!chain_op(3, l, b, ch, false)) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+  for (int ch = 0; ch < nchains; ++ch)
+    if (!chain_op(4, L - 1, 0, ch, false)) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+  for (int l = L - 1; l >= 0; --l) {
+    const int nout = l == 0 ? S : m.dims[l];  // inputs whose cotangent is needed
+    for (int b = 0; b * 256 < nout; ++b)
+      for (int ch = 0; ch < (l == 0 ? 1 : nchains); ++ch)
+        if (!chain_op(3, l, b, ch, true)) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
   }
-  {
-    const int l = L - 1;
+  if (ffj) {
+    // pdotbar_0 feeds no product, only layer 0's second weight-gradient pair
     tc::GemmOp* o = next_op(t.ops);
     if (!o) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
     o->kind = 4;
-    o->nchunk = (m.dims[l] + 63) / 64;
-    stash_op(*o, l & 1, 1);
-    o->img_off = (int)t.aoff[l];
-    o->img_isA = (uint8_t)t.a_isA[l];
-    o->img_nblk = (uint8_t)((m.dims[l] + 63) / 64);
-    o->img_nh = (uint16_t)t.nh[l];
-  }
-  for (int l = L - 1; l >= 0; --l) {
-    const int in = m.dims[l], out = m.dims[l + 1];
-    const int nout = l == 0 ? S : in;  // inputs whose cotangent is needed
-    for (int b = 0; b * 256 < nout; ++b) {
-      tc::GemmOp* o = next_op(t.ops);
-      if (!o) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
-      o->kind = 3;
-      o->wimg = c->wimg.as<uint8_t>() + c->wbT_off[l][b];
-      o->npad = c->wbT_npad[l][b];  // the image's row padding (its pieces are npad rows apart)
-      o->nchunk = (out + 63) / 64;
-      stash_op(*o, (l + 1) & 1, b == 0);
-      o->img_off = b == 0 ? (int)t.doff[l] : -1;
-      o->img_isA = (uint8_t)(!t.a_isA[l]);
-      o->img_nblk = (uint8_t)((out + 63) / 64);
-      o->img_nh = (uint16_t)t.nh[l];
-    }
+    o->nchunk = (m.dims[1] + 63) / 64;
+    stash_op(*o, 2 + 1, 1);
+    o->img_off = (int)(t.doff[0] + img0);
+    o->img_isA = (uint8_t)(!t.a_isA[0]);
+    o->img_nblk = (uint8_t)((m.dims[1] + 63) / 64);
+    o->img_nh = (uint16_t)t.nh[0];
   }
   t.ops.nops = n;
   t.ops7 = t.ops;
@@ -1216,7 +1249,10 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
         o->b_off0 = (uint32_t)(4 * nbk * 8192);
         o->b_pstride = (uint32_t)(nblk * 8192);
         o->npad = (std::min(256, nside - 256 * nbk) + 15) / 16 * 16;
-        o->nchunk = 2 * 6 * tpc;
+        o->nchunk = 2 * 6 * tpc * nchains;
+        o->npairs = nchains;
+        o->pair_aoff = (uint32_t)img0;
+        o->pair_boff = (uint32_t)img0;
         o->first_dw = 0;
         o->img_off = -1;
         t.dw_chunks += o->nchunk;
@@ -1226,6 +1262,10 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
   t.dwops.nops = n;
   w.stash = stash;
   w.nsc = c->nsc;
+  if (ffj) {
+    if ((r = c->ttrs.ensure((size_t)grid * 512 * 4))) return r;
+    w.trs = c->ttrs.as<float>();
+  }
   CK(cudaEventRecord(c->ev[2], st));
   if (launch_bwd_tcw(w, grid, st)) {
     cudaError_t e = cudaGetLastError();
@@ -1258,8 +1298,9 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   // engine, after a tensor-core forward) replaying each interval from its checkpoint
   const bool tc_replay = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && !gauss &&
                          !c->dense_valid && c->dense_tl && !c->fwd_wide && !c->ff_on;
+  const bool ffj_tc = c->ff_on && c->fwd_wide && c->dense_tl && c->ffj_tc_ok && !c->ff_exact;
   const bool tcbwd = (c->precision == GBNDE_PREC_BF16 && (c->fwd_wide ? c->tc_wide_bwd : c->tc_bwd_ok) &&
-                      !backsolve && !gauss && c->dense_valid && !c->ff_on) ||
+                      !backsolve && !gauss && c->dense_valid && (!c->ff_on || ffj_tc)) ||
                      tc_replay;
   // the FP32 adjoint reads dense slots only in its own layout; after a
   // tensor-core forward it recomputes each interval from the checkpoints

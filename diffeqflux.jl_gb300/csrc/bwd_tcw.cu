@@ -23,6 +23,21 @@
 //  * state vectors are kept in 64-component chunks (virtual tiles
 //    T * nsc + c), and every evaluation runs in full (no reuse of the
 //    previous evaluation's activations).
+//
+// FFJORD mode (b.ffj; state [z; delta_logp], d + 1 <= 64): the right-hand
+// side is g = [f(z [, t]); -e . (J e)] (src/ffjord.jl:81-136), and the VJP
+// with cotangent [lam_z; lam_D] runs reverse mode over the forward's primal
+// chain a_{l+1} = act(p_l), p_l = W_l a_l + b_l, and tangent chain
+// adot_{l+1} = act'(p_l) pdot_l, pdot_l = W_l adot_l (adot_0 = e):
+//   abar_L = lam_z, achk_L = -lam_D e;   per layer, from the top:
+//   pdotbar_l = achk_{l+1} act'(p_l),
+//   pbar_l = abar_{l+1} act'(p_l) + achk_{l+1} act''(p_l) pdot_l,
+//   abar_l = W_l^T pbar_l,  achk_l = W_l^T pdotbar_l,
+//   dW_l += pbar_l a_l^T + pdotbar_l adot_l^T,  db_l += pbar_l,
+// with kl_z = abar_0 on the z inputs and kl_D = 0. The primal and tangent
+// chains use stash buffers 0/1 and 2/3; the two VJP ops of an N-block
+// (abar and achk) are drained together (both accumulator regions); the
+// weight-gradient ops stack both operand pairs along K.
 #include "tc_args.h"
 
 namespace gbnde {
@@ -162,6 +177,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
     const size_t SB = (size_t)S * a.B;
     const double Nn = (double)SB;
     const bool timein = m.timein != 0;
+    const bool ffj = a.ffj != 0;
+    const int netS = ffj ? a.ffd : S;  // state inputs of the network (z without delta_logp)
+    float* trs = ffj ? W.trs + (size_t)blockIdx.x * 512 : nullptr;
     ThrW th;
     th.lane = threadIdx.x & 31;
     th.q = warp & 3;
@@ -327,6 +345,165 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
       return true;
     };
 
+    // ---- FFJORD adjoint right-hand side of one tile (same contract as adj_eval) -----------
+    // scratch per thread: a_l (l = 1..L-1) at hoff[l], pdot_l (l = 0..L-2) at hoff2[l]
+    auto adj_eval_ffj = [&](int tile, int slot, float* P, float cw, auto&& in_x, auto&& in_lam,
+                            auto&& out_kl) -> bool {
+      const int d = a.ffd;
+      const uint32_t tj = (uint32_t)((tile - (int)blockIdx.x) / G);
+      if (threadIdx.x == 0 &&
+          !tc::epi_post(cmdp, sh, tc::CMD_EVAL | ((uint32_t)(slot + 1) << 8) | (tj << 24)))
+        return false;
+      const float* erow = (rowok(tile) && a.noise != nullptr) ? a.noise + ((size_t)tile * 128 + th.r) * d : nullptr;
+      // forward recompute of both chains: a_0 = (z [, t]) into buffer 0, adot_0 = e into buffer 2
+      {
+        float x[tc::kCW];
+        in_x(0, x);
+        tc::stash_write(stash, sh, 0, 0, th.r, th.ch, x);
+#pragma unroll
+        for (int i = 0; i < tc::kCW; ++i) {
+          const int col = tc::kCW * th.ch + i;
+          x[i] = (erow != nullptr && col < d) ? erow[col] : 0.f;
+        }
+        tc::stash_write(stash, sh, 2, 0, th.r, th.ch, x);
+      }
+      for (int l = 0; l < L - 1; ++l) {
+        const int N = m.dims[l + 1];
+        const int ob = (l + 1) & 1;
+        for (int b = 0; b * 256 < N; ++b) {  // primal
+          uint32_t col;
+          if (!tc::epi_wait_acc(es, sh, &col)) return false;
+          const int nch = (min(256, N - 256 * b) + 63) / 64;
+          for (int cc = 0; cc < nch; ++cc) {
+            const int n0 = 256 * b + 64 * cc + tc::kCW * th.ch;
+            float v[tc::kCW], bc[tc::kCW];
+            tc::load_bias_cw(A.bias[l], n0, N, bc);
+            tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
+            tc::bias_act_cw(v, bc, m.act[l], n0, N);
+            hs_stv(hs4, (A.hoff[l + 1] + tc::kCW * (4 * b + cc)) / 4, v);
+            tc::stash_write(stash, sh, ob, 4 * b + cc, th.r, th.ch, v);
+          }
+          tc::epi_release_acc(es, sh);
+        }
+        for (int b = 0; b * 256 < N; ++b) {  // tangent: pdot_l kept, adot_{l+1} = act' pdot_l
+          uint32_t col;
+          if (!tc::epi_wait_acc(es, sh, &col)) return false;
+          const int nch = (min(256, N - 256 * b) + 63) / 64;
+          for (int cc = 0; cc < nch; ++cc) {
+            const int n0 = 256 * b + 64 * cc + tc::kCW * th.ch;
+            float v[tc::kCW], y[tc::kCW];
+            tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
+            hs_stv(hs4, (A.hoff2[l] + tc::kCW * (4 * b + cc)) / 4, v);
+            hs_ldv(hs4, (A.hoff[l + 1] + tc::kCW * (4 * b + cc)) / 4, y);
+            tc::deriv_mul_cw(v, y, m.act[l], n0, N);
+            tc::stash_write(stash, sh, 2 + ob, 4 * b + cc, th.r, th.ch, v);
+          }
+          tc::epi_release_acc(es, sh);
+        }
+      }
+      // a_{L-1} and adot_{L-1} reach their images through copy-only ops.
+      // Output cotangents (identity output layer): pbar_{L-1} = cw lam_z into
+      // buffer L % 2 (with its bias column sums), pdotbar_{L-1} = -cw lam_D e
+      // into buffer 2 + L % 2; lam_D (row d of the state) comes from the thread
+      // owning that column, through the CTA's scratch.
+      const float cs = P ? cw : 1.f;
+      {
+        float y[tc::kCW];
+        in_lam(0, y);
+#pragma unroll
+        for (int i = 0; i < tc::kCW; ++i)
+          if (tc::kCW * th.ch + i == d) trs[th.r] = y[i];
+        tc::epi_bar();
+        const float lamD = trs[th.r];
+        tc::epi_bar();
+        float v[tc::kCW];
+#pragma unroll
+        for (int i = 0; i < tc::kCW; ++i) {
+          const int col = tc::kCW * th.ch + i;
+          v[i] = col < d ? cs * y[i] : 0.f;
+          y[i] = (erow != nullptr && col < d) ? -cs * lamD * erow[col] : 0.f;
+        }
+        tc::stash_write(stash, sh, L & 1, 0, th.r, th.ch, v);
+        tc::stash_write(stash, sh, 2 + (L & 1), 0, th.r, th.ch, y);
+        if (P) {
+          const float sm = warp_colsum(v, th.lane);
+          if (th.lane < tc::kCW && tc::kCW * th.ch + th.lane < d)
+            tc::red_add(P + th.q * A.nbias + A.boffp[L - 1] + tc::kCW * th.ch + th.lane, sm);
+        }
+      }
+      // VJP pairs per N-block over the inputs of layer l (l >= 1): abar_l and
+      // achk_l drained together into pbar_{l-1} (buffer l % 2, bias sums) and
+      // pdotbar_{l-1} (buffer 2 + l % 2)
+      for (int l = L - 1; l >= 1; --l) {
+        const int N = m.dims[l];
+        const int act = m.act[l - 1];
+        for (int b = 0; b * 256 < N; ++b) {
+          const int r0 = (int)(es.g & 1), r1 = r0 ^ 1;
+          if (!tc::mbar_wait(&sh.acc_full[r0], es.use[r0] & 1, &sh.err)) return false;
+          if (!tc::mbar_wait(&sh.acc_full[r1], es.use[r1] & 1, &sh.err)) return false;
+          tc::tc_fence_after();
+          const uint32_t c0 = (uint32_t)(r0 * 256), c1 = (uint32_t)(r1 * 256);
+          const int nch = (min(256, N - 256 * b) + 63) / 64;
+          for (int cc = 0; cc < nch; ++cc) {
+            const int n0 = 256 * b + 64 * cc + tc::kCW * th.ch;
+            const uint32_t co = (uint32_t)(64 * cc + tc::kCW * th.ch);
+            float ab[tc::kCW], ak[tc::kCW];
+            tc::tmem_ld_cw(sh.tmem_base + lane_base + c0 + co, ab);
+            tc::tmem_ld_cw(sh.tmem_base + lane_base + c1 + co, ak);
+            const int ka = (A.hoff[l] + tc::kCW * (4 * b + cc)) / 4;
+            const int kp = (A.hoff2[l - 1] + tc::kCW * (4 * b + cc)) / 4;
+#pragma unroll
+            for (int j = 0; j < tc::kCW / 4; ++j) {
+              const float4 a4 = hs4[(size_t)(ka + j) * tc::kEpiThreads + threadIdx.x];
+              const float4 p4 = hs4[(size_t)(kp + j) * tc::kEpiThreads + threadIdx.x];
+              const float av[4] = {a4.x, a4.y, a4.z, a4.w}, pv[4] = {p4.x, p4.y, p4.z, p4.w};
+#pragma unroll
+              for (int q = 0; q < 4; ++q) {
+                const int i = 4 * j + q;
+                float s1 = 1.f, s2 = 0.f;
+                if (act == GBNDE_ACT_TANH) {
+                  s1 = fmaf(-av[q], av[q], 1.f);
+                  s2 = -2.f * av[q] * s1;
+                } else if (act == GBNDE_ACT_SOFTPLUS) {
+                  s1 = -expm1f(-av[q]);
+                  s2 = s1 * (1.f - s1);
+                }
+                const bool inside = n0 + i < N;
+                const float pb = fmaf(ak[i] * s2, pv[q], ab[i] * s1);
+                ab[i] = inside ? pb : 0.f;           // pbar_{l-1}
+                ak[i] = inside ? ak[i] * s1 : 0.f;   // pdotbar_{l-1}
+              }
+            }
+            tc::stash_write(stash, sh, 2 + (l & 1), 4 * b + cc, th.r, th.ch, ak);
+            tc::stash_write(stash, sh, l & 1, 4 * b + cc, th.r, th.ch, ab);
+            if (P) {
+              const float sm = warp_colsum(ab, th.lane);
+              if (th.lane < tc::kCW) tc::red_add(P + th.q * A.nbias + A.boffp[l - 1] + n0 + th.lane, sm);
+            }
+          }
+          tc::epi_release_acc(es, sh);
+          tc::epi_release_acc(es, sh);
+        }
+      }
+      // kl_z = abar_0 on the z inputs; kl_D = 0
+      const float inv = 1.f / cs;
+      for (int b = 0; b * 256 < d; ++b) {
+        uint32_t col;
+        if (!tc::epi_wait_acc(es, sh, &col)) return false;
+        float v[tc::kCW];
+        tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(tc::kCW * th.ch), v);
+#pragma unroll
+        for (int i = 0; i < tc::kCW; ++i) v[i] = (tc::kCW * th.ch + i < d) ? v[i] * inv : 0.f;
+        out_kl(0, v);
+        tc::epi_release_acc(es, sh);
+      }
+      return true;
+    };
+    auto adj = [&](int tile, int slot, float* P, float cw, auto&& in_x, auto&& in_lam, auto&& out_kl) -> bool {
+      if (ffj) return adj_eval_ffj(tile, slot, P, cw, in_x, in_lam, out_kl);
+      return adj_eval(tile, slot, P, cw, in_x, in_lam, out_kl);
+    };
+
     // ---- weight gradients of an accepted step ------------------------------------------
     auto kahan = [&](float& acc, float& cmp, float x) {
       const float y = x - cmp;
@@ -434,10 +611,13 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
 #pragma unroll
         for (int q = 0; q < tc::kCW; ++q) x[q] = 0.f;
       }
-      if (timein)
+      if (timein || netS != S)
 #pragma unroll
-        for (int q = 0; q < tc::kCW; ++q)
-          if (64 * c + tc::kCW * th.ch + q == S) x[q] = (float)tq;
+        for (int q = 0; q < tc::kCW; ++q) {
+          const int col = 64 * c + tc::kCW * th.ch + q;
+          if (col == netS) x[q] = timein ? (float)tq : 0.f;
+          else if (col > netS && col < S) x[q] = 0.f;
+        }
     };
 
     for (int ivi = 0; ivi < a.niv && ok && ret == GBNDE_RET_SUCCESS; ++ivi) {
@@ -453,7 +633,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
         dense_setup(iv, t, &n, hb);
         for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
           const bool v = rowok(tile);
-          ok = adj_eval(
+          ok = adj(
               tile, fs, Pb[iP1], (float)c_tab.b[0],
               [&](int c, float* x) {
                 dense_x(tile, c, n, hb, t, x);
@@ -512,7 +692,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
         double p2 = 0.0;
         for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
           const bool v = rowok(tile);
-          ok = adj_eval(
+          ok = adj(
               tile, -1, nullptr, 0.f,
               [&](int c, float* x) {
                 dense_x(tile, c, n, hb, tp, x);
@@ -588,7 +768,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
           const double ti = t - c_tab.c[i] * H;
           for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
             const bool v = rowok(tile);
-            ok = adj_eval(
+            ok = adj(
                 tile, slot, P, cw,
                 [&](int c, float* x) {
                   float hb[7];

@@ -40,6 +40,21 @@ __device__ __forceinline__ void stv_api(float* p, int n, const float* x) {
     if (i < n) p[i] = x[i];
 }
 
+// Thread-private FP32 activation scratch, slot-major (float4 slot k of thread
+// t at hs4[k * kEpiThreads + t]): contiguous per warp.
+__device__ __forceinline__ void hs_ldv(const float4* hs4, int k0, float* x) {
+#pragma unroll
+  for (int j = 0; j < tc::kCW / 4; ++j) {
+    const float4 q = hs4[(size_t)(k0 + j) * tc::kEpiThreads + threadIdx.x];
+    x[4 * j] = q.x; x[4 * j + 1] = q.y; x[4 * j + 2] = q.z; x[4 * j + 3] = q.w;
+  }
+}
+__device__ __forceinline__ void hs_stv(float4* hs4, int k0, const float* x) {
+#pragma unroll
+  for (int j = 0; j < tc::kCW / 4; ++j)
+    hs4[(size_t)(k0 + j) * tc::kEpiThreads + threadIdx.x] = make_float4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
+}
+
 __device__ __forceinline__ bool epi_grid_barrier(const FwdArgs& a, unsigned int& gen, int* okflag) {
   tc::epi_bar();
   gen += 1;
@@ -131,6 +146,107 @@ __device__ __forceinline__ bool epi_rhs_w(const FwdTcwArgs& A, tc::EpiState& e, 
   return true;
 }
 
+// FFJORD right-hand side of one tile (state [z; delta_logp], d = ffd rows of
+// z, d + 1 <= 64): [f(z [, t]); -e . (J e)] with the Hutchinson direction e of
+// the trajectory (src/ffjord.jl:81-115, e fixed per solve). The primal chain
+// a_{l+1} = act(W_l a_l + b_l) and the tangent chain
+// adot_{l+1} = act'(.) (W_l adot_l) (the forward-mode derivative along e) run
+// interleaved per layer on the same weights: P_l from stash buffer l % 2, T_l
+// from buffer 2 + l % 2. The primal activations go to the thread's scratch
+// for the tangent drain's act'. in(c, x) fills the network input chunk c;
+// out(0, k) receives the state chunk of the derivative (f and, at row d,
+// minus the trace estimate, reduced over the row's four column groups through
+// the CTA's slice of trs).
+template <class In, class Out>
+__device__ __forceinline__ bool epi_rhs_ffj(const FwdTcwArgs& A, tc::EpiState& e, tc::Shared& sh, uint8_t* stash,
+                                            const ThrW& th, float4* hs4, const float* erow, float* trs, In&& in,
+                                            Out&& out) {
+  const MlpDev& m = A.t.f.mlp;
+  const int L = m.nlayers, d = A.t.f.ffd;
+  const uint32_t lane_base = ((uint32_t)((threadIdx.x >> 5) & 3) * 32) << 16;
+  const int kc0 = (m.dims[0] + 63) / 64;
+  for (int c = 0; c < kc0; ++c) {
+    float x[tc::kCW];
+    in(c, x);
+    tc::stash_write(stash, sh, 0, c, th.r, th.ch, x);
+#pragma unroll
+    for (int i = 0; i < tc::kCW; ++i) {
+      const int col = 64 * c + tc::kCW * th.ch + i;
+      x[i] = (erow != nullptr && col < d) ? erow[col] : 0.f;
+    }
+    tc::stash_write(stash, sh, 2, c, th.r, th.ch, x);
+  }
+  int hoff = 0;
+  for (int l = 0; l < L - 1; ++l) {
+    const int N = m.dims[l + 1];
+    const int ob = (l + 1) & 1;
+    for (int b = 0; b * 256 < N; ++b) {  // primal P_l
+      uint32_t col;
+      if (!tc::epi_wait_acc(e, sh, &col)) return false;
+      const int nch = (min(256, N - 256 * b) + 63) / 64;
+      for (int cc = 0; cc < nch; ++cc) {
+        const int n0 = 256 * b + 64 * cc + tc::kCW * th.ch;
+        float v[tc::kCW], bc[tc::kCW];
+        tc::load_bias_cw(A.t.bias[l], n0, N, bc);
+        tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
+        tc::bias_act_cw(v, bc, m.act[l], n0, N);
+        hs_stv(hs4, (hoff + tc::kCW * (4 * b + cc)) / 4, v);
+        tc::stash_write(stash, sh, ob, 4 * b + cc, th.r, th.ch, v);
+      }
+      tc::epi_release_acc(e, sh);
+    }
+    for (int b = 0; b * 256 < N; ++b) {  // tangent T_l
+      uint32_t col;
+      if (!tc::epi_wait_acc(e, sh, &col)) return false;
+      const int nch = (min(256, N - 256 * b) + 63) / 64;
+      for (int cc = 0; cc < nch; ++cc) {
+        const int n0 = 256 * b + 64 * cc + tc::kCW * th.ch;
+        float v[tc::kCW], y[tc::kCW];
+        hs_ldv(hs4, (hoff + tc::kCW * (4 * b + cc)) / 4, y);
+        tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
+        tc::deriv_mul_cw(v, y, m.act[l], n0, N);
+        tc::stash_write(stash, sh, 2 + ob, 4 * b + cc, th.r, th.ch, v);
+      }
+      tc::epi_release_acc(e, sh);
+    }
+    hoff += tc::kCW * ((N + 63) / 64);
+  }
+  // output layer (d outputs, one chunk): f from P, J e from T
+  const int n0 = tc::kCW * th.ch;
+  float f[tc::kCW];
+  {
+    uint32_t col;
+    if (!tc::epi_wait_acc(e, sh, &col)) return false;
+    float bc[tc::kCW];
+    tc::load_bias_cw(A.t.bias[L - 1], n0, d, bc);
+    tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, f);
+    tc::bias_act_cw(f, bc, m.act[L - 1], n0, d);
+    tc::epi_release_acc(e, sh);
+  }
+  float part = 0.f;
+  {
+    uint32_t col;
+    if (!tc::epi_wait_acc(e, sh, &col)) return false;
+    float v[tc::kCW];
+    tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
+    tc::deriv_mul_cw(v, f, m.act[L - 1], n0, d);
+#pragma unroll
+    for (int i = 0; i < tc::kCW; ++i)
+      if (erow != nullptr && n0 + i < d) part = fmaf(erow[n0 + i], v[i], part);
+    tc::epi_release_acc(e, sh);
+  }
+  // the row's trace: its four column groups' parts, in a fixed order
+  trs[th.ch * 128 + th.r] = part;
+  tc::epi_bar();
+  const float tr = ((trs[th.r] + trs[128 + th.r]) + trs[256 + th.r]) + trs[384 + th.r];
+  tc::epi_bar();
+#pragma unroll
+  for (int i = 0; i < tc::kCW; ++i)
+    if (n0 + i == d) f[i] = -tr;
+  out(0, f);
+  return true;
+}
+
 __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -159,10 +275,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
     const double N = (double)SB;
     const double tdir = a.t1 >= a.t0 ? 1.0 : -1.0;
     const bool timein = a.mlp.timein != 0;
+    // state inputs of the network: the whole state, or z without FFJORD's
+    // delta_logp row (the time row, if any, takes column netS)
+    const int netS = a.ffj ? a.ffd : S;
     ThrW th;
     th.r = 32 * (warp & 3) + (threadIdx.x & 31);
     th.ch = warp >> 2;
     uint8_t* stash = A.stash + (size_t)blockIdx.x * tc::kStashCta;
+    float4* hs4 = a.ffj ? reinterpret_cast<float4*>(A.hscr + (size_t)blockIdx.x * tc::kEpiThreads * A.hvals) : nullptr;
+    float* trs = a.ffj ? A.trs + (size_t)blockIdx.x * 512 : nullptr;
     tc::EpiState es;
     tc::epi_state_init(es);
     unsigned int gen = 0;
@@ -187,21 +308,33 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
     // (S % 64 != 0) is filled by the callers
     auto tcol = [&](int c, double tt, float* x) {
 #pragma unroll
-      for (int i = 0; i < tc::kCW; ++i) x[i] = (timein && 64 * c + tc::kCW * th.ch + i == S) ? (float)tt : 0.f;
+      for (int i = 0; i < tc::kCW; ++i) x[i] = (timein && 64 * c + tc::kCW * th.ch + i == netS) ? (float)tt : 0.f;
     };
     auto with_t = [&](int c, double tt, float* x) {
-      if (!timein) return;
+      if (!timein && netS == S) return;
 #pragma unroll
-      for (int i = 0; i < tc::kCW; ++i)
-        if (64 * c + tc::kCW * th.ch + i == S) x[i] = (float)tt;
+      for (int i = 0; i < tc::kCW; ++i) {
+        const int col = 64 * c + tc::kCW * th.ch + i;
+        if (col == netS) x[i] = timein ? (float)tt : 0.f;
+        else if (col > netS && col < S) x[i] = 0.f;
+      }
+    };
+    // one right-hand side of a tile: the MLP, or FFJORD's augmented one
+    auto rhs = [&](int tile, auto&& in, auto&& out) -> bool {
+      if (a.ffj) {
+        const float* erow =
+            (rowok(tile) && a.noise != nullptr) ? a.noise + ((size_t)tile * 128 + th.r) * a.ffd : nullptr;
+        return epi_rhs_ffj(A, es, sh, stash, th, hs4, erow, trs, in, out);
+      }
+      return epi_rhs_w(A, es, sh, stash, th, in, out);
     };
     bool ok = true;
 
     // ---- k1 = f(u0); state, compensation and slot 0 ---------------------------
     for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
       const bool v = rowok(tile);
-      ok = epi_rhs_w(
-          A, es, sh, stash, th,
+      ok = rhs(
+          tile,
           [&](int c, float* x) {
             if (c >= nsc) { tcol(c, a.t0, x); return; }
             const int nm = nmine_of(S, c, th.ch);
@@ -277,8 +410,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
       double p2 = 0.0;
       for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
         const bool v = rowok(tile);
-        ok = epi_rhs_w(
-            A, es, sh, stash, th,
+        ok = rhs(
+            tile,
             [&](int c, float* x) {
               if (c >= nsc) { tcol(c, a.t0 + tdir * dt0, x); return; }
               float u[tc::kCW], f0[tc::kCW];
@@ -340,8 +473,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
           const double ti = t + c_tab.c[i] * h;
           for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
             const bool v = rowok(tile);
-            ok = epi_rhs_w(
-                A, es, sh, stash, th,
+            ok = rhs(
+                tile,
                 [&](int c, float* Y) {
                   if (c >= nsc) { tcol(c, ti, Y); return; }
                   const size_t g = tofs(tile, c);

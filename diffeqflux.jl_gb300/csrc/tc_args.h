@@ -32,6 +32,7 @@ struct BwdTcArgs {
   int hvals;                    // values per thread in hscr
   int hoff[GBNDE_MAX_LAYERS];   // offset of hidden layer l (1..L-1) inside a thread's hscr
   int hx;                       // offset of the 32 state values kept for the cube prefix
+  int hoff2[GBNDE_MAX_LAYERS];  // FFJORD (stash mode): offset of the tangent pre-activations pdot_l
   uint8_t* img;                 // [grid][tpc][kImgSlots][img_cta] weight-gradient operand images
   size_t img_cta;               // bytes of one stage's images
   int tpc;                      // 128-trajectory tiles per CTA (image sets per CTA)
@@ -57,8 +58,13 @@ int launch_bwd_tc(const BwdTcArgs& a, int grid, cudaStream_t st);
 // widths up to 1024, optional time row. The ops are N-block ops of kind 3.
 struct FwdTcwArgs {
   FwdTcArgs t;
-  uint8_t* stash;  // [grid][2][kStashChunks][kASlotBytes]
+  uint8_t* stash;  // [grid][kStashBufs][kStashChunks][kASlotBytes]
   int nsc;         // 64-component chunks of the state
+  // FFJORD mode (t.f.ffj): the tangent chain's activation scratch (hvals
+  // floats per epilogue thread, slot-major) and the trace partials [grid][512]
+  float* hscr;
+  int hvals;
+  float* trs;
 };
 int launch_fwd_tcw(const FwdTcwArgs& a, int grid, cudaStream_t st);
 
@@ -68,6 +74,7 @@ struct BwdTcwArgs {
   BwdTcArgs t;
   uint8_t* stash;
   int nsc;
+  float* trs;  // FFJORD mode: per-CTA scratch of 512 floats (row broadcasts)
 };
 int launch_bwd_tcw(const BwdTcwArgs& a, int grid, cudaStream_t st);
 

@@ -68,17 +68,19 @@ constexpr int kCmdRing = 4;
 constexpr int kImgSlots = 7;    // weight-gradient image slots per CTA: stages 1..6 + the next stage 1
 // Split pieces kept in the weight-gradient images, and the products of a
 // weight-gradient op: 1 (hi, one BF16 product) or 2 (hi and mid; hi.hi +
-// hi.lo + lo.hi). Measured at B = 16384, 64-256-256-64: one piece makes the
-// adjoint 10 % faster with the same step counts, at 1.2e-4 relative gradient
-// difference from the FP32 form (2 pieces: 6e-6); the chain GEMMs keep five
-// products (three make the forward take 23 steps instead of 12).
-constexpr int kImgPieces = 1;
+// hi.lo + lo.hi). One piece makes the adjoint 10 % faster at B = 16384,
+// 64-256-256-64, but its parameter gradients differ from the FP64 oracle by
+// 1.1e-3 to 3e-3 (relative norm) on batches of 130 to 1000 trajectories,
+// above the 1e-3 bar; two pieces stay below it on every shape. The chain
+// GEMMs keep five products (three make the forward take 23 steps instead of 12).
+constexpr int kImgPieces = 2;
 // Stash mode (layers wider than one 256-column accumulator): every chain A
 // operand goes through a per-CTA global "stash" of two buffers of up to
 // kStashChunks K-chunks (ring-slot layout: 3 pieces x 128 rows x 128 B each),
 // written by the epilogue with plain stores and bulk-loaded by the producer.
 constexpr int kStashChunks = 16;                                   // K <= 1024
-constexpr size_t kStashCta = (size_t)2 * kStashChunks * kASlotBytes;  // bytes per CTA
+constexpr int kStashBufs = 4;  // two per chain: the primal chain and (FFJORD) the tangent chain
+constexpr size_t kStashCta = (size_t)kStashBufs * kStashChunks * kASlotBytes;  // bytes per CTA
 
 // kind 0 (chain GEMM): A chunks written by the epilogue (3 pieces, K-major),
 //   B = weight image chunks (2 pieces, K-major), five split products.
@@ -123,6 +125,11 @@ struct GemmOp {
   // blocks each, starting b_off0 bytes into each piece, pieces b_pstride
   // bytes apart (b_pstride == 0: one contiguous copy)
   uint32_t b_off0, b_pstride;
+  // kind 1: operand pairs stacked along K per stage (FFJORD: (pbar, a) and
+  // (pdotbar, adot)); pair q's images sit q * pair_aoff / q * pair_boff
+  // bytes after pair 0's in the stage slot (npairs 0 or 1: one pair)
+  int npairs;
+  uint32_t pair_aoff, pair_boff;
 };
 
 struct OpList {
@@ -137,7 +144,7 @@ struct Shared {
   uint64_t img_ready;
   uint64_t img_done;  // command mode: the MMA warp's image copies of the step have landed
   uint64_t cmd_full[kCmdRing], cmd_empty[kCmdRing];
-  uint64_t stash_full[2][kStashChunks];  // stash mode: chunk written by all epilogue threads
+  uint64_t stash_full[kStashBufs][kStashChunks];  // stash mode: chunk written by all epilogue threads
   uint32_t cmd[kCmdRing];
   uint32_t tmem_base;
   int stop;
@@ -190,7 +197,7 @@ __device__ __forceinline__ void init_shared(Shared& sh) {
       mbar_init(&sh.cmd_full[i], 1);
       mbar_init(&sh.cmd_empty[i], 2);
     }
-    for (int b = 0; b < 2; ++b)
+    for (int b = 0; b < kStashBufs; ++b)
       for (int i = 0; i < kStashChunks; ++i) mbar_init(&sh.stash_full[b][i], kEpiThreads);
     sh.stop = 0;
     sh.err = 0;
@@ -459,8 +466,8 @@ struct TmaState {
   // stash mode: per buffer, bit c = phase parity of chunk c's next fill, and
   // the parities of the fill being read (chunks are refilled unevenly: a
   // buffer holds inputs of different widths in turn)
-  uint32_t ph[2] = {0, 0};
-  uint32_t cur[2] = {0, 0};
+  uint32_t ph[kStashBufs] = {0, 0, 0, 0};
+  uint32_t cur[kStashBufs] = {0, 0, 0, 0};
 };
 
 __device__ __forceinline__ bool tma_wait_or_stop(Shared& sh, uint64_t* bar, uint32_t par) {
@@ -473,8 +480,8 @@ __device__ __forceinline__ bool tma_wait_or_stop(Shared& sh, uint64_t* bar, uint
 }
 
 // One op's copies; `f` is the image slot of stage 1 for stage-stacked
-// weight-gradient ops (K chunk c: tile c / 12 of the CTA, stage (c % 12) / 2,
-// trajectory block c % 2).
+// weight-gradient ops (K chunk c: tile c / (12 np) of the CTA, operand pair
+// (c % (12 np)) / 12, stage (c % 12) / 2, trajectory block c % 2; np pairs).
 __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh, uint8_t* aring,
                                        uint8_t* wring, int f) {
   const bool leader = (threadIdx.x & 31) == 0;
@@ -537,12 +544,14 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
   for (int c = 0; c < op.nchunk; ++c) {
     size_t aoff = 0, boff = 0;
     if (op.kind == 1) {
-      // K chunk c: tile j of the CTA, stage s, 64-trajectory block kb
-      const int j = c / 12, cw = c - 12 * j;
+      // K chunk c: tile j of the CTA, operand pair q, stage s, 64-trajectory block kb
+      const int np = op.npairs > 1 ? op.npairs : 1;
+      const int j = c / (12 * np), rem = c - 12 * np * j;
+      const int q = rem / 12, cw = rem - 12 * q;
       const int s = cw >> 1, kb = cw & 1;
       const size_t slot = ((size_t)j * kImgSlots + stage_slot(s, f)) * op.slot_stride;
-      aoff = slot + (size_t)kb * op.a_step;
-      boff = slot + (size_t)kb * op.b_step;
+      aoff = slot + (size_t)kb * op.a_step + (size_t)q * op.pair_aoff;
+      boff = slot + (size_t)kb * op.b_step + (size_t)q * op.pair_boff;
       if (!tma_wait_or_stop(sh, &sh.a_empty[t.aslot], t.aph ^ 1)) return false;
       if (leader) {
         mbar_arrive_expect_tx(&sh.a_full[t.aslot], op.a_bytes);

@@ -159,3 +159,49 @@ def test_ffjord_user_basedist_value_and_gradient():
     gu, gp, _ = ots.adjoint_interpolating(rhs, fwd, [1.0], dy[..., None], 0.0, tol, tol)
     rel = np.linalg.norm(pt.grad.numpy() - gp) / np.linalg.norm(gp)
     assert rel < 1e-3, rel
+
+
+def _case_bf16(d, H, B, act, seed, tol=1e-6):
+    """FFJORD in the BF16 form: the stash engine's primal and tangent chains
+    in the forward (Hutchinson), reverse-over-forward on the tensor cores in
+    the adjoint. Against the FP64 oracle: logpx 1e-3 (relative to max|logpx|),
+    z(t1) 1e-3, gradients of the mean NLL 1e-3 (relative norm)."""
+    import gbnde
+    from gbnde import _lib
+    from oracle import ffjord as off
+    from oracle import mlp as omlp
+    from oracle import tsit5 as ots
+    rng = np.random.default_rng(seed)
+    model = gbnde.Chain(gbnde.Dense(d + 1, H, act), gbnde.Dense(H, H, act), gbnde.Dense(H, d))
+    p = model.init_params(rng)
+    x = rng.standard_normal((d, B)).astype(np.float32)
+    fj = gbnde.FFJORD(model, (0.0, 1.0), (d,), gbnde.Tsit5("bf16"), abstol=tol, reltol=tol, time_input=True)
+    noise = fj.draw_noise(rng, B)
+    logpx, zT, st = fj.forward_np(x, p, noise)
+    assert st.retcode == 0
+    assert st.fwd_path == _lib.PATH_TC
+    om = omlp.MLP(model.dims, model.acts, time_input=True)
+    rhs = off.FFJORDRHS(om, p.astype(np.float64), noise=noise.T.astype(np.float64), exact=False)
+    y0 = np.vstack([x.astype(np.float64), np.zeros((1, B))])
+    ys, fwd = ots.solve_forward(rhs, y0, 0.0, 1.0, [1.0], tol, tol)
+    ref = off.logpx_from_final(ys[..., 0], d)
+    assert np.abs(logpx - ref).max() < 1e-3 * np.abs(ref).max()
+    assert np.abs(zT - ys[:d, :, 0]).max() < 1e-3 * np.abs(ys[:d]).max()
+    g = -np.ones(B) / B
+    dx, dp, sta = fj.backward_np(g.astype(np.float32))
+    assert sta.retcode_adj == 0
+    assert sta.adj_path == _lib.PATH_TC
+    dy = np.vstack([-ys[:d, :, 0] * g, -g[None, :]])
+    gu, gp, _ = ots.adjoint_interpolating(rhs, fwd, [1.0], dy[..., None], 0.0, tol, tol)
+    rel = lambda a, b: np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b)  # noqa: E731
+    assert rel(dp, gp) < 1e-3, rel(dp, gp)
+    assert rel(dx, gu[:d]) < 1e-3, rel(dx, gu[:d])
+
+
+def test_ffjord_bf16_small():
+    _case_bf16(2, 32, 300, "tanh", 5)
+
+
+def test_ffjord_bf16_config3_structure():
+    """d = 16, (16+1) -> 512 -> 512 -> 16 softplus with time concatenated, on the tensor cores."""
+    _case_bf16(16, 512, 256, "softplus", 6, tol=1e-5)

@@ -142,7 +142,7 @@ def test_autotune_keeps_results(prec):
     if prec == "fp32":
         assert tiles[0] in (8, 16, 32, 64) and tiles[1] in (8, 16, 32, 64), tiles
     else:
-        assert tiles == (128, 128)
+        assert tiles[0] == 128 and tiles[1] in (0, 1), tiles
     after = run()
     assert abs(after[1] - before[1]) <= 1e-5 * abs(before[1])
     for a, b in zip((after[0], after[2], after[3]), (before[0], before[2], before[3])):
