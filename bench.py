@@ -77,7 +77,9 @@ def gemm_flops_per_rhs(dims, B):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms; start()
+    returns once the first sample has arrived (at most 5 s), so the samples
+    cover the timed region that follows it."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -92,9 +94,12 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
 
@@ -344,7 +349,9 @@ def aux_spiral(device):
 def aux_ffjord(device, B=65536, d=16, H=512):
     """FFJORD, (d+1) -> H -> H -> d softplus with time input, B samples of a
     seeded 8-component Gaussian mixture, Hutchinson trace, Tsit5 1e-5 / 1e-5;
-    negative log-likelihood and its adjoint gradient."""
+    negative log-likelihood and its adjoint gradient. The BF16 form (primal
+    and tangent chains on the tensor cores) is the reported value; the FP32
+    form runs the same inputs beside it and bounds its error."""
     import gbnde
     rng = np.random.default_rng(3)
     means = 2.0 * rng.standard_normal((8, d))
@@ -353,28 +360,42 @@ def aux_ffjord(device, B=65536, d=16, H=512):
     x = (means[comp] + np.sqrt(var[comp]) * rng.standard_normal((B, d))).T.astype(np.float32)
     model = gbnde.Chain(gbnde.Dense(d + 1, H, "softplus"), gbnde.Dense(H, H, "softplus"), gbnde.Dense(H, d))
     p = model.init_params(rng)
-    fj = gbnde.FFJORD(model, (0.0, 1.0), (d,), gbnde.Tsit5("fp32"), abstol=1e-5, reltol=1e-5,
-                      time_input=True)
-    noise = fj.draw_noise(rng, B)
-    out = {}
+    noise = None
     g = (-np.ones(B) / B).astype(np.float32)
-
-    def step():
-        logpx, zT, st = fj.forward_np(x, p, noise)
-        dx, dp, sb = fj.backward_np(g)
-        out["st"], out["sb"], out["nll"] = st, sb, -float(np.mean(logpx))
-    sec = _timed(step, 2)
-    kf, kb = _kernel_ms(fj.solver)
-    st, sb = out["st"], out["sb"]
     F = gemm_flops_per_rhs([d + 1, H, H, d], B)
-    # forward RHS = MLP + one VJP (2F with the VJP's two products ~ 3F); the
-    # adjoint RHS counted as 4F (recompute, VJP, double backward)
-    flops = 3 * F * st.nf + 4 * F * sb.nf_adj
-    return {"workload": f"ffjord_b{B}_d{d}_h{H}x2_softplus", "value": 1.0 / sec, "unit": "grad_evals/s",
-            "ms_per_eval": 1000.0 * sec, "precision": "fp32", "nf_fwd": st.nf, "nf_adj": sb.nf_adj,
-            "nll": out["nll"], "gemm_tflops_per_s": flops / sec / 1e12,
-            "fwd_kernel_ms": kf, "bwd_kernel_ms": kb,
-            "note": "host API (x, noise, logpx, gradients through host memory); FP32 SIMT kernels"}
+    res = {}
+    for prec in ("bf16", "fp32"):
+        fj = gbnde.FFJORD(model, (0.0, 1.0), (d,), gbnde.Tsit5(prec), abstol=1e-5, reltol=1e-5,
+                          time_input=True)
+        if noise is None:
+            noise = fj.draw_noise(rng, B)
+        out = {}
+
+        def step():
+            logpx, zT, st = fj.forward_np(x, p, noise)
+            dx, dp, sb = fj.backward_np(g)
+            out["st"], out["sb"], out["nll"], out["dp"] = st, sb, -float(np.mean(logpx)), dp
+        sec = _timed(step, 2)
+        kf, kb = _kernel_ms(fj.solver)
+        st, sb = out["st"], out["sb"]
+        # algorithmic GEMM work: a forward evaluation is the primal chain and
+        # one Jacobian-vector chain (2F); an adjoint evaluation recomputes both
+        # (2F), runs both chains backwards (2F) and forms the weight gradient (2F)
+        flops = 2 * F * st.nf + 6 * F * sb.nf_adj
+        res[prec] = {"value": 1.0 / sec, "ms_per_eval": 1000.0 * sec, "nf_fwd": st.nf, "nf_adj": sb.nf_adj,
+                     "nll": out["nll"], "gemm_tflops_per_s": flops / sec / 1e12,
+                     "fwd_kernel_ms": kf, "bwd_kernel_ms": kb,
+                     "kernels": {"fwd": _lib_path_name(st.fwd_path), "adj": _lib_path_name(sb.adj_path)},
+                     "dp": out["dp"]}
+        fj.solver.close()
+    tc, f32 = res["bf16"], res["fp32"]
+    d_tc, d_32 = tc.pop("dp").astype(np.float64), f32.pop("dp").astype(np.float64)
+    return {"workload": f"ffjord_b{B}_d{d}_h{H}x2_softplus", "value": tc["value"], "unit": "grad_evals/s",
+            "precision": "bf16", **{k: v for k, v in tc.items() if k != "value"},
+            "fp32_form": {**f32, "speedup_of_bf16_form": tc["value"] / f32["value"],
+                          "nll_rel_diff": abs(tc["nll"] - f32["nll"]) / abs(f32["nll"]),
+                          "grad_rel_diff": float(np.linalg.norm(d_tc - d_32) / np.linalg.norm(d_32))},
+            "note": "host API (x, noise, logpx, gradients through host memory)"}
 
 
 def aux_multishoot(device, ntraj=256, S=32, H=128):

@@ -177,6 +177,43 @@ __device__ __forceinline__ double epi_sum(double v, Shared& sh) {
   return s;
 }
 
+// The step controller's scalar FP64 work runs on epilogue thread 0 (FP64
+// executes at a small fraction of the FP32 rate on this GPU, and every
+// epilogue warp would repeat it); the results reach the other threads through
+// this block of shared memory, read after an epi_bar.
+struct StepCtl {
+  double t, h, habs, tnew, d1, dt0;
+  float ha[6][6], hbt[7], hb[7], hf;
+  int go, clipped, accept, ret, nsv, need_ckpt, exact;
+};
+
+// Sum of one float per epilogue thread, valid in epilogue thread 0 only:
+// FP32 within each warp (fixed shuffle order), FP64 over the warps.
+__device__ __forceinline__ double epi_sum0_f(float v, Shared& sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) sh.red[w] = (double)v;
+  epi_bar();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < kEpiThreads / 32; ++i) s += sh.red[i];
+  epi_bar();  // sh.red is reused by the next sum
+  return s;
+}
+
+// Sum of the grid's n per-CTA partials (FP64, in a fixed order), valid in
+// epilogue thread 0 only: warp 0 reads them.
+__device__ __forceinline__ double epi_partials_sum0(const double* p, int n) {
+  double v = 0.0;
+  if (threadIdx.x < 32) {
+    for (int i = threadIdx.x; i < n; i += 32) v += __ldcg(p + i);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  return v;
+}
+
 __device__ __forceinline__ void init_shared(Shared& sh) {
   if (threadIdx.x == 0) {
     for (int i = 0; i < kARing; ++i) {
