@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
   __shared__ int s_ok;
   __shared__ float s_ha[6][6], s_hb[6][7], s_hbt[7];
   __shared__ int s_n[6];
+  __shared__ tc::StepCtl s_ctl;
   const BwdTcArgs& A = W.t;
   const BwdArgs& a = A.b;
   const int warp = threadIdx.x >> 5;
@@ -627,10 +628,12 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
       // ---- FSAL stage at the interval start: kl1 and P1 = b1 * mu ----
       {
         zero_bias(Pb[iP1]);
+        if (threadIdx.x == 0) dense_setup(iv, t, &s_n[0], s_hb[0]);
         tc::epi_bar();
-        int n;
+        const int n = s_n[0];
         float hb[7];
-        dense_setup(iv, t, &n, hb);
+#pragma unroll
+        for (int j = 0; j < 7; ++j) hb[j] = s_hb[0][j];
         for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
           const bool v = rowok(tile);
           ok = adj(
@@ -653,8 +656,14 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
         if (!ok) break;
       }
       // ---- initial step (first interval) ----
+      // The controller's scalar FP64 work runs in warp 0 (every lane computes
+      // the same values; lane 0 publishes them in s_ctl): FP64 executes at a
+      // small fraction of the FP32 rate, and each epilogue warp would repeat
+      // it. t, dt and qold are kept by warp 0 only. Per-thread parts of the
+      // norms are FP32 sums of a thread's own components; the sums across
+      // threads and CTAs are FP64.
       if (ivi == 0) {
-        double p0 = 0.0, p1 = 0.0;
+        float p0 = 0.f, p1 = 0.f;
         for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
           if (!rowok(tile)) continue;
           for (int c = 0; c < nsc; ++c) {
@@ -665,31 +674,42 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
             for (int i = 0; i < tc::kCW; ++i) {
               if (i >= nm) continue;
               const float sk = (float)a.abstol + fabsf(l[i]) * (float)a.reltol;
-              const double xx = (double)(l[i] / sk), yy = (double)(f[i] / sk);
-              p0 += xx * xx;
-              p1 += yy * yy;
+              const float xx = l[i] / sk, yy = f[i] / sk;
+              p0 = fmaf(xx, xx, p0);
+              p1 = fmaf(yy, yy, p1);
             }
           }
         }
-        p0 = tc::epi_sum(p0, sh);
-        p1 = tc::epi_sum(p1, sh);
+        const double s0 = tc::epi_sum0_f(p0, sh);
+        const double s1 = tc::epi_sum0_f(p1, sh);
         double* pp = a.partials + (size_t)par * 2 * G;
         if (threadIdx.x == 0) {
-          pp[blockIdx.x] = p0;
-          pp[G + blockIdx.x] = p1;
+          pp[blockIdx.x] = s0;
+          pp[G + blockIdx.x] = s1;
         }
         if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
-        const double d0 = sqrt(epi_partials_sum(pp, G, sh) / Nn);
-        const double d1 = sqrt(epi_partials_sum(pp + G, G, sh) / Nn);
+        {
+          const double q0 = tc::epi_partials_sum0(pp, G), q1 = tc::epi_partials_sum0(pp + G, G);
+          if (threadIdx.x == 0) {
+            const double d0 = sqrt(q0 / Nn), d1 = sqrt(q1 / Nn);
+            double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+            dt0 = fmin(dt0, a.dtmax);
+            s_ctl.d1 = d1;
+            s_ctl.dt0 = dt0;
+            s_ctl.hf = (float)dt0;
+            s_ctl.tst[0] = t - dt0;
+            dense_setup(iv, t - dt0, &s_n[0], s_hb[0]);
+          }
+        }
+        tc::epi_bar();
         par ^= 1;
-        double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
-        dt0 = fmin(dt0, a.dtmax);
-        const float hf = (float)dt0;
-        const double tp = t - dt0;
-        int n;
+        const float hf = s_ctl.hf;
+        const double tp = s_ctl.tst[0];
+        const int n = s_n[0];
         float hb[7];
-        dense_setup(iv, tp, &n, hb);
-        double p2 = 0.0;
+#pragma unroll
+        for (int j = 0; j < 7; ++j) hb[j] = s_hb[0][j];
+        float p2 = 0.f;
         for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
           const bool v = rowok(tile);
           ok = adj(
@@ -718,44 +738,63 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
                 for (int i = 0; i < tc::kCW; ++i) {
                   if (i >= nm) continue;
                   const float sk = (float)a.abstol + fabsf(l[i]) * (float)a.reltol;
-                  const double z = (double)((f1[i] - f0[i]) / sk);
-                  p2 += z * z;
+                  const float z = (f1[i] - f0[i]) / sk;
+                  p2 = fmaf(z, z, p2);
                 }
               });
         }
         ++nf_adj;
         if (!ok) break;
-        p2 = tc::epi_sum(p2, sh);
+        const double s2 = tc::epi_sum0_f(p2, sh);
         pp = a.partials + (size_t)par * 2 * G;
-        if (threadIdx.x == 0) pp[blockIdx.x] = p2;
+        if (threadIdx.x == 0) pp[blockIdx.x] = s2;
         if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
-        const double d2 = sqrt(epi_partials_sum(pp, G, sh) / Nn) / dt0;
+        {
+          const double q2 = tc::epi_partials_sum0(pp, G);
+          if (threadIdx.x == 0) s_ctl.d1 = fmax(s_ctl.d1, sqrt(q2 / Nn) / s_ctl.dt0);
+          tc::epi_bar();
+          if (threadIdx.x < 32) {
+            const double dt0 = s_ctl.dt0, mm = s_ctl.d1;
+            const double dt1 = (mm <= 1e-15) ? fmax(1e-6, dt0 * 1e-3) : pow(10.0, -(2.0 + log10(mm)) / 5.0);
+            dt = fmin(100.0 * dt0, fmin(dt1, a.dtmax));
+          }
+        }
         par ^= 1;
-        const double mm = fmax(d1, d2);
-        const double dt1 = (mm <= 1e-15) ? fmax(1e-6, dt0 * 1e-3) : pow(10.0, -(2.0 + log10(mm)) / 5.0);
-        dt = fmin(100.0 * dt0, fmin(dt1, a.dtmax));
       }
       // ---- adaptive steps down to t_lo ----
-      while (t > t_lo && ok) {
+      while (ok) {
+        zero_bias(Pmid);
+        if (threadIdx.x < 32) {
+          // warp 0: the step, its stage times, coefficients and interpolation weights
+          const double rem = t - t_lo;
+          const bool clipped = dt >= rem;
+          const double H = clipped ? rem : dt;
+          if (threadIdx.x == 0) {
+            s_ctl.go = t > t_lo;
+            s_ctl.clipped = clipped;
+            s_ctl.h = H;
+            s_ctl.hf = (float)H;
+            for (int i = 1; i < 7; ++i) s_ctl.tst[i] = t - c_tab.c[i] * H;
+          }
+          if (t > t_lo) {
+            if (threadIdx.x < 6) {
+              const int i = threadIdx.x + 1;
+              for (int j = 0; j < 6; ++j) s_ha[i - 1][j] = (float)(H * c_tab.a[i][j]);
+              dense_setup(iv, t - c_tab.c[i] * H, &s_n[i - 1], s_hb[i - 1]);
+            } else if (threadIdx.x == 6) {
+              for (int j = 0; j < 7; ++j) s_hbt[j] = (float)(H * c_tab.btilde[j]);
+            }
+          }
+        }
+        tc::epi_bar();
+        if (!s_ctl.go) break;
         if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
         ++iter;
-        const double rem = t - t_lo;
-        const bool clipped = dt >= rem;
-        const double H = clipped ? rem : dt;
         const float* lcur = a.lam[cur];
         float* lnew = a.lam[cur ^ 1];
         const float* ccur = A.lam_comp[cur];
         float* cnew = A.lam_comp[cur ^ 1];
-        zero_bias(Pmid);
-        if (threadIdx.x < 6) {
-          const int i = threadIdx.x + 1;
-          for (int j = 0; j < 6; ++j) s_ha[i - 1][j] = (float)(H * c_tab.a[i][j]);
-          dense_setup(iv, t - c_tab.c[i] * H, &s_n[i - 1], s_hb[i - 1]);
-        } else if (threadIdx.x == 32) {
-          for (int j = 0; j < 7; ++j) s_hbt[j] = (float)(H * c_tab.btilde[j]);
-        }
-        tc::epi_bar();
-        double perr = 0.0;
+        float perr = 0.f;
         for (int i = 1; i < 7 && ok; ++i) {
           float* P = (i < 6) ? Pmid : Pb[iP7];
           const int slot = (i < 6) ? i : tc::kImgSlots - 1 - fs;
@@ -765,7 +804,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
           }
           const float cw = (i < 6) ? (float)c_tab.b[i] : (float)c_tab.b[0];
           const int n = s_n[i - 1];
-          const double ti = t - c_tab.c[i] * H;
+          const double ti = s_ctl.tst[i];
           for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
             const bool v = rowok(tile);
             ok = adj(
@@ -831,8 +870,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
                       if (q >= nm) continue;
                       const float e = fmaf(hbt6, kl[q], lt[q]);
                       const float sc = (float)a.abstol + fmaxf(fabsf(lv[q]), fabsf(yv[q])) * (float)a.reltol;
-                      const double rr = (double)(e / sc);
-                      perr += isfinite(yv[q]) ? rr * rr : (double)INFINITY;
+                      const float rr = e / sc;
+                      perr = isfinite(yv[q]) ? fmaf(rr, rr, perr) : INFINITY;
                     }
                   }
                   tc::tl_stv(klb(i) + g, kl);
@@ -841,17 +880,44 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
           ++nf_adj;
         }
         if (!ok) break;
-        perr = tc::epi_sum(perr, sh);
+        const double se = tc::epi_sum0_f(perr, sh);
         double* pp = a.partials + (size_t)par * 2 * G;
-        if (threadIdx.x == 0) pp[blockIdx.x] = perr;
+        if (threadIdx.x == 0) pp[blockIdx.x] = se;
         if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
-        const double eest = sqrt(epi_partials_sum(pp, G, sh) / Nn);
+        {
+          // error norm and PI controller (warp 0)
+          const double qe = tc::epi_partials_sum0(pp, G);
+          if (threadIdx.x < 32) {
+            const double eest = sqrt(qe / Nn);
+            const double H = s_ctl.h;
+            int rc = GBNDE_RET_SUCCESS, acc = 0;
+            if (!isfinite(eest)) {
+              rc = GBNDE_RET_UNSTABLE;
+            } else {
+              double q11;
+              double q = pi_q(eest, qold, &q11);
+              if (eest <= 1.0) {
+                acc = 1;
+                t = s_ctl.clipped ? t_lo : t - H;
+                if (q >= 1.0 && q <= 1.0) q = 1.0;
+                qold = fmax(eest, kQoldInit);
+                dt = fmin(H / q, a.dtmax);
+              } else {
+                dt = H / fmin(1.0 / kQmin, q11 / kGamma);
+              }
+            }
+            __syncwarp();
+            if (threadIdx.x == 0) {
+              s_ctl.ret = rc;
+              s_ctl.accept = acc;
+            }
+          }
+          tc::epi_bar();
+        }
         par ^= 1;
-        if (!isfinite(eest)) { ret = GBNDE_RET_UNSTABLE; break; }
-        double q11;
-        double q = pi_q(eest, qold, &q11);
-        if (eest <= 1.0) {
-          if (!commit_step((float)H)) { ok = false; break; }
+        if (s_ctl.ret != GBNDE_RET_SUCCESS) { ret = s_ctl.ret; break; }
+        if (s_ctl.accept) {
+          if (!commit_step(s_ctl.hf)) { ok = false; break; }
           const int tmp = iP1;
           iP1 = iP7;
           iP7 = tmp;
@@ -859,13 +925,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
           ++nacc;
           cur ^= 1;
           swp = !swp;
-          t = clipped ? t_lo : t - H;
-          if (q >= 1.0 && q <= 1.0) q = 1.0;
-          qold = fmax(eest, kQoldInit);
-          dt = fmin(H / q, a.dtmax);
         } else {
           ++nrej;
-          dt = H / fmin(1.0 / kQmin, q11 / kGamma);
         }
       }
       if (!ok || ret != GBNDE_RET_SUCCESS) break;

@@ -254,6 +254,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
   uint8_t* wring = smem + tc::kARing * tc::kASlotBytes;
   __shared__ tc::Shared sh;
   __shared__ int s_ok;
+  __shared__ tc::StepCtl s_ctl;
   const FwdArgs& a = A.t.f;
   const int warp = threadIdx.x >> 5;
 
@@ -372,11 +373,16 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
     if (!ok) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto epi_done; }
 
     // ---- initial step ---------------------------------------------------------------
-    double dt;
-    if (a.dt0 > 0.0) {
-      dt = a.dt0;
-    } else {
-      double p0 = 0.0, p1 = 0.0;
+    // The controller's scalar FP64 work (norms, the initial step, the PI
+    // update, stage coefficients and times, save weights) runs on epilogue
+    // thread 0 and reaches the others through shared memory (s_ctl): FP64
+    // executes at a small fraction of the FP32 rate, and each of the epilogue
+    // warps would repeat it. Per-thread parts of the norms are FP32 sums of a
+    // thread's own components; the sums across threads and CTAs are FP64.
+    double dt;  // thread 0's controller state (t, dt, qold) is the one used
+    dt = a.dt0;
+    if (!(a.dt0 > 0.0)) {
+      float p0 = 0.f, p1 = 0.f;
       for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
         if (!rowok(tile)) continue;
         for (int c = 0; c < nsc; ++c) {
@@ -387,38 +393,48 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
           for (int i = 0; i < tc::kCW; ++i) {
             if (i >= nm) continue;
             const float sk = (float)a.abstol + fabsf(u[i]) * (float)a.reltol;
-            const double x = (double)(u[i] / sk), y = (double)(f[i] / sk);
-            p0 += x * x;
-            p1 += y * y;
+            const float x = u[i] / sk, y = f[i] / sk;
+            p0 = fmaf(x, x, p0);
+            p1 = fmaf(y, y, p1);
           }
         }
       }
-      p0 = tc::epi_sum(p0, sh);
-      p1 = tc::epi_sum(p1, sh);
+      const double s0 = tc::epi_sum0_f(p0, sh);
+      const double s1 = tc::epi_sum0_f(p1, sh);
       double* pp = a.partials + (size_t)par * 2 * G;
       if (threadIdx.x == 0) {
-        pp[blockIdx.x] = p0;
-        pp[G + blockIdx.x] = p1;
+        pp[blockIdx.x] = s0;
+        pp[G + blockIdx.x] = s1;
       }
       if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto epi_done; }
-      const double d0 = sqrt(epi_partials_sum(pp, G, sh) / N);
-      const double d1 = sqrt(epi_partials_sum(pp + G, G, sh) / N);
+      {
+        const double q0 = tc::epi_partials_sum0(pp, G), q1 = tc::epi_partials_sum0(pp + G, G);
+        if (threadIdx.x == 0) {
+          const double d0 = sqrt(q0 / N), d1 = sqrt(q1 / N);
+          double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? fmax(a.dtmin, 1e-6) : 0.01 * (d0 / d1);
+          dt0 = fmin(dt0, a.dtmax);
+          s_ctl.d1 = d1;
+          s_ctl.dt0 = dt0;
+          s_ctl.hf = (float)(tdir * dt0);
+          s_ctl.tst[0] = a.t0 + tdir * dt0;
+        }
+      }
+      tc::epi_bar();
       par ^= 1;
-      double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? fmax(a.dtmin, 1e-6) : 0.01 * (d0 / d1);
-      dt0 = fmin(dt0, a.dtmax);
-      const float hf = (float)(tdir * dt0);
-      double p2 = 0.0;
+      const float hf = s_ctl.hf;
+      const double t1p = s_ctl.tst[0];
+      float p2 = 0.f;
       for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
         const bool v = rowok(tile);
         ok = rhs(
             tile,
             [&](int c, float* x) {
-              if (c >= nsc) { tcol(c, a.t0 + tdir * dt0, x); return; }
+              if (c >= nsc) { tcol(c, t1p, x); return; }
               float u[tc::kCW], f0[tc::kCW];
               tc::tl_ldv(a.ubuf[0] + tofs(tile, c), u);
               tc::tl_ldv(kptr(0) + tofs(tile, c), f0);
               for (int i = 0; i < tc::kCW; ++i) x[i] = u[i] + hf * f0[i];
-              with_t(c, a.t0 + tdir * dt0, x);
+              with_t(c, t1p, x);
             },
             [&](int c, const float* f1) {
               if (!v) return;
@@ -429,48 +445,67 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
               for (int i = 0; i < tc::kCW; ++i) {
                 if (i >= nm) continue;
                 const float sk = (float)a.abstol + fabsf(u[i]) * (float)a.reltol;
-                const double z = (double)((f1[i] - f0[i]) / sk);
-                p2 += z * z;
+                const float z = (f1[i] - f0[i]) / sk;
+                p2 = fmaf(z, z, p2);
               }
             });
       }
       nf += 1;
       if (!ok) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto epi_done; }
-      p2 = tc::epi_sum(p2, sh);
+      const double s2 = tc::epi_sum0_f(p2, sh);
       pp = a.partials + (size_t)par * 2 * G;
-      if (threadIdx.x == 0) pp[blockIdx.x] = p2;
+      if (threadIdx.x == 0) pp[blockIdx.x] = s2;
       if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; goto epi_done; }
-      const double d2 = sqrt(epi_partials_sum(pp, G, sh) / N) / dt0;
+      {
+        const double q2 = tc::epi_partials_sum0(pp, G);
+        if (threadIdx.x == 0) {
+          const double dt0 = s_ctl.dt0;
+          const double d2 = sqrt(q2 / N) / dt0;
+          const double mm = fmax(s_ctl.d1, d2);
+          const double dt1 = (mm <= 1e-15) ? fmax(1e-6, dt0 * 1e-3) : pow(10.0, -(2.0 + log10(mm)) / 5.0);
+          dt = fmax(a.dtmin, fmin(100.0 * dt0, fmin(dt1, a.dtmax)));
+        }
+      }
       par ^= 1;
-      const double mm = fmax(d1, d2);
-      const double dt1 = (mm <= 1e-15) ? fmax(1e-6, dt0 * 1e-3) : pow(10.0, -(2.0 + log10(mm)) / 5.0);
-      dt = fmax(a.dtmin, fmin(100.0 * dt0, fmin(dt1, a.dtmax)));
     }
 
     // ---- step loop ---------------------------------------------------------------------
     {
       double t = a.t0, qold = kQoldInit;
       int ib = 0, nck = 0;
-      while (tdir * (a.t1 - t) > 0.0) {
+      for (;;) {
+        // step setup (thread 0): continue?, the step size, the stage coefficients and times
+        if (threadIdx.x == 0) {
+          s_ctl.go = tdir * (a.t1 - t) > 0.0;
+          const double rem = fabs(a.t1 - t);
+          s_ctl.clipped = dt >= rem;
+          s_ctl.habs = s_ctl.clipped ? rem : dt;
+          const double h = tdir * s_ctl.habs;
+          s_ctl.t = t;
+          s_ctl.h = h;
+          for (int i = 1; i < 7; ++i) {
+            for (int j = 0; j < i; ++j) s_ctl.ha[i - 1][j] = (float)(h * c_tab.a[i][j]);
+            s_ctl.tst[i] = t + c_tab.c[i] * h;
+          }
+          for (int j = 0; j < 7; ++j) s_ctl.hbt[j] = (float)(h * c_tab.btilde[j]);
+        }
+        tc::epi_bar();
+        if (!s_ctl.go) break;
         if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
         ++iter;
-        const double rem = fabs(a.t1 - t);
-        const bool clipped = dt >= rem;
-        const double habs = clipped ? rem : dt;
-        const double h = tdir * habs;
         const float* ucur = a.ubuf[cur];
         float* unew = a.ubuf[cur ^ 1];
         const float* ccur = A.t.comp[cur];
         float* cnew = A.t.comp[cur ^ 1];
-        double perr = 0.0;
+        float perr = 0.f;
         for (int i = 1; i < 7 && ok; ++i) {
           float ha[6];
 #pragma unroll
-          for (int j = 0; j < 6; ++j) ha[j] = (float)(h * c_tab.a[i][j]);
+          for (int j = 0; j < 6; ++j) ha[j] = j < i ? s_ctl.ha[i - 1][j] : 0.f;
           float hbt[7];
 #pragma unroll
-          for (int j = 0; j < 7; ++j) hbt[j] = (float)(h * c_tab.btilde[j]);
-          const double ti = t + c_tab.c[i] * h;
+          for (int j = 0; j < 7; ++j) hbt[j] = s_ctl.hbt[j];
+          const double ti = s_ctl.tst[i];
           for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
             const bool v = rowok(tile);
             ok = rhs(
@@ -533,8 +568,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
                       if (q >= nm) continue;
                       const float e = fmaf(hbt[6], k[q], ut[q]);
                       const float sc = (float)a.abstol + fmaxf(fabsf(u[q]), fabsf(Y[q])) * (float)a.reltol;
-                      const double rr = (double)(e / sc);
-                      perr += isfinite(Y[q]) ? rr * rr : (double)INFINITY;
+                      const float rr = e / sc;
+                      perr = isfinite(Y[q]) ? fmaf(rr, rr, perr) : INFINITY;
                     }
                   }
                   tc::tl_stv(kptr(i) + g, k);
@@ -543,61 +578,117 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
         }
         if (!ok) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
         nf += 6;
-        perr = tc::epi_sum(perr, sh);
+        const double se = tc::epi_sum0_f(perr, sh);
         double* pp = a.partials + (size_t)par * 2 * G;
-        if (threadIdx.x == 0) pp[blockIdx.x] = perr;
+        if (threadIdx.x == 0) pp[blockIdx.x] = se;
         if (!epi_grid_barrier(a, gen, &s_ok)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
-        const double eest = sqrt(epi_partials_sum(pp, G, sh) / N);
-        par ^= 1;
-        if (!isfinite(eest)) { ret = GBNDE_RET_UNSTABLE; break; }
-        double q11;
-        double q = pi_q(eest, qold, &q11);
-        if (blockIdx.x == 0 && threadIdx.x == 0 && iter - 1 < a.maxsteps) {
-          double* tr = a.trace + 4 * (iter - 1);
-          tr[0] = t;
-          tr[1] = h;
-          tr[2] = eest;
-          tr[3] = eest <= 1.0 ? 1.0 : 0.0;
-        }
-        if (eest <= 1.0) {
-          const double tnew = clipped ? a.t1 : t + h;
-          while (isave < a.nsave && tdir * (a.saveat[isave] - tnew) <= 0.0) {
-            const double sv = a.saveat[isave];
-            float* dst = a.usave + (size_t)isave * SB;
-            float hb[7];
-            if (sv != tnew) {
-              float bw[7];
-              interp_weights((sv - t) / h, bw);
-              for (int j = 0; j < 7; ++j) hb[j] = (float)(h * (double)bw[j]);
+        {
+          // error norm, PI controller, saves and checkpoints of the step (thread 0)
+          const double qe = tc::epi_partials_sum0(pp, G);
+          if (threadIdx.x == 0) {
+            const double eest = sqrt(qe / N);
+            const double h = s_ctl.h, habs = s_ctl.habs;
+            s_ctl.ret = GBNDE_RET_SUCCESS;
+            s_ctl.accept = 0;
+            if (!isfinite(eest)) {
+              s_ctl.ret = GBNDE_RET_UNSTABLE;
+            } else {
+              double q11;
+              double q = pi_q(eest, qold, &q11);
+              if (blockIdx.x == 0 && iter - 1 < a.maxsteps) {
+                double* tr = a.trace + 4 * (iter - 1);
+                tr[0] = t;
+                tr[1] = h;
+                tr[2] = eest;
+                tr[3] = eest <= 1.0 ? 1.0 : 0.0;
+              }
+              if (eest <= 1.0) {
+                const double tnew = s_ctl.clipped ? a.t1 : t + h;
+                s_ctl.accept = 1;
+                s_ctl.tnew = tnew;
+                int ns = 0;
+                while (isave + ns < a.nsave && tdir * (a.saveat[isave + ns] - tnew) <= 0.0) ++ns;
+                s_ctl.nsv = ns;
+                bool need = false;
+                while (ib < a.nbnd && tdir * (a.bnd[ib] - tnew) < 0.0) { need = true; ++ib; }
+                s_ctl.need_ckpt = need;
+                if (blockIdx.x == 0 && naccept < a.maxsteps) {
+                  a.steplog[2 * naccept] = t;
+                  a.steplog[2 * naccept + 1] = h;
+                }
+                t = tnew;
+                if (q >= 1.0 && q <= 1.0) q = 1.0;
+                qold = fmax(eest, kQoldInit);
+                dt = fmax(fmin(habs / q, a.dtmax), a.dtmin);
+              } else {
+                dt = habs / fmin(1.0 / kQmin, q11 / kGamma);
+                if (a.dtmin > 0.0 && dt <= a.dtmin) s_ctl.ret = GBNDE_RET_DTLESSTHANMIN;
+              }
             }
+          }
+          tc::epi_bar();
+        }
+        par ^= 1;
+        if (s_ctl.ret != GBNDE_RET_SUCCESS) {
+          ret = s_ctl.ret;
+          if (ret == GBNDE_RET_DTLESSTHANMIN) ++nreject;
+          break;
+        }
+        if (s_ctl.accept) {
+          const int nsv = s_ctl.nsv;
+          for (int k = 0; k < nsv; ++k, ++isave) {
+            if (threadIdx.x == 0) {
+              const double sv = a.saveat[isave];
+              s_ctl.exact = sv == s_ctl.tnew;
+              if (!s_ctl.exact) {
+                float bw[7];
+                interp_weights((sv - s_ctl.t) / s_ctl.h, bw);
+                for (int j = 0; j < 7; ++j) s_ctl.hb[j] = (float)(s_ctl.h * (double)bw[j]);
+              }
+            }
+            tc::epi_bar();
+            const bool exact = s_ctl.exact;
+            float hb[7];
+#pragma unroll
+            for (int j = 0; j < 7; ++j) hb[j] = s_ctl.hb[j];
+            float* dst = a.usave + (size_t)isave * SB;
             for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
               if (!rowok(tile)) continue;
               for (int c = 0; c < nsc; ++c) {
                 const size_t tg = tofs(tile, c);
                 float o[tc::kCW];
-                if (sv == tnew) {
+                if (exact) {
                   tc::tl_ldv(unew + tg, o);
                 } else {
-                  float u[tc::kCW];
-                  tc::tl_ldv(ucur + tg, u);
-                  tc::tl_ldv(ccur + tg, o);
-                  for (int j = 0; j < 7; ++j) {
-                    float kj[tc::kCW];
-                    tc::tl_ldv(kptr(j) + tg, kj);
+                  // u + (comp + sum_j hb_j k_j), one float4 group of the
+                  // thread's components at a time, its nine loads in flight
 #pragma unroll
-                    for (int q = 0; q < tc::kCW; ++q) o[q] = fmaf(hb[j], kj[q], o[q]);
+                  for (int jg = 0; jg < tc::kCW / 4; ++jg) {
+                    float4 v9[9];
+                    v9[0] = *reinterpret_cast<const float4*>(ucur + tg + jg * 512);
+                    v9[1] = *reinterpret_cast<const float4*>(ccur + tg + jg * 512);
+#pragma unroll
+                    for (int j = 0; j < 7; ++j) v9[2 + j] = *reinterpret_cast<const float4*>(kptr(j) + tg + jg * 512);
+                    float4 e = v9[1];
+#pragma unroll
+                    for (int j = 0; j < 7; ++j) {
+                      e.x = fmaf(hb[j], v9[2 + j].x, e.x);
+                      e.y = fmaf(hb[j], v9[2 + j].y, e.y);
+                      e.z = fmaf(hb[j], v9[2 + j].z, e.z);
+                      e.w = fmaf(hb[j], v9[2 + j].w, e.w);
+                    }
+                    o[4 * jg] = v9[0].x + e.x;
+                    o[4 * jg + 1] = v9[0].y + e.y;
+                    o[4 * jg + 2] = v9[0].z + e.z;
+                    o[4 * jg + 3] = v9[0].w + e.w;
                   }
-#pragma unroll
-                  for (int q = 0; q < tc::kCW; ++q) o[q] = u[q] + o[q];
                 }
                 stv_api(dst + gofs(tile, c), nmine_of(S, c, th.ch), o);
               }
             }
-            ++isave;
+            tc::epi_bar();  // s_ctl.hb is rewritten for the next save
           }
-          bool need = false;
-          while (ib < a.nbnd && tdir * (a.bnd[ib] - tnew) < 0.0) { need = true; ++ib; }
-          if (need && nck < a.max_ckpt) {
+          if (s_ctl.need_ckpt && nck < a.max_ckpt) {
             float* dst = a.ckpt + (size_t)nck * SB;
             for (int tile = blockIdx.x; tile < a.ntiles; tile += G)
               if (rowok(tile))
@@ -609,10 +700,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
             if (blockIdx.x == 0 && threadIdx.x == 0) a.ckpt_step[nck] = (int)naccept;
             ++nck;
           }
-          if (blockIdx.x == 0 && threadIdx.x == 0 && naccept < a.maxsteps) {
-            a.steplog[2 * naccept] = t;
-            a.steplog[2 * naccept + 1] = h;
-          }
           // FSAL: k7 becomes k1 of the next step (next dense slot, or in place)
           const float* k7 = kptr(6);
           ++naccept;
@@ -622,23 +709,17 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
               const size_t g = tofs(tile, c);
               float kk[tc::kCW];
               tc::tl_ldv(k7 + g, kk);
-              tc::tl_stv(kptr(0) + g, kk);
               if (dense && naccept < A.t.dense_slots) {
                 float un[tc::kCW];
                 tc::tl_ldv(unew + g, un);
                 tc::tl_stv(A.t.dense + (size_t)naccept * 8 * SBt + g, un);
               }
+              tc::tl_stv(kptr(0) + g, kk);
             }
           }
           cur ^= 1;
-          t = tnew;
-          if (q >= 1.0 && q <= 1.0) q = 1.0;
-          qold = fmax(eest, kQoldInit);
-          dt = fmax(fmin(habs / q, a.dtmax), a.dtmin);
         } else {
           ++nreject;
-          dt = habs / fmin(1.0 / kQmin, q11 / kGamma);
-          if (a.dtmin > 0.0 && dt <= a.dtmin) { ret = GBNDE_RET_DTLESSTHANMIN; break; }
         }
       }
       if (blockIdx.x == 0 && threadIdx.x == 0) {

@@ -183,6 +183,7 @@ __device__ __forceinline__ double epi_sum(double v, Shared& sh) {
 // this block of shared memory, read after an epi_bar.
 struct StepCtl {
   double t, h, habs, tnew, d1, dt0;
+  double tst[7];  // stage times (tst[0]: the initial step's probe time)
   float ha[6][6], hbt[7], hb[7], hf;
   int go, clipped, accept, ret, nsv, need_ckpt, exact;
 };
