@@ -195,6 +195,7 @@ struct gbnde_ctx {
   int wb_npad[GBNDE_MAX_LAYERS][4] = {}, wbT_npad[GBNDE_MAX_LAYERS][4] = {};
   DBuf stash;
   DBuf timg, thscr, tmucomp, tlamcomp;
+  size_t timg_cleared = 0;  // bytes of timg set to zero since its allocation
   DBuf tr_us, tr_dl, tr_du0, tr_dp;  // training-step scratch
   // graph-mode training step
   bool recording = false;
@@ -231,6 +232,22 @@ struct gbnde_ctx {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double fwd_ms = 0.0, bwd_ms = 0.0;
 };
+
+namespace {
+// The weight-gradient images' padding rows and blocks are never written (the
+// products that read them land in accumulator rows and columns that are not
+// stored), so the image buffer is set to zero once per allocation rather than
+// at every adjoint launch.
+int clear_images(gbnde_ctx* c) {
+  if (c->timg_cleared == c->timg.n) return 0;
+  if (cudaMemsetAsync(c->timg.p, 0, c->timg.n, c->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(GBNDE_ERR_CUDA, "clearing the weight-gradient images failed");
+  }
+  c->timg_cleared = c->timg.n;
+  return 0;
+}
+}  // namespace
 
 namespace {
 
@@ -953,6 +970,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
       (r = c->tmucomp.ensure((size_t)grid * P * 4)) || (r = c->tlamcomp.ensure(2 * SBt * 4)) ||
       (r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4)))
     return r;
+  if ((r = clear_images(c))) return r;
   // per-CTA quadrature slots padded to a multiple of 4 floats (float4 sweeps)
   const int Ppad = (P + 3) / 4 * 4;
   t.b.P = Ppad;
@@ -994,9 +1012,15 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   // op is copy-only: a_{L-1} passes through the ring just to reach its image.
   int n = 0;
   if (2 * L > tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
+  // The adjoint's chain GEMMs (recompute and VJP) issue three of the five
+  // split products: their 16-bit operands keep the gradient within 1e-5 of
+  // the five-product form, while the forward needs all five (its error
+  // estimate reaches the rounding noise of fewer). The replay list (fwops)
+  // keeps five: it must reproduce the forward's steps exactly.
   for (int l = 0; l < L; ++l) {
     tc::GemmOp& o = t.ops.op[n++];
     o.kind = (l == L - 1) ? 2 : 0;
+    o.nprod = 3;
     o.wimg = c->wimg.as<uint8_t>() + c->wimg_off[l];
     o.npad = c->npad[l];
     o.nchunk = c->nchunk[l];
@@ -1008,6 +1032,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   for (int l = L - 1; l >= 0; --l) {
     tc::GemmOp& o = t.ops.op[n++];
     o.kind = 0;
+    o.nprod = 3;
     o.wimg = c->wimg.as<uint8_t>() + c->wtimg_off[l];
     o.npad = c->npadT[l];
     o.nchunk = c->nchunkT[l];
@@ -1142,6 +1167,7 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
       (r = c->mu_acc.ensure((size_t)grid * Ppad * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * 4 * t.nbias * 4)) ||
       (r = c->stash.ensure((size_t)grid * tc::kStashCta)))
     return r;
+  if ((r = clear_images(c))) return r;
   t.b.mu_acc = c->mu_acc.as<float>();
   t.b.mu_stage = c->mu_stage.as<float>();
   t.pbias = c->mu_stage.as<float>();

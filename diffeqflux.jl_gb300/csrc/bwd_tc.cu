@@ -274,9 +274,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       for (int i = threadIdx.x; i < 4 * A.nbias; i += tc::kEpiThreads) p[i] = 0.f;
     };
 
-    // scratch images start at zero (padding rows/blocks are never written)
-    for (size_t i = threadIdx.x; i < (size_t)A.tpc * tc::kImgSlots * A.img_cta / 16; i += tc::kEpiThreads)
-      reinterpret_cast<uint4*>(img)[i] = make_uint4(0, 0, 0, 0);
+    // (the images' padding rows and blocks are never written: the host clears
+    // the image buffer once when it is allocated)
     zero_cta(mu_acc);
     zero_cta(mu_comp);
     // the weight-gradient images are read by the producer warp (async proxy)

@@ -130,6 +130,9 @@ struct GemmOp {
   // bytes after pair 0's in the stage slot (npairs 0 or 1: one pair)
   int npairs;
   uint32_t pair_aoff, pair_boff;
+  // kind 0 / 3: split products issued: 0 (all five) or 3 (A_hi W_hi +
+  // A_mid W_hi + A_hi W_lo, about 16 bits of both operands)
+  int nprod;
 };
 
 struct OpList {
@@ -394,8 +397,10 @@ __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh
       const bool copy = chain && img_base != nullptr && op.img_off >= 0;
       if (copy) copy_a_image(op, c, aring + m.aslot * kASlotBytes, img_base);
       if (chain) {
+        const int np = op.nprod == 3 ? 3 : 5;
 #pragma unroll
         for (int pr = 0; pr < 5; ++pr) {
+          if (pr >= np) break;
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
             const uint64_t ad = sdesc_sw128(a0 + pa[pr] * 16384 + kk * 32);
