@@ -1205,6 +1205,7 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
     const int in = m.dims[l], out = m.dims[l + 1];
     const int k = vjp ? out : in;  // K of the op: the operand's width
     o->kind = kind;
+    o->nprod = 3;  // the adjoint's chains: three split products (as in the single-accumulator engine)
     if (kind == 3) {
       o->wimg = c->wimg.as<uint8_t>() + (vjp ? c->wbT_off[l][b] : c->wb_off[l][b]);
       o->npad = vjp ? c->wbT_npad[l][b] : c->wb_npad[l][b];  // the image's row padding

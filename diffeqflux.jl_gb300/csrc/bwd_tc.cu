@@ -157,8 +157,7 @@ __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* a
       *reinterpret_cast<uint4*>(base + 16384 + off) = mid[j];
       *reinterpret_cast<uint4*>(base + 32768 + off) = lo[j];
     }
-    tc::fence_proxy_async_smem();
-    tc::mbar_arrive(&sh.a_full[e.aslot]);
+    tc::epi_warp_arrive_smem(&sh.a_full[e.aslot]);
     if (++e.aslot == tc::kARing) { e.aslot = 0; e.aph ^= 1; }
   }
   return true;

@@ -40,6 +40,7 @@ constexpr int kNWG = GBNDE_TC_NWG;   // epilogue warpgroups: 2 or 4
 static_assert(kNWG == 2 || kNWG == 4, "two or four epilogue warpgroups");
 constexpr int kCW = 64 / kNWG;       // columns of each 64-column chunk per epilogue thread
 constexpr int kEpiThreads = 128 * kNWG;
+constexpr int kEpiWarps = kEpiThreads / 32;  // arrivals of the epilogue on a barrier: one per warp
 constexpr int kThreads = kEpiThreads + 128;
 constexpr int kMmaWarp = 4 * kNWG;
 constexpr int kTmaWarp = kMmaWarp + 1;
@@ -147,7 +148,7 @@ struct Shared {
   uint64_t img_ready;
   uint64_t img_done;  // command mode: the MMA warp's image copies of the step have landed
   uint64_t cmd_full[kCmdRing], cmd_empty[kCmdRing];
-  uint64_t stash_full[kStashBufs][kStashChunks];  // stash mode: chunk written by all epilogue threads
+  uint64_t stash_full[kStashBufs][kStashChunks];  // stash mode: chunk written by all epilogue warps
   uint32_t cmd[kCmdRing];
   uint32_t tmem_base;
   int stop;
@@ -221,7 +222,7 @@ __device__ __forceinline__ double epi_partials_sum0(const double* p, int n) {
 __device__ __forceinline__ void init_shared(Shared& sh) {
   if (threadIdx.x == 0) {
     for (int i = 0; i < kARing; ++i) {
-      mbar_init(&sh.a_full[i], kEpiThreads);
+      mbar_init(&sh.a_full[i], kEpiWarps);
       mbar_init(&sh.a_empty[i], 1);
     }
     for (int i = 0; i < kWRing; ++i) {
@@ -230,16 +231,16 @@ __device__ __forceinline__ void init_shared(Shared& sh) {
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&sh.acc_full[i], 1);
-      mbar_init(&sh.acc_empty[i], kEpiThreads);
+      mbar_init(&sh.acc_empty[i], kEpiWarps);
     }
-    mbar_init(&sh.img_ready, kEpiThreads);
+    mbar_init(&sh.img_ready, kEpiWarps);
     mbar_init(&sh.img_done, 1);
     for (int i = 0; i < kCmdRing; ++i) {
       mbar_init(&sh.cmd_full[i], 1);
       mbar_init(&sh.cmd_empty[i], 2);
     }
     for (int b = 0; b < kStashBufs; ++b)
-      for (int i = 0; i < kStashChunks; ++i) mbar_init(&sh.stash_full[b][i], kEpiThreads);
+      for (int i = 0; i < kStashChunks; ++i) mbar_init(&sh.stash_full[b][i], kEpiWarps);
     sh.stop = 0;
     sh.err = 0;
     fence_mbar_init();
@@ -553,7 +554,7 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
         mbar_arrive_expect_tx(&sh.a_full[t.aslot], (uint32_t)kASlotBytes);
         asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
                          smem_u32(&sh.a_full[t.aslot])),
-                     "r"(kEpiThreads - 1)
+                     "r"(kEpiWarps - 1)
                      : "memory");
         bulk_g2s(aring + t.aslot * kASlotBytes, sbase + (size_t)c * kASlotBytes, (uint32_t)kASlotBytes,
                  &sh.a_full[t.aslot]);
@@ -600,7 +601,7 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
         mbar_arrive_expect_tx(&sh.a_full[t.aslot], op.a_bytes);
         asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
                          smem_u32(&sh.a_full[t.aslot])),
-                     "r"(kEpiThreads - 1)
+                     "r"(kEpiWarps - 1)
                      : "memory");
         bulk_g2s(aring + t.aslot * kASlotBytes, abase + aoff, op.a_bytes, &sh.a_full[t.aslot]);
       }
@@ -705,6 +706,16 @@ __device__ __forceinline__ void epi_state_init(EpiState& e) {
   e.g = 0;
 }
 
+// A chunk's shared-memory writes by the warp are complete: each lane fences
+// its writes for the async proxy (the tensor cores read the chunk), then one
+// lane arrives for the warp. One arrival per warp instead of one per thread
+// keeps the 512-thread epilogue off the barrier's serialised arrive path.
+__device__ __forceinline__ void epi_warp_arrive_smem(uint64_t* bar) {
+  fence_proxy_async_smem();
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(bar);
+}
+
 // Write this thread's kCW columns (its row r, column group ch) of an A chunk:
 // values x[0 .. kCW) for columns [kCW*ch, kCW*ch + kCW) of the chunk, split in
 // 3 pieces.
@@ -723,8 +734,7 @@ __device__ __forceinline__ bool epi_write_a(EpiState& e, Shared& sh, uint8_t* ar
     *reinterpret_cast<uint4*>(base + 16384 + off) = mid;
     *reinterpret_cast<uint4*>(base + 32768 + off) = lo;
   }
-  fence_proxy_async_smem();
-  mbar_arrive(&sh.a_full[e.aslot]);
+  epi_warp_arrive_smem(&sh.a_full[e.aslot]);
   if (++e.aslot == kARing) { e.aslot = 0; e.aph ^= 1; }
   return true;
 }
@@ -747,7 +757,8 @@ __device__ __forceinline__ void stash_write(uint8_t* stash_cta, Shared& sh, int 
     *reinterpret_cast<uint4*>(base + 32768 + off) = lo;
   }
   asm volatile("fence.proxy.async.global;" ::: "memory");
-  mbar_arrive(&sh.stash_full[b][c]);
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(&sh.stash_full[b][c]);
 }
 
 // Bias values of columns [n0, n0 + kCW) of a layer with N outputs (zero past
@@ -845,7 +856,8 @@ __device__ __forceinline__ bool epi_post(CmdPoster& p, Shared& sh, uint32_t cmd)
 __device__ __forceinline__ void epi_release_acc(EpiState& e, Shared& sh) {
   const int reg = (int)(e.g & 1);
   tc_fence_before();
-  mbar_arrive(&sh.acc_empty[reg]);
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(&sh.acc_empty[reg]);
   e.use[reg] += 1;
   e.g += 1;
 }
