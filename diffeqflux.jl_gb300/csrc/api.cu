@@ -194,7 +194,7 @@ struct gbnde_ctx {
   size_t wb_off[GBNDE_MAX_LAYERS][4] = {}, wbT_off[GBNDE_MAX_LAYERS][4] = {};
   int wb_npad[GBNDE_MAX_LAYERS][4] = {}, wbT_npad[GBNDE_MAX_LAYERS][4] = {};
   DBuf stash;
-  DBuf timg, thscr, tmucomp, tlamcomp;
+  DBuf timg, thscr, tmucomp, tlamcomp, txst;
   size_t timg_cleared = 0;  // bytes of timg set to zero since its allocation
   DBuf tr_us, tr_dl, tr_du0, tr_dp;  // training-step scratch
   // graph-mode training step
@@ -394,7 +394,7 @@ void gbnde_destroy(gbnde_ctx* c) {
                   &c->ms_usave, &c->ms_dense, &c->ms_steplog, &c->ms_nacc, &c->ms_ret, &c->ms_cnt,
                   &c->ms_dldu, &c->ms_dldu0, &c->ms_bar, &c->ms_mu, &c->ms_dldp, &c->ffnoise,
                   &c->ffu0, &c->ffus, &c->tr_us, &c->tr_dl, &c->tr_du0, &c->tr_dp, &c->stash,
-                  &c->ms_data, &c->ms_map, &c->ms_part, &c->ckcomp, &c->trep};
+                  &c->ms_data, &c->ms_map, &c->ms_part, &c->ckcomp, &c->trep, &c->txst};
   for (DBuf* b : bufs) b->release();
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -968,9 +968,11 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   if ((r = c->timg.ensure((size_t)grid * tpc * tc::kImgSlots * t.img_cta)) ||
       (r = c->thscr.ensure((size_t)grid * tc::kEpiThreads * t.hvals * 4)) ||
       (r = c->tmucomp.ensure((size_t)grid * P * 4)) || (r = c->tlamcomp.ensure(2 * SBt * 4)) ||
-      (r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4)))
+      (r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4)) ||
+      (r = c->txst.ensure(6 * SBt * 4)))
     return r;
   if ((r = clear_images(c))) return r;
+  t.xst = c->txst.as<float>();
   // per-CTA quadrature slots padded to a multiple of 4 floats (float4 sweeps)
   const int Ppad = (P + 3) / 4 * 4;
   t.b.P = Ppad;

@@ -561,6 +561,41 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       }
     };
 
+    // u(t) at the six stage times of an adjoint step (s_n, s_hb), into xst:
+    // a forward slot's eight vectors are loaded once for all the stages that
+    // interpolate in it (usually all six), instead of once per stage. One
+    // float4 group of the thread's components at a time; the arithmetic is
+    // dense_u's.
+    auto stage_u = [&](int tile) {
+      const size_t g = tofs(tile);
+#pragma unroll 1
+      for (int jg = 0; jg < tc::kCW / 4; ++jg) {
+        float4 v8[8];
+        int cur_n = -1;
+#pragma unroll 1
+        for (int i = 0; i < 6; ++i) {
+          const int n = s_n[i];
+          if (n != cur_n) {
+            const float* sp = slot_of(n) + g + jg * 512;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v8[j] = *reinterpret_cast<const float4*>(sp + (size_t)j * SBt);
+            cur_n = n;
+          }
+          float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int j = 0; j < 7; ++j) {
+            const float w = s_hb[i][j];
+            e.x = fmaf(w, v8[j + 1].x, e.x);
+            e.y = fmaf(w, v8[j + 1].y, e.y);
+            e.z = fmaf(w, v8[j + 1].z, e.z);
+            e.w = fmaf(w, v8[j + 1].w, e.w);
+          }
+          *reinterpret_cast<float4*>(A.xst + (size_t)i * SBt + g + jg * 512) =
+              make_float4(v8[0].x + e.x, v8[0].y + e.y, v8[0].z + e.z, v8[0].w + e.w);
+        }
+      }
+    };
+
     // The plain right-hand side of one tile (the forward list): Y -> kout,
     // with the forward kernel's arithmetic.
     auto fwd_eval = [&](const float* Y, float* kout) -> bool {
@@ -834,6 +869,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         float* lnew = a.lam[cur ^ 1];
         const float* ccur = A.lam_comp[cur];
         float* cnew = A.lam_comp[cur ^ 1];
+        for (int tile = blockIdx.x; tile < a.ntiles; tile += G)
+          if (valid(tile)) stage_u(tile);
         float perr = 0.f;
         for (int i = 1; i < 7 && ok; ++i) {
           float ha[6];
@@ -846,10 +883,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             tc::epi_bar();
           }
           const float cw = (i < 6) ? (float)c_tab.b[i] : (float)c_tab.b[0];
-          const int n = s_n[i - 1];
-          float hb[7];
-#pragma unroll
-          for (int j = 0; j < 7; ++j) hb[j] = s_hb[i - 1][j];
           for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += G) {
             const bool v = valid(tile);
             const size_t g = tofs(tile);  // tile layout
@@ -892,7 +925,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
                   tc::tl_stp(cnew + g, hf, cn);
                 }
               }
-              dense_u(tile, n, hb, x);
+              tc::tl_ldv(A.xst + (size_t)(i - 1) * SBt + g, x);
             } else {
               for (int q = 0; q < tc::kCW; ++q) Y[q] = x[q] = 0.f;
             }

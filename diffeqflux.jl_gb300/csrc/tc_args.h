@@ -49,6 +49,8 @@ struct BwdTcArgs {
   tc::OpList fwops;
   const float* ckcomp;
   float* rep[2];                // replayed state and its compensation (tile layout)
+  float* xst;                   // [6][ntiles * kTileVec] u(t) at the six stage times of the
+                                //   current adjoint step (tile layout)
 };
 
 
