@@ -934,14 +934,18 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   size_t off = 0;
   for (int l = 0; l < L; ++l) {
     const int out = m.dims[l + 1], in = m.dims[l];
-    t.a_isA[l] = in > out ? 1 : 0;
+    // the smaller side is the M side (128-row halves), the larger the N side
+    // (up to 256 columns): fewer, wider products (each tcgen05.mma costs about
+    // the same to issue whatever its N, so two N = 64 ops cost twice one
+    // N = 256 op although they do half its work)
+    t.a_isA[l] = in < out ? 1 : 0;
     const int mside = t.a_isA[l] ? in : out;
     t.nh[l] = (mside + 127) / 128;
     // per 64-trajectory block (2 of them): the M side in 128-row halves of
     // 16 KB per piece, the N side in 64-feature blocks of 8 KB per piece
+    // (one FP16 piece: the epilogue writes the images itself)
     auto img_bytes = [&](int dim, int isA) -> size_t {
-      return isA ? (size_t)2 * t.nh[l] * tc::kImgPieces * 16384
-                 : (size_t)2 * tc::kImgPieces * ((dim + 63) / 64) * 8192;
+      return isA ? (size_t)2 * t.nh[l] * 16384 : (size_t)2 * ((dim + 63) / 64) * 8192;
     };
     t.aoff[l] = (long long)off;
     off += img_bytes(in, t.a_isA[l]);
@@ -1019,17 +1023,17 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   // the five-product form, while the forward needs all five (its error
   // estimate reaches the rounding noise of fewer). The replay list (fwops)
   // keeps five: it must reproduce the forward's steps exactly.
-  for (int l = 0; l < L; ++l) {
+  // The epilogue writes the weight-gradient images (FP16) itself, so the
+  // chain ops copy nothing, and the output layer is not recomputed: the
+  // list is the forward ops of layers 0..L-2, then the VJP ops of L-1..0.
+  for (int l = 0; l < L - 1; ++l) {
     tc::GemmOp& o = t.ops.op[n++];
-    o.kind = (l == L - 1) ? 2 : 0;
+    o.kind = 0;
     o.nprod = 3;
     o.wimg = c->wimg.as<uint8_t>() + c->wimg_off[l];
     o.npad = c->npad[l];
     o.nchunk = c->nchunk[l];
-    o.img_off = (int)t.aoff[l];
-    o.img_isA = (uint8_t)t.a_isA[l];
-    o.img_nblk = (uint8_t)((m.dims[l] + 63) / 64);
-    o.img_nh = (uint16_t)t.nh[l];
+    o.img_off = -1;
   }
   for (int l = L - 1; l >= 0; --l) {
     tc::GemmOp& o = t.ops.op[n++];
@@ -1038,17 +1042,10 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
     o.wimg = c->wimg.as<uint8_t>() + c->wtimg_off[l];
     o.npad = c->npadT[l];
     o.nchunk = c->nchunkT[l];
-    o.img_off = (int)t.doff[l];
-    o.img_isA = (uint8_t)(!t.a_isA[l]);
-    o.img_nblk = (uint8_t)((m.dims[l + 1] + 63) / 64);
-    o.img_nh = (uint16_t)t.nh[l];
+    o.img_off = -1;
   }
   t.ops.nops = n;
-  // re-emission list: the same ops with the forward ones copy-only (their
-  // chunks, stored activations re-emitted by the epilogue, only reach the
-  // images); for an evaluation at the same t and u(t) as the previous one
-  t.ops7 = t.ops;
-  for (int l = 0; l < L; ++l) t.ops7.op[l].kind = 2;
+  t.ops7 = t.ops;  // (unused: an evaluation that reuses activations starts at the VJP ops)
   n = 0;
   t.dw_chunks = 0;
   for (int l = 0; l < L; ++l) {
@@ -1061,14 +1058,16 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
       if (n >= tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
       tc::GemmOp& o = t.dwops.op[n++];
       o.kind = 1;
-      o.aimg = t.img + aimg + (size_t)hh * tc::kImgPieces * 16384;
+      o.aimg = t.img + aimg + (size_t)hh * 16384;
       o.wimg = t.img + bimg;
       o.cta_stride = (size_t)tpc * tc::kImgSlots * t.img_cta;
       o.slot_stride = t.img_cta;
-      o.a_bytes = tc::kImgPieces * 16384;
-      o.a_step = (uint32_t)(t.nh[l] * tc::kImgPieces * 16384);
-      o.b_step = (uint32_t)(tc::kImgPieces * nblk * 8192);
+      o.a_bytes = 16384;
+      o.a_step = (uint32_t)(t.nh[l] * 16384);
+      o.b_step = (uint32_t)(nblk * 8192);
       o.nblk_b = nblk;
+      o.img_pieces = 1;
+      o.img_f16 = 1;
       o.npad = (nside + 15) / 16 * 16;
       o.nchunk = 2 * 6 * tpc;  // K = (tile, stage, 64-trajectory block)
       o.first_dw = 0;
@@ -1121,7 +1120,11 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
   int nblkN[GBNDE_MAX_LAYERS] = {};
   for (int l = 0; l < L; ++l) {
     const int out = m.dims[l + 1], in = m.dims[l];
-    t.a_isA[l] = in > out ? 1 : 0;
+    // the smaller side is the M side (128-row halves), the larger the N side
+    // (up to 256 columns): fewer, wider products (each tcgen05.mma costs about
+    // the same to issue whatever its N, so two N = 64 ops cost twice one
+    // N = 256 op although they do half its work)
+    t.a_isA[l] = in < out ? 1 : 0;
     const int mside = t.a_isA[l] ? in : out;
     t.nh[l] = (mside + 127) / 128;
     nblkN[l] = ((t.a_isA[l] ? out : in) + 63) / 64;

@@ -72,6 +72,11 @@ __device__ __forceinline__ const float* fwd_eval_tile(const BwdArgs& a, int tile
 __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
   extern __shared__ __align__(16) float smem[];
   __shared__ double red[40];
+  // the step's scalars from thread 0 (see StepCtl): stage i's interpolation
+  // weights and forward step, or quadrature point q's
+  __shared__ StepCtl s_ctl;
+  __shared__ float s_hb6[6][7], s_bl4[4][7];
+  __shared__ int s_n6[6];
   const int S = a.S, TM = a.TM, LD = a.LD, G = gridDim.x;
   const bool backsolve = (a.sensealg == GBNDE_SENSE_BACKSOLVE);
   // quadrature adjoint: lam only in the solve, mu by Gauss-Legendre per step
@@ -325,11 +330,27 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
     {
       float* P1 = Pb[iP1];
       for (size_t i = threadIdx.x; i < (size_t)a.P; i += blockDim.x) P1[i] = 0.f;
+      if (threadIdx.x == 0 && !backsolve) {
+        // u(t) weights on thread 0 (FP64), read by all after the barrier
+        const int n = find_step(a, iv, t);
+        const double tn = a.fsteps[2 * n], h = a.fsteps[2 * n + 1];
+        float bw[7];
+        interp_weights((t - tn) / h, bw);
+        for (int q = 0; q < 7; ++q) s_hb6[0][q] = (float)(h * (double)bw[q]);
+        s_n6[0] = n;
+      }
       __syncthreads();
       float hb[7];
       const float* kk[7];
       const float* un = nullptr;
-      if (!backsolve) udense(t, hb, kk, un);
+      if (!backsolve) {
+        const size_t SB = (size_t)S * a.B;
+        un = a.dense ? a.dense + (size_t)s_n6[0] * 8 * SB : a.ibuf + (size_t)(s_n6[0] - iv.nlo) * 8 * SB;
+        for (int q = 0; q < 7; ++q) {
+          hb[q] = s_hb6[0][q];
+          kk[q] = un + (size_t)(q + 1) * SB;
+        }
+      }
       float* lcur = a.lam[cur];
       float* ucurb = a.ub[cur];
       for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
@@ -428,12 +449,46 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
     }
 
     // ---- adaptive steps down to t_lo ----------------------------------------
-    while (t > t_lo) {
+    // The scalar FP64 work of a step (stage times and coefficients, the
+    // forward step and interpolation weights of every stage, the norm's square
+    // root, the PI update) runs on thread 0 and reaches the others through
+    // shared memory; t, dt and qold are thread 0's.
+    auto dense_of = [&](int n) -> const float* {
+      const size_t SB = (size_t)S * a.B;
+      return a.dense ? a.dense + (size_t)n * 8 * SB : a.ibuf + (size_t)(n - iv.nlo) * 8 * SB;
+    };
+    auto dense_weights = [&](double tt, float* hb) -> int {
+      const int n = find_step(a, iv, tt);
+      const double tn = a.fsteps[2 * n], h = a.fsteps[2 * n + 1];
+      float bw[7];
+      interp_weights((tt - tn) / h, bw);
+      for (int q = 0; q < 7; ++q) hb[q] = (float)(h * (double)bw[q]);
+      return n;
+    };
+    for (;;) {
+      if (threadIdx.x == 0) {
+        s_ctl.go = t > t_lo;
+        const double rem = rt32(t - t_lo, a.f32time);
+        s_ctl.clipped = dt >= rem;
+        const double Hs = s_ctl.clipped ? rem : dt;
+        s_ctl.t = t;
+        s_ctl.h = Hs;
+        s_ctl.hf = (float)Hs;
+        if (s_ctl.go) {
+          for (int i = 1; i < 7; ++i) {
+            const double tt = t - c_tab.c[i] * Hs;
+            s_ctl.tst[i] = tt;
+            for (int q = 0; q < 6; ++q) s_ctl.ha[i - 1][q] = (float)(Hs * c_tab.a[i][q]);
+            if (!backsolve) s_n6[i - 1] = dense_weights(tt, s_hb6[i - 1]);
+          }
+          for (int q = 0; q < 7; ++q) s_ctl.hbt[q] = (float)(Hs * c_tab.btilde[q]);
+        }
+      }
+      __syncthreads();
+      if (!s_ctl.go) break;
       if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
       ++iter;
-      const double rem = rt32(t - t_lo, a.f32time);
-      const bool clipped = dt >= rem;
-      const double H = clipped ? rem : dt;
+      const double H = s_ctl.h;
       float* lcur = a.lam[cur];
       float* lnew = a.lam[cur ^ 1];
       float* ucurb = a.ub[cur];
@@ -442,9 +497,9 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       __syncthreads();
       double perr = 0.0;
       for (int i = 1; i < 7; ++i) {
-        const double tt = t - c_tab.c[i] * H;
+        const double tt = s_ctl.tst[i];
         float ha[6];
-        for (int q = 0; q < 6; ++q) ha[q] = (float)(H * c_tab.a[i][q]);
+        for (int q = 0; q < 6; ++q) ha[q] = s_ctl.ha[i - 1][q];
         const float* kl[6];
         const float* ku[6];
         for (int q = 0; q < 6; ++q) {
@@ -454,7 +509,13 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
         float hb[7];
         const float* kk[7];
         const float* un = nullptr;
-        if (!backsolve) udense(tt, hb, kk, un);
+        if (!backsolve) {
+          un = dense_of(s_n6[i - 1]);
+          for (int q = 0; q < 7; ++q) {
+            hb[q] = s_hb6[i - 1][q];
+            kk[q] = un + (size_t)(q + 1) * S * a.B;
+          }
+        }
         float* P = gauss ? nullptr : (i < 6) ? Pmid : Pb[iP7];
         if (i == 6 && P) {
           for (size_t q = threadIdx.x; q < (size_t)a.P; q += blockDim.x) P[q] = 0.f;
@@ -483,7 +544,7 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
           if (i == 6) {
             // error contribution of this tile
             float hbt[7];
-            for (int q = 0; q < 7; ++q) hbt[q] = (float)(H * c_tab.btilde[q]);
+            for (int q = 0; q < 7; ++q) hbt[q] = s_ctl.hbt[q];
             const size_t base = (size_t)tile * TM * S, n = (size_t)nvalid_of(a, tile) * S;
             for (size_t e = threadIdx.x; e < n; e += blockDim.x) {
               const size_t g = base + e;
@@ -509,31 +570,67 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       double* pp = a.partials + (size_t)par * 2 * G;
       if (threadIdx.x == 0) pp[blockIdx.x] = perr;
       if (!grid_barrier(a.bar, gen, a.status)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
-      const double eest = rt32(sqrt(grid_partials_sum(pp, G, red) / Nnorm), a.f32time);
+      {
+        const double qe = grid_partials_sum(pp, G, red);
+        if (threadIdx.x == 0) {
+          const double eest = rt32(sqrt(qe / Nnorm), a.f32time);
+          s_ctl.ret = GBNDE_RET_SUCCESS;
+          s_ctl.accept = 0;
+          if (!isfinite(eest)) {
+            s_ctl.ret = GBNDE_RET_UNSTABLE;
+          } else {
+            double q11;
+            double q = pi_q(eest, qold, &q11);
+            if (eest <= 1.0) {
+              s_ctl.accept = 1;
+              if (gauss) {
+                // the quadrature points of the step: u(t) weights and lam's
+                // interpolant weights
+                const double gth[4] = {0.06943184420297371, 0.33000947820757187, 0.6699905217924281,
+                                       0.9305681557970262};
+                const double gw[4] = {0.17392742256872679, 0.3260725774312732, 0.3260725774312732,
+                                      0.17392742256872679};
+                for (int gq = 0; gq < 4; ++gq) {
+                  const double tt = t - gth[gq] * H;
+                  s_ctl.tst[gq] = tt;
+                  float bl[7];
+                  interp_weights(gth[gq], bl);
+                  for (int q2 = 0; q2 < 7; ++q2) s_bl4[gq][q2] = (float)(H * (double)bl[q2]);
+                  s_ctl.hb[gq] = (float)(H * gw[gq]);
+                  s_n6[gq] = dense_weights(tt, s_hb6[gq]);
+                }
+              }
+              t = s_ctl.clipped ? t_lo : rt32(t - H, a.f32time);
+              if (q >= 1.0 && q <= 1.0) q = 1.0;
+              qold = rt32(fmax(eest, kQoldInit), a.f32time);
+              dt = rt32(fmin(H / q, a.dtmax), a.f32time);
+            } else {
+              dt = rt32(H / fmin(1.0 / kQmin, q11 / kGamma), a.f32time);
+            }
+          }
+        }
+        __syncthreads();
+      }
       par ^= 1;
-      if (!isfinite(eest)) { ret = GBNDE_RET_UNSTABLE; break; }
-      double q11;
-      double q = pi_q(eest, qold, &q11);
-      if (eest <= 1.0) {
+      if (s_ctl.ret != GBNDE_RET_SUCCESS) { ret = s_ctl.ret; break; }
+      if (s_ctl.accept) {
         if (gauss) {
           // mu += int over the step of lam^T df/dp: 4-point Gauss-Legendre on
           // [t - H, t], lam(theta) = lam_n + H sum_j b_j(theta) k_j from this
           // step's stages (the free interpolant), u from the forward
-          const double gth[4] = {0.06943184420297371, 0.33000947820757187, 0.6699905217924281,
-                                 0.9305681557970262};
-          const double gw[4] = {0.17392742256872679, 0.3260725774312732, 0.3260725774312732,
-                                0.17392742256872679};
           const float* kl7[7];
           for (int q = 0; q < 7; ++q) kl7[q] = klb(q);
           for (int gq = 0; gq < 4; ++gq) {
-            const double tt = t - gth[gq] * H;
+            const double tt = s_ctl.tst[gq];
             float bl[7];
-            interp_weights(gth[gq], bl);
-            for (int q = 0; q < 7; ++q) bl[q] = (float)(H * (double)bl[q]);
+            for (int q = 0; q < 7; ++q) bl[q] = s_bl4[gq][q];
             float hb[7];
             const float* kk[7];
-            const float* un = nullptr;
-            udense(tt, hb, kk, un);
+            const float* un = dense_of(s_n6[gq]);
+            for (int q = 0; q < 7; ++q) {
+              hb[q] = s_hb6[gq][q];
+              kk[q] = un + (size_t)(q + 1) * S * a.B;
+            }
             for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
               adj_eval(tile, tt, iv,
                        [&](size_t g) {
@@ -546,14 +643,14 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
                          for (int q = 0; q < 7; ++q) acc = fmaf(hb[q], kk[q][g], acc);
                          return un[g] + acc;
                        },
-                       nullptr, nullptr, mu_acc, (float)(H * gw[gq]), nullptr, nullptr);
+                       nullptr, nullptr, mu_acc, s_ctl.hb[gq], nullptr, nullptr);
             }
             ++nf_adj;
           }
           __syncthreads();
         } else {
           // mu += H * (P1 + Pmid)
-          const float Hf = (float)H;
+          const float Hf = s_ctl.hf;
           const float* P1 = Pb[iP1];
           for (size_t i = threadIdx.x; i < (size_t)a.P; i += blockDim.x)
             mu_acc[i] = fmaf(Hf, P1[i] + Pmid[i], mu_acc[i]);
@@ -565,13 +662,8 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
         ++nacc;
         cur ^= 1;
         swp = !swp;
-        t = clipped ? t_lo : rt32(t - H, a.f32time);
-        if (q >= 1.0 && q <= 1.0) q = 1.0;
-        qold = rt32(fmax(eest, kQoldInit), a.f32time);
-        dt = rt32(fmin(H / q, a.dtmax), a.f32time);
       } else {
         ++nrej;
-        dt = rt32(H / fmin(1.0 / kQmin, q11 / kGamma), a.f32time);
       }
     }
     if (ret != GBNDE_RET_SUCCESS) break;

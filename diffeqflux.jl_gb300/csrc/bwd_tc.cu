@@ -39,6 +39,8 @@
 // bit-identical -- into the interval buffer b.ibuf, which u(t) is then
 // interpolated from. Each CTA reads only its own tiles, so no grid-wide sync
 // is needed between the replay and the adjoint steps.
+#include <cuda_fp16.h>
+
 #include "tc_args.h"
 
 namespace gbnde {
@@ -163,6 +165,36 @@ __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* a
   return true;
 }
 
+// This thread's kCW columns (trajectory row r, column group ch) of K chunk cc
+// (64 features) of a weight-gradient operand image, as FP16 times `scale`.
+// The image is made of 8 KB blocks of 64 trajectories x 64 features (128-byte
+// rows, SW128 swizzle), arranged as the weight-gradient ops read them: on the M
+// side [trajectory block][128-row half][two 64-feature blocks], on the N side
+// [trajectory block][64-feature block]. Streaming stores (the step's commit
+// reads them once). Returns false if a value does not fit FP16.
+__device__ __forceinline__ bool img_put_f16(uint8_t* base, int isA, int nh, int nblk, int cc, int r, int ch,
+                                            const float* v, float scale) {
+  const int kc = r >> 6, rr = r & 63;
+  const size_t blk = isA ? (size_t)(kc * nh + (cc >> 1)) * 16384 + (size_t)(cc & 1) * 8192
+                         : (size_t)(kc * nblk + cc) * 8192;
+  uint8_t* p = base + blk;
+  bool fine = true;
+#pragma unroll
+  for (int j = 0; j < tc::kCW / 8; ++j) {
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float a0 = v[8 * j + 2 * i] * scale, a1 = v[8 * j + 2 * i + 1] * scale;
+      fine = fine && fabsf(a0) <= 65504.f && fabsf(a1) <= 65504.f;
+      const __half2 h2 = __floats2half2_rn(a0, a1);
+      w[i] = *reinterpret_cast<const uint32_t*>(&h2);
+    }
+    __stcs(reinterpret_cast<uint4*>(p + tc::sw128_offset(rr, (tc::kCW / 8) * ch + j)),
+           make_uint4(w[0], w[1], w[2], w[3]));
+  }
+  return fine;
+}
+
 // Column sums over the warp's 32 trajectory rows of kCW values per lane:
 // after the butterfly, lane j holds the sum of value j % kCW over the 32 lanes.
 __device__ __forceinline__ float warp_colsum(float* v, int lane) {
@@ -195,7 +227,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
   // and the error weights h btilde_j
   __shared__ float s_ha[6][6], s_hb[6][7], s_hbt[7];
   __shared__ int s_n[6];
-  __shared__ tc::StepCtl s_ctl;
+  __shared__ StepCtl s_ctl;
   const BwdArgs& a = A.b;
   const int warp = threadIdx.x >> 5;
 
@@ -239,6 +271,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // slots 1..5, stage 7 in slot 6 - fs (stage 1 of the next step)
     uint8_t* img = A.img + (size_t)blockIdx.x * A.tpc * tc::kImgSlots * A.img_cta;
     int fs = 0;
+    // scale of the cotangent images over the current save interval (a power
+    // of two, inv_isc its inverse) and whether an image value overflowed FP16
+    float isc = 1.f, inv_isc = 1.f;
     float4* hs4 = reinterpret_cast<float4*>(A.hscr + (size_t)blockIdx.x * tc::kEpiThreads * A.hvals);
     float* mu_acc = a.mu_acc + (size_t)blockIdx.x * a.P;
     float* mu_comp = A.mu_comp + (size_t)blockIdx.x * a.P;
@@ -297,22 +332,40 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // lam_in: stage input lam (own components), x: u(t) (own components).
     // slot: image slot of the stage's weight-gradient operands (-1: none);
     // P/c: pending bias quadrature buffer and the stage weight (P == nullptr:
-    // no quadrature). The cotangent images carry the weight c.
+    // no quadrature). The cotangent images carry the weight c and the
+    // interval's scale isc.
     // vjp_only: the activations of u(t) are those of the previous evaluation
     // (same t and u, in the activation scratch, and their images already in
     // `slot`): only the VJP ops run (x is not read).
     // reemit: the previous evaluation was at the same t and u(t) (Tsit5's
-    // stages 6 and 7 share c = 1): x and the stored activations are emitted
-    // again, only to reach this stage's images, instead of being recomputed.
+    // stages 6 and 7 share c = 1): the activation images of this stage are
+    // written from x and the stored activations instead of being recomputed,
+    // and only the VJP ops run.
     // tile: the tile being evaluated (its index within the CTA selects the
     // CTA's image set for that tile).
+    // The weight-gradient images (FP16, one piece) are written here, with
+    // plain stores, as each operand chunk is formed: a_0 = x (or x^3) and the
+    // recomputed activations a_1 .. a_{L-1}, and the cotangents delta_L ..
+    // delta_1. a_{L-1} feeds no GEMM of the evaluation (the output layer is
+    // not recomputed), so it only goes to its image.
     auto adj_eval = [&](const float* lam_in, const float* x, int slot, float* P, float c, float* kl,
                         bool vjp_only, int tile, bool reemit) -> bool {
       const uint32_t tj = (uint32_t)((tile - (int)blockIdx.x) / G);
+      const bool skip_fwd = vjp_only || reemit;
       if (threadIdx.x == 0 &&
-          !tc::epi_post(cmdp, sh, (reemit ? tc::CMD_EVAL_RE : tc::CMD_EVAL) | ((uint32_t)(slot + 1) << 8) |
-                                      ((vjp_only ? (uint32_t)L : 0u) << 16) | (tj << 24)))
+          !tc::epi_post(cmdp, sh, tc::CMD_EVAL | ((uint32_t)(slot + 1) << 8) |
+                                      ((skip_fwd ? (uint32_t)(L - 1) : 0u) << 16) | (tj << 24)))
         return false;
+      uint8_t* simg = slot >= 0 ? img + ((size_t)tj * tc::kImgSlots + slot) * A.img_cta : nullptr;
+      // image chunk cc of operand a_l (act = 1) or delta_{l+1} (act = 0) of layer l
+      auto put = [&](int l, bool act, int cc, const float* val, float scale) {
+        if (!simg) return;
+        const int isA = act ? A.a_isA[l] : !A.a_isA[l];
+        const int dim = act ? m.dims[l] : m.dims[l + 1];
+        if (!img_put_f16(simg + (act ? A.aoff[l] : A.doff[l]), isA, A.nh[l], (dim + 63) / 64, cc, th.r, th.ch,
+                         val, scale))
+          atomicExch(&a.status[3], 1);  // seen by CTA 0 after the last grid barrier
+      };
       float v[tc::kCW];
       if (reemit && !vjp_only) {
 #pragma unroll
@@ -320,12 +373,12 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           const float y = (i < th.nmine) ? x[i] : 0.f;
           v[i] = m.cube ? y * y * y : y;
         }
-        if (!emit(es, sh, aring, th, v)) return false;
+        put(0, true, 0, v, 1.f);
         for (int l = 0; l < L - 1; ++l) {
           const int nch = (m.dims[l + 1] + 63) / 64;
           for (int cc = 0; cc < nch; ++cc) {
             hs_ldv(hs4, (A.hoff[l + 1] + tc::kCW * cc) / 4, v);
-            if (!emit(es, sh, aring, th, v)) return false;
+            put(l + 1, true, cc, v, 1.f);
           }
         }
       } else if (!vjp_only) {
@@ -337,6 +390,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       }
       if (m.cube) hs_stv(hs4, A.hx / 4, x);  // for the chain rule through x^3 at the end
       if (!emit(es, sh, aring, th, v)) return false;
+      put(0, true, 0, v, 1.f);
       // forward recompute of the hidden layers
       for (int l = 0; l < L - 1; ++l) {
         const int N = m.dims[l + 1];
@@ -353,21 +407,20 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
           tc::bias_act_cw(v, bc, m.act[l], n0, N);
           hs_stv(hs4, (A.hoff[l + 1] + tc::kCW * cc) / 4, v);
-          if (!emit(es, sh, aring, th, v)) return false;
+          if (l + 1 < L - 1 && !emit(es, sh, aring, th, v)) return false;
+          put(l + 1, true, cc, v, 1.f);
         }
         tc::epi_release_acc(es, sh);
       }
       }
-      // a_{L-1} went through the ring only to reach its image (a copy-only
-      // op: no product, nothing to wait for)
       // delta_L = c lam (identity output layer). The VJP chain is linear in
-      // its input, so every cotangent below carries the stage weight c: the
-      // chain chunks double as the weight-gradient images, and kl is divided
-      // by c at the end.
+      // its input, so every cotangent below carries the stage weight c (and
+      // the images the scale isc), and kl is divided by c at the end.
       const float cs = P ? c : 1.f;
 #pragma unroll
       for (int i = 0; i < tc::kCW; ++i) v[i] = (i < th.nmine) ? cs * lam_in[i] : 0.f;
       if (!emit(es, sh, aring, th, v)) return false;
+      put(L - 1, false, 0, v, isc);
       if (P) {
         float w[tc::kCW];
 #pragma unroll
@@ -390,6 +443,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
           tc::deriv_mul_cw(v, h, m.act[l - 1], n0, N);
           if (!emit(es, sh, aring, th, v)) return false;
+          put(l - 1, false, cc, v, isc);
           if (P) {
             const float s = warp_colsum(v, th.lane);
             if (th.lane < tc::kCW) tc::red_add(P + th.q * A.nbias + A.boffp[l - 1] + n0 + th.lane, s);
@@ -426,7 +480,12 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       cmp = (t2 - acc) - y;
       acc = t2;
     };
-    auto commit_step = [&](float Hf) -> bool {
+    auto commit_step = [&](float Hf0) -> bool {
+      // the images' FP16 writes are complete and ordered before the
+      // producer's bulk loads of them (async proxy)
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+      // the cotangent images carry the interval's scale isc (a power of two)
+      const float Hf = Hf0 * inv_isc;
       tc::epi_bar();
       if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_DW | ((uint32_t)fs << 8))) return false;
       tc::epi_skip_a(es, A.dw_chunks);
@@ -515,7 +574,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         const int o = f - A.boffp[l];
         if (o < m.dims[l + 1])
           kahan(mu_acc[m.boff[l] + o], mu_comp[m.boff[l] + o],
-                Hf * ((((__ldcg(P1 + f) + __ldcg(P1 + A.nbias + f)) + __ldcg(P1 + 2 * A.nbias + f)) +
+                Hf0 * ((((__ldcg(P1 + f) + __ldcg(P1 + A.nbias + f)) + __ldcg(P1 + 2 * A.nbias + f)) +
                        __ldcg(P1 + 3 * A.nbias + f)) +
                       (((__ldcg(Pmid + f) + __ldcg(Pmid + A.nbias + f)) + __ldcg(Pmid + 2 * A.nbias + f)) +
                        __ldcg(Pmid + 3 * A.nbias + f))));
@@ -715,6 +774,40 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       if (!a.dense) {
         nlo_cur = iv.nlo;
         if (!replay(iv)) { ok = false; break; }
+      }
+      // ---- the interval's image scale: the power of two that takes this
+      // CTA's largest |lam| (after the jump) into [2^7, 2^8). FP16 reaches
+      // 2^16, which leaves the cotangents of the inner layers and lam's
+      // growth over the interval 256x; values below 2^-22 of the largest
+      // keep full precision. A value that does not fit ends the solve with
+      // an error instead of a wrong gradient.
+      {
+        float mx = 0.f;
+        for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
+          if (!valid(tile)) continue;
+          float lv[tc::kCW];
+          tc::tl_ldv(a.lam[cur] + tofs(tile), lv);
+#pragma unroll
+          for (int i = 0; i < tc::kCW; ++i)
+            if (i < th.nmine) mx = fmaxf(mx, fabsf(lv[i]));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (th.lane == 0) sh.red[warp] = (double)mx;
+        tc::epi_bar();
+        if (threadIdx.x == 0) {
+          float m2 = 0.f;
+          for (int w = 0; w < tc::kEpiWarps; ++w) m2 = fmaxf(m2, (float)sh.red[w]);
+          int e = 0;
+          if (m2 > 0.f && isfinite(m2)) {
+            frexpf(m2, &e);  // m2 in [2^(e-1), 2^e)
+            e = 8 - e;
+          }
+          s_ctl.exact = max(-120, min(120, e));
+        }
+        tc::epi_bar();
+        isc = ldexpf(1.f, s_ctl.exact);
+        inv_isc = ldexpf(1.f, -s_ctl.exact);
       }
       // ---- FSAL stage at the interval start: kl1 and P1 = b1 * mu ----
       {
@@ -1045,6 +1138,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       a.counters[CT_NREJECT] = nrej;
       a.counters[CT_NRECOMP] = nf_rec;
       const int e = ((volatile int*)&sh.err)[0];
+      // a weight-gradient image value that did not fit FP16 (status word 3,
+      // set before the solve's last grid barrier) makes the gradient invalid
+      if (ret == GBNDE_RET_SUCCESS && ((volatile int*)a.status)[3] != 0) ret = GBNDE_RET_UNSTABLE;
       a.status[ST_RETCODE] = (a.status[ST_BARRIER] != 0 || e != 0) ? GBNDE_RET_BARRIER_TIMEOUT : ret;
       if (e) a.status[2] = e;
     }

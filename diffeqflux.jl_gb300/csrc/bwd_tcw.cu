@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
   __shared__ int s_ok;
   __shared__ float s_ha[6][6], s_hb[6][7], s_hbt[7];
   __shared__ int s_n[6];
-  __shared__ tc::StepCtl s_ctl;
+  __shared__ StepCtl s_ctl;
   const BwdTcArgs& A = W.t;
   const BwdArgs& a = A.b;
   const int warp = threadIdx.x >> 5;

@@ -154,6 +154,18 @@ __device__ __forceinline__ double grid_partials_sum(const double* partials, int 
 // the error estimate and qold are kept as Float32 values), else unchanged.
 __device__ __forceinline__ double rt32(double x, int on) { return on ? (double)(float)x : x; }
 
+// The step controller's scalar FP64 work (step size, stage coefficients and
+// times, the norm's square root, the PI update, save weights) runs on one
+// thread of a CTA: FP64 executes at a small fraction of the FP32 rate on this
+// GPU, and every warp of the CTA would repeat it. The results reach the other
+// threads through this block of shared memory, read after a barrier.
+struct StepCtl {
+  double t, h, habs, tnew, d1, dt0;
+  double tst[7];  // stage times (tst[0]: the initial step's probe time)
+  float ha[6][6], hbt[7], hb[7], hf;
+  int go, clipped, accept, ret, nsv, need_ckpt, exact;
+};
+
 // PI controller (FP64). Returns q, writes q11.
 __device__ __forceinline__ double pi_q(double eest, double qold, double* q11) {
   if (eest == 0.0) {

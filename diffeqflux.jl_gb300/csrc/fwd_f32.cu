@@ -147,6 +147,7 @@ __device__ __forceinline__ void rhs_tile(const FwdArgs& a, int tile, float* smem
 __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
   extern __shared__ __align__(16) float smem[];
   __shared__ double red[40];
+  __shared__ StepCtl s_ctl;  // the step's scalars from thread 0
   const int G = gridDim.x;
   const double N = (double)a.S * (double)a.B;
   const double tdir = a.t1 >= a.t0 ? 1.0 : -1.0;
@@ -241,31 +242,47 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
   }
 
   // ---- step loop ------------------------------------------------------------
+  // The scalar FP64 work of a step (step size, stage coefficients and times,
+  // the norm's square root, the PI update, save weights) runs on thread 0 and
+  // reaches the others through shared memory; t, dt and qold are thread 0's.
   {
     double t = a.t0, qold = kQoldInit;
     long long iter = 0;
     int ib = 0, nck = 0;
-    while (tdir * (a.t1 - t) > 0.0) {
+    for (;;) {
+      if (threadIdx.x == 0) {
+        s_ctl.go = tdir * (a.t1 - t) > 0.0;
+        const double rem = rt32(fabs(a.t1 - t), f32t);
+        s_ctl.clipped = dt >= rem;
+        s_ctl.habs = s_ctl.clipped ? rem : dt;
+        const double h = tdir * s_ctl.habs;
+        s_ctl.t = t;
+        s_ctl.h = h;
+        for (int i = 1; i < 7; ++i) {
+          for (int j = 0; j < 6; ++j) s_ctl.ha[i - 1][j] = (float)(h * c_tab.a[i][j]);
+          s_ctl.tst[i] = t + c_tab.c[i] * h;
+        }
+        for (int j = 0; j < 7; ++j) s_ctl.hbt[j] = (float)(h * c_tab.btilde[j]);
+      }
+      __syncthreads();
+      if (!s_ctl.go) break;
       if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
       ++iter;
-      const double rem = rt32(fabs(a.t1 - t), f32t);
-      const bool clipped = dt >= rem;
-      const double habs = clipped ? rem : dt;
-      const double h = tdir * habs;
       float* ucur = a.ubuf[cur];
       float* unew = a.ubuf[cur ^ 1];
       double perr = 0.0;
       for (int i = 1; i < 7; ++i) {
         float ha[6];
 #pragma unroll
-        for (int j = 0; j < 6; ++j) ha[j] = (float)(h * c_tab.a[i][j]);
+        for (int j = 0; j < 6; ++j) ha[j] = s_ctl.ha[i - 1][j];
         const float* kj[6];
 #pragma unroll
         for (int j = 0; j < 6; ++j) kj[j] = kb(a, j, swp);
         float* ki = kb(a, i, swp);
         float hbt[7];
 #pragma unroll
-        for (int j = 0; j < 7; ++j) hbt[j] = (float)(h * c_tab.btilde[j]);
+        for (int j = 0; j < 7; ++j) hbt[j] = s_ctl.hbt[j];
+        const double ts = s_ctl.tst[i];
         for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
           auto stage_in = [&](size_t g) {
             float s = 0.f;
@@ -275,9 +292,9 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
             return y;
           };
           if (i < 6) {
-            rhs_tile(a, tile, smem, t + c_tab.c[i] * h, stage_in, [&](size_t g, float v) { ki[g] = v; });
+            rhs_tile(a, tile, smem, ts, stage_in, [&](size_t g, float v) { ki[g] = v; });
           } else {
-            rhs_tile(a, tile, smem, t + c_tab.c[i] * h, stage_in, [&](size_t g, float v) {
+            rhs_tile(a, tile, smem, ts, stage_in, [&](size_t g, float v) {
               ki[g] = v;
               float ut = hbt[6] * v;
 #pragma unroll
@@ -295,35 +312,81 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
       double* pp = a.partials + (size_t)par * 2 * G;
       if (threadIdx.x == 0) pp[blockIdx.x] = perr;
       if (!grid_barrier(a.bar, gen, a.status)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
-      const double eest = rt32(sqrt(grid_partials_sum(pp, G, red) / N), f32t);
-      par ^= 1;
-      if (!isfinite(eest)) { ret = GBNDE_RET_UNSTABLE; break; }
-      double q11;
-      double q = pi_q(eest, qold, &q11);
-      if (blockIdx.x == 0 && threadIdx.x == 0 && iter - 1 < a.maxsteps) {
-        double* tr = a.trace + 4 * (iter - 1);
-        tr[0] = t;
-        tr[1] = h;
-        tr[2] = eest;
-        tr[3] = eest <= 1.0 ? 1.0 : 0.0;
+      {
+        const double qe = grid_partials_sum(pp, G, red);
+        if (threadIdx.x == 0) {
+          const double eest = rt32(sqrt(qe / N), f32t);
+          const double h = s_ctl.h, habs = s_ctl.habs;
+          s_ctl.ret = GBNDE_RET_SUCCESS;
+          s_ctl.accept = 0;
+          if (!isfinite(eest)) {
+            s_ctl.ret = GBNDE_RET_UNSTABLE;
+          } else {
+            double q11;
+            double q = pi_q(eest, qold, &q11);
+            if (blockIdx.x == 0 && iter - 1 < a.maxsteps) {
+              double* tr = a.trace + 4 * (iter - 1);
+              tr[0] = t;
+              tr[1] = h;
+              tr[2] = eest;
+              tr[3] = eest <= 1.0 ? 1.0 : 0.0;
+            }
+            if (eest <= 1.0) {
+              const double tnew = s_ctl.clipped ? a.t1 : rt32(t + h, f32t);
+              s_ctl.accept = 1;
+              s_ctl.tnew = tnew;
+              int ns = 0;
+              while (isave + ns < a.nsave && tdir * (a.saveat[isave + ns] - tnew) <= 0.0) ++ns;
+              s_ctl.nsv = ns;
+              bool need = false;
+              while (ib < a.nbnd && tdir * (a.bnd[ib] - tnew) < 0.0) { need = true; ++ib; }
+              s_ctl.need_ckpt = need;
+              if (blockIdx.x == 0 && naccept < a.maxsteps) {
+                a.steplog[2 * naccept] = t;
+                a.steplog[2 * naccept + 1] = h;
+              }
+              t = tnew;
+              if (q >= 1.0 && q <= 1.0) q = 1.0;
+              qold = rt32(fmax(eest, kQoldInit), f32t);
+              dt = rt32(fmax(fmin(habs / q, a.dtmax), a.dtmin), f32t);
+            } else {
+              dt = rt32(habs / fmin(1.0 / kQmin, q11 / kGamma), f32t);
+              if (a.dtmin > 0.0 && dt <= a.dtmin) s_ctl.ret = GBNDE_RET_DTLESSTHANMIN;
+            }
+          }
+        }
+        __syncthreads();
       }
-      if (eest <= 1.0) {
-        const double tnew = clipped ? a.t1 : rt32(t + h, f32t);
+      par ^= 1;
+      if (s_ctl.ret != GBNDE_RET_SUCCESS) {
+        ret = s_ctl.ret;
+        if (ret == GBNDE_RET_DTLESSTHANMIN) ++nreject;
+        break;
+      }
+      if (s_ctl.accept) {
         // saveat points in (t, tnew]
-        while (isave < a.nsave && tdir * (a.saveat[isave] - tnew) <= 0.0) {
-          const double s = a.saveat[isave];
+        const int nsv = s_ctl.nsv;
+        for (int k = 0; k < nsv; ++k, ++isave) {
+          if (threadIdx.x == 0) {
+            const double sv = a.saveat[isave];
+            s_ctl.exact = sv == s_ctl.tnew;
+            if (!s_ctl.exact) {
+              float bw[7];
+              interp_weights((sv - s_ctl.t) / s_ctl.h, bw);
+              for (int j = 0; j < 7; ++j) s_ctl.hb[j] = (float)(s_ctl.h * (double)bw[j]);
+            }
+          }
+          __syncthreads();
           float* dst = a.usave + (size_t)isave * a.S * a.B;
-          if (s == tnew) {
+          if (s_ctl.exact) {
             for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
               const size_t base = (size_t)tile * a.TM * a.S, n = tile_elems(a, tile);
               for (size_t e = threadIdx.x; e < n; e += blockDim.x) dst[base + e] = unew[base + e];
             }
           } else {
-            float bw[7];
-            interp_weights((s - t) / h, bw);
             float hb[7];
 #pragma unroll
-            for (int j = 0; j < 7; ++j) hb[j] = (float)(h * (double)bw[j]);
+            for (int j = 0; j < 7; ++j) hb[j] = s_ctl.hb[j];
             const float* kk[7];
 #pragma unroll
             for (int j = 0; j < 7; ++j) kk[j] = kb(a, j, swp);
@@ -338,12 +401,10 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
               }
             }
           }
-          ++isave;
+          __syncthreads();  // s_ctl.hb is rewritten for the next save
         }
         // checkpoint the state at the start of this step if it holds a boundary
-        bool need = false;
-        while (ib < a.nbnd && tdir * (a.bnd[ib] - tnew) < 0.0) { need = true; ++ib; }
-        if (need && nck < a.max_ckpt) {
+        if (s_ctl.need_ckpt && nck < a.max_ckpt) {
           float* dst = a.ckpt + (size_t)nck * a.S * a.B;
           for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
             const size_t base = (size_t)tile * a.TM * a.S, n = tile_elems(a, tile);
@@ -351,10 +412,6 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
           }
           if (blockIdx.x == 0 && threadIdx.x == 0) a.ckpt_step[nck] = (int)naccept;
           ++nck;
-        }
-        if (blockIdx.x == 0 && threadIdx.x == 0 && naccept < a.maxsteps) {
-          a.steplog[2 * naccept] = t;
-          a.steplog[2 * naccept + 1] = h;
         }
         ++naccept;
         if (a.dense) {
@@ -373,14 +430,8 @@ __global__ void __launch_bounds__(256, 1) fwd_f32_kernel(FwdArgs a) {
           swp = !swp;
         }
         cur ^= 1;
-        t = tnew;
-        if (q >= 1.0 && q <= 1.0) q = 1.0;
-        qold = rt32(fmax(eest, kQoldInit), f32t);
-        dt = rt32(fmax(fmin(habs / q, a.dtmax), a.dtmin), f32t);
       } else {
         ++nreject;
-        dt = rt32(habs / fmin(1.0 / kQmin, q11 / kGamma), f32t);
-        if (a.dtmin > 0.0 && dt <= a.dtmin) { ret = GBNDE_RET_DTLESSTHANMIN; break; }
       }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {

@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) fwd_tcw_kernel(FwdTcwArgs A) 
   uint8_t* wring = smem + tc::kARing * tc::kASlotBytes;
   __shared__ tc::Shared sh;
   __shared__ int s_ok;
-  __shared__ tc::StepCtl s_ctl;
+  __shared__ StepCtl s_ctl;
   const FwdArgs& a = A.t.f;
   const int warp = threadIdx.x >> 5;
 

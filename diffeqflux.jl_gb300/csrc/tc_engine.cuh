@@ -134,6 +134,11 @@ struct GemmOp {
   // kind 0 / 3: split products issued: 0 (all five) or 3 (A_hi W_hi +
   // A_mid W_hi + A_hi W_lo, about 16 bits of both operands)
   int nprod;
+  // kind 1: pieces per image chunk (0: kImgPieces, BF16 copies of the chain
+  // chunks) and whether the images are FP16 (one piece, written by the
+  // epilogue: one FP16 product)
+  int img_pieces;
+  int img_f16;
 };
 
 struct OpList {
@@ -180,17 +185,6 @@ __device__ __forceinline__ double epi_sum(double v, Shared& sh) {
   epi_bar();
   return s;
 }
-
-// The step controller's scalar FP64 work runs on epilogue thread 0 (FP64
-// executes at a small fraction of the FP32 rate on this GPU, and every
-// epilogue warp would repeat it); the results reach the other threads through
-// this block of shared memory, read after an epi_bar.
-struct StepCtl {
-  double t, h, habs, tnew, d1, dt0;
-  double tst[7];  // stage times (tst[0]: the initial step's probe time)
-  float ha[6][6], hbt[7], hb[7], hf;
-  int go, clipped, accept, ret, nsv, need_ckpt, exact;
-};
 
 // Sum of one float per epilogue thread, valid in epilogue thread 0 only:
 // FP32 within each warp (fixed shuffle order), FP64 over the warps.
@@ -378,7 +372,9 @@ __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh
   }
   const uint32_t d = sh.tmem_base + (uint32_t)(reg * 256);
   const bool chain = op.kind == 0 || op.kind == 3;  // K-major chain GEMM (five split products)
-  const uint32_t idesc = chain ? idesc_bf16(128, op.npad) : idesc_bf16_mn(128, op.npad);
+  const uint32_t idesc = chain ? idesc_bf16(128, op.npad)
+                               : (op.img_f16 ? idesc_f16_mn(128, op.npad) : idesc_bf16_mn(128, op.npad));
+  const int wg_products = (op.img_pieces ? op.img_pieces : kImgPieces) == 2 ? 3 : 1;
   const uint32_t wpiece = chain ? (uint32_t)op.npad * 128 : (uint32_t)op.nblk_b * 8192;
   for (int c = 0; c < op.nchunk; ++c) {
     // A chunk ready? (bounded by the stop flag: the epilogue may be done)
@@ -414,7 +410,8 @@ __device__ __forceinline__ bool mma_op(const GemmOp& op, MmaState& m, Shared& sh
         // 8 KB. Products hi.hi (and hi.lo, lo.hi with two pieces); K step of
         // 16 trajectories = 2048 bytes.
 #pragma unroll
-        for (int pr = 0; pr < (kImgPieces == 2 ? 3 : 1); ++pr) {
+        for (int pr = 0; pr < 3; ++pr) {
+          if (pr >= wg_products) break;
           const int qa = (pr == 2) ? 1 : 0, qb = (pr == 1) ? 1 : 0;
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
@@ -576,8 +573,9 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
     ++t.g;
     return true;
   }
+  const uint32_t ipieces = op.img_pieces ? (uint32_t)op.img_pieces : (uint32_t)kImgPieces;
   const uint32_t bbytes =
-      op.kind == 0 ? 2u * (uint32_t)op.npad * 128u : (uint32_t)kImgPieces * (uint32_t)op.nblk_b * 8192u;
+      op.kind == 0 ? 2u * (uint32_t)op.npad * 128u : ipieces * (uint32_t)op.nblk_b * 8192u;
   const uint8_t* bbase = op.kind == 0 ? op.wimg : op.wimg + (size_t)blockIdx.x * op.cta_stride;
   const uint8_t* abase = op.kind == 0 ? nullptr : op.aimg + (size_t)blockIdx.x * op.cta_stride;
   if (op.kind == 1 && op.first_dw) {
@@ -617,8 +615,8 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
       mbar_arrive_expect_tx(&sh.w_full[t.wslot], bbytes);
       if (op.kind == 1 && op.b_pstride != 0) {
         // one N-block of the B image: its blocks in each piece
-        const uint32_t part = bbytes / kImgPieces;
-        for (int q = 0; q < kImgPieces; ++q)
+        const uint32_t part = bbytes / ipieces;
+        for (uint32_t q = 0; q < ipieces; ++q)
           bulk_g2s(wring + t.wslot * kWSlotBytes + q * part, bbase + boff + op.b_off0 + (size_t)q * op.b_pstride,
                    part, &sh.w_full[t.wslot]);
       } else {

@@ -158,6 +158,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16_mn(int M, int N) {
   return idesc_bf16(M, N) | (1u << 15) | (1u << 16);
 }
 
+// kind::f16 with FP16 operands (A = B = F16, format code 0), both MN-major.
+__host__ __device__ constexpr uint32_t idesc_f16_mn(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24) | (1u << 15) | (1u << 16);
+}
+
 // ---- MMA --------------------------------------------------------------------------
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
                                          uint32_t idesc, uint32_t accumulate) {
