@@ -140,15 +140,21 @@ __device__ __forceinline__ double epi_partials_sum(const double* p, int n, tc::S
   return v;
 }
 
-// kCW values of this thread's row into the next chain A chunk (3 split
-// pieces). The MMA warp also copies the chunk's first two pieces to the
-// stage's weight-gradient image when the op asks for it.
+// kCW values of this thread's row into the next chain A chunk (split BF16
+// pieces) of the shared-memory ring.
+// NP = 3: all three pieces (the forward list's five products); NP = 2: hi and
+// mid only, for chunks that only three-product GEMMs read (the adjoint's
+// chains), whose lo piece is never loaded.
+template <int NP = 3>
 __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* aring, const Thr& th,
                                      const float* x) {
   constexpr int nu = tc::kCW / 8;  // 16-byte units per piece
   uint4 hi[nu], mid[nu], lo[nu];
 #pragma unroll
-  for (int j = 0; j < nu; ++j) tc::split3_bf16(x + 8 * j, hi[j], mid[j], lo[j]);
+  for (int j = 0; j < nu; ++j) {
+    if constexpr (NP == 3) tc::split3_bf16(x + 8 * j, hi[j], mid[j], lo[j]);
+    else tc::split2_bf16(x + 8 * j, hi[j], mid[j]);
+  }
   {
     if (!tc::mbar_wait(&sh.a_empty[e.aslot], e.aph ^ 1, &sh.err)) return false;
     uint8_t* base = aring + e.aslot * tc::kASlotBytes;
@@ -157,7 +163,7 @@ __device__ __forceinline__ bool emit(tc::EpiState& e, tc::Shared& sh, uint8_t* a
       const uint32_t off = tc::sw128_offset(th.r, nu * th.ch + j);
       *reinterpret_cast<uint4*>(base + off) = hi[j];
       *reinterpret_cast<uint4*>(base + 16384 + off) = mid[j];
-      *reinterpret_cast<uint4*>(base + 32768 + off) = lo[j];
+      if constexpr (NP == 3) *reinterpret_cast<uint4*>(base + 32768 + off) = lo[j];
     }
     tc::epi_warp_arrive_smem(&sh.a_full[e.aslot]);
     if (++e.aslot == tc::kARing) { e.aslot = 0; e.aph ^= 1; }
@@ -389,7 +395,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         v[i] = m.cube ? y * y * y : y;
       }
       if (m.cube) hs_stv(hs4, A.hx / 4, x);  // for the chain rule through x^3 at the end
-      if (!emit(es, sh, aring, th, v)) return false;
+      if (!emit<2>(es, sh, aring, th, v)) return false;
       put(0, true, 0, v, 1.f);
       // forward recompute of the hidden layers
       for (int l = 0; l < L - 1; ++l) {
@@ -407,7 +413,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
           tc::bias_act_cw(v, bc, m.act[l], n0, N);
           hs_stv(hs4, (A.hoff[l + 1] + tc::kCW * cc) / 4, v);
-          if (l + 1 < L - 1 && !emit(es, sh, aring, th, v)) return false;
+          if (l + 1 < L - 1 && !emit<2>(es, sh, aring, th, v)) return false;
           put(l + 1, true, cc, v, 1.f);
         }
         tc::epi_release_acc(es, sh);
@@ -419,7 +425,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       const float cs = P ? c : 1.f;
 #pragma unroll
       for (int i = 0; i < tc::kCW; ++i) v[i] = (i < th.nmine) ? cs * lam_in[i] : 0.f;
-      if (!emit(es, sh, aring, th, v)) return false;
+      if (!emit<2>(es, sh, aring, th, v)) return false;
       put(L - 1, false, 0, v, isc);
       if (P) {
         float w[tc::kCW];
@@ -442,7 +448,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
           hs_ldv(hs4, (A.hoff[l] + tc::kCW * cc) / 4, h);
           tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)n0, v);
           tc::deriv_mul_cw(v, h, m.act[l - 1], n0, N);
-          if (!emit(es, sh, aring, th, v)) return false;
+          if (!emit<2>(es, sh, aring, th, v)) return false;
           put(l - 1, false, cc, v, isc);
           if (P) {
             const float s = warp_colsum(v, th.lane);

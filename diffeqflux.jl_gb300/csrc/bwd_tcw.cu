@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
       for (int c = 0; c < kc0; ++c) {
         float x[tc::kCW];
         in_x(c, x);
-        tc::stash_write(stash, sh, 0, c, th.r, th.ch, x);
+        tc::stash_write<2>(stash, sh, 0, c, th.r, th.ch, x);
       }
       for (int l = 0; l < L - 1; ++l) {
         const int N = m.dims[l + 1];
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
             tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
             tc::bias_act_cw(v, bc, m.act[l], n0, N);
             hs_stv(hs4, (A.hoff[l + 1] + tc::kCW * (4 * b + cc)) / 4, v);
-            tc::stash_write(stash, sh, ob, 4 * b + cc, th.r, th.ch, v);
+            tc::stash_write<2>(stash, sh, ob, 4 * b + cc, th.r, th.ch, v);
           }
           tc::epi_release_acc(es, sh);
         }
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
         in_lam(c, v);
 #pragma unroll
         for (int i = 0; i < tc::kCW; ++i) v[i] *= cs;
-        tc::stash_write(stash, sh, L & 1, c, th.r, th.ch, v);
+        tc::stash_write<2>(stash, sh, L & 1, c, th.r, th.ch, v);
         if (P) {
           const float s = warp_colsum(v, th.lane);
           if (th.lane < tc::kCW && 64 * c + tc::kCW * th.ch + th.lane < S)
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
             hs_ldv(hs4, (A.hoff[l] + tc::kCW * (4 * b + cc)) / 4, h);
             tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
             tc::deriv_mul_cw(v, h, m.act[l - 1], n0, N);
-            tc::stash_write(stash, sh, l & 1, 4 * b + cc, th.r, th.ch, v);
+            tc::stash_write<2>(stash, sh, l & 1, 4 * b + cc, th.r, th.ch, v);
             if (P) {
               const float s = warp_colsum(v, th.lane);
               if (th.lane < tc::kCW) tc::red_add(P + th.q * A.nbias + A.boffp[l - 1] + n0 + th.lane, s);
@@ -360,13 +360,13 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
       {
         float x[tc::kCW];
         in_x(0, x);
-        tc::stash_write(stash, sh, 0, 0, th.r, th.ch, x);
+        tc::stash_write<2>(stash, sh, 0, 0, th.r, th.ch, x);
 #pragma unroll
         for (int i = 0; i < tc::kCW; ++i) {
           const int col = tc::kCW * th.ch + i;
           x[i] = (erow != nullptr && col < d) ? erow[col] : 0.f;
         }
-        tc::stash_write(stash, sh, 2, 0, th.r, th.ch, x);
+        tc::stash_write<2>(stash, sh, 2, 0, th.r, th.ch, x);
       }
       for (int l = 0; l < L - 1; ++l) {
         const int N = m.dims[l + 1];
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
             tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
             tc::bias_act_cw(v, bc, m.act[l], n0, N);
             hs_stv(hs4, (A.hoff[l + 1] + tc::kCW * (4 * b + cc)) / 4, v);
-            tc::stash_write(stash, sh, ob, 4 * b + cc, th.r, th.ch, v);
+            tc::stash_write<2>(stash, sh, ob, 4 * b + cc, th.r, th.ch, v);
           }
           tc::epi_release_acc(es, sh);
         }
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
             hs_stv(hs4, (A.hoff2[l] + tc::kCW * (4 * b + cc)) / 4, v);
             hs_ldv(hs4, (A.hoff[l + 1] + tc::kCW * (4 * b + cc)) / 4, y);
             tc::deriv_mul_cw(v, y, m.act[l], n0, N);
-            tc::stash_write(stash, sh, 2 + ob, 4 * b + cc, th.r, th.ch, v);
+            tc::stash_write<2>(stash, sh, 2 + ob, 4 * b + cc, th.r, th.ch, v);
           }
           tc::epi_release_acc(es, sh);
         }
@@ -424,8 +424,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
           v[i] = col < d ? cs * y[i] : 0.f;
           y[i] = (erow != nullptr && col < d) ? -cs * lamD * erow[col] : 0.f;
         }
-        tc::stash_write(stash, sh, L & 1, 0, th.r, th.ch, v);
-        tc::stash_write(stash, sh, 2 + (L & 1), 0, th.r, th.ch, y);
+        tc::stash_write<2>(stash, sh, L & 1, 0, th.r, th.ch, v);
+        tc::stash_write<2>(stash, sh, 2 + (L & 1), 0, th.r, th.ch, y);
         if (P) {
           const float sm = warp_colsum(v, th.lane);
           if (th.lane < tc::kCW && tc::kCW * th.ch + th.lane < d)
@@ -475,8 +475,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
                 ak[i] = inside ? ak[i] * s1 : 0.f;   // pdotbar_{l-1}
               }
             }
-            tc::stash_write(stash, sh, 2 + (l & 1), 4 * b + cc, th.r, th.ch, ak);
-            tc::stash_write(stash, sh, l & 1, 4 * b + cc, th.r, th.ch, ab);
+            tc::stash_write<2>(stash, sh, 2 + (l & 1), 4 * b + cc, th.r, th.ch, ak);
+            tc::stash_write<2>(stash, sh, l & 1, 4 * b + cc, th.r, th.ch, ab);
             if (P) {
               const float sm = warp_colsum(ab, th.lane);
               if (th.lane < tc::kCW) tc::red_add(P + th.q * A.nbias + A.boffp[l - 1] + n0 + th.lane, sm);

@@ -541,6 +541,9 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
     }
     const uint8_t* sbase = op.aimg + (size_t)blockIdx.x * op.cta_stride;
     const uint32_t wbytes = 2u * (uint32_t)op.npad * 128u;
+    // the pieces the op reads: three-product GEMMs and image copies only the
+    // first two (hi, mid; the adjoint's stash chunks hold no lo piece)
+    const uint32_t abytes = (op.kind == 4 || op.nprod == 3) ? 2u * 16384u : (uint32_t)kASlotBytes;
     for (int c = 0; c < op.nchunk; ++c) {
       // the epilogue's generic-proxy writes of chunk c are complete (each
       // writer fenced them for the async proxy before arriving)
@@ -548,13 +551,12 @@ __device__ __forceinline__ bool tma_op(const GemmOp& op, TmaState& t, Shared& sh
       if (!tma_wait_or_stop(sh, &sh.a_empty[t.aslot], t.aph ^ 1)) return false;
       if (leader) {
         asm volatile("fence.proxy.async.global;" ::: "memory");
-        mbar_arrive_expect_tx(&sh.a_full[t.aslot], (uint32_t)kASlotBytes);
+        mbar_arrive_expect_tx(&sh.a_full[t.aslot], abytes);
         asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
                          smem_u32(&sh.a_full[t.aslot])),
                      "r"(kEpiWarps - 1)
                      : "memory");
-        bulk_g2s(aring + t.aslot * kASlotBytes, sbase + (size_t)c * kASlotBytes, (uint32_t)kASlotBytes,
-                 &sh.a_full[t.aslot]);
+        bulk_g2s(aring + t.aslot * kASlotBytes, sbase + (size_t)c * kASlotBytes, abytes, &sh.a_full[t.aslot]);
       }
       __syncwarp();
       t.a_pending[t.aslot] = 1;
@@ -742,17 +744,21 @@ __device__ __forceinline__ bool epi_write_a(EpiState& e, Shared& sh, uint8_t* ar
 // the ring-slot layout; then fenced for the async proxy (the producer's bulk
 // loads) and marked on the chunk's barrier. Every epilogue thread writes its
 // part of every chunk of a layer input exactly once per fill.
+// NP = 2 writes only the hi and mid pieces: chunks that only three-product
+// GEMMs and image copies read (the adjoint's chains).
+template <int NP = 3>
 __device__ __forceinline__ void stash_write(uint8_t* stash_cta, Shared& sh, int b, int c, int r, int ch,
                                             const float* x) {
   uint8_t* base = stash_cta + ((size_t)b * kStashChunks + c) * kASlotBytes;
 #pragma unroll
   for (int j = 0; j < kCW / 8; ++j) {
     uint4 hi, mid, lo;
-    split3_bf16(x + 8 * j, hi, mid, lo);
+    if constexpr (NP == 3) split3_bf16(x + 8 * j, hi, mid, lo);
+    else split2_bf16(x + 8 * j, hi, mid);
     const uint32_t off = sw128_offset(r, (kCW / 8) * ch + j);
     *reinterpret_cast<uint4*>(base + off) = hi;
     *reinterpret_cast<uint4*>(base + 16384 + off) = mid;
-    *reinterpret_cast<uint4*>(base + 32768 + off) = lo;
+    if constexpr (NP == 3) *reinterpret_cast<uint4*>(base + 32768 + off) = lo;
   }
   asm volatile("fence.proxy.async.global;" ::: "memory");
   __syncwarp();

@@ -235,6 +235,18 @@ __device__ __forceinline__ uint4 pack8_bf16(const float* x) {
 
 // Split 8 floats into hi/mid/lo bf16 pieces (x ~= hi + mid + lo) and return the
 // three 16-byte chunks.
+// The first two of the same pieces (hi, mid), for GEMMs that issue only the
+// products A_hi W_hi + A_mid W_hi + A_hi W_lo.
+__device__ __forceinline__ void split2_bf16(const float* x, uint4& hi, uint4& mid) {
+  float r[8];
+  uint4 ph = pack8_bf16(x);
+  const __nv_bfloat16* hb = reinterpret_cast<const __nv_bfloat16*>(&ph);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r[i] = x[i] - __bfloat162float(hb[i]);
+  hi = ph;
+  mid = pack8_bf16(r);
+}
+
 __device__ __forceinline__ void split3_bf16(const float* x, uint4& hi, uint4& mid, uint4& lo) {
   float r[8], h[8];
   uint4 ph = pack8_bf16(x);
