@@ -92,6 +92,7 @@ _SIGS = {
     "gbnde_set_params": (C.c_int, [_P, _P, C.c_size_t]),
     "gbnde_set_params_device": (C.c_int, [_P, _P, C.c_size_t]),
     "gbnde_set_stage_memory": (C.c_int, [_P, C.c_size_t]),
+    "gbnde_set_grid_cap": (C.c_int, [_P, C.c_int]),
     "gbnde_forward": (C.c_int, [_P, C.POINTER(SolveDesc), C.c_int, C.c_int, _P, _P, C.POINTER(Stats)]),
     "gbnde_forward_device": (C.c_int, [_P, C.POINTER(SolveDesc), C.c_int, C.c_int, _P, _P, C.POINTER(Stats)]),
     "gbnde_backward": (C.c_int, [_P, _P, _P, _P, C.POINTER(Stats)]),

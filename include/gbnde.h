@@ -176,6 +176,13 @@ int gbnde_set_params_device(gbnde_ctx* ctx, const float* p_dev, size_t n);
  * reference's memory switch, src/neural_de.jl:57). */
 int gbnde_set_stage_memory(gbnde_ctx* ctx, size_t max_bytes);
 
+/* Upper bound on the CTAs of the tensor-core solver kernels (persistent, one
+ * CTA per SM, each CTA looping over its 128-trajectory tiles). 0 (the
+ * default): one CTA per SM. Fewer CTAs keep the stash engine's per-CTA
+ * operand buffers in L2 at large batches (FFJORD, wide layers). No reference
+ * counterpart (a tuning knob of this implementation). */
+int gbnde_set_grid_cap(gbnde_ctx* ctx, int max_ctas);
+
 /* ---- NeuralODE forward solve ------------------------------------------------
  * Replaces solve(ODEProblem{false}(dudt, x, tspan, p), Tsit5(); saveat, abstol,
  * reltol, ...) at src/neural_de.jl:52-58. u0: S x B. usave: S x B x nsave.

@@ -87,3 +87,9 @@ def test_layer_api_validation():
     assert p.dtype == np.float32 and p.size == 252
     # bias entries are zero, weights bounded by the Glorot limit
     assert np.all(p[100:150] == 0) and np.abs(p[:100]).max() <= np.sqrt(6 / 52)
+
+
+def test_tuning_knobs_reject_bad_arguments(lib):
+    import gbnde._lib as L
+    assert lib.gbnde_set_grid_cap(None, 0) == L.ERR_INVALID
+    assert lib.gbnde_set_stage_memory(None, 0) == L.ERR_INVALID
