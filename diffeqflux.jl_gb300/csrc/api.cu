@@ -1007,7 +1007,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   t.pbias = c->mu_stage.as<float>();
   t.img = c->timg.as<uint8_t>();
   t.hscr = c->thscr.as<float>();
-  t.mu_comp = c->tmucomp.as<float>();
+  t.mu_comp = nullptr;  // plain FP32 accumulation (no compensation) in this engine
   t.lam_comp[0] = c->tlamcomp.as<float>();
   t.lam_comp[1] = c->tlamcomp.as<float>() + SBt;
   // dense storage, or (O(checkpoints) mode) replay of each interval into b.ibuf

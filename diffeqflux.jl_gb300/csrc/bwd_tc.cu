@@ -282,7 +282,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     float isc = 1.f, inv_isc = 1.f;
     float4* hs4 = reinterpret_cast<float4*>(A.hscr + (size_t)blockIdx.x * tc::kEpiThreads * A.hvals);
     float* mu_acc = a.mu_acc + (size_t)blockIdx.x * a.P;
-    float* mu_comp = A.mu_comp + (size_t)blockIdx.x * a.P;
     // pending bias quadrature: stage 1, stages 2..6, stage 7; each holds one
     // nbias row per 32-row group of the tile (rows q = warp % 4), into which
     // that group's warps add their column sums (one adder per element, so the
@@ -317,7 +316,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     // (the images' padding rows and blocks are never written: the host clears
     // the image buffer once when it is allocated)
     zero_cta(mu_acc);
-    zero_cta(mu_comp);
     // the weight-gradient images are read by the producer warp (async proxy)
     asm volatile("fence.proxy.async.global;" ::: "memory");
     for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
@@ -477,15 +475,9 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
     };
 
     // ---- weight gradients of an accepted step -------------------------------------
-    // One stage-stacked op per layer and 128-row half; mu += H * accumulator
-    // with Kahan compensation (mu_comp), each mu element owned by one thread of
-    // the CTA. Then the bias quadrature mu_b += H (P1 + Pmid), compensated too.
-    auto kahan = [&](float& acc, float& cmp, float x) {
-      const float y = x - cmp;
-      const float t2 = acc + y;
-      cmp = (t2 - acc) - y;
-      acc = t2;
-    };
+    // One stage-stacked op per layer and 128-row half; mu += H * accumulator,
+    // each mu element owned by one thread of the CTA. Then the bias quadrature
+    // mu_b += H (P1 + Pmid).
     auto commit_step = [&](float Hf0) -> bool {
       // the images' FP16 writes are complete and ordered before the
       // producer's bulk loads of them (async proxy)
@@ -495,13 +487,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
       tc::epi_bar();
       if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_DW | ((uint32_t)fs << 8))) return false;
       tc::epi_skip_a(es, A.dw_chunks);
+      // mu += H * accumulator, plain FP32 (19-odd accepted steps per solve add
+      // about 1e-6 of rounding, far inside the FP16 images' 2e-4; a compensated
+      // sum doubled the per-step read-modify-write traffic of mu)
       float v[tc::kCW];
       for (int l = 0; l < L; ++l) {
         const int out = m.dims[l + 1], in = m.dims[l];
         const int isA = A.a_isA[l];
         const int Nn2 = isA ? out : in;  // N side of the dW op
         float* __restrict__ Pw = mu_acc + m.woff[l];
-        float* __restrict__ Cw = mu_comp + m.woff[l];
         for (int hh = 0; hh < A.nh[l]; ++hh) {
           const int mrow = 128 * hh + th.r;  // M-side feature of this lane
           // element i of chunk cc of this lane: isA -> row mrow (in feature),
@@ -512,13 +506,12 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             *okp = isA ? (mrow < in && n0 + i < out) : (mrow < out && n0 + i < in);
             return isA ? (size_t)mrow * out + n0 + i : (size_t)(n0 + i) * out + mrow;
           };
-          float av[tc::kCW], cv[tc::kCW];
+          float av[tc::kCW];
           // a full row of kCW contiguous, 16-byte aligned elements (isA)
           auto vec4 = [&](int cc) -> bool {
             const int n0 = 64 * cc + tc::kCW * th.ch;
             return isA && mrow < in && n0 + tc::kCW <= out &&
-                   (reinterpret_cast<uintptr_t>(Pw + (size_t)mrow * out + n0) & 15) == 0 &&
-                   (reinterpret_cast<uintptr_t>(Cw + (size_t)mrow * out + n0) & 15) == 0;
+                   (reinterpret_cast<uintptr_t>(Pw + (size_t)mrow * out + n0) & 15) == 0;
           };
           auto fetch = [&](int cc) {
             if (vec4(cc)) {
@@ -526,9 +519,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
 #pragma unroll
               for (int i = 0; i < tc::kCW; i += 4) {
                 const float4 a4 = *reinterpret_cast<const float4*>(Pw + o + i);
-                const float4 c4 = *reinterpret_cast<const float4*>(Cw + o + i);
                 av[i] = a4.x; av[i + 1] = a4.y; av[i + 2] = a4.z; av[i + 3] = a4.w;
-                cv[i] = c4.x; cv[i + 1] = c4.y; cv[i + 2] = c4.z; cv[i + 3] = c4.w;
               }
               return;
             }
@@ -537,7 +528,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
               bool okp;
               const size_t o = addr(cc, i, &okp);
               av[i] = okp ? Pw[o] : 0.f;
-              cv[i] = okp ? Cw[o] : 0.f;
             }
           };
           // the first chunk's mu is read while the accumulator is computed
@@ -551,21 +541,16 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
             if (vec4(cc)) {
               const size_t o = (size_t)mrow * out + 64 * cc + tc::kCW * th.ch;
 #pragma unroll
-              for (int i = 0; i < tc::kCW; ++i) kahan(av[i], cv[i], Hf * v[i]);
-#pragma unroll
-              for (int i = 0; i < tc::kCW; i += 4) {
-                *reinterpret_cast<float4*>(Pw + o + i) = make_float4(av[i], av[i + 1], av[i + 2], av[i + 3]);
-                *reinterpret_cast<float4*>(Cw + o + i) = make_float4(cv[i], cv[i + 1], cv[i + 2], cv[i + 3]);
-              }
+              for (int i = 0; i < tc::kCW; i += 4)
+                *reinterpret_cast<float4*>(Pw + o + i) =
+                    make_float4(fmaf(Hf, v[i], av[i]), fmaf(Hf, v[i + 1], av[i + 1]), fmaf(Hf, v[i + 2], av[i + 2]),
+                                fmaf(Hf, v[i + 3], av[i + 3]));
             } else {
 #pragma unroll
               for (int i = 0; i < tc::kCW; ++i) {
                 bool okp;
                 const size_t o = addr(cc, i, &okp);
-                if (!okp) continue;
-                kahan(av[i], cv[i], Hf * v[i]);
-                Pw[o] = av[i];
-                Cw[o] = cv[i];
+                if (okp) Pw[o] = fmaf(Hf, v[i], av[i]);
               }
             }
           }
@@ -579,11 +564,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
         while (l + 1 < L && f >= A.boffp[l + 1]) ++l;
         const int o = f - A.boffp[l];
         if (o < m.dims[l + 1])
-          kahan(mu_acc[m.boff[l] + o], mu_comp[m.boff[l] + o],
-                Hf0 * ((((__ldcg(P1 + f) + __ldcg(P1 + A.nbias + f)) + __ldcg(P1 + 2 * A.nbias + f)) +
-                       __ldcg(P1 + 3 * A.nbias + f)) +
-                      (((__ldcg(Pmid + f) + __ldcg(Pmid + A.nbias + f)) + __ldcg(Pmid + 2 * A.nbias + f)) +
-                       __ldcg(Pmid + 3 * A.nbias + f))));
+          mu_acc[m.boff[l] + o] +=
+              Hf0 * ((((__ldcg(P1 + f) + __ldcg(P1 + A.nbias + f)) + __ldcg(P1 + 2 * A.nbias + f)) +
+                      __ldcg(P1 + 3 * A.nbias + f)) +
+                     (((__ldcg(Pmid + f) + __ldcg(Pmid + A.nbias + f)) + __ldcg(Pmid + 2 * A.nbias + f)) +
+                      __ldcg(Pmid + 3 * A.nbias + f)));
       }
       tc::epi_bar();
       return true;
@@ -1158,11 +1143,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tc_kernel(BwdTcArgs A) {
   if (warp == tc::kMmaWarp) tc::tmem_dealloc(sh.tmem_base, 512);
 }
 
-// dLdp[i] = sum over CTAs of (mu_acc - mu_comp), in CTA order, as a
-// compensated (Kahan) FP32 sum: FP64 arithmetic is slow on this GPU and
-// made this pass compute-bound; the compensation keeps the sum of the ~100
-// per-CTA terms to FP32 rounding. Per-CTA slots are `stride` floats apart;
-// `P` parameters are written.
+// dLdp[i] = sum over CTAs of (mu_acc - mu_comp) (mu_comp == nullptr: mu_acc
+// alone), in CTA order, as a compensated (Kahan) FP32 sum: FP64 arithmetic is
+// slow on this GPU and made this pass compute-bound; the compensation keeps
+// the sum of the ~100 per-CTA terms to FP32 rounding. Per-CTA slots are
+// `stride` floats apart; `P` parameters are written.
 __global__ void reduce_mu_comp_kernel(const float* __restrict__ acc, const float* __restrict__ comp,
                                       int nblk, int stride, int P, float* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1178,7 +1163,7 @@ __global__ void reduce_mu_comp_kernel(const float* __restrict__ acc, const float
     const size_t o = (size_t)b * stride + i;
     // both parts of the CTA's compensated sum enter as terms
     add(__ldcs(acc + o));
-    add(-__ldcs(comp + o));
+    if (comp) add(-__ldcs(comp + o));
   }
   out[i] = s - c;
 }
