@@ -990,7 +990,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   t.tpc = tpc;
   if ((r = c->timg.ensure((size_t)grid * tpc * tc::kImgSlots * t.img_cta)) ||
       (r = c->thscr.ensure((size_t)grid * tc::kEpiThreads * t.hvals * 4)) ||
-      (r = c->tmucomp.ensure((size_t)grid * P * 4)) || (r = c->tlamcomp.ensure(2 * SBt * 4)) ||
+      (r = c->tlamcomp.ensure(2 * SBt * 4)) ||
       (r = c->mu_acc.ensure((size_t)grid * P * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * P * 4)) ||
       (r = c->txst.ensure(6 * SBt * 4)))
     return r;
@@ -999,8 +999,7 @@ static int backward_tc(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, float
   // per-CTA quadrature slots padded to a multiple of 4 floats (float4 sweeps)
   const int Ppad = (P + 3) / 4 * 4;
   t.b.P = Ppad;
-  if ((r = c->mu_acc.ensure((size_t)grid * Ppad * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * 4 * t.nbias * 4)) ||
-      (r = c->tmucomp.ensure((size_t)grid * Ppad * 4)))
+  if ((r = c->mu_acc.ensure((size_t)grid * Ppad * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * 4 * t.nbias * 4)))
     return r;
   t.b.mu_acc = c->mu_acc.as<float>();
   t.b.mu_stage = c->mu_stage.as<float>();
@@ -1188,7 +1187,7 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
   int r = 0;
   if ((r = c->timg.ensure((size_t)grid * tpc * tc::kImgSlots * t.img_cta)) ||
       (r = c->thscr.ensure((size_t)grid * tc::kEpiThreads * t.hvals * 4)) ||
-      (r = c->tmucomp.ensure((size_t)grid * Ppad * 4)) || (r = c->tlamcomp.ensure(2 * SBt * 4)) ||
+      (r = c->tlamcomp.ensure(2 * SBt * 4)) ||
       (r = c->mu_acc.ensure((size_t)grid * Ppad * 4)) || (r = c->mu_stage.ensure((size_t)grid * 3 * 4 * t.nbias * 4)) ||
       (r = c->stash.ensure((size_t)grid * tc::kStashCta)))
     return r;
@@ -1198,7 +1197,7 @@ static int backward_tcw(gbnde_ctx* c, const BwdArgs& base, cudaStream_t st, floa
   t.pbias = c->mu_stage.as<float>();
   t.img = c->timg.as<uint8_t>();
   t.hscr = c->thscr.as<float>();
-  t.mu_comp = c->tmucomp.as<float>();
+  t.mu_comp = nullptr;  // plain FP32 accumulation (no compensation)
   t.lam_comp[0] = c->tlamcomp.as<float>();
   t.lam_comp[1] = c->tlamcomp.as<float>() + SBt;
   t.b.dense = c->dense.as<float>();

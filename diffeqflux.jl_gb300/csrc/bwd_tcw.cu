@@ -200,7 +200,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
     int fs = 0;
     float4* hs4 = reinterpret_cast<float4*>(A.hscr + (size_t)blockIdx.x * tc::kEpiThreads * A.hvals);
     float* mu_acc = a.mu_acc + (size_t)blockIdx.x * a.P;
-    float* mu_comp = A.mu_comp + (size_t)blockIdx.x * a.P;
     float* Pb[3] = {A.pbias + (size_t)blockIdx.x * 12 * A.nbias, A.pbias + ((size_t)blockIdx.x * 12 + 4) * A.nbias,
                     A.pbias + ((size_t)blockIdx.x * 12 + 8) * A.nbias};
     int iP1 = 0, iP7 = 2;
@@ -229,7 +228,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
     // (the images' padding rows and blocks are never written: the host clears
     // the image buffer once when it is allocated)
     zero_cta(mu_acc);
-    zero_cta(mu_comp);
     asm volatile("fence.proxy.async.global;" ::: "memory");
     for (int tile = blockIdx.x; tile < a.ntiles; tile += G) {
       if (!rowok(tile)) continue;
@@ -506,12 +504,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
     };
 
     // ---- weight gradients of an accepted step ------------------------------------------
-    auto kahan = [&](float& acc, float& cmp, float x) {
-      const float y = x - cmp;
-      const float t2 = acc + y;
-      cmp = (t2 - acc) - y;
-      acc = t2;
-    };
+    // mu += H * accumulator, plain FP32 per CTA (a compensated sum doubled the
+    // read-modify-write traffic for rounding far below the BF16 images')
     auto commit_step = [&](float Hf) -> bool {
       tc::epi_bar();
       if (threadIdx.x == 0 && !tc::epi_post(cmdp, sh, tc::CMD_DW | ((uint32_t)fs << 8))) return false;
@@ -521,7 +515,6 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
         const int isA = A.a_isA[l];
         const int Nn2 = isA ? out : in;  // N side of the dW ops
         float* __restrict__ Pw = mu_acc + m.woff[l];
-        float* __restrict__ Cw = mu_comp + m.woff[l];
         for (int hh = 0; hh < A.nh[l]; ++hh) {
           const int mrow = 128 * hh + th.r;  // M-side feature of this lane
           for (int nb = 0; nb * 256 < Nn2; ++nb) {
@@ -532,24 +525,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
               const int n0 = 256 * nb + 64 * cc + tc::kCW * th.ch;  // N-side feature of element 0
               tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
               const bool vec = isA && mrow < in && n0 + tc::kCW <= out &&
-                               (reinterpret_cast<uintptr_t>(Pw + (size_t)mrow * out + n0) & 15) == 0 &&
-                               (reinterpret_cast<uintptr_t>(Cw + (size_t)mrow * out + n0) & 15) == 0;
+                               (reinterpret_cast<uintptr_t>(Pw + (size_t)mrow * out + n0) & 15) == 0;
               if (vec) {
                 const size_t o = (size_t)mrow * out + n0;
-                float av[tc::kCW], cv[tc::kCW];
 #pragma unroll
                 for (int i = 0; i < tc::kCW; i += 4) {
                   const float4 a4 = *reinterpret_cast<const float4*>(Pw + o + i);
-                  const float4 c4 = *reinterpret_cast<const float4*>(Cw + o + i);
-                  av[i] = a4.x; av[i + 1] = a4.y; av[i + 2] = a4.z; av[i + 3] = a4.w;
-                  cv[i] = c4.x; cv[i + 1] = c4.y; cv[i + 2] = c4.z; cv[i + 3] = c4.w;
-                }
-#pragma unroll
-                for (int i = 0; i < tc::kCW; ++i) kahan(av[i], cv[i], Hf * v[i]);
-#pragma unroll
-                for (int i = 0; i < tc::kCW; i += 4) {
-                  *reinterpret_cast<float4*>(Pw + o + i) = make_float4(av[i], av[i + 1], av[i + 2], av[i + 3]);
-                  *reinterpret_cast<float4*>(Cw + o + i) = make_float4(cv[i], cv[i + 1], cv[i + 2], cv[i + 3]);
+                  *reinterpret_cast<float4*>(Pw + o + i) =
+                      make_float4(fmaf(Hf, v[i], a4.x), fmaf(Hf, v[i + 1], a4.y), fmaf(Hf, v[i + 2], a4.z),
+                                  fmaf(Hf, v[i + 3], a4.w));
                 }
               } else {
 #pragma unroll
@@ -558,10 +542,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
                   const bool okp = isA ? (mrow < in && n < out) : (mrow < out && n < in);
                   if (!okp) continue;
                   const size_t o = isA ? (size_t)mrow * out + n : (size_t)n * out + mrow;
-                  float av = Pw[o], cv = Cw[o];
-                  kahan(av, cv, Hf * v[i]);
-                  Pw[o] = av;
-                  Cw[o] = cv;
+                  Pw[o] = fmaf(Hf, v[i], Pw[o]);
                 }
               }
             }
@@ -575,11 +556,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) bwd_tcw_kernel(BwdTcwArgs W) 
         while (l + 1 < L && f >= A.boffp[l + 1]) ++l;
         const int o = f - A.boffp[l];
         if (o < m.dims[l + 1])
-          kahan(mu_acc[m.boff[l] + o], mu_comp[m.boff[l] + o],
-                Hf * ((((__ldcg(P1 + f) + __ldcg(P1 + A.nbias + f)) + __ldcg(P1 + 2 * A.nbias + f)) +
-                       __ldcg(P1 + 3 * A.nbias + f)) +
-                      (((__ldcg(Pmid + f) + __ldcg(Pmid + A.nbias + f)) + __ldcg(Pmid + 2 * A.nbias + f)) +
-                       __ldcg(Pmid + 3 * A.nbias + f))));
+          mu_acc[m.boff[l] + o] +=
+              Hf * ((((__ldcg(P1 + f) + __ldcg(P1 + A.nbias + f)) + __ldcg(P1 + 2 * A.nbias + f)) +
+                     __ldcg(P1 + 3 * A.nbias + f)) +
+                    (((__ldcg(Pmid + f) + __ldcg(Pmid + A.nbias + f)) + __ldcg(Pmid + 2 * A.nbias + f)) +
+                     __ldcg(Pmid + 3 * A.nbias + f)));
       }
       tc::epi_bar();
       return true;
