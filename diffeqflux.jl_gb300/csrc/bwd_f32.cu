@@ -45,6 +45,92 @@ __device__ __forceinline__ int find_step(const BwdArgs& a, const Interval& iv, d
   return n;
 }
 
+// u(t) weights of the forward step holding tt: hb[j] = h b_j(theta); returns
+// the step.
+__device__ __forceinline__ int dense_weights_at(const BwdArgs& a, const Interval& iv, double tt, float* hb) {
+  const int n = find_step(a, iv, tt);
+  const double tn = a.fsteps[2 * n], h = a.fsteps[2 * n + 1];
+  float bw[7];
+  interp_weights((tt - tn) / h, bw);
+  for (int q = 0; q < 7; ++q) hb[q] = (float)(h * (double)bw[q]);
+  return n;
+}
+
+// The scalar FP64 work of an adjoint step, run by warp 0 (every lane keeps
+// the same t, dt and qold) and kept out of line so that its registers do not
+// weigh on the tile loops: the step setup (lane i: stage i's time,
+// coefficients and u(t) weights; lane 7: the error weights) ...
+__device__ __noinline__ void adj_step_setup(const BwdArgs& a, const Interval& iv, double t, double t_lo, double dt,
+                                            bool backsolve, StepCtl* c, float (*hb6)[7], int* n6) {
+  const int lane = threadIdx.x;
+  const bool go = t > t_lo;
+  const double rem = rt32(t - t_lo, a.f32time);
+  const bool clipped = dt >= rem;
+  const double Hs = clipped ? rem : dt;
+  if (lane == 0) {
+    c->go = go;
+    c->clipped = clipped;
+    c->t = t;
+    c->h = Hs;
+    c->hf = (float)Hs;
+  }
+  if (go && lane >= 1 && lane < 7) {
+    const int i = lane;
+    const double tt = t - c_tab.c[i] * Hs;
+    c->tst[i] = tt;
+    for (int q = 0; q < 6; ++q) c->ha[i - 1][q] = (float)(Hs * c_tab.a[i][q]);
+    if (!backsolve) n6[i - 1] = dense_weights_at(a, iv, tt, hb6[i - 1]);
+  } else if (go && lane == 7) {
+    for (int q = 0; q < 7; ++q) c->hbt[q] = (float)(Hs * c_tab.btilde[q]);
+  }
+}
+
+// ... and the controller after the error norm (qe: the grid's sum of squares):
+// accept or reject, the next step size, and for an accepted step with the
+// Gauss quadrature its four points (lane gq).
+__device__ __noinline__ void adj_step_control(const BwdArgs& a, const Interval& iv, double qe, double Nnorm,
+                                              double t_lo, bool gauss, double* t, double* dt, double* qold,
+                                              StepCtl* c, float (*hb6)[7], int* n6, float (*bl4)[7]) {
+  const int lane = threadIdx.x;
+  const double H = c->h;
+  const double eest = rt32(sqrt(qe / Nnorm), a.f32time);
+  int rc = GBNDE_RET_SUCCESS, acc = 0;
+  if (!isfinite(eest)) {
+    rc = GBNDE_RET_UNSTABLE;
+  } else {
+    double q11;
+    double q = pi_q(eest, *qold, &q11);
+    if (eest <= 1.0) {
+      acc = 1;
+      if (gauss && lane < 4) {
+        const double gth[4] = {0.06943184420297371, 0.33000947820757187, 0.6699905217924281,
+                               0.9305681557970262};
+        const double gw[4] = {0.17392742256872679, 0.3260725774312732, 0.3260725774312732,
+                              0.17392742256872679};
+        const int gq = lane;
+        const double tt = *t - gth[gq] * H;
+        c->tst[gq] = tt;
+        float bl[7];
+        interp_weights(gth[gq], bl);
+        for (int q2 = 0; q2 < 7; ++q2) bl4[gq][q2] = (float)(H * (double)bl[q2]);
+        c->hb[gq] = (float)(H * gw[gq]);
+        n6[gq] = dense_weights_at(a, iv, tt, hb6[gq]);
+      }
+      *t = c->clipped ? t_lo : rt32(*t - H, a.f32time);
+      if (q >= 1.0 && q <= 1.0) q = 1.0;
+      *qold = rt32(fmax(eest, kQoldInit), a.f32time);
+      *dt = rt32(fmin(H / q, a.dtmax), a.f32time);
+    } else {
+      *dt = rt32(H / fmin(1.0 / kQmin, q11 / kGamma), a.f32time);
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    c->ret = rc;
+    c->accept = acc;
+  }
+}
+
 // Forward RHS on a tile into `out` rows (plain, no kept activations), input
 // produced per element.
 template <class Fn>
@@ -457,33 +543,8 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       const size_t SB = (size_t)S * a.B;
       return a.dense ? a.dense + (size_t)n * 8 * SB : a.ibuf + (size_t)(n - iv.nlo) * 8 * SB;
     };
-    auto dense_weights = [&](double tt, float* hb) -> int {
-      const int n = find_step(a, iv, tt);
-      const double tn = a.fsteps[2 * n], h = a.fsteps[2 * n + 1];
-      float bw[7];
-      interp_weights((tt - tn) / h, bw);
-      for (int q = 0; q < 7; ++q) hb[q] = (float)(h * (double)bw[q]);
-      return n;
-    };
     for (;;) {
-      if (threadIdx.x == 0) {
-        s_ctl.go = t > t_lo;
-        const double rem = rt32(t - t_lo, a.f32time);
-        s_ctl.clipped = dt >= rem;
-        const double Hs = s_ctl.clipped ? rem : dt;
-        s_ctl.t = t;
-        s_ctl.h = Hs;
-        s_ctl.hf = (float)Hs;
-        if (s_ctl.go) {
-          for (int i = 1; i < 7; ++i) {
-            const double tt = t - c_tab.c[i] * Hs;
-            s_ctl.tst[i] = tt;
-            for (int q = 0; q < 6; ++q) s_ctl.ha[i - 1][q] = (float)(Hs * c_tab.a[i][q]);
-            if (!backsolve) s_n6[i - 1] = dense_weights(tt, s_hb6[i - 1]);
-          }
-          for (int q = 0; q < 7; ++q) s_ctl.hbt[q] = (float)(Hs * c_tab.btilde[q]);
-        }
-      }
+      if (threadIdx.x < 32) adj_step_setup(a, iv, t, t_lo, dt, backsolve, &s_ctl, s_hb6, s_n6);
       __syncthreads();
       if (!s_ctl.go) break;
       if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
@@ -572,43 +633,8 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       if (!grid_barrier(a.bar, gen, a.status)) { ret = GBNDE_RET_BARRIER_TIMEOUT; break; }
       {
         const double qe = grid_partials_sum(pp, G, red);
-        if (threadIdx.x == 0) {
-          const double eest = rt32(sqrt(qe / Nnorm), a.f32time);
-          s_ctl.ret = GBNDE_RET_SUCCESS;
-          s_ctl.accept = 0;
-          if (!isfinite(eest)) {
-            s_ctl.ret = GBNDE_RET_UNSTABLE;
-          } else {
-            double q11;
-            double q = pi_q(eest, qold, &q11);
-            if (eest <= 1.0) {
-              s_ctl.accept = 1;
-              if (gauss) {
-                // the quadrature points of the step: u(t) weights and lam's
-                // interpolant weights
-                const double gth[4] = {0.06943184420297371, 0.33000947820757187, 0.6699905217924281,
-                                       0.9305681557970262};
-                const double gw[4] = {0.17392742256872679, 0.3260725774312732, 0.3260725774312732,
-                                      0.17392742256872679};
-                for (int gq = 0; gq < 4; ++gq) {
-                  const double tt = t - gth[gq] * H;
-                  s_ctl.tst[gq] = tt;
-                  float bl[7];
-                  interp_weights(gth[gq], bl);
-                  for (int q2 = 0; q2 < 7; ++q2) s_bl4[gq][q2] = (float)(H * (double)bl[q2]);
-                  s_ctl.hb[gq] = (float)(H * gw[gq]);
-                  s_n6[gq] = dense_weights(tt, s_hb6[gq]);
-                }
-              }
-              t = s_ctl.clipped ? t_lo : rt32(t - H, a.f32time);
-              if (q >= 1.0 && q <= 1.0) q = 1.0;
-              qold = rt32(fmax(eest, kQoldInit), a.f32time);
-              dt = rt32(fmin(H / q, a.dtmax), a.f32time);
-            } else {
-              dt = rt32(H / fmin(1.0 / kQmin, q11 / kGamma), a.f32time);
-            }
-          }
-        }
+        if (threadIdx.x < 32)
+          adj_step_control(a, iv, qe, Nnorm, t_lo, gauss, &t, &dt, &qold, &s_ctl, s_hb6, s_n6, s_bl4);
         __syncthreads();
       }
       par ^= 1;
