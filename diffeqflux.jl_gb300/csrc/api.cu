@@ -730,6 +730,9 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
           if (n >= tc::kMaxOps) return fail(GBNDE_ERR_UNSUPPORTED, "too many tensor-core ops");
           tc::GemmOp& o = ta.ops.op[n++];
           o.kind = 3;
+          // the tangent chain (FFJORD's J e, read only through the trace)
+          // issues three split products, and its stash chunks carry two pieces
+          o.nprod = chain == 1 ? 3 : 0;
           o.wimg = c->wimg.as<uint8_t>() + c->wb_off[l][b];
           o.npad = c->wb_npad[l][b];
           o.nchunk = (c->mlp.dims[l] + 63) / 64;

@@ -174,7 +174,7 @@ __device__ __forceinline__ bool epi_rhs_ffj(const FwdTcwArgs& A, tc::EpiState& e
       const int col = 64 * c + tc::kCW * th.ch + i;
       x[i] = (erow != nullptr && col < d) ? erow[col] : 0.f;
     }
-    tc::stash_write(stash, sh, 2, c, th.r, th.ch, x);
+    tc::stash_write<2>(stash, sh, 2, c, th.r, th.ch, x);
   }
   int hoff = 0;
   for (int l = 0; l < L - 1; ++l) {
@@ -205,7 +205,7 @@ __device__ __forceinline__ bool epi_rhs_ffj(const FwdTcwArgs& A, tc::EpiState& e
         hs_ldv(hs4, (hoff + tc::kCW * (4 * b + cc)) / 4, y);
         tc::tmem_ld_cw(sh.tmem_base + lane_base + col + (uint32_t)(64 * cc + tc::kCW * th.ch), v);
         tc::deriv_mul_cw(v, y, m.act[l], n0, N);
-        tc::stash_write(stash, sh, 2 + ob, 4 * b + cc, th.r, th.ch, v);
+        tc::stash_write<2>(stash, sh, 2 + ob, 4 * b + cc, th.r, th.ch, v);
       }
       tc::epi_release_acc(e, sh);
     }
