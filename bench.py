@@ -339,10 +339,26 @@ def aux_spiral(device):
         out["st"], out["sb"] = st, sb
     sec = _timed(step, 20)
     kf, kb = _kernel_ms(s)
+    # the CPU path on the same problem: the FP32 C++ restatement, one thread
+    # (one trajectory leaves nothing to spread over cores)
+    cpu = None
+    try:
+        from oracle import cpu_fp32
+        m = cpu_fp32.CpuNeuralODE([2, 50, 2], [1, 0], p, 1, cube=True, nthreads=1)
+        m.grad(u0, (0.0, 1.5), ts, 1e-7, 1e-5, tgt, loss_kind=0)
+        reps = 20
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            m.grad(u0, (0.0, 1.5), ts, 1e-7, 1e-5, tgt, loss_kind=0)
+        cpu = {"latency_ms": 1000.0 * (time.perf_counter() - t0) / reps, "cores": 1, "kind": "port",
+               "cpu": cpu_model(), "sample": f"{reps} gradient evaluations (FP32 C++ restatement, one thread)"}
+        m.close()
+    except Exception as e:  # reported, never silently dropped
+        cpu = {"error": f"{type(e).__name__}: {e}"}
     return {"workload": "spiral_b1_s2_cube_h50_nsave30", "latency_ms": 1000.0 * sec,
             "fwd_kernel_ms": kf, "bwd_kernel_ms": kb,
             "unit": "ms per gradient evaluation (forward + adjoint, host API)", "precision": "fp32",
-            "nf_fwd": out["st"].nf, "nf_adj": out["sb"].nf_adj,
+            "nf_fwd": out["st"].nf, "nf_adj": out["sb"].nf_adj, "cpu": cpu,
             "note": "batch 1: latency-bound (launch and controller round trips), no roofline"}
 
 

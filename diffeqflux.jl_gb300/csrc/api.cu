@@ -1377,7 +1377,15 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
     else if (c->tm_force_bwd) return fail(GBNDE_ERR_UNSUPPORTED, "%d tile rows do not fit", want);
   }
   const int LD = TM + 4;
-  const size_t smem = (size_t)rows * LD * sizeof(float);
+  size_t smem = (size_t)rows * LD * sizeof(float);
+  // a small model's pending quadrature (3 x P floats) fits beside the tile in
+  // shared memory: the per-stage weight-gradient sums then make no global
+  // round trips (the batch-1 spiral: P = 252)
+  int pb_smem_off = 0;
+  if (smem + (size_t)3 * P * sizeof(float) <= std::min<size_t>(kSmemBudget, 64 * 1024)) {
+    pb_smem_off = rows * LD;
+    smem += (size_t)3 * P * sizeof(float);
+  }
   const int ntiles = (B + TM - 1) / TM;
   int gmax = 0;
   if (max_grid_bwd_f32(smem, &gmax)) return fail(GBNDE_ERR_CUDA, "occupancy query failed");
@@ -1448,6 +1456,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   }
   a.mu_acc = c->mu_acc.as<float>();
   a.mu_stage = c->mu_stage.as<float>();
+  a.pb_smem_off = pb_smem_off;
   a.dLdu0 = du0_d;
   a.partials = c->partials.as<double>();
   a.bar = c->bsync.as<unsigned int>();

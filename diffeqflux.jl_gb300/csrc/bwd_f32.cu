@@ -183,9 +183,8 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
     sm.uraw = p;
   }
   float* mu_acc = a.mu_acc + (size_t)blockIdx.x * a.P;
-  float* Pb[3] = {a.mu_stage + (size_t)blockIdx.x * 3 * a.P,
-                  a.mu_stage + ((size_t)blockIdx.x * 3 + 1) * a.P,
-                  a.mu_stage + ((size_t)blockIdx.x * 3 + 2) * a.P};
+  float* pbase = a.pb_smem_off > 0 ? smem + a.pb_smem_off : a.mu_stage + (size_t)blockIdx.x * 3 * a.P;
+  float* Pb[3] = {pbase, pbase + a.P, pbase + 2 * (size_t)a.P};
   int iP1 = 0, iP7 = 2;  // roles of Pb[0] and Pb[2] swap on accept
   float* Pmid = Pb[1];
 

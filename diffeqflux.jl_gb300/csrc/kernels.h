@@ -92,6 +92,8 @@ struct BwdArgs {
   float* kf[7];           // forward recompute stage buffers
   float* mu_acc;          // per-CTA committed parameter gradient [grid][P]
   float* mu_stage;        // per-CTA pending quadrature [grid][3][P]  (P1, Pmid, P7)
+  int pb_smem_off;        // > 0: the pending quadrature lives in dynamic shared memory at this
+                          //   float offset instead (small models: no global round trips)
   float* dLdu0;           // output S*B
   double* partials;
   unsigned int* bar;
