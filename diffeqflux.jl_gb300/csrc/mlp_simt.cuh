@@ -92,10 +92,47 @@ __device__ __forceinline__ void dense_fwd_tile(const float* __restrict__ Wt,
   }
 }
 
+// Skinny layers (few outputs, long K; small batches such as the batch-1
+// spiral fit): each output (trajectory m, column n) is summed by a group of G
+// lanes of one warp over a strided share of K and reduced with shuffles in a
+// fixed order, so that a long dot product is not one thread's serial chain.
+// Every lane of a warp runs the same number of rounds (the shuffles need the
+// whole warp); lanes past the last output compute nothing.
+template <int G>
+__device__ __forceinline__ void dense_fwd_splitk(const float* __restrict__ Wt, const float* __restrict__ bias,
+                                                 int K, int N, int act, const float* in_s, float* out_s,
+                                                 int LD, int TM) {
+  const int lg = threadIdx.x % G, grp = threadIdx.x / G, ngrp = blockDim.x / G;
+  const int nout = N * TM;
+  with_act(act, [&](auto A) {
+    for (int ob = 0; ob < nout; ob += ngrp) {
+      const int o = ob + grp;
+      const bool mine = o < nout;
+      const int n = mine ? o / TM : 0, m = mine ? o - (o / TM) * TM : 0;
+      float sum = 0.f;
+      if (mine)
+        for (int k = lg; k < K; k += G) sum = fmaf(in_s[k * LD + m], __ldg(Wt + (size_t)k * N + n), sum);
+#pragma unroll
+      for (int off = G / 2; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off, G);
+      if (mine && lg == 0) out_s[n * LD + m] = A.f(sum + (bias ? __ldg(bias + n) : 0.f));
+    }
+  });
+}
+
 __device__ __forceinline__ void dense_fwd(const float* Wt, const float* bias, int K, int N, int act,
                                           const float* in_s, float* out_s, int LD, int TM) {
   const int rgroups = TM / 8;
   const int cgroups = blockDim.x / rgroups;
+  // few outputs per thread and a long K: split K over lanes (the rounds of
+  // the per-thread path would be one thread's K-long serial chain)
+  if (K >= 16 && N * TM * 4 <= (int)blockDim.x) {
+    const int per = (int)blockDim.x / (N * TM);
+    if (per >= 32) dense_fwd_splitk<32>(Wt, bias, K, N, act, in_s, out_s, LD, TM);
+    else if (per >= 16) dense_fwd_splitk<16>(Wt, bias, K, N, act, in_s, out_s, LD, TM);
+    else if (per >= 8) dense_fwd_splitk<8>(Wt, bias, K, N, act, in_s, out_s, LD, TM);
+    else dense_fwd_splitk<4>(Wt, bias, K, N, act, in_s, out_s, LD, TM);
+    return;
+  }
   if (N >= cgroups * 8)
     dense_fwd_tile<8, 8>(Wt, bias, K, N, act, in_s, out_s, LD, TM);
   else if (N >= cgroups * 4)
