@@ -222,6 +222,8 @@ struct gbnde_ctx {
   DBuf ffnoise, ffu0, ffus;
   int fS = 0;          // state dim of the last forward (d + 1 for FFJORD)
   int ff_on = 0, ff_d = 0, ff_exact = 0;
+  int ff_reg = 0;      // FFJORD with the |f|^2 and |e^T J| rows
+  int ff_reg_g2 = 0;   // the |e^T J| row's cotangent is nonzero (set by the backward)
   int ms_S = 0, ms_nseg = 0, ms_nsave = 0, ms_MS = 0;
   // dense stage storage of the last forward
   DBuf comp, dense;
@@ -531,7 +533,7 @@ int gbnde_set_params_device(gbnde_ctx* c, const float* p, size_t n) {
 
 static int validate_desc(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B) {
   if (!d) return fail(GBNDE_ERR_INVALID, "null solve descriptor");
-  if (S != c->S + (c->ff_on ? 1 : 0))
+  if (S != c->S + (c->ff_on ? (c->ff_reg ? 3 : 1) : 0))
     return fail(GBNDE_ERR_INVALID, "state dim %d does not match the model (%d)", S, c->S);
   if (B < 1) return fail(GBNDE_ERR_INVALID, "batch must be >= 1");
   if (!(d->t1 != d->t0)) return fail(GBNDE_ERR_INVALID, "tspan must satisfy t1 != t0");
@@ -578,7 +580,8 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
 
   int sumdims = 0;
   for (int l = 0; l <= c->mlp.nlayers; ++l) sumdims += c->mlp.dims[l];
-  const int frows = c->ff_on ? 2 * sumdims + c->mlp.maxdim + 1 : 2 * c->mlp.maxdim;
+  const int frows = c->ff_on ? 2 * sumdims + c->mlp.maxdim + 1 + (c->ff_reg ? c->mlp.maxdim + 2 : 0)
+                             : 2 * c->mlp.maxdim;
   int TM = 0;
   if (choose_tm(frows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "layer too wide");
   while (TM > 8 && TM / 2 >= B) TM /= 2;  // small batches: no tile rows past the batch
@@ -592,7 +595,8 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   const int LD = TM + 4;
   const size_t smem = (size_t)frows * LD * sizeof(float);
   // FFJORD with the Hutchinson trace runs on the stash engine where it covers the model
-  const bool ffj_tc = c->precision == GBNDE_PREC_BF16 && c->ff_on && c->ffj_tc_ok && !c->ff_exact;
+  const bool ffj_tc =
+      c->precision == GBNDE_PREC_BF16 && c->ff_on && c->ffj_tc_ok && !c->ff_exact && !c->ff_reg;
   const bool tcform = c->precision == GBNDE_PREC_BF16 && (!c->ff_on || ffj_tc);
   bool wide = tcform && c->tc_wide && (!c->tc_shape_ok || ffj_tc);
   if (tcform && c->tc_wide && c->tc_shape_ok && !ffj_tc) {
@@ -711,6 +715,7 @@ static int forward_impl(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, c
   a.ffj = c->ff_on;
   a.ffd = c->ff_d;
   a.exact = c->ff_exact;
+  a.ffreg = c->ff_on && c->ff_reg;
   a.noise = c->ff_on ? c->ffnoise.as<float>() : nullptr;
   if (wide && (r = c->stash.ensure((size_t)grid * tc::kStashCta))) return r;
   CK(cudaEventRecord(c->ev[0], st));
@@ -1352,7 +1357,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   // engine, after a tensor-core forward) replaying each interval from its checkpoint
   const bool tc_replay = c->precision == GBNDE_PREC_BF16 && c->tc_bwd_ok && !backsolve && !gauss &&
                          !c->dense_valid && c->dense_tl && !c->fwd_wide && !c->ff_on;
-  const bool ffj_tc = c->ff_on && c->fwd_wide && c->dense_tl && c->ffj_tc_ok && !c->ff_exact;
+  const bool ffj_tc = c->ff_on && c->fwd_wide && c->dense_tl && c->ffj_tc_ok && !c->ff_exact && !c->ff_reg;
   const bool tcbwd = (c->precision == GBNDE_PREC_BF16 && (c->fwd_wide ? c->tc_wide_bwd : c->tc_bwd_ok) &&
                       !backsolve && !gauss && c->dense_valid && (!c->ff_on || ffj_tc)) ||
                      tc_replay;
@@ -1365,7 +1370,8 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   for (int l = 0; l <= c->mlp.nlayers; ++l) rows += c->mlp.dims[l];
   // activations of every layer, two work buffers and, with the cube prefix,
   // the state before it
-  rows = c->ff_on ? 2 * rows + 4 * c->mlp.maxdim + 1 : rows + 2 * c->mlp.maxdim + (c->mlp.cube ? S : 0);
+  rows = c->ff_on ? 2 * rows + 4 * c->mlp.maxdim + 1 + (c->ff_reg ? 3 : 0)
+                  : rows + 2 * c->mlp.maxdim + (c->mlp.cube ? S : 0);
   int TM = 0;
   if (choose_tm(rows, kSmemBudget, &TM)) return fail(GBNDE_ERR_UNSUPPORTED, "network too wide");
   while (TM > 8 && TM / 2 >= B) TM /= 2;
@@ -1465,6 +1471,7 @@ static int backward_impl(gbnde_ctx* c, const float* dLdu, bool in_host, float* d
   a.ffj = c->ff_on;
   a.ffd = c->ff_d;
   a.exact = c->ff_exact;
+  a.ffreg = (c->ff_on && c->ff_reg) ? (1 | (c->ff_reg_g2 ? 2 : 0)) : 0;
   a.noise = c->ff_on ? c->ffnoise.as<float>() : nullptr;
   if (tcbwd && c->fwd_wide) {
     if (c->recording) c->rec.bwd = false;  // stash-mode steps run eagerly
@@ -1760,13 +1767,20 @@ int gbnde_forward_device(gbnde_ctx* c, const gbnde_solve_desc* d, int S, int B, 
   return forward_impl(c, d, S, B, u0, false, usave, false, stats);
 }
 
-int gbnde_ffjord_forward(gbnde_ctx* c, const gbnde_solve_desc* desc, int d, int B, const float* x,
-                         const float* noise, float* logpx, float* zT, gbnde_stats* stats) {
+namespace {
+
+// FFJORD forward: the augmented system [z; delta_logp (; |f|^2; |e^T J|)] from
+// (x, 0) over [t0, t1], keeping the end state; logpx for the standard-normal
+// base, z(t1) and the two regulariser integrals when reg.
+int ffjord_forward_impl(gbnde_ctx* c, const gbnde_solve_desc* desc, int d, int B, const float* x,
+                        const float* noise, int exact, int reg, float* logpx, float* zT, float* rf, float* rj,
+                        gbnde_stats* stats) {
   if (!c || !desc || !x || !logpx) return fail(GBNDE_ERR_INVALID, "null argument");
   if (d != c->S) return fail(GBNDE_ERR_INVALID, "data dim %d does not match the model (%d)", d, c->S);
   if (c->mlp.cube) return fail(GBNDE_ERR_UNSUPPORTED, "FFJORD with a cube prefix");
+  if (!exact && !noise) return fail(GBNDE_ERR_INVALID, "the Hutchinson trace needs noise");
   if (int r = set_device(c)) return r;
-  const int S = d + 1;
+  const int S = d + (reg ? 3 : 1);
   const size_t SB = (size_t)S * B;
   int r = 0;
   if ((r = c->ffu0.ensure(SB * 4)) || (r = c->ffus.ensure(SB * 4)) ||
@@ -1784,7 +1798,9 @@ int gbnde_ffjord_forward(gbnde_ctx* c, const gbnde_solve_desc* desc, int d, int 
   dd.sensealg = GBNDE_SENSE_INTERPOLATING;
   c->ff_on = 1;
   c->ff_d = d;
-  c->ff_exact = noise ? 0 : 1;
+  c->ff_exact = exact ? 1 : 0;
+  c->ff_reg = reg ? 1 : 0;
+  c->ff_reg_g2 = 0;
   r = forward_impl(c, &dd, S, B, c->ffu0.as<float>(), false, c->ffus.as<float>(), false, stats);
   if (r) return r;
   std::vector<float> yT(SB);
@@ -1798,30 +1814,66 @@ int gbnde_ffjord_forward(gbnde_ctx* c, const gbnde_solve_desc* desc, int d, int 
       if (zT) zT[(size_t)b * d + s] = (float)z;
     }
     logpx[b] = (float)(-0.5 * q - lognorm - (double)yT[(size_t)b * S + d]);
+    if (reg && rf) rf[b] = yT[(size_t)b * S + d + 1];
+    if (reg && rj) rj[b] = yT[(size_t)b * S + d + 2];
   }
   return 0;
 }
 
-int gbnde_ffjord_backward(gbnde_ctx* c, const float* dLdlogpx, const float* dLdzT, float* dLdx, float* dLdp,
-                          gbnde_stats* stats) {
+int ffjord_backward_impl(gbnde_ctx* c, const float* dLdlogpx, const float* dLdzT, const float* dLdrf,
+                         const float* dLdrj, float* dLdx, float* dLdp, gbnde_stats* stats) {
   if (!c || !dLdlogpx || !dLdx || !dLdp) return fail(GBNDE_ERR_INVALID, "null argument");
   if (!c->ff_on || !c->have_fwd) return fail(GBNDE_ERR_STATE, "backward needs a successful FFJORD forward");
   if (int r = set_device(c)) return r;
-  const int d = c->ff_d, S = d + 1, B = c->B;
+  const int d = c->ff_d, S = d + (c->ff_reg ? 3 : 1), B = c->B;
   const size_t SB = (size_t)S * B;
   std::vector<float> yT(SB), g(SB), du0(SB);
   CK(cudaMemcpy(yT.data(), c->ffus.p, SB * 4, cudaMemcpyDeviceToHost));
+  int g2 = 0;
   for (int b = 0; b < B; ++b) {
     const float gl = dLdlogpx[b];
     for (int s = 0; s < d; ++s)
       g[(size_t)b * S + s] = -yT[(size_t)b * S + s] * gl + (dLdzT ? dLdzT[(size_t)b * d + s] : 0.f);
     g[(size_t)b * S + d] = -gl;
+    if (c->ff_reg) {
+      g[(size_t)b * S + d + 1] = dLdrf ? dLdrf[b] : 0.f;
+      g[(size_t)b * S + d + 2] = dLdrj ? dLdrj[b] : 0.f;
+      g2 |= (dLdrj && dLdrj[b] != 0.f);
+    }
   }
+  c->ff_reg_g2 = g2;
   const int r = backward_impl(c, g.data(), true, du0.data(), dLdp, true, stats);
   if (r) return r;
   for (int b = 0; b < B; ++b)
     for (int s = 0; s < d; ++s) dLdx[(size_t)b * d + s] = du0[(size_t)b * S + s];
   return 0;
+}
+
+}  // namespace
+
+int gbnde_ffjord_forward(gbnde_ctx* c, const gbnde_solve_desc* desc, int d, int B, const float* x,
+                         const float* noise, float* logpx, float* zT, gbnde_stats* stats) {
+  return ffjord_forward_impl(c, desc, d, B, x, noise, noise ? 0 : 1, 0, logpx, zT, nullptr, nullptr, stats);
+}
+
+int gbnde_ffjord_forward_reg(gbnde_ctx* c, const gbnde_solve_desc* desc, int d, int B, const float* x,
+                             const float* noise, int exact_trace, float* logpx, float* zT, float* reg_f2,
+                             float* reg_ej, gbnde_stats* stats) {
+  if (!noise) return fail(GBNDE_ERR_INVALID, "the |e^T J| row needs noise");
+  return ffjord_forward_impl(c, desc, d, B, x, noise, exact_trace ? 1 : 0, 1, logpx, zT, reg_f2, reg_ej,
+                             stats);
+}
+
+int gbnde_ffjord_backward(gbnde_ctx* c, const float* dLdlogpx, const float* dLdzT, float* dLdx, float* dLdp,
+                          gbnde_stats* stats) {
+  return ffjord_backward_impl(c, dLdlogpx, dLdzT, nullptr, nullptr, dLdx, dLdp, stats);
+}
+
+int gbnde_ffjord_backward_reg(gbnde_ctx* c, const float* dLdlogpx, const float* dLdzT, const float* dL_dreg_f2,
+                              const float* dL_dreg_ej, float* dLdx, float* dLdp, gbnde_stats* stats) {
+  if (c && c->ff_on && !c->ff_reg)
+    return fail(GBNDE_ERR_STATE, "the last FFJORD forward ran without the regulariser rows");
+  return ffjord_backward_impl(c, dLdlogpx, dLdzT, dL_dreg_f2, dL_dreg_ej, dLdx, dLdp, stats);
 }
 
 int gbnde_backward(gbnde_ctx* c, const float* dLdu, float* dLdu0, float* dLdp, gbnde_stats* stats) {

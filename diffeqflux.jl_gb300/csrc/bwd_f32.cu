@@ -153,6 +153,51 @@ __device__ __forceinline__ const float* fwd_eval_tile(const BwdArgs& a, int tile
   return mlp_fwd_tile(a.mlp, sm.gA, sm.gB, LD, TM, nullptr);
 }
 
+// The |e^T J| row's share of the FFJORD adjoint right-hand side (out of line:
+// it runs only with the regulariser rows and keeps its registers out of the
+// main kernel). v = J^T e by a reverse pass, w = v / |v| (0 where v = 0), then
+// the cotangent of e^T J w with w held fixed: a reverse-over-forward pass
+// along w with lam_j e on the tangent output; adds its z rows to kl_out and
+// its parameter cotangent to P (scaled by c). act holds the primal pass.
+__device__ __noinline__ void ffj_reg_pass(const BwdArgs& a, int tile, float* const* fact, float* const* fzd,
+                                          float* const* fcot, const float* flj, float* fnrm, float* kl_out,
+                                          float* P, float c) {
+  const MlpDev& m = a.mlp;
+  const int d = a.ffd, S = a.S, TM = a.TM, LD = a.LD;
+  const size_t base = (size_t)tile * TM * S;
+  const int nv = nvalid_of(a, tile);
+  for (int e = threadIdx.x; e < d * TM; e += blockDim.x) {
+    const int s = e / TM, mm = e - s * TM;
+    fcot[0][s * LD + mm] = mm < nv ? a.noise[((size_t)tile * TM + mm) * d + s] : 0.f;
+  }
+  __syncthreads();
+  const float* v = mlp_vjp_tile(m, fact, fcot[0], fcot[1], LD, TM, nullptr, 0.f);
+  for (int mm = threadIdx.x; mm < TM; mm += blockDim.x) {
+    float q = 0.f;
+    for (int s = 0; s < d; ++s) q = fmaf(v[s * LD + mm], v[s * LD + mm], q);
+    fnrm[mm] = q > 0.f ? 1.f / sqrtf(q) : 0.f;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < m.dims[0] * TM; e += blockDim.x) {
+    const int s = e / TM, mm = e - s * TM;
+    fzd[0][s * LD + mm] = s < d ? v[s * LD + mm] * fnrm[mm] : 0.f;
+  }
+  __syncthreads();
+  mlp_tangent_tile(m, fact, fzd, fcot[3], LD, TM);
+  for (int e = threadIdx.x; e < d * TM; e += blockDim.x) {
+    const int s = e / TM, mm = e - s * TM;
+    fcot[0][s * LD + mm] = 0.f;
+    fcot[2][s * LD + mm] = mm < nv ? flj[mm] * a.noise[((size_t)tile * TM + mm) * d + s] : 0.f;
+  }
+  __syncthreads();
+  const float* gi = ffjord_vjp_tile(m, fact, fzd, fcot[0], fcot[1], fcot[2], fcot[3], LD, TM, P, c);
+  for (int e = threadIdx.x; e < nv * S; e += blockDim.x) {
+    const int mm = e / S, s = e - mm * S;
+    if (s < d) kl_out[base + e] += gi[s * LD + mm];
+  }
+  __syncthreads();
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
@@ -230,6 +275,9 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
   float* fcot[4];
   float* ftmp = nullptr;
   float* flam = nullptr;  // lam_l per trajectory of the tile
+  float* flf = nullptr;   // cotangents of the |f|^2 and |e^T J| rows (ffreg)
+  float* flj = nullptr;
+  float* fnrm = nullptr;  // |J^T e| per trajectory
   if (a.ffj) {
     float* p = smem;
     for (int l = 0; l <= a.mlp.nlayers; ++l) { fact[l] = p; p += (size_t)a.mlp.dims[l] * LD; }
@@ -237,9 +285,17 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
     for (int q = 0; q < 4; ++q) { fcot[q] = p; p += (size_t)a.mlp.maxdim * LD; }
     ftmp = fcot[3];  // the tangent pass runs before fcot[3] is used as a cotangent
     flam = p;
+    flf = p + LD;
+    flj = p + 2 * LD;
+    fnrm = p + 3 * LD;
   }
   // FFJORD adjoint right-hand side: cotangent [lam_z; lam_l] of [f; -trace];
   // writes kl = lam_z^T df/dz - lam_l d(trace)/dz (z rows; 0 for the logp row).
+  // With the regulariser rows (cotangents lam_f, lam_j; src/ffjord.jl:131-132):
+  // |f|^2 adds 2 lam_f f to the primal output's cotangent, and |e^T J| adds the
+  // cotangent of e^T J w with w = J^T e / |J^T e| held fixed (d|v| = w^T dv),
+  // one more reverse-over-forward pass along w with e lam_j on the tangent
+  // output.
   auto ffj_eval = [&](int tile, double tt, auto&& lamv, auto&& uval, float* kl_out, float* P, float c,
                       float* lam_store) {
     const MlpDev& m = a.mlp;
@@ -257,14 +313,26 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       if (s < d) {
         fact[0][s * LD + mm] = u;
         fcot[0][s * LD + mm] = l;     // cotangent of f (primal output), rows < d
-      } else {
+      } else if (s == d) {
         flam[mm] = l;
+      } else if (s == d + 1) {
+        flf[mm] = l;
+      } else {
+        flj[mm] = l;
       }
     }
     if (m.timein)
       for (int mm = threadIdx.x; mm < TM; mm += blockDim.x) fact[0][d * LD + mm] = (float)tt;
     __syncthreads();
     mlp_fwd_tile(m, fact[0], nullptr, LD, TM, fact + 1);
+    if (a.ffreg) {
+      __syncthreads();
+      for (int e = threadIdx.x; e < d * TM; e += blockDim.x) {
+        const int s = e / TM, mm = e - s * TM;
+        fcot[0][s * LD + mm] = fmaf(2.f * flf[mm], fact[L][s * LD + mm], fcot[0][s * LD + mm]);
+      }
+      __syncthreads();
+    }
     const int ndir = a.exact ? d : 1;
     for (int k = 0; k < ndir; ++k) {
       for (int e = threadIdx.x; e < m.dims[0] * TM; e += blockDim.x) {
@@ -290,6 +358,7 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       }
       __syncthreads();
     }
+    if (a.ffreg & 2) ffj_reg_pass(a, tile, fact, fzd, fcot, flj, fnrm, kl_out, P, c);
   };
 
   auto adj_eval = [&](int tile, double tt, const Interval& iv, auto&& lamv, auto&& uval,

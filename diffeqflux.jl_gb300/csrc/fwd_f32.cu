@@ -72,8 +72,11 @@ __device__ __forceinline__ size_t tile_elems(const FwdArgs& a, int tile) {
 
 // FFJORD right-hand side of a tile: [f(z, t); -trace(df/dz)], the trace as
 // e^T (J e) along the sample's noise e (Hutchinson) or summed over the unit
-// directions (exact). smem: act[0..L], zd[0..L] (sum(dims) rows each), tmp
-// (maxdim rows), trace sums (TM).
+// directions (exact). With a.ffreg two more rows: |f|^2 and |e^T J|, the
+// latter through a reverse pass of the chain from the output cotangent e
+// (src/ffjord.jl:131-132). smem: act[0..L], zd[0..L] (sum(dims) rows each),
+// tmp (maxdim rows), trace sums (TM); with ffreg also the two row values (TM
+// each) and a second work buffer (maxdim rows).
 template <class Fn, class Sink>
 __device__ __forceinline__ void ffjord_rhs_tile(const FwdArgs& a, int tile, float* smem, double tstage,
                                                 Fn&& val, Sink&& sink) {
@@ -87,6 +90,12 @@ __device__ __forceinline__ void ffjord_rhs_tile(const FwdArgs& a, int tile, floa
   float* tmp = p;
   p += (size_t)m.maxdim * LD;
   float* tr = p;
+  p += LD;
+  float* rf = p;   // |f|^2
+  p += LD;
+  float* rj = p;   // |e^T J|
+  p += LD;
+  float* wk = p;   // second work buffer of the reverse pass
   const size_t base = (size_t)tile * TM * S;
   const int nvalid = min(TM, a.B - tile * TM);
   for (int e = threadIdx.x; e < TM * S; e += blockDim.x) {
@@ -120,9 +129,29 @@ __device__ __forceinline__ void ffjord_rhs_tile(const FwdArgs& a, int tile, floa
     });
     __syncthreads();
   }
+  if (a.ffreg) {
+    // v = J^T e: the chain's reverse pass from the output cotangent e
+    for (int e = threadIdx.x; e < d * TM; e += blockDim.x) {
+      const int s = e / TM, mm = e - s * TM;
+      tmp[s * LD + mm] = mm < nvalid ? a.noise[((size_t)tile * TM + mm) * d + s] : 0.f;
+    }
+    __syncthreads();
+    const float* v = mlp_vjp_tile(m, act, tmp, wk, LD, TM, nullptr, 0.f);
+    for (int mm = threadIdx.x; mm < TM; mm += blockDim.x) {
+      float sf = 0.f, sj = 0.f;
+      for (int s = 0; s < d; ++s) {
+        const float f = act[L][s * LD + mm], g = v[s * LD + mm];
+        sf = fmaf(f, f, sf);
+        sj = fmaf(g, g, sj);
+      }
+      rf[mm] = sf;
+      rj[mm] = sqrtf(sj);
+    }
+    __syncthreads();
+  }
   for (int e = threadIdx.x; e < nvalid * S; e += blockDim.x) {
     const int mm = e / S, s = e - mm * S;
-    sink(base + e, s < d ? act[L][s * LD + mm] : -tr[mm]);
+    sink(base + e, s < d ? act[L][s * LD + mm] : s == d ? -tr[mm] : s == d + 1 ? rf[mm] : rj[mm]);
   }
   __syncthreads();
 }

@@ -47,9 +47,10 @@ struct FwdArgs {
   int* status;
   long long* counters;
   double* tfinal;
-  // FFJORD mode: state = [z (ffd rows); delta_logp], RHS = [f(z); -trace]
-  int ffj, ffd, exact;
-  const float* noise;    // ffd x B (Hutchinson directions)
+  // FFJORD mode: state = [z (ffd rows); delta_logp], RHS = [f(z); -trace];
+  // with ffreg two more rows integrate |f|^2 and |e^T J| (e = noise)
+  int ffj, ffd, exact, ffreg;
+  const float* noise;    // ffd x B (Hutchinson directions; the e of |e^T J|)
 };
 
 // One backward interval of InterpolatingAdjoint: forward steps [nlo, nhi]
@@ -100,6 +101,8 @@ struct BwdArgs {
   int* status;
   long long* counters;
   int ffj, ffd, exact;    // FFJORD mode (see FwdArgs)
+  int ffreg;              // bit 0: the two regulariser rows; bit 1: the |e^T J|
+                          // row has a nonzero cotangent (its extra pass runs)
   const float* noise;
 };
 

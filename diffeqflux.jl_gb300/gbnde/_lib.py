@@ -101,6 +101,9 @@ _SIGS = {
     "gbnde_ffjord_forward": (C.c_int, [_P, C.POINTER(SolveDesc), C.c_int, C.c_int, _P, _P, _P, _P,
                                       C.POINTER(Stats)]),
     "gbnde_ffjord_backward": (C.c_int, [_P, _P, _P, _P, _P, C.POINTER(Stats)]),
+    "gbnde_ffjord_forward_reg": (C.c_int, [_P, C.POINTER(SolveDesc), C.c_int, C.c_int, _P, _P, C.c_int, _P, _P,
+                                          _P, _P, C.POINTER(Stats)]),
+    "gbnde_ffjord_backward_reg": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, C.POINTER(Stats)]),
     "gbnde_multishoot_forward": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Segment), C.POINTER(C.c_double),
                                           C.c_int, _P, C.c_double, C.c_double, C.c_longlong, _P,
                                           C.POINTER(C.c_int), C.POINTER(Stats)]),

@@ -6,7 +6,12 @@ the augmented system [z; delta_logp] with right-hand side
 [f(z [, t]); -trace(df/dz)] is solved from (x, 0), keeping only the end state,
 and logpx = logpz(z(t1)) - delta_logp(t1) with the standard-normal base.
 `st` carries the reference's flags: monte_carlo (Hutchinson trace, the
-default) or the exact trace; regularize=True is not offered. `basedist` is the
+default) or the exact trace, and regularize: two more rows integrate |f|^2
+and |e^T J| (src/ffjord.jl:131-132), returned as lambda1 and lambda2 (1 x B
+each) and differentiable like logpx. (The reference selects its lambda1 and
+lambda2 along the batch dimension of the end state, src/ffjord.jl:164-166,
+which returns batch columns rather than those two rows; the reference's tests
+use only logpx. This layer returns the two rows.) `basedist` is the
 base density: None for the standard normal, or an object with
 ``logpdf(z) -> (B,)`` on z of shape (d, B) (a torch-differentiable function of
 z when the layer is called with torch tensors); logpx = basedist.logpdf(z(t1))
@@ -86,6 +91,42 @@ class FFJORD:
         self._keep = nz
         return logpx, zT.T, st
 
+    def forward_reg_np(self, x, p, noise, exact):
+        """regularize = true: returns (logpx, z(t1), |f|^2 integral, |e^T J|
+        integral, stats); noise (B x d) is the e of |e^T J| and, unless exact,
+        the Hutchinson direction."""
+        s = self.solver
+        s.set_params(p)
+        x = np.ascontiguousarray(np.asarray(x, np.float32).T)
+        B = x.shape[0]
+        logpx = np.empty(B, np.float32)
+        zT = np.empty((B, self.d), np.float32)
+        rf = np.empty(B, np.float32)
+        rj = np.empty(B, np.float32)
+        st = _lib.Stats()
+        nz = np.ascontiguousarray(noise, np.float32)
+        s.bump()
+        _lib.check(s.lib.gbnde_ffjord_forward_reg(s.h, C.byref(self.desc()), self.d, B, x.ctypes.data,
+                                                  nz.ctypes.data, 1 if exact else 0, logpx.ctypes.data,
+                                                  zT.ctypes.data, rf.ctypes.data, rj.ctypes.data, C.byref(st)))
+        self._keep = nz
+        return logpx, zT.T, rf, rj, st
+
+    def backward_reg_np(self, dlogpx, dzT=None, drf=None, drj=None):
+        s = self.solver
+        g = np.ascontiguousarray(dlogpx, np.float32)
+        B = g.size
+        opt = lambda a: None if a is None else np.ascontiguousarray(np.asarray(a, np.float32))  # noqa: E731
+        gz = None if dzT is None else np.ascontiguousarray(np.asarray(dzT, np.float32).T)
+        gf, gj = opt(drf), opt(drj)
+        dx = np.empty((B, self.d), np.float32)
+        dp = np.empty(s.nparams, np.float32)
+        st = _lib.Stats()
+        ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+        _lib.check(s.lib.gbnde_ffjord_backward_reg(s.h, g.ctypes.data, ptr(gz), ptr(gf), ptr(gj),
+                                                   dx.ctypes.data, dp.ctypes.data, C.byref(st)))
+        return dx.T, dp, st
+
     def logpz_std(self, z):
         """log density of the standard-normal base at z (d x B): the library's logpx uses it."""
         return -0.5 * (z ** 2).sum(0) - 0.5 * self.d * np.log(2.0 * np.pi)
@@ -104,7 +145,7 @@ class FFJORD:
 
     def __call__(self, x, ps, st):
         if st.get("regularize", False):
-            raise NotImplementedError("regularize=True is not offered by the GB300 FFJORD")
+            return self._call_reg(x, ps, st)
         mc = st.get("monte_carlo", True)
         rng = st.get("rng") or np.random.default_rng(0)
         B = np.asarray(x.shape)[-1]
@@ -155,6 +196,56 @@ class FFJORD:
         return (lp.reshape(1, -1), dl, dl), st
 
 
+    def _call_reg(self, x, ps, st):
+        """regularize = true: (logpx, lambda1, lambda2) with lambda1 = the
+        integral of |f|^2 and lambda2 = that of |e^T J| (1 x B each)."""
+        exact = not st.get("monte_carlo", True)
+        rng = st.get("rng") or np.random.default_rng(0)
+        B = int(np.asarray(x.shape)[-1])
+        noise = self.draw_noise(rng, B)
+        try:
+            import torch
+            is_torch = isinstance(x, torch.Tensor) or isinstance(ps, torch.Tensor)
+        except ImportError:  # pragma: no cover
+            is_torch = False
+        if not is_torch:
+            logpx, zT, rf, rj, _ = self.forward_reg_np(x, ps, noise, exact)
+            if self.basedist is not None:
+                delta = self.logpz_std(zT.astype(np.float64)) - logpx
+                logpx = np.asarray(self.basedist.logpdf(zT)) - delta
+            return (logpx.reshape(1, -1), rf.reshape(1, -1), rj.reshape(1, -1)), st
+        import torch
+        layer = self
+
+        class _Fn(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, xt, pt):
+                ctx.inputs = (xt.detach().cpu().numpy(), pt.detach().cpu().numpy())
+                lp, zT, rf, rj, _ = layer.forward_reg_np(ctx.inputs[0], ctx.inputs[1], noise, exact)
+                ctx.generation = layer.solver.generation
+                dev = pt.device
+                return (torch.from_numpy(lp).to(dev), torch.from_numpy(np.ascontiguousarray(zT)).to(dev),
+                        torch.from_numpy(rf).to(dev), torch.from_numpy(rj).to(dev))
+
+            @staticmethod
+            def backward(ctx, g, gz, gf, gj):
+                if layer.solver.generation != ctx.generation:
+                    layer.forward_reg_np(ctx.inputs[0], ctx.inputs[1], noise, exact)
+                host = lambda a: None if a is None else a.detach().cpu().numpy()  # noqa: E731
+                dx, dp, _ = layer.backward_reg_np(host(g), host(gz), host(gf), host(gj))
+                return torch.from_numpy(np.ascontiguousarray(dx)).to(g.device), torch.from_numpy(dp).to(g.device)
+
+        xt = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x, np.float32))
+        pt = ps if isinstance(ps, torch.Tensor) else torch.as_tensor(np.asarray(ps, np.float32))
+        lp_std, zT, rf, rj = _Fn.apply(xt, pt)
+        if self.basedist is not None:
+            delta = (-0.5 * (zT.double() ** 2).sum(0) - 0.5 * self.d * np.log(2.0 * np.pi)) - lp_std.double()
+            lp = (self.basedist.logpdf(zT).double() - delta).to(lp_std.dtype)
+        else:
+            lp = lp_std
+        return (lp.reshape(1, -1), rf.reshape(1, -1), rj.reshape(1, -1)), st
+
+
 class FFJORDDistribution:
     """``FFJORDDistribution(model, ps, st)`` (src/ffjord.jl:217-246): `rand` solves
     the flow backwards in time from base samples (``reverse(tspan)``, :183-214)
@@ -182,7 +273,13 @@ class FFJORDDistribution:
     def rand(self, n, rng=None):
         rng = rng or self.st.get("rng") or np.random.default_rng(0)
         x = rng.standard_normal((self.model.d, n)).astype(np.float32)
+        mc = self.st.get("monte_carlo", True)
         noise = self._rev.draw_noise(rng, n)
-        _, zT, st = self._rev.forward_np(x, self.ps, noise)
+        if self.st.get("regularize", False):
+            # the regulariser rows ride along (and enter the step-size control)
+            # as in the reference's reversed solve (src/ffjord.jl:192-213)
+            _, zT, _, _, st = self._rev.forward_reg_np(x, self.ps, noise, not mc)
+        else:
+            _, zT, st = self._rev.forward_np(x, self.ps, noise if mc else None)
         _lib.check(0 if st.retcode == 0 else _lib.ERR_INVALID)
         return zT

@@ -324,9 +324,65 @@ function ChainRulesCore.rrule(::typeof(gb300_ffjord), x, p, ctx, tspan, abstol, 
     (logpx, zT), gb300_ffjord_pullback
 end
 
+"""
+    gb300_ffjord_reg(x, p, ctx, tspan, abstol, reltol, noise, exact)
+        -> (logpx (1 x B), z(t1) (d x B), λ₁ (1 x B), λ₂ (1 x B))
+
+`regularize = true` (src/ffjord.jl:131-135): two more rows integrate |f|^2 and
+|eᵀJ| from 0; λ₁ and λ₂ are their values at t1. `noise` (d x B) is the e of
+|eᵀJ| and, unless `exact`, the Hutchinson direction.
+"""
+function gb300_ffjord_reg(x::AbstractMatrix{Float32}, p::AbstractVector{Float32}, ctx::Ctx, tspan, abstol,
+                          reltol, noise::AbstractMatrix{Float32}, exact::Bool)
+    d, B = size(x)
+    set_params!(ctx, p)
+    logpx = Vector{Float32}(undef, B)
+    zT = Matrix{Float32}(undef, d, B)
+    rf = Vector{Float32}(undef, B)
+    rj = Vector{Float32}(undef, B)
+    st = Stats()
+    sv = Float64[tspan[2]]
+    GC.@preserve sv noise begin
+        sd = Ref(SolveDesc(tspan[1], tspan[2], abstol, reltol, 0, 0, 100000, pointer(sv), 1, 0, 0))
+        check(ccall((:gbnde_ffjord_forward_reg, libgbnde), Cint,
+                    (Ptr{Cvoid}, Ref{SolveDesc}, Cint, Cint, Ptr{Float32}, Ptr{Float32}, Cint, Ptr{Float32},
+                     Ptr{Float32}, Ptr{Float32}, Ptr{Float32}, Ref{Stats}),
+                    ctx.h, sd, d, B, Matrix{Float32}(x), pointer(noise), Cint(exact), logpx, zT, rf, rj, st))
+    end
+    ctx.gen += 1
+    ctx.stats = st
+    reshape(logpx, 1, B), zT, reshape(rf, 1, B), reshape(rj, 1, B)
+end
+
+function ChainRulesCore.rrule(::typeof(gb300_ffjord_reg), x, p, ctx, tspan, abstol, reltol, noise, exact)
+    out = gb300_ffjord_reg(x, p, ctx, tspan, abstol, reltol, noise, exact)
+    gen = ctx.gen
+    function gb300_ffjord_reg_pullback(Δ)
+        d, B = size(x)
+        Δl, Δz, Δf, Δj = unthunk(Δ[1]), unthunk(Δ[2]), unthunk(Δ[3]), unthunk(Δ[4])
+        gl = Δl isa AbstractZero ? zeros(Float32, B) : vec(Float32.(Δl))
+        gz = Δz isa AbstractZero ? nothing : Matrix{Float32}(Δz)
+        gf = Δf isa AbstractZero ? nothing : vec(Float32.(Δf))
+        gj = Δj isa AbstractZero ? nothing : vec(Float32.(Δj))
+        ctx.gen == gen || gb300_ffjord_reg(x, p, ctx, tspan, abstol, reltol, noise, exact)
+        dx = Matrix{Float32}(undef, d, B)
+        dp = Vector{Float32}(undef, length(p))
+        bst = Stats()
+        ptr(a) = a === nothing ? Ptr{Float32}(C_NULL) : pointer(a)
+        GC.@preserve gz gf gj begin
+            check(ccall((:gbnde_ffjord_backward_reg, libgbnde), Cint,
+                        (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Ptr{Float32}, Ptr{Float32}, Ptr{Float32},
+                         Ptr{Float32}, Ref{Stats}),
+                        ctx.h, gl, ptr(gz), ptr(gf), ptr(gj), dx, dp, bst))
+        end
+        (NoTangent(), dx, dp, NoTangent(), NoTangent(), NoTangent(), NoTangent(), NoTangent(), NoTangent())
+    end
+    out, gb300_ffjord_reg_pullback
+end
+
 function _ffjord_forward(n::FFJORD, x::AbstractMatrix, ps, st, alg::GB300Tsit5)
     (; regularize, monte_carlo) = st
-    regularize && throw(ArgumentError("regularize = true is not offered by the GB300 FFJORD"))
+    regularize && return _ffjord_forward_reg(n, x, ps, st, alg)
     d, B = size(x)
     ctx = ctx_for(n.model, alg.precision)
     kw = Dict(n.kwargs)
@@ -340,6 +396,24 @@ function _ffjord_forward(n::FFJORD, x::AbstractMatrix, ps, st, alg::GB300Tsit5)
     delta_logp = logpz_std .- logpx_std
     logpx = n.basedist === nothing ? logpx_std : reshape(logpdf(n.basedist, zT), 1, B) .- delta_logp
     (logpx, delta_logp, delta_logp), st
+end
+
+# regularize = true: (logpx, λ₁, λ₂) with λ₁, λ₂ the two regulariser rows at t1.
+# (The reference selects λ₁ and λ₂ along the batch dimension of the end state,
+# src/ffjord.jl:164-166, i.e. batch columns; its tests read only logpx.)
+function _ffjord_forward_reg(n::FFJORD, x::AbstractMatrix, ps, st, alg::GB300Tsit5)
+    d, B = size(x)
+    ctx = ctx_for(n.model, alg.precision)
+    kw = Dict(n.kwargs)
+    noise = ChainRulesCore.@ignore_derivatives(randn(Float32, d, B))
+    logpx_std, zT, λ₁, λ₂ = gb300_ffjord_reg(Float32.(x), Float32.(collect(ps)), ctx, Float64.(n.tspan),
+                                             get(kw, :abstol, 1e-6), get(kw, :reltol, 1e-3), noise,
+                                             !st.monte_carlo)
+    T = Float32
+    logpz_std = -sum(abs2, zT; dims = 1) / T(2) .- T(d / 2 * log(2π))
+    delta_logp = logpz_std .- logpx_std
+    logpx = n.basedist === nothing ? logpx_std : reshape(logpdf(n.basedist, zT), 1, B) .- delta_logp
+    (logpx, λ₁, λ₂), st
 end
 
 # ---- multiple shooting on the GB300 path (src/multiple_shooting.jl:36-94) ---------------

@@ -218,6 +218,24 @@ int gbnde_ffjord_forward(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int d, in
  * src/ffjord.jl:143). dL_dzT may be NULL. Outputs dL/dx (d x B) and dL/dp. */
 int gbnde_ffjord_backward(gbnde_ctx* ctx, const float* dL_dlogpx, const float* dL_dzT, float* dL_dx,
                           float* dL_dp, gbnde_stats* stats);
+/* FFJORD with regularize = true (src/ffjord.jl:131-135, :151-168): the
+ * augmented system gains two rows that integrate |f|^2 (the sum of squares
+ * of the model's d outputs) and |e^T (df/dz)| (the 2-norm of the
+ * vector-Jacobian product along the sample's noise e) from 0; reg_f2 and
+ * reg_ej (B each, may be NULL) receive their values at t1 -- the lambda1 and
+ * lambda2 the reference returns beside logpx. Both rows enter the step-size
+ * control like the reference's. noise (d x B) is required: it is the e of
+ * |e^T J| and, unless exact_trace, the Hutchinson direction of the trace.
+ * Runs on the FP32 kernels in both precisions (gbnde_stats.fwd_path). */
+int gbnde_ffjord_forward_reg(gbnde_ctx* ctx, const gbnde_solve_desc* desc, int d, int B, const float* x,
+                             const float* noise, int exact_trace, float* logpx, float* zT, float* reg_f2,
+                             float* reg_ej, gbnde_stats* stats);
+/* Gradient through the last gbnde_ffjord_forward_reg of a loss of logpx,
+ * z(t1) and the two regulariser values (dL_dzT, dL_dreg_f2, dL_dreg_ej may be
+ * NULL for zero). Outputs dL/dx (d x B) and dL/dp. */
+int gbnde_ffjord_backward_reg(gbnde_ctx* ctx, const float* dL_dlogpx, const float* dL_dzT,
+                              const float* dL_dreg_f2, const float* dL_dreg_ej, float* dL_dx, float* dL_dp,
+                              gbnde_stats* stats);
 
 /* ---- multiple shooting -------------------------------------------------------------
  * Replaces the per-group solves of multiple_shoot (src/multiple_shooting.jl:52-62):

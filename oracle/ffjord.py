@@ -7,7 +7,11 @@ Follows src/ffjord.jl:
     (monte_carlo = false, :120-129) or the Hutchinson estimate e^T (df/dz) e
     (monte_carlo = true, :92-115);
   * logpx = logpz(z(t1)) - delta_logp(t1) with the standard-normal base
-    logpz = -|z|^2/2 - d/2 log(2 pi) (:171-176).
+    logpz = -|z|^2/2 - d/2 log(2 pi) (:171-176);
+  * regularize = true (:131-132, :151-168): two more rows integrate |f|^2
+    (sum over the d outputs) and |e^T J| (the 2-norm of the vector-Jacobian
+    product along the noise e; the exact-trace mode draws e for this row
+    only).
 Deliberate, documented differences: the noise e is drawn once per sample per
 solve (Rademacher or Gaussian) instead of fresh on every RHS call, so that
 the ODE -- and its adjoint -- is well defined; e^T J e is evaluated as e . (J e)
@@ -16,6 +20,9 @@ pass); the two are the same number.
 
 The adjoint needs d/d(z, p) of e^T J e: reverse mode over the forward-mode
 tangent computation ("reverse over forward"), written out per layer below.
+For the |e^T J| row: with v = J^T e and w = v / |v|, d|v| = w^T dv =
+e^T (dJ) w, so its cotangent is that of e^T J w with w held fixed -- the same
+reverse-over-forward pass along the direction w, with e as the weight.
 """
 import numpy as np
 
@@ -45,12 +52,14 @@ def _d2(code, a, z):
 class FFJORDRHS:
     """RHS of the augmented FFJORD state y = [z (d x B); delta_logp (1 x B)]."""
 
-    def __init__(self, mlp, p, noise=None, exact=False):
+    def __init__(self, mlp, p, noise=None, exact=False, regularize=False):
         assert not mlp.cube_input
+        assert not regularize or noise is not None, "the |e^T J| row needs the noise e"
         self.mlp = mlp
         self.p = np.asarray(p, dtype=np.float64)
         self.noise = noise
         self.exact = exact
+        self.regularize = regularize
         self.d = mlp.state_dim
         self.nf = 0
 
@@ -90,30 +99,57 @@ class FFJORDRHS:
         c = self._fwd_tangent(z, t, self.noise)
         return c[-1][1], np.sum(self.noise * c[-1][3], axis=0, keepdims=True)
 
+    def _vjp_input(self, z, t, g):
+        """J^T g: the cotangent of the chain input (z rows only) for the output
+        cotangent g, by a plain reverse pass."""
+        layers = self.mlp.unflatten(self.p)
+        a = self._input(z, t)
+        acts = [a]
+        for l, (W, b) in enumerate(layers):
+            a = omlp._act(self.mlp.acts[l], W @ a + b[:, None])
+            acts.append(a)
+        for l in range(len(layers) - 1, -1, -1):
+            zl = layers[l][0] @ acts[l] + layers[l][1][:, None]
+            g = layers[l][0].T @ (g * _d1(self.mlp.acts[l], acts[l + 1], zl))
+        return g[: self.d]
+
     def f(self, y, t):
         self.nf += 1
         z = y[: self.d]
         f, tr = self._trace(z, t)
-        return np.vstack([f, -tr])
+        if not self.regularize:
+            return np.vstack([f, -tr])
+        v = self._vjp_input(z, t, self.noise)
+        return np.vstack([f, -tr, np.sum(f * f, axis=0, keepdims=True),
+                          np.sqrt(np.sum(v * v, axis=0, keepdims=True))])
 
     def vjp(self, y, t, lam):
         """(lam^T dg/dy, lam^T dg/dp) for g = [f; -e^T J e] (Hutchinson) or
         g = [f; -tr J] (exact)."""
         z = y[: self.d]
-        lz, ll = lam[: self.d], lam[self.d:]
+        lz, ll = lam[: self.d], lam[self.d:self.d + 1]
         layers = self.mlp.unflatten(self.p)
-        es = [self.noise] if not self.exact else []
+        # (tangent direction, weight of the tangent output) per pass
+        es = [(self.noise, -ll * self.noise)] if not self.exact else []
         if self.exact:
             for i in range(self.d):
                 e = np.zeros_like(z)
                 e[i] = 1.0
-                es.append(e)
+                es.append((e, -ll * e))
+        if self.regularize:
+            # |f|^2 row: cotangent 2 lam f on the primal output
+            f = self._fwd_tangent(z, t, np.zeros_like(z))[-1][1]
+            lz = lz + 2.0 * lam[self.d + 1:self.d + 2] * f
+            # |e^T J| row: direction w = v/|v|, weight lam e
+            v = self._vjp_input(z, t, self.noise)
+            nv = np.sqrt(np.sum(v * v, axis=0, keepdims=True))
+            w = np.divide(v, nv, out=np.zeros_like(v), where=nv > 0)
+            es.append((w, lam[self.d + 2:self.d + 3] * self.noise))
         gz_tot = np.zeros_like(z)
         grads_tot = None
-        for k, e in enumerate(es):
+        for k, (e, adbar) in enumerate(es):
             c = self._fwd_tangent(z, t, e)
             abar = lz if k == 0 else np.zeros_like(lz)   # primal cotangent (f appears once)
-            adbar = -ll * e                               # cotangent of the tangent output
             grads = [None] * len(layers)
             for l in range(len(layers) - 1, -1, -1):
                 zl, al, zd, _ = c[l + 1]
@@ -131,7 +167,7 @@ class FFJORDRHS:
             g = self.mlp.flatten(grads)
             grads_tot = g if grads_tot is None else grads_tot + g
             gz_tot += abar[: self.d]
-        return np.vstack([gz_tot, np.zeros_like(ll)]), grads_tot
+        return np.vstack([gz_tot, np.zeros_like(lam[self.d:])]), grads_tot
 
 
 def logpx_from_final(yT, d):

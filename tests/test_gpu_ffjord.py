@@ -205,3 +205,90 @@ def test_ffjord_bf16_small():
 def test_ffjord_bf16_config3_structure():
     """d = 16, (16+1) -> 512 -> 512 -> 16 softplus with time concatenated, on the tensor cores."""
     _case_bf16(16, 512, 256, "softplus", 6, tol=1e-5)
+
+
+def _case_reg(d, H, B, act, exact, seed, wa, wb, precision="fp32", tol=1e-7):
+    """regularize = true (src/ffjord.jl:131-132): the |f|^2 and |e^T J| rows
+    against the FP64 oracle (values 1e-4 relative to their max), and the
+    gradient of -mean(logpx) + wa mean(lambda1) + wb mean(lambda2) through the
+    adjoint (1e-3 relative norm). Either precision runs the FP32 kernels."""
+    import gbnde
+    from gbnde import _lib
+    from oracle import ffjord as off
+    from oracle import mlp as omlp
+    from oracle import tsit5 as ots
+    rng = np.random.default_rng(seed)
+    model = gbnde.Chain(gbnde.Dense(d + 1, H, act), gbnde.Dense(H, H, act), gbnde.Dense(H, d))
+    p = model.init_params(rng)
+    x = rng.standard_normal((d, B)).astype(np.float32)
+    fj = gbnde.FFJORD(model, (0.0, 1.0), (d,), gbnde.Tsit5(precision), abstol=tol, reltol=tol,
+                      time_input=True, noise="gaussian")
+    noise = fj.draw_noise(rng, B)
+    logpx, zT, rf, rj, st = fj.forward_reg_np(x, p, noise, exact)
+    assert st.retcode == 0 and st.fwd_path == _lib.PATH_FP32
+    om = omlp.MLP(model.dims, model.acts, time_input=True)
+    rhs = off.FFJORDRHS(om, p.astype(np.float64), noise=noise.T.astype(np.float64), exact=exact,
+                        regularize=True)
+    y0 = np.vstack([x.astype(np.float64), np.zeros((3, B))])
+    ys, fwd = ots.solve_forward(rhs, y0, 0.0, 1.0, [1.0], tol, tol)
+    yT = ys[..., 0]
+    ref = off.logpx_from_final(yT, d)
+    assert np.abs(logpx - ref).max() < 1e-4 * np.abs(ref).max()
+    assert np.abs(zT - yT[:d]).max() < 1e-4 * np.abs(yT[:d]).max()
+    assert np.abs(rf - yT[d + 1]).max() < 1e-4 * np.abs(yT[d + 1]).max()
+    assert np.abs(rj - yT[d + 2]).max() < 1e-4 * np.abs(yT[d + 2]).max()
+    g = -np.ones(B) / B
+    drf = np.full(B, wa / B, np.float32)
+    drj = np.full(B, wb / B, np.float32)
+    dx, dp, sta = fj.backward_reg_np(g.astype(np.float32), None, drf, drj)
+    assert sta.retcode_adj == 0 and sta.adj_path == _lib.PATH_FP32
+    dy = np.vstack([-yT[:d] * g, -g[None, :], drf[None, :].astype(np.float64), drj[None, :].astype(np.float64)])
+    gu, gp, _ = ots.adjoint_interpolating(rhs, fwd, [1.0], dy[..., None], 0.0, tol, tol)
+    rel = lambda a, b: np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b)  # noqa: E731
+    assert rel(dp, gp) < 1e-3, rel(dp, gp)
+    assert rel(dx, gu[:d]) < 1e-3, rel(dx, gu[:d])
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_ffjord_regularized_rows_and_gradient(exact):
+    _case_reg(2, 16, 64, "tanh", exact, 11, 0.5, 0.8)
+
+
+def test_ffjord_regularized_without_the_ej_cotangent():
+    """lambda2 unused in the loss (the reference's tests): the |e^T J| pass of
+    the adjoint is skipped, the |f|^2 term still enters."""
+    _case_reg(2, 16, 64, "softplus", False, 12, 0.3, 0.0)
+
+
+def test_ffjord_regularized_config3_structure_bf16_request():
+    """d = 16, (16+1) -> 512 -> 512 -> 16 softplus, BF16 requested: the
+    regularised system runs on the FP32 kernels and the stats say so."""
+    _case_reg(16, 512, 96, "softplus", False, 13, 0.1, 0.1, precision="bf16", tol=1e-5)
+
+
+def test_ffjord_regularized_layer_torch_autograd():
+    """(logpx, lambda1, lambda2) from the layer with st regularize = true; the
+    gradient of a loss using all three matches the C-ABI backward."""
+    import torch
+
+    import gbnde
+    d, H, B = 2, 12, 32
+    rng = np.random.default_rng(14)
+    model = gbnde.Chain(gbnde.Dense(d + 1, H, "tanh"), gbnde.Dense(H, d))
+    fj = gbnde.FFJORD(model, (0.0, 1.0), (d,), gbnde.Tsit5(), abstol=1e-6, reltol=1e-6, time_input=True)
+    p, st = fj.setup(rng)
+    st["regularize"] = True
+    st["rng"] = np.random.default_rng(5)
+    x = rng.standard_normal((d, B)).astype(np.float32)
+    pt = torch.tensor(p, requires_grad=True)
+    (logpx, l1, l2), _ = fj(torch.tensor(x), pt, st)
+    assert logpx.shape == (1, B) and l1.shape == (1, B) and l2.shape == (1, B)
+    assert torch.all(l1 > 0) and torch.all(l2 > 0)
+    loss = -logpx.mean() + 0.1 * l1.mean() + 0.2 * l2.mean()
+    loss.backward()
+    noise = fj.draw_noise(np.random.default_rng(5), B)
+    lp2, _, rf, rj, _ = fj.forward_reg_np(x, p, noise, False)
+    assert np.allclose(lp2, logpx.detach().numpy().ravel()) and np.allclose(rf, l1.detach().numpy().ravel())
+    _, dp, _ = fj.backward_reg_np(np.full(B, -1.0 / B, np.float32), None, np.full(B, 0.1 / B, np.float32),
+                                  np.full(B, 0.2 / B, np.float32))
+    assert np.allclose(pt.grad.numpy(), dp, rtol=1e-5, atol=1e-7)
