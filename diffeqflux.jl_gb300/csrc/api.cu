@@ -213,6 +213,7 @@ struct gbnde_ctx {
   DBuf ms_segs, ms_saveat, ms_u0, ms_usave, ms_dense, ms_steplog, ms_nacc, ms_ret, ms_cnt, ms_dldu,
       ms_dldu0, ms_bar, ms_mu, ms_dldp;
   bool ms_have = false;
+  bool ms_saves = false;  // ms_usave holds the saves of the last multishoot forward
   // multiple-shooting loss on the device: the data, the column/segment maps
   // and the per-block partials; ms_dl_ok: ms_dldu holds the last loss's cotangent
   DBuf ms_data, ms_map, ms_part;
@@ -1570,7 +1571,7 @@ int gbnde_multishoot_forward(gbnde_ctx* c, int S, int nseg, const gbnde_segment*
                              const double* saveat, int nsave_total, const float* u0, double abstol,
                              double reltol, long long maxiters, float* usave, int* retcodes,
                              gbnde_stats* stats) {
-  if (!c || !segs || !saveat || !u0 || !usave) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (!c || !segs || !saveat || !u0) return fail(GBNDE_ERR_INVALID, "null argument");
   if (!c->have_params) return fail(GBNDE_ERR_STATE, "parameters not set");
   if (S != c->S || nseg < 1 || nsave_total < 1) return fail(GBNDE_ERR_INVALID, "bad sizes");
   if (c->mlp.timein) return fail(GBNDE_ERR_UNSUPPORTED, "multiple shooting with a time input");
@@ -1588,6 +1589,7 @@ int gbnde_multishoot_forward(gbnde_ctx* c, int S, int nseg, const gbnde_segment*
   if (int r = set_device(c)) return r;
   c->ms_have = false;
   c->ms_dl_ok = false;
+  c->ms_saves = false;
   c->ms_hsegs.assign(segs, segs + nseg);
   c->ms_S = S;
   c->ms_nseg = nseg;
@@ -1623,7 +1625,7 @@ int gbnde_multishoot_forward(gbnde_ctx* c, int S, int nseg, const gbnde_segment*
   CK(cudaEventRecord(c->ev[1], st));
   long long cnt[8];
   CK(cudaMemcpyAsync(cnt, c->ms_cnt.p, sizeof cnt, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(usave, c->ms_usave.p, (size_t)S * nsave_total * 4, cudaMemcpyDeviceToHost, st));
+  if (usave) CK(cudaMemcpyAsync(usave, c->ms_usave.p, (size_t)S * nsave_total * 4, cudaMemcpyDeviceToHost, st));
   std::vector<int> ret(nseg);
   CK(cudaMemcpyAsync(ret.data(), c->ms_ret.p, nseg * sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -1644,6 +1646,17 @@ int gbnde_multishoot_forward(gbnde_ctx* c, int S, int nseg, const gbnde_segment*
     stats->fwd_path = GBNDE_PATH_FP32;
   }
   c->ms_have = (worst == GBNDE_RET_SUCCESS);
+  c->ms_saves = true;
+  return 0;
+}
+
+int gbnde_multishoot_saves(gbnde_ctx* c, float* usave) {
+  if (!c || !usave) return fail(GBNDE_ERR_INVALID, "null argument");
+  if (!c->ms_saves) return fail(GBNDE_ERR_STATE, "no multishoot forward to read the saves of");
+  if (int r = set_device(c)) return r;
+  CK(cudaMemcpyAsync(usave, c->ms_usave.p, (size_t)c->ms_S * c->ms_nsave * 4, cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   return 0;
 }
 

@@ -107,6 +107,7 @@ _SIGS = {
     "gbnde_multishoot_forward": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Segment), C.POINTER(C.c_double),
                                           C.c_int, _P, C.c_double, C.c_double, C.c_longlong, _P,
                                           C.POINTER(C.c_int), C.POINTER(Stats)]),
+    "gbnde_multishoot_saves": (C.c_int, [_P, _P]),
     "gbnde_multishoot_backward": (C.c_int, [_P, _P, _P, _P, C.POINTER(Stats)]),
     "gbnde_multishoot_loss": (C.c_int, [_P, _P, _P, C.c_int, C.c_double, C.POINTER(C.c_double)]),
     "gbnde_loss_noalloc": (C.c_int, [_P, _P, C.c_size_t, C.c_int, _P, C.POINTER(C.c_double), _P]),

@@ -75,6 +75,11 @@ class _Layout:
         self.saveat = np.ascontiguousarray(saveat, dtype=np.float64)
         self.seg_next = np.ascontiguousarray(nxt, dtype=np.int32)
         self.nseg = len(segs)
+        # the same indices into the trajectories' data concatenated along time
+        self.lengths = np.asarray([len(ts) for ts, _ in shapes], dtype=np.int64)
+        offs = np.concatenate([[0], np.cumsum(self.lengths)[:-1]]).astype(np.int64)
+        self.gcols = np.concatenate([c + o for c, o in zip(self.cols, offs)])
+        self.gstarts = np.concatenate([st + o for st, o in zip(self.starts, offs)])
 
 
 class _Packed:
@@ -94,9 +99,14 @@ class _Packed:
         self.layout = lay
         self.segs, self.saveat, self.nseg, self.groups = lay.segs, lay.saveat, lay.nseg, lay.groups
         ds = [np.asarray(d, dtype=np.float32) for d, _, _ in trajectories]
-        # u0: nseg x S (column-major S x nseg); data at the saves: nsave_total x S
-        self.u0 = np.ascontiguousarray(np.concatenate([d[:, st].T for d, st in zip(ds, lay.starts)], axis=0))
-        self.data = np.ascontiguousarray(np.concatenate([d[:, c].T for d, c in zip(ds, lay.cols)], axis=0))
+        for d, n in zip(ds, lay.lengths):
+            if d.ndim != 2 or d.shape[1] != n:
+                raise ValueError(f"trajectory data of shape {d.shape} does not have {n} time points")
+        # u0: nseg x S (column-major S x nseg); data at the saves: nsave_total x S,
+        # both gathered as rows of the time-major view of the concatenated data
+        allT = np.concatenate(ds, axis=1).T
+        self.u0 = allT[lay.gstarts]
+        self.data = allT[lay.gcols]
 
 
 class MultipleShooter:
@@ -106,22 +116,31 @@ class MultipleShooter:
         self.solver = solver
         self.abstol, self.reltol, self.maxiters = float(abstol), float(reltol), int(maxiters)
 
-    def forward(self, packed, p):
+    def forward(self, packed, p, fetch=True):
+        """Solves every segment; returns (saves S x nsave_total, or None when
+        fetch is False and they stay on the device, retcodes, stats)."""
         s = self.solver
         if hasattr(p, "is_cuda") and p.is_cuda:
             s.set_params_device(p.detach().to(dtype=__import__("torch").float32).contiguous())
         else:
             s.set_params(p.detach().cpu().numpy() if hasattr(p, "detach") else p)
         S = s.state_dim
-        out = np.empty((len(packed.saveat), S), dtype=np.float32)
+        out = np.empty((len(packed.saveat), S), dtype=np.float32) if fetch else None
         ret = np.zeros(packed.nseg, dtype=np.int32)
         st = _lib.Stats()
         s.bump()
         _lib.check(s.lib.gbnde_multishoot_forward(
             s.h, S, packed.nseg, packed.segs, packed.saveat.ctypes.data_as(C.POINTER(C.c_double)),
             len(packed.saveat), packed.u0.ctypes.data, self.abstol, self.reltol, self.maxiters,
-            out.ctypes.data, ret.ctypes.data_as(C.POINTER(C.c_int)), C.byref(st)))
-        return out.T, ret, st  # S x nsave_total
+            None if out is None else out.ctypes.data, ret.ctypes.data_as(C.POINTER(C.c_int)), C.byref(st)))
+        return (None if out is None else out.T), ret, st  # S x nsave_total
+
+    def saves(self, packed):
+        """The saves of the last forward (S x nsave_total), copied from the device."""
+        s = self.solver
+        out = np.empty((len(packed.saveat), s.state_dim), dtype=np.float32)
+        _lib.check(s.lib.gbnde_multishoot_saves(s.h, out.ctypes.data))
+        return out.T
 
     def backward(self, dL_dusave):
         s = self.solver
@@ -152,10 +171,19 @@ class MultipleShooter:
 
 
 class _Groups:
-    """The group predictions (S x len(range) each), sliced from the packed saves on access."""
+    """The group predictions (S x len(range) each), sliced from the packed saves
+    on access. `us` is the S x nsave_total array, or a function returning it
+    (called once, on the first access)."""
 
     def __init__(self, us, groups, segs):
-        self._us, self._groups, self._segs = us, groups, segs
+        self._src, self._groups, self._segs = us, groups, segs
+        self._arr = None
+
+    @property
+    def _us(self):
+        if self._arr is None:
+            self._arr = self._src() if callable(self._src) else self._src
+        return self._arr
 
     def __len__(self):
         return len(self._groups)
@@ -177,16 +205,23 @@ def _fused_loss(shooter, packed, p, kind, continuity_term):
         import torch
     except ImportError:  # pragma: no cover
         torch = None
-    us, ret, _ = shooter.forward(packed, p)
+    # the saves stay on the device; the predictions are copied out on first use
+    _, ret, _ = shooter.forward(packed, p, fetch=False)
     shooter._nseg = packed.nseg
-    preds = _Groups(us, packed.groups, packed.segs)
+    solver = shooter.solver
+    gen = solver.generation
+
+    def fetch():
+        if solver.generation != gen:
+            # another solve ran on the context since: this call's forward again
+            return shooter.forward(packed, p)[0]
+        return shooter.saves(packed)
+    preds = _Groups(fetch, packed.groups, packed.segs)
     if np.any(ret != 0):
         return math.inf, preds
     L = shooter.loss(packed, kind, continuity_term)
     if torch is None or not isinstance(p, torch.Tensor):
         return L, preds
-    solver = shooter.solver
-    gen = solver.generation
 
     class _Fn(torch.autograd.Function):
         @staticmethod

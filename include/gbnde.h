@@ -243,8 +243,10 @@ int gbnde_ffjord_backward_reg(gbnde_ctx* ctx, const float* dL_dlogpx, const floa
  * step-size control and saves at saveat[save_off .. save_off + nsave - 1]
  * (times inside [t0, t1], increasing). All segments run in one launch.
  * FP32 arithmetic in both precisions. usave: S x nsave_total (column j = save
- * time j). retcodes[i] is segment i's gbnde_retcode (the reference turns any
- * failure into an Inf loss, src/multiple_shooting.jl:66-67). */
+ * time j), or NULL to keep the saves on the device only (gbnde_multishoot_loss
+ * reads them there; gbnde_multishoot_saves copies them out later). retcodes[i]
+ * is segment i's gbnde_retcode (the reference turns any failure into an Inf
+ * loss, src/multiple_shooting.jl:66-67). */
 typedef struct {
   double t0, t1;
   int save_off;
@@ -255,6 +257,10 @@ int gbnde_multishoot_forward(gbnde_ctx* ctx, int S, int nseg, const gbnde_segmen
                              const double* saveat, int nsave_total, const float* u0,
                              double abstol, double reltol, long long maxiters, float* usave,
                              int* retcodes, gbnde_stats* stats);
+/* Copies the saves (S x nsave_total) of the last gbnde_multishoot_forward to
+ * host memory: the group predictions of multiple_shoot
+ * (src/multiple_shooting.jl:83-93) when the forward kept them on the device. */
+int gbnde_multishoot_saves(gbnde_ctx* ctx, float* usave);
 /* The loss of multiple_shoot on the device (src/multiple_shooting.jl:69-81):
  * over the saves of the last gbnde_multishoot_forward,
  *   loss = sum_g lf(data_g, pred_g)

@@ -191,16 +191,23 @@ def test_fused_device_loss_matches_host_loop_and_oracle(kind, device):
     host = (lambda u, uh: ((u - uh) ** 2).mean()) if kind == "mse" else (lambda u, uh: ((u - uh) ** 2).sum())
     dev = torch.device(device, 0) if device == "cuda" else torch.device("cpu")
     pf = torch.tensor(p, device=dev, requires_grad=True)
+    # the fused path keeps the saves on the device: `early` is read right
+    # after the call (gbnde_multishoot_saves), `preds` only after another solve
+    # ran on the context (the forward is solved again)
+    _, early = gbnde.multiple_shoot_batch(pf, trajs, solver, lf, abstol=tol, reltol=tol)
+    early = [np.asarray(a).copy() for a in early]
     Lf, preds = gbnde.multiple_shoot_batch(pf, trajs, solver, lf, abstol=tol, reltol=tol)
     Lf.backward()
     ph = torch.tensor(p, requires_grad=True)
     Lh, preds_h = gbnde.multiple_shoot_batch(ph, trajs, solver, host, abstol=tol, reltol=tol)
     Lh.backward()
-    assert abs(float(Lf) - float(Lh)) / abs(float(Lh)) < 1e-6
+    Lf, Lh = float(Lf.detach()), float(Lh.detach())
+    assert abs(Lf - Lh) / abs(Lh) < 1e-6
     assert _rel(pf.grad.cpu().numpy(), ph.grad.numpy()) < 1e-5
-    assert len(preds) == len(preds_h)
-    for a, b in zip(preds, preds_h):
+    assert len(preds) == len(preds_h) == len(early)
+    for a, b, c in zip(preds, preds_h, early):
         assert np.array_equal(np.asarray(a), b.detach().numpy())
+        assert np.array_equal(c, b.detach().numpy())
     om = omlp.MLP(model.dims, model.acts)
     ofn = (lambda u, uh: float(np.mean((u - uh) ** 2))) if kind == "mse" else None
     Lref = 0.0

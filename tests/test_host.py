@@ -54,3 +54,33 @@ def test_sweep_targets_solve_the_linear_ode():
         assert torch.allclose(tg[k], u0 @ E[k].T, atol=1e-5)
     # M is stable (eigenvalues in [-2, -0.1]): the targets shrink
     assert float(tg[-1].norm()) < float(tg[0].norm())
+
+
+def test_multishoot_packing_matches_per_trajectory_slices():
+    """The packed initial states and save-point data of many trajectories
+    (rows of the concatenated data, gathered through the cached layout) equal
+    each trajectory's own group slices (src/multiple_shooting.jl:52-62,
+    group_ranges at :231-239); data whose length disagrees with its times is
+    rejected."""
+    import pytest
+
+    from gbnde import multiple_shooting as ms
+    rng = np.random.default_rng(7)
+    S = 5
+    trajs = []
+    for _ in range(9):
+        n = int(rng.integers(6, 30))
+        trajs.append((rng.standard_normal((S, n)).astype(np.float32), 0.1 * np.arange(n), int(rng.integers(2, 7))))
+    P = ms._Packed(trajs)
+    u0, data = [], []
+    for d, ts, gs in trajs:
+        for rg in ms.group_ranges(len(ts), gs):
+            u0.append(d[:, rg.start])
+            data.extend(d[:, k] for k in rg)
+    assert np.array_equal(P.u0, np.array(u0)) and np.array_equal(P.data, np.array(data))
+    assert P.u0.flags.c_contiguous and P.data.flags.c_contiguous
+    assert P.nseg == len(u0) and len(P.saveat) == len(data)
+    bad = list(trajs)
+    bad[3] = (bad[3][0][:, :-1], bad[3][1], bad[3][2])
+    with pytest.raises(ValueError):
+        ms._Packed(bad)
