@@ -617,7 +617,6 @@ __global__ void __launch_bounds__(256, 1) bwd_f32_kernel(BwdArgs a) {
       if (!s_ctl.go) break;
       if (iter >= a.maxiters) { ret = GBNDE_RET_MAXITERS; break; }
       ++iter;
-      const double H = s_ctl.h;
       float* lcur = a.lam[cur];
       float* lnew = a.lam[cur ^ 1];
       float* ucurb = a.ub[cur];
