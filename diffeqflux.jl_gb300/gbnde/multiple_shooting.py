@@ -80,19 +80,26 @@ class _Layout:
         offs = np.concatenate([[0], np.cumsum(self.lengths)[:-1]]).astype(np.int64)
         self.gcols = np.concatenate([c + o for c, o in zip(self.cols, offs)])
         self.gstarts = np.concatenate([st + o for st, o in zip(self.starts, offs)])
+        # every trajectory's times, concatenated: a cached layout is reused
+        # only for the same times
+        self.tcat = np.concatenate([np.asarray(ts, dtype=np.float64) for ts, _ in shapes])
 
 
 class _Packed:
     """Segment table and packed values (initial states, data at the saves) of
     one or many trajectories; the table is reused across calls with the same
-    lengths and group sizes."""
+    lengths, group sizes and times."""
 
     _cache = {}
 
     def __init__(self, trajectories):
         # trajectories: list of (data S x n, tsteps n, group_size)
-        key = tuple((len(ts), int(gs), float(ts[0]), float(ts[-1])) for _, ts, gs in trajectories)
+        key = tuple((len(ts), int(gs)) for _, ts, gs in trajectories)
         lay = _Packed._cache.get(key)
+        if lay is not None:
+            tcat = np.concatenate([np.asarray(ts, dtype=np.float64) for _, ts, _ in trajectories])
+            if not np.array_equal(tcat, lay.tcat):
+                lay = None
         if lay is None:
             lay = _Layout([(ts, gs) for _, ts, gs in trajectories])
             _Packed._cache = {key: lay}  # keep the last layout only

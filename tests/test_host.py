@@ -84,3 +84,18 @@ def test_multishoot_packing_matches_per_trajectory_slices():
     bad[3] = (bad[3][0][:, :-1], bad[3][1], bad[3][2])
     with pytest.raises(ValueError):
         ms._Packed(bad)
+
+
+def test_multishoot_layout_cache_follows_the_times():
+    """A cached segment table is reused only for the same times: trajectories
+    with the same lengths, group sizes and end points but other interior
+    times get their own save times."""
+    from gbnde import multiple_shooting as ms
+    d = np.zeros((2, 7), np.float32)
+    t1 = np.linspace(0.0, 1.0, 7)
+    t2 = t1.copy()
+    t2[3] = 0.55
+    a = ms._Packed([(d, t1, 3)])
+    b = ms._Packed([(d, t2, 3)])
+    c = ms._Packed([(d, t1, 3)])
+    assert np.array_equal(a.saveat[[0, 1, 2]], t1[:3]) and 0.55 in b.saveat and 0.55 not in c.saveat
