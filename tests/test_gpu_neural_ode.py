@@ -354,3 +354,58 @@ def test_save_everystep_states_and_gradient(device):
     gu, gp, _ = ots.adjoint_interpolating(rhs, fwd, sol.t, w.cpu().numpy().astype(np.float64), 0.0, 1e-6, 1e-4)
     assert _rel(x.grad.cpu().numpy(), gu) < 2e-4
     assert _rel(pt.grad.cpu().numpy(), gp) < 2e-4
+
+
+def test_c_abi_rejects_malformed_calls_before_any_launch():
+    """Argument checks of the C entry points (the host side of the boundary;
+    each call returns its error code before anything reaches the device):
+    empty batch, t1 == t0, save times outside tspan or out of order, bad
+    tolerances, a state size that does not match the model, unknown sensealg
+    and flags, a backward before any forward, FFJORD's regularised form
+    without noise, malformed multiple-shooting segments and reading saves
+    before a multiple-shooting forward."""
+    import ctypes as C
+
+    import gbnde
+    from gbnde import _lib as L
+    S, H = 4, 8
+    model = gbnde.Chain(gbnde.Dense(S, H, "tanh"), gbnde.Dense(H, S))
+    s = gbnde.Solver(model, "fp32", 0)
+    s.set_params(model.init_params(np.random.default_rng(0)))
+    lib, h = s.lib, s.h
+    u0 = np.zeros((2, S), np.float32)
+    us = np.zeros((4, 2, S), np.float32)
+    st = L.Stats()
+
+    def fwd(desc, S_=S, B=2):
+        return lib.gbnde_forward(h, C.byref(desc), S_, B, u0.ctypes.data, us.ctypes.data, C.byref(st))
+
+    D = gbnde.Solver.solve_desc
+    assert fwd(D(0.0, 1.0, [0.0, 1.0], 1e-6, 1e-6), B=0) == L.ERR_INVALID
+    assert fwd(D(0.0, 0.0, [0.0], 1e-6, 1e-6)) == L.ERR_INVALID
+    assert fwd(D(0.0, 1.0, [0.0, 1.5], 1e-6, 1e-6)) == L.ERR_INVALID
+    assert fwd(D(0.0, 1.0, [0.5, 0.2], 1e-6, 1e-6)) == L.ERR_INVALID
+    assert fwd(D(0.0, 1.0, [1.0], 0.0, 1e-6)) == L.ERR_INVALID
+    assert fwd(D(0.0, 1.0, [1.0], 1e-6, 1e-6), S_=S + 1) == L.ERR_INVALID
+    assert fwd(D(0.0, 1.0, [1.0], 1e-6, 1e-6, sensealg=7)) == L.ERR_INVALID
+    assert fwd(D(0.0, 1.0, [1.0], 1e-6, 1e-6, flags=0x100)) == L.ERR_INVALID
+    dl = np.zeros((1, 2, S), np.float32)
+    du0 = np.zeros((2, S), np.float32)
+    dp = np.zeros(s.nparams, np.float32)
+    assert lib.gbnde_backward(h, dl.ctypes.data, du0.ctypes.data, dp.ctypes.data, C.byref(st)) == L.ERR_STATE
+    x = np.zeros((2, S), np.float32)
+    lp = np.zeros(2, np.float32)
+    desc = D(0.0, 1.0, [1.0], 1e-6, 1e-6)
+    assert lib.gbnde_ffjord_forward_reg(h, C.byref(desc), S, 2, x.ctypes.data, None, 0, lp.ctypes.data, None,
+                                        None, None, C.byref(st)) == L.ERR_INVALID
+    seg = (L.Segment * 1)()
+    seg[0].t0, seg[0].t1, seg[0].save_off, seg[0].nsave = 1.0, 0.0, 0, 1
+    sv = np.array([0.5])
+    ret = np.zeros(1, np.int32)
+    assert lib.gbnde_multishoot_forward(h, S, 1, seg, sv.ctypes.data_as(C.POINTER(C.c_double)), 1,
+                                        u0.ctypes.data, 1e-6, 1e-6, 1000, None,
+                                        ret.ctypes.data_as(C.POINTER(C.c_int)), C.byref(st)) == L.ERR_INVALID
+    assert lib.gbnde_multishoot_saves(h, us.ctypes.data) == L.ERR_STATE
+    # a well-formed call still runs after the rejected ones
+    assert fwd(D(0.0, 1.0, [0.0, 1.0], 1e-6, 1e-6)) == 0 and st.retcode == 0
+    s.close()
