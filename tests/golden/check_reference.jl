@@ -16,7 +16,14 @@
 # oracle values, and the accepted/rejected step counts of the reference's
 # forward solve against the oracle's. With --gb300 the same problems also run
 # through DiffEqFluxGB300 (:fp32 form), so one session compares all three.
-using DiffEqFlux, OrdinaryDiffEq, SciMLSensitivity, Lux, ComponentArrays, Zygote, NPZ, Random, LinearAlgebra
+#
+# ffjord.npz runs the reference's FFJORD (src/ffjord.jl:138-178) with the exact
+# trace (st.monte_carlo = false, deterministic) and compares logpx and the
+# gradients of -mean(logpx); multishoot.npz runs the reference's
+# multiple_shoot (src/multiple_shooting.jl:36-94) with the SSE loss and
+# compares the loss, the group predictions and dL/dp.
+using DiffEqFlux, OrdinaryDiffEq, SciMLSensitivity, Lux, ComponentArrays, Zygote, NPZ, Random, LinearAlgebra,
+      Statistics
 
 const HERE = @__DIR__
 const WITH_GB300 = "--gb300" in ARGS
@@ -75,3 +82,50 @@ end
 
 check("spiral"; loss_kind = :sse)
 check("batched"; loss_kind = :mse)
+
+function check_ffjord()
+    fx = npzread(joinpath(HERE, "ffjord.npz"))
+    d, H = Int(fx["dims"][1]), Int(fx["dims"][2])
+    nn = Chain(Dense(d => H, tanh), Dense(H => d))
+    x = Float32.(fx["x"])
+    ff = FFJORD(nn, (0.0f0, 1.0f0), (d,), Tsit5(); abstol = fx["abstol"], reltol = fx["reltol"])
+    ps0, st = Lux.setup(Random.default_rng(), ff)
+    st = (; st..., monte_carlo = false, regularize = false)
+    p = ComponentArray(Float32.(vec(fx["p"])), getaxes(ComponentArray(ps0)))
+    nll(q, xx) = -mean(first(first(ff(xx, q, st))))
+    logpx = vec(first(first(ff(x, p, st))))
+    gp, gx = Zygote.gradient(nll, p, x)
+    println("== ffjord: d $d, $(size(x, 2)) samples, exact trace")
+    println("  reference: logpx rel diff $(reldiff(logpx, fx["logpx"])), ",
+            "dL/dp rel diff $(reldiff(gp, fx["gp"])), dL/dx rel diff $(reldiff(gx, fx["gx"]))")
+    if WITH_GB300
+        gff = gb300(ff, GB300Tsit5(:fp32))
+        glogpx = vec(first(first(gff(x, p, st))))
+        ggp = first(Zygote.gradient(q -> -mean(first(first(gff(x, q, st)))), p))
+        println("  GB300 fp32: logpx vs reference $(reldiff(glogpx, logpx)), dL/dp $(reldiff(ggp, gp))")
+    end
+end
+
+function check_multishoot()
+    fx = npzread(joinpath(HERE, "multishoot.npz"))
+    S, H = Int(fx["dims"][1]), Int(fx["dims"][2])
+    nn = Chain(Dense(S => H, tanh), Dense(H => S))
+    ps0, st = Lux.setup(Random.default_rng(), nn)
+    p = ComponentArray(Float32.(vec(fx["p"])), getaxes(ComponentArray(ps0)))
+    smodel = StatefulLuxLayer{true}(nn, nothing, st)
+    data = Float32.(fx["data"])
+    ts = Float32.(vec(fx["ts"]))
+    prob = ODEProblem((u, q, t) -> smodel(u, q), data[:, 1], (ts[1], ts[end]), p)
+    sse(u, uh) = sum(abs2, u .- uh)
+    ms(q) = multiple_shoot(q, data, ts, prob, sse, Tsit5(), Int(fx["group_size"]);
+                           continuity_term = fx["continuity_term"], abstol = fx["abstol"], reltol = fx["reltol"])
+    loss, preds = ms(p)
+    gp = first(Zygote.gradient(q -> first(ms(q)), p))
+    println("== multishoot: state $S, $(size(data, 2)) points, group size $(Int(fx["group_size"]))")
+    println("  reference: loss rel diff $(abs(loss - fx["loss"]) / abs(fx["loss"])), ",
+            "predictions rel diff $(reldiff(reduce(hcat, Array.(preds)), fx["preds"])), ",
+            "dL/dp rel diff $(reldiff(gp, fx["gp"]))")
+end
+
+check_ffjord()
+check_multishoot()

@@ -17,6 +17,17 @@ the reference -- can be checked on identical inputs.
   batched.npz  state 16, MLP 16->64->64->16 tanh, 8 trajectories, 20 save
                points, abstol 1e-7 reltol 1e-5, MSE loss (the headline configuration's
                structure at a size that keeps the fixture small).
+  ffjord.npz   FFJORD with the exact trace (monte_carlo = false, deterministic in
+               the reference too; src/ffjord.jl:120-129), d = 2, model
+               Dense(2,16,tanh) -> Dense(16,2) without a time input, 16 samples,
+               tspan (0,1), 1e-8 / 1e-8: logpx, z(t1), and the gradients of
+               -mean(logpx) with respect to p and x (the oracle's adjoint, checked
+               here against central differences).
+  multishoot.npz  multiple_shoot of one trajectory (src/multiple_shooting.jl:36-94):
+               state 2, 21 data points at dt = 0.1 from du/dt = A u^3, model
+               Dense(2,16,tanh) -> Dense(16,2), group size 5, continuity_term 100,
+               SSE loss, 1e-8 / 1e-8: the loss, the group predictions, and dL/dp by
+               central differences of the oracle's loss.
 """
 import os
 import sys
@@ -27,7 +38,9 @@ from scipy.linalg import expm
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
+from oracle import ffjord as off  # noqa: E402
 from oracle import mlp as omlp  # noqa: E402
+from oracle import multishoot as oms  # noqa: E402
 from oracle import tsit5 as ots  # noqa: E402
 
 
@@ -95,10 +108,69 @@ def batched():
              naccept=fwd.naccept, nreject=fwd.nreject)
 
 
+def ffjord():
+    rng = np.random.default_rng(3)
+    d, H, B, tol = 2, 16, 16, 1e-8
+    m = omlp.MLP([d, H, d], ["tanh", "identity"])
+    p = m.glorot_uniform(rng).astype(np.float32)
+    x = (rng.standard_normal((d, B)) * 0.7 + rng.choice([-1.0, 1.0], size=(1, B))).astype(np.float32)
+    x = x.astype(np.float64)
+
+    def solve(pp, xx):
+        rhs = off.FFJORDRHS(m, pp, exact=True)
+        ys, fwd = ots.solve_forward(rhs, np.vstack([xx, np.zeros((1, B))]), 0.0, 1.0, [1.0], tol, tol)
+        return rhs, ys[..., 0], fwd
+
+    rhs, yT, fwd = solve(p.astype(np.float64), x)
+    logpx = off.logpx_from_final(yT, d)
+    g = -np.ones(B) / B                      # dL/dlogpx of L = -mean(logpx)
+    dy = np.vstack([-yT[:d] * g, -g[None, :]])
+    gx, gp, _ = ots.adjoint_interpolating(rhs, fwd, [1.0], dy[..., None], 0.0, tol, tol)
+    nll = lambda pp, xx: -np.mean(off.logpx_from_final(solve(pp, xx)[1], d))  # noqa: E731
+    eps = 1e-6
+    p64 = p.astype(np.float64)
+    fdp = np.array([(nll(p64 + eps * v, x) - nll(p64 - eps * v, x)) / (2 * eps) for v in np.eye(p.size)])
+    assert np.linalg.norm(gp - fdp) / np.linalg.norm(fdp) < 1e-5
+    np.savez(os.path.join(HERE, "ffjord.npz"), dims=np.array([d, H, d]), p=p, x=x, tspan=np.array([0.0, 1.0]),
+             abstol=tol, reltol=tol, logpx=logpx, zT=yT[:d], delta_logp=yT[d], gp=gp, gx=gx[:d],
+             naccept=fwd.naccept, nreject=fwd.nreject)
+
+
+def multishoot():
+    rng = np.random.default_rng(4)
+    S, H, n, gs, tol = 2, 16, 21, 5, 1e-8
+    A = np.array([[-0.1, 2.0], [-2.0, -0.1]])
+
+    class Cubic:
+        def f(self, u, t):
+            return ((u ** 3).T @ A).T
+
+    ts = 0.1 * np.arange(n)
+    data, _ = ots.solve_forward(Cubic(), np.array([[2.0], [0.0]]), 0.0, ts[-1], ts, 1e-10, 1e-10)
+    data = data[:, 0, :].astype(np.float32).astype(np.float64)
+    m = omlp.MLP([S, H, S], ["tanh", "identity"])
+    p = m.glorot_uniform(rng).astype(np.float32)
+
+    def loss(pp):
+        preds, ok = oms.solve_groups(omlp.MLPRHS(m, pp), data, ts, gs, tol, tol)
+        assert ok
+        return oms.multiple_shoot_loss(preds, data, gs, 100.0), preds
+
+    p64 = p.astype(np.float64)
+    L, preds = loss(p64)
+    eps = 1e-6
+    gp = np.array([(loss(p64 + eps * v)[0] - loss(p64 - eps * v)[0]) / (2 * eps) for v in np.eye(p.size)])
+    np.savez(os.path.join(HERE, "multishoot.npz"), dims=np.array([S, H, S]), p=p, data=data, ts=ts,
+             group_size=gs, continuity_term=100.0, abstol=tol, reltol=tol, loss=L,
+             preds=np.concatenate(preds, axis=1), gp=gp)
+
+
 if __name__ == "__main__":
     spiral()
     linear()
     batched()
+    ffjord()
+    multishoot()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")

@@ -56,3 +56,44 @@ def test_fixture_forward_and_gradient(name, prec, sense):
     gtol = 5e-4 if prec == "fp32" else 1e-3
     assert _rel(du0, g["gu_" + key]) < gtol
     assert _rel(dp, g["gp_" + key]) < gtol
+
+
+def test_ffjord_fixture_fp32():
+    """ffjord.npz (exact trace, no time input): logpx and z(t1) 1e-4 relative
+    to their max, and the gradients of -mean(logpx) in p and x 5e-4 (the
+    fixture's oracle adjoint agrees with central differences to 1e-5)."""
+    import gbnde
+    g = dict(np.load(os.path.join(GOLDEN, "ffjord.npz")))
+    d, H = int(g["dims"][0]), int(g["dims"][1])
+    model = gbnde.Chain(gbnde.Dense(d, H, "tanh"), gbnde.Dense(H, d))
+    fj = gbnde.FFJORD(model, (0.0, 1.0), (d,), gbnde.Tsit5(), abstol=float(g["abstol"]),
+                      reltol=float(g["reltol"]))
+    B = g["x"].shape[1]
+    logpx, zT, st = fj.forward_np(g["x"].astype(np.float32), g["p"], None)
+    assert st.retcode == 0
+    assert np.abs(logpx - g["logpx"]).max() < 1e-4 * np.abs(g["logpx"]).max()
+    assert np.abs(zT - g["zT"]).max() < 1e-4 * np.abs(g["zT"]).max()
+    dx, dp, sta = fj.backward_np(np.full(B, -1.0 / B, np.float32))
+    assert sta.retcode_adj == 0
+    assert _rel(dp, g["gp"]) < 5e-4 and _rel(dx, g["gx"]) < 5e-4
+
+
+def test_multishoot_fixture_fp32():
+    """multishoot.npz: the fused device loss (SSE, continuity term 100) 1e-5
+    relative, the group predictions 1e-4, dL/dp through the discrete adjoint
+    against the fixture's central differences 1e-3."""
+    import torch
+
+    import gbnde
+    g = dict(np.load(os.path.join(GOLDEN, "multishoot.npz")))
+    S, H = int(g["dims"][0]), int(g["dims"][1])
+    model = gbnde.Chain(gbnde.Dense(S, H, "tanh"), gbnde.Dense(H, S))
+    pt = torch.tensor(g["p"], requires_grad=True)
+    loss, preds = gbnde.multiple_shoot(pt, g["data"].astype(np.float32), g["ts"], model, gbnde.sse_loss,
+                                       int(g["group_size"]), continuity_term=float(g["continuity_term"]),
+                                       abstol=float(g["abstol"]), reltol=float(g["reltol"]))
+    L = float(loss.detach())
+    loss.backward()
+    assert abs(L - float(g["loss"])) / float(g["loss"]) < 1e-5
+    assert _rel(np.concatenate([np.asarray(a) for a in preds], axis=1), g["preds"]) < 1e-4
+    assert _rel(pt.grad.numpy(), g["gp"]) < 1e-3

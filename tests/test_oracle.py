@@ -229,3 +229,25 @@ def test_adjoint_linear_known_answer(sense):
         E[j] = eps
         fd[j] = (loss(M + E.reshape(S, S)) - loss(M - E.reshape(S, S))) / (2 * eps)
     assert np.abs(gp - fd).max() < 1e-6 * np.abs(fd).max()
+
+
+def test_oracle_reproduces_the_ffjord_and_multishoot_fixtures():
+    """ffjord.npz (exact trace) and multishoot.npz recomputed by the oracle:
+    logpx, z(t1) and the step count; the group predictions and the loss."""
+    from oracle import ffjord as off
+    from oracle import multishoot as oms
+    f = _load("ffjord.npz")
+    dims = [int(x) for x in f["dims"]]
+    d, B = dims[0], f["x"].shape[1]
+    m = omlp.MLP(dims, ["tanh", "identity"])
+    rhs = off.FFJORDRHS(m, f["p"].astype(np.float64), exact=True)
+    ys, fwd = ots.solve_forward(rhs, np.vstack([f["x"], np.zeros((1, B))]), 0.0, 1.0, [1.0],
+                                float(f["abstol"]), float(f["reltol"]))
+    assert np.array_equal(off.logpx_from_final(ys[..., 0], d), f["logpx"])
+    assert np.array_equal(ys[:d, :, 0], f["zT"]) and fwd.naccept == int(f["naccept"])
+    g = _load("multishoot.npz")
+    m2 = omlp.MLP([int(x) for x in g["dims"]], ["tanh", "identity"])
+    preds, ok = oms.solve_groups(omlp.MLPRHS(m2, g["p"].astype(np.float64)), g["data"], g["ts"],
+                                 int(g["group_size"]), float(g["abstol"]), float(g["reltol"]))
+    assert ok and np.array_equal(np.concatenate(preds, axis=1), g["preds"])
+    assert oms.multiple_shoot_loss(preds, g["data"], int(g["group_size"]), float(g["continuity_term"])) == g["loss"]
